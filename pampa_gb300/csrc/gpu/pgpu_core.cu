@@ -1,0 +1,116 @@
+// pgpu_* entry points shared by both solver kinds: error state, options, problem
+// accessors and destruction.
+#include <cstdio>
+#include <cstring>
+
+#include "pgpu_internal.cuh"
+
+namespace pgpu {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int dev_alloc(DevBuf& b, size_t bytes, long long* counter) {
+  b.release();
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(&b.ptr, bytes);
+  if (e != cudaSuccess) {
+    b.ptr = nullptr;
+    return fail(e == cudaErrorMemoryAllocation ? PGPU_ERR_NO_MEMORY : PGPU_ERR_CUDA,
+                std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+  }
+  b.bytes = bytes;
+  if (counter) *counter += (long long)bytes;
+  return PGPU_OK;
+}
+
+int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter) {
+  int st = dev_alloc(b, bytes, counter);
+  if (st != PGPU_OK) return st;
+  if (host && bytes) PGPU_CUDA(cudaMemcpy(b.ptr, host, bytes, cudaMemcpyHostToDevice));
+  return PGPU_OK;
+}
+
+}  // namespace pgpu
+
+extern "C" {
+
+void pgpu_default_options(pgpu_options* opt) {
+  std::memset(opt, 0, sizeof(*opt));
+  opt->precision = PGPU_FP64;
+  opt->tol_k = 1e-10;
+  opt->tol_flux = 1e-9;
+  opt->max_outer = 5000;
+  opt->max_inner = 2000;
+  opt->power = 1.0;
+  opt->verbose = 0;
+}
+
+const char* pgpu_last_error(void) { return pgpu::g_last_error.c_str(); }
+
+int pgpu_problem_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
+  if (!p) return pgpu::fail(PGPU_ERR_INVALID, "null problem");
+  pgpu_options def;
+  pgpu_default_options(&def);
+  if (!opt) opt = &def;
+  pgpu_stats local;
+  std::memset(&local, 0, sizeof(local));
+  if (!stats) stats = &local;
+  std::memset(stats, 0, sizeof(*stats));
+  PGPU_CUDA(cudaSetDevice(p->device));
+  int st = PGPU_ERR_INVALID;
+  if (p->kind == 1) st = pgpu::diffusion_solve(p, opt, stats);
+  else if (p->kind == 2) st = pgpu::sn_solve(p, opt, stats);
+  stats->status = st;
+  p->solved = (st == PGPU_OK);
+  if (p->solved) p->keff = stats->keff;
+  return st;
+}
+
+int pgpu_problem_get_keff(pgpu_problem* p, double* keff) {
+  if (!p || !p->solved) return pgpu::fail(PGPU_ERR_INVALID, "problem not solved");
+  *keff = p->keff;
+  return PGPU_OK;
+}
+
+int pgpu_problem_get_scalar_flux(pgpu_problem* p, double* phi) {
+  if (!p || !p->solved) return pgpu::fail(PGPU_ERR_INVALID, "problem not solved");
+  PGPU_CUDA(cudaSetDevice(p->device));
+  return p->kind == 1 ? pgpu::diffusion_get_flux(p, phi) : pgpu::sn_get_flux(p, phi);
+}
+
+int pgpu_problem_get_angular_flux(pgpu_problem* p, double* psi) {
+  if (!p || !p->solved) return pgpu::fail(PGPU_ERR_INVALID, "problem not solved");
+  if (p->kind != 2) return pgpu::fail(PGPU_ERR_INVALID, "angular flux exists only for SN problems");
+  PGPU_CUDA(cudaSetDevice(p->device));
+  return pgpu::sn_get_angular(p, psi);
+}
+
+int pgpu_problem_get_power(pgpu_problem* p, double* q, double* P, double* total) {
+  if (!p || !p->solved) return pgpu::fail(PGPU_ERR_INVALID, "problem not solved");
+  PGPU_CUDA(cudaSetDevice(p->device));
+  return p->kind == 1 ? pgpu::diffusion_get_power(p, q, P, total)
+                      : pgpu::sn_get_power(p, q, P, total);
+}
+
+long long pgpu_problem_device_bytes(pgpu_problem* p) { return p ? p->bytes : 0; }
+
+void pgpu_problem_destroy(pgpu_problem* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  if (p->kind == 1) pgpu::diffusion_destroy(p);
+  if (p->kind == 2) pgpu::sn_destroy(p);
+  if (p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+}
+
+}  // extern "C"

@@ -1,0 +1,701 @@
+// Multigroup diffusion k-eigenvalue solve on one GPU.
+//
+// Replaces the EPSSolve that DiffusionSolver::getSolution hands to SLEPc
+// (DiffusionSolver.cxx:323-350, petsc.cxx:175-204): instead of Krylov-Schur with a
+// sparse LU of R, the dominant eigenpair of R x = (1/k) F x is found by power iteration
+// on R^-1 F with device-resident BiCGStab inner solves.  The converged eigenpair is the
+// same (largest k); only the iteration history differs.
+//
+// Layout in HBM (cell-major, group-interleaved rows l = i*G + g, as NeutronicSolver::index):
+//   diag[l], off[f][l] (face-major so a warp reads 32 consecutive rows), nbr[f][i],
+//   mat[i], vol[i]; per-material sigma_s[m][g_from][g_to], chi, nu_sigma_f, kappa_sigma_f.
+// The in-cell scattering block of R is rebuilt from the material table (-sigma_s * V)
+// instead of being stored, which removes G-1 stored values per row.
+//
+// Mixed precision (PGPU_MIXED): the outer residual r = b - R y, the fission source, the
+// k update and the normalisation stay FP64; the BiCGStab correction solves R d = r run in
+// FP32 with FP32 accumulation, and y += d refines in FP64 (iterative refinement).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "pgpu_internal.cuh"
+
+namespace pgpu {
+
+template <typename T>
+struct DiffOp {
+  int n, G, F;
+  const int* __restrict__ nbr;  // [F][n]
+  const T* __restrict__ off;    // [F][n*G]
+  const T* __restrict__ diag;   // [n*G]
+  const int* __restrict__ mat;  // [n]
+  const T* __restrict__ vol;    // [n]
+  const T* __restrict__ ss;     // [nm][G][G]
+};
+
+// Device-resident BiCGStab state; every scalar of the iteration stays on the GPU.
+struct BiScal {
+  double rho, rho_old, alpha, omega;
+  double rr, bb, tol2;
+  int converged, breakdown, iters, max_iters;
+};
+
+// Outer (power iteration) state.
+struct OuterScal {
+  double k, k_old, S, change, p0, total_power;
+  double rr, bb;
+  int negatives, nonfinite;
+};
+
+struct DiffusionData {
+  int n = 0, G = 0, F = 0, nm = 0;
+  DevBuf nbr, mat, off64, diag64, vol64, ss64, chi, nsf, ksf;
+  DevBuf off32, diag32, vol32, ss32;
+  DevBuf x, y, b, r64, r32, fs, fs_old, phi, q, P;
+  DevBuf w64[9];  // BiCGStab vectors for FP64
+  DevBuf w32[9];  // BiCGStab vectors for FP32
+  DevBuf partials, ticket, bscal, oscal;
+  bool have32 = false;
+};
+
+// ---------------------------------------------------------------------------------
+// Operator pieces
+// ---------------------------------------------------------------------------------
+
+// y_l = (R x)_l for one row l = i*G + g.
+template <typename T>
+__device__ __forceinline__ T apply_row(const DiffOp<T>& A, const T* __restrict__ x, int i, int g) {
+  const int G = A.G;
+  const size_t l = (size_t)i * G + g;
+  T acc = A.diag[l] * x[l];
+  const int m = A.mat[i];
+  const T* ssm = A.ss + (size_t)m * G * G;
+  T sc = T(0);
+  for (int g2 = 0; g2 < G; g2++)
+    if (g2 != g) sc += ssm[g2 * G + g] * x[(size_t)i * G + g2];
+  acc -= A.vol[i] * sc;
+  const size_t nG = (size_t)A.n * G;
+  for (int f = 0; f < A.F; f++) {
+    const int j = A.nbr[(size_t)f * A.n + i];
+    if (j >= 0) acc += A.off[f * nG + l] * x[(size_t)j * G + g];
+  }
+  return acc;
+}
+
+// z = M^-1 r for the cell block: forward substitution over groups with the lower
+// (down-scatter) part of the in-cell block; up-scatter is left to the Krylov method.
+template <typename T>
+__device__ __forceinline__ void precond_cell(const DiffOp<T>& A, int i, const T* rin, T* zout) {
+  const int G = A.G;
+  const int m = A.mat[i];
+  const T* ssm = A.ss + (size_t)m * G * G;
+  const T V = A.vol[i];
+  for (int g = 0; g < G; g++) {
+    T s = rin[g];
+    for (int g2 = 0; g2 < g; g2++) s += V * ssm[g2 * G + g] * zout[g2];
+    zout[g] = s / A.diag[(size_t)i * G + g];
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// BiCGStab kernels (right preconditioned), T = double or float.
+// ---------------------------------------------------------------------------------
+
+// rhat = r = rin; x = p = v = 0; rho = rr = bb = (r, r).
+template <typename T>
+__global__ void k_bicg_init(int N, const T* __restrict__ rin, T* r, T* rhat, T* x, T* p, T* v,
+                            BiScal* sc, ReduceSlots<1> slots, double rtol, int max_iters) {
+  double acc[1] = {0.0};
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    T val = rin[l];
+    r[l] = val;
+    rhat[l] = val;
+    x[l] = T(0);
+    p[l] = T(0);
+    v[l] = T(0);
+    acc[0] += (double)val * (double)val;
+  }
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
+    sc->rho = tot[0];
+    sc->rho_old = 1.0;
+    sc->alpha = 1.0;
+    sc->omega = 1.0;
+    sc->rr = tot[0];
+    sc->bb = tot[0];
+    sc->tol2 = rtol * rtol * tot[0];
+    sc->iters = 0;
+    sc->max_iters = max_iters;
+    sc->breakdown = 0;
+    sc->converged = (tot[0] <= sc->tol2) || !(tot[0] == tot[0]) ? 1 : 0;
+    if (tot[0] == 0.0) sc->converged = 1;
+  }
+}
+
+// p = r + beta (p - omega v); phat = M^-1 p (per cell).
+template <typename T>
+__global__ void k_bicg_p(DiffOp<T> A, const T* __restrict__ r, T* p, const T* __restrict__ v,
+                         T* phat, const BiScal* sc) {
+  if (sc->converged) return;
+  const double beta = (sc->rho / sc->rho_old) * (sc->alpha / sc->omega);
+  const T tb = (T)beta, tw = (T)sc->omega;
+  const int G = A.G;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    T pc[kMaxGroups], zc[kMaxGroups];
+    for (int g = 0; g < G; g++) {
+      size_t l = (size_t)i * G + g;
+      T val = r[l] + tb * (p[l] - tw * v[l]);
+      p[l] = val;
+      pc[g] = val;
+    }
+    precond_cell(A, i, pc, zc);
+    for (int g = 0; g < G; g++) phat[(size_t)i * G + g] = zc[g];
+  }
+}
+
+// v = A phat; alpha = rho / (rhat, v).
+template <typename T>
+__global__ void k_bicg_v(DiffOp<T> A, const T* __restrict__ phat, T* v, const T* __restrict__ rhat,
+                         BiScal* sc, ReduceSlots<1> slots) {
+  if (sc->converged) return;
+  const int N = A.n * A.G;
+  double acc[1] = {0.0};
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
+    const int i = l / A.G, g = l - i * A.G;
+    T val = apply_row(A, phat, i, g);
+    v[l] = val;
+    acc[0] += (double)rhat[l] * (double)val;
+  }
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
+    if (tot[0] == 0.0 || !(tot[0] == tot[0])) {
+      sc->breakdown = 1;
+      sc->converged = 1;
+    } else {
+      sc->alpha = sc->rho / tot[0];
+    }
+  }
+}
+
+// s = r - alpha v; shat = M^-1 s (per cell).
+template <typename T>
+__global__ void k_bicg_s(DiffOp<T> A, const T* __restrict__ r, const T* __restrict__ v, T* s, T* shat,
+                         const BiScal* sc) {
+  if (sc->converged) return;
+  const T ta = (T)sc->alpha;
+  const int G = A.G;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    T sc_[kMaxGroups], zc[kMaxGroups];
+    for (int g = 0; g < G; g++) {
+      size_t l = (size_t)i * G + g;
+      T val = r[l] - ta * v[l];
+      s[l] = val;
+      sc_[g] = val;
+    }
+    precond_cell(A, i, sc_, zc);
+    for (int g = 0; g < G; g++) shat[(size_t)i * G + g] = zc[g];
+  }
+}
+
+// t = A shat; omega = (t, s) / (t, t).
+template <typename T>
+__global__ void k_bicg_t(DiffOp<T> A, const T* __restrict__ shat, T* t, const T* __restrict__ s,
+                         BiScal* sc, ReduceSlots<2> slots) {
+  if (sc->converged) return;
+  const int N = A.n * A.G;
+  double acc[2] = {0.0, 0.0};
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
+    const int i = l / A.G, g = l - i * A.G;
+    T val = apply_row(A, shat, i, g);
+    t[l] = val;
+    acc[0] += (double)val * (double)s[l];
+    acc[1] += (double)val * (double)val;
+  }
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
+    if (tot[1] == 0.0 || !(tot[1] == tot[1])) {
+      sc->omega = 0.0;
+      sc->breakdown = 1;
+    } else {
+      sc->omega = tot[0] / tot[1];
+    }
+  }
+}
+
+// x += alpha phat + omega shat; r = s - omega t; rho = (rhat, r); rr = (r, r).
+template <typename T>
+__global__ void k_bicg_x(int N, T* x, T* r, const T* __restrict__ phat, const T* __restrict__ shat,
+                         const T* __restrict__ s, const T* __restrict__ t, const T* __restrict__ rhat,
+                         BiScal* sc, ReduceSlots<2> slots) {
+  if (sc->converged) return;
+  const T ta = (T)sc->alpha, tw = (T)sc->omega;
+  double acc[2] = {0.0, 0.0};
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
+    x[l] += ta * phat[l] + tw * shat[l];
+    T rv = s[l] - tw * t[l];
+    r[l] = rv;
+    acc[0] += (double)rhat[l] * (double)rv;
+    acc[1] += (double)rv * (double)rv;
+  }
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
+    sc->rho_old = sc->rho;
+    sc->rho = tot[0];
+    sc->rr = tot[1];
+    sc->iters += 1;
+    bool bad = !(tot[1] == tot[1]);
+    if (tot[1] <= sc->tol2 || sc->iters >= sc->max_iters || sc->breakdown || bad) sc->converged = 1;
+    if (tot[0] == 0.0) sc->converged = 1;
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Outer-iteration kernels (always FP64)
+// ---------------------------------------------------------------------------------
+
+// r = b - R y (FP64), optional FP32 copy; rr = (r, r), bb = (b, b).
+template <typename T2>
+__global__ void k_residual(DiffOp<double> A, const double* __restrict__ b, const double* __restrict__ y,
+                           double* r, T2* r2, OuterScal* os, ReduceSlots<2> slots) {
+  const int N = A.n * A.G;
+  double acc[2] = {0.0, 0.0};
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
+    const int i = l / A.G, g = l - i * A.G;
+    double bv = b[l];
+    double rv = bv - apply_row(A, y, i, g);
+    r[l] = rv;
+    if (r2) r2[l] = (T2)rv;
+    acc[0] += rv * rv;
+    acc[1] += bv * bv;
+  }
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
+    os->rr = tot[0];
+    os->bb = tot[1];
+  }
+}
+
+// y += d (d in T).
+template <typename T>
+__global__ void k_axpy_update(int N, double* y, const T* __restrict__ d) {
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) y[l] += (double)d[l];
+}
+
+// fs_i = V_i sum_g nu_sigma_f x_ig; S = sum_i fs_i; k_new = k * S.
+__global__ void k_fission_total(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
+                                const double* __restrict__ nsf, const double* __restrict__ y,
+                                double* fs, OuterScal* os, ReduceSlots<1> slots) {
+  double acc[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* ns = nsf + (size_t)mat[i] * G;
+    double s = 0.0;
+    for (int g = 0; g < G; g++) s += ns[g] * y[(size_t)i * G + g];
+    s *= vol[i];
+    fs[i] = s;
+    acc[0] += s;
+  }
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
+    os->S = tot[0];
+    os->k_old = os->k;
+    os->k = os->k * tot[0];
+    os->nonfinite = !(tot[0] == tot[0]) || tot[0] == 0.0;
+  }
+}
+
+// x = y / S; fs normalised; change = |fs - fs_old| / |fs|; b = chi fs / k.
+__global__ void k_normalize_source(int n, int G, const int* __restrict__ mat, const double* __restrict__ chi,
+                                   const double* __restrict__ y, double* x, double* fs, double* fs_old,
+                                   double* b, OuterScal* os, ReduceSlots<2> slots) {
+  const double invS = 1.0 / os->S;
+  const double invk = 1.0 / os->k;
+  double acc[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int g = 0; g < G; g++) x[(size_t)i * G + g] = y[(size_t)i * G + g] * invS;
+    double f = fs[i] * invS;
+    double d = f - fs_old[i];
+    fs_old[i] = f;
+    acc[0] += d * d;
+    acc[1] += f * f;
+    const double* ch = chi + (size_t)mat[i] * G;
+    for (int g = 0; g < G; g++) b[(size_t)i * G + g] = ch[g] * f * invk;
+  }
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) os->change = sqrt(tot[0] / tot[1]);
+}
+
+// Initial flat flux: x = y = 1, fission source and b for k = 1.
+__global__ void k_fill(int N, double* a, double v) {
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) a[l] = v;
+}
+
+// p0 = sum phi kappa_sigma_f V (NeutronicSolver::normalizeScalarFlux).
+__global__ void k_power_norm(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
+                             const double* __restrict__ ksf, const double* __restrict__ x, OuterScal* os,
+                             ReduceSlots<1> slots) {
+  double acc[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* ks = ksf + (size_t)mat[i] * G;
+    for (int g = 0; g < G; g++) acc[0] += x[(size_t)i * G + g] * ks[g] * vol[i];
+  }
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) os->p0 = tot[0];
+}
+
+// phi = x * power / p0; q_i, P_i (NeutronicSolver::calculatePowerAndProductionRate);
+// counts negative entries.
+__global__ void k_power_fields(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
+                               const double* __restrict__ ksf, const double* __restrict__ nsf,
+                               const double* __restrict__ x, double power, double* phi, double* q,
+                               double* P, OuterScal* os, ReduceSlots<2> slots) {
+  const double f = power / os->p0;
+  const double k = os->k;
+  double acc[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* ks = ksf + (size_t)mat[i] * G;
+    const double* ns = nsf + (size_t)mat[i] * G;
+    const double V = vol[i];
+    double qi = 0.0, Pi = 0.0;
+    for (int g = 0; g < G; g++) {
+      double v = x[(size_t)i * G + g] * f;
+      phi[(size_t)i * G + g] = v;
+      if (v < 0.0) acc[1] += 1.0;
+      qi += v * ks[g] * V;
+      Pi += v * ns[g] * V / k;
+    }
+    q[i] = qi;
+    P[i] = Pi;
+    acc[0] += qi;
+  }
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
+    os->total_power = tot[0];
+    os->negatives = (int)tot[1];
+  }
+}
+
+// Test hook: y = R x.
+__global__ void k_apply(DiffOp<double> A, const double* __restrict__ x, double* y) {
+  const int N = A.n * A.G;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
+    const int i = l / A.G, g = l - i * A.G;
+    y[l] = apply_row(A, x, i, g);
+  }
+}
+
+template <typename S, typename D>
+__global__ void k_convert(long long N, const S* __restrict__ a, D* b) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    b[l] = (D)a[l];
+}
+
+
+// ---------------------------------------------------------------------------------
+// Host driver
+// ---------------------------------------------------------------------------------
+
+namespace {
+
+DiffOp<double> op64(const DiffusionData& d) {
+  return DiffOp<double>{d.n, d.G, d.F, d.nbr.as<int>(), d.off64.as<double>(), d.diag64.as<double>(),
+                        d.mat.as<int>(), d.vol64.as<double>(), d.ss64.as<double>()};
+}
+
+DiffOp<float> op32(const DiffusionData& d) {
+  return DiffOp<float>{d.n, d.G, d.F, d.nbr.as<int>(), d.off32.as<float>(), d.diag32.as<float>(),
+                       d.mat.as<int>(), d.vol32.as<float>(), d.ss32.as<float>()};
+}
+
+template <int NV>
+ReduceSlots<NV> slots_of(DiffusionData& d) {
+  return ReduceSlots<NV>{d.partials.as<double>(), d.ticket.as<unsigned int>()};
+}
+
+int make_fp32(pgpu_problem* p) {
+  DiffusionData& d = *p->diff;
+  if (d.have32) return PGPU_OK;
+  const size_t nG = (size_t)d.n * d.G;
+  int st;
+  if ((st = dev_alloc(d.off32, (size_t)d.F * nG * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.diag32, nG * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.vol32, (size_t)d.n * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.ss32, (size_t)d.nm * d.G * d.G * 4, &p->bytes))) return st;
+  cudaStream_t s = p->stream;
+  k_convert<double, float><<<grid_for((long long)d.F * nG), kThreads, 0, s>>>((long long)d.F * nG, d.off64.as<double>(), d.off32.as<float>());
+  k_convert<double, float><<<grid_for(nG), kThreads, 0, s>>>(nG, d.diag64.as<double>(), d.diag32.as<float>());
+  k_convert<double, float><<<grid_for(d.n), kThreads, 0, s>>>(d.n, d.vol64.as<double>(), d.vol32.as<float>());
+  k_convert<double, float><<<1, kThreads, 0, s>>>((long long)d.nm * d.G * d.G, d.ss64.as<double>(), d.ss32.as<float>());
+  for (int k = 0; k < 9; k++)
+    if ((st = dev_alloc(d.w32[k], nG * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.r32, nG * 4, &p->bytes))) return st;
+  PGPU_CUDA(cudaGetLastError());
+  d.have32 = true;
+  return PGPU_OK;
+}
+
+// BiCGStab on A d = rin in precision T.  Kernels are launched in chunks; each kernel
+// returns at once when the device-side `converged` flag is set, so the host only reads
+// the state once per chunk.  The solution is left in w[0].
+template <typename T>
+int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, double rtol, int max_iters,
+             int* iters_out) {
+  DiffusionData& d = *p->diff;
+  const int N = d.n * d.G;
+  const int gN = grid_for(N), gC = grid_for(d.n);
+  T *x = w[0].as<T>(), *r = w[1].as<T>(), *rhat = w[2].as<T>(), *pp = w[3].as<T>(), *v = w[4].as<T>(),
+    *s = w[5].as<T>(), *t = w[6].as<T>(), *phat = w[7].as<T>(), *shat = w[8].as<T>();
+  BiScal* sc = d.bscal.as<BiScal>();
+  cudaStream_t st = p->stream;
+  k_bicg_init<T><<<gN, kThreads, 0, st>>>(N, rin, r, rhat, x, pp, v, sc, slots_of<1>(d), rtol, max_iters);
+  PGPU_CUDA(cudaGetLastError());
+  BiScal hs;
+  int chunk = 4;
+  for (int launched = 0; launched < max_iters; launched += chunk) {
+    for (int c = 0; c < chunk; c++) {
+      k_bicg_p<T><<<gC, kThreads, 0, st>>>(A, r, pp, v, phat, sc);
+      k_bicg_v<T><<<gN, kThreads, 0, st>>>(A, phat, v, rhat, sc, slots_of<1>(d));
+      k_bicg_s<T><<<gC, kThreads, 0, st>>>(A, r, v, s, shat, sc);
+      k_bicg_t<T><<<gN, kThreads, 0, st>>>(A, shat, t, s, sc, slots_of<2>(d));
+      k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phat, shat, s, t, rhat, sc, slots_of<2>(d));
+    }
+    PGPU_CUDA(cudaGetLastError());
+    PGPU_CUDA(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    PGPU_CUDA(cudaStreamSynchronize(st));
+    if (hs.converged) break;
+    if (chunk < 16) chunk *= 2;
+  }
+  PGPU_CUDA(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, st));
+  PGPU_CUDA(cudaStreamSynchronize(st));
+  *iters_out = hs.iters;
+  if (!(hs.rr == hs.rr)) return fail(PGPU_ERR_NAN, "NaN in the inner Krylov solve");
+  return PGPU_OK;
+}
+
+int read_outer(pgpu_problem* p, OuterScal& os) {
+  PGPU_CUDA(cudaMemcpyAsync(&os, p->diff->oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  return PGPU_OK;
+}
+
+}  // namespace
+
+int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
+  DiffusionData& d = *p->diff;
+  const int n = d.n, G = d.G, N = n * G;
+  const bool mixed = opt->precision == PGPU_MIXED;
+  int st;
+  if (mixed && (st = make_fp32(p))) return st;
+  cudaStream_t s = p->stream;
+  const int gN = grid_for(N), gC = grid_for(n);
+  DiffOp<double> A = op64(d);
+  OuterScal* dos = d.oscal.as<OuterScal>();
+  cudaEvent_t e0, e1;
+  PGPU_CUDA(cudaEventCreate(&e0));
+  PGPU_CUDA(cudaEventCreate(&e1));
+  PGPU_CUDA(cudaEventRecord(e0, s));
+
+  // flat start: y = 1, k = 1; fs_old = 0 so the first change is 1
+  OuterScal init;
+  std::memset(&init, 0, sizeof(init));
+  init.k = 1.0;
+  PGPU_CUDA(cudaMemcpyAsync(dos, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+  k_fill<<<gN, kThreads, 0, s>>>(N, d.y.as<double>(), 1.0);
+  k_fill<<<gC, kThreads, 0, s>>>(n, d.fs_old.as<double>(), 0.0);
+  k_fission_total<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
+                                          d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d));
+  // the first total only normalises the start vector: keep k = 1
+  OuterScal os;
+  if ((st = read_outer(p, os))) return st;
+  if (os.nonfinite || os.S <= 0.0) return fail(PGPU_ERR_INVALID, "no fission source in the initial flux");
+  os.k = 1.0;
+  PGPU_CUDA(cudaMemcpyAsync(dos, &os, sizeof(os), cudaMemcpyHostToDevice, s));
+  k_normalize_source<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.chi.as<double>(), d.y.as<double>(),
+                                             d.x.as<double>(), d.fs.as<double>(), d.fs_old.as<double>(),
+                                             d.b.as<double>(), dos, slots_of<2>(d));
+  PGPU_CUDA(cudaGetLastError());
+
+  int outer = 0, inner_total = 0;
+  double change = 1.0, dk = 1.0, k_prev = 1.0;
+  bool converged = false;
+  int status = PGPU_OK;
+  for (outer = 1; outer <= opt->max_outer; outer++) {
+    // inner solve R y = b by refinement: r = b - R y, correction solve, y += d
+    const double tol_in = fmin(1e-3, fmax(1e-13, 0.02 * fmin(change, dk * 1e3)));
+    for (int ref = 0; ref < 50; ref++) {
+      k_residual<float><<<gN, kThreads, 0, s>>>(A, d.b.as<double>(), d.y.as<double>(), d.r64.as<double>(),
+                                                mixed ? d.r32.as<float>() : (float*)nullptr, dos, slots_of<2>(d));
+      if ((st = read_outer(p, os))) return st;
+      if (!(os.rr == os.rr)) return fail(PGPU_ERR_NAN, "NaN in the residual");
+      const double rel = os.bb > 0 ? sqrt(os.rr / os.bb) : 0.0;
+      if (rel <= tol_in) break;
+      int it = 0;
+      if (mixed) {
+        // FP32 correction solve on the FP32 copy of the FP64 residual
+        DiffOp<float> A32 = op32(d);
+        const double rt = fmax(tol_in / rel, 2e-5);
+        if ((st = bicgstab<float>(p, A32, d.w32, d.r32.as<float>(), fmin(rt, 0.5), opt->max_inner, &it))) return st;
+        k_axpy_update<float><<<gN, kThreads, 0, s>>>(N, d.y.as<double>(), d.w32[0].as<float>());
+      } else {
+        const double rt = fmax(0.5 * tol_in / rel, 1e-15);
+        if ((st = bicgstab<double>(p, A, d.w64, d.r64.as<double>(), fmin(rt, 0.5), opt->max_inner, &it))) return st;
+        k_axpy_update<double><<<gN, kThreads, 0, s>>>(N, d.y.as<double>(), d.w64[0].as<double>());
+      }
+      inner_total += it;
+      if (it == 0) break;
+    }
+    k_fission_total<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
+                                            d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d));
+    k_normalize_source<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.chi.as<double>(), d.y.as<double>(),
+                                               d.x.as<double>(), d.fs.as<double>(), d.fs_old.as<double>(),
+                                               d.b.as<double>(), dos, slots_of<2>(d));
+    PGPU_CUDA(cudaGetLastError());
+    if ((st = read_outer(p, os))) return st;
+    if (os.nonfinite || !(os.k == os.k)) return fail(PGPU_ERR_NAN, "non-finite fission source");
+    change = os.change;
+    dk = fabs(os.k - k_prev);
+    k_prev = os.k;
+    if (opt->verbose)
+      std::printf("pgpu diffusion outer %d: k = %.12f  dk = %.3e  source change = %.3e  inner = %d\n",
+                  outer, os.k, dk, change, inner_total);
+    // y keeps the unnormalised iterate; restart the next inner solve from x
+    PGPU_CUDA(cudaMemcpyAsync(d.y.ptr, d.x.ptr, (size_t)N * 8, cudaMemcpyDeviceToDevice, s));
+    if (dk < opt->tol_k && change < opt->tol_flux) {
+      converged = true;
+      break;
+    }
+  }
+  if (!converged) status = PGPU_ERR_NOT_CONVERGED;
+
+  // normalisation and power (NeutronicSolver.cxx:46-116)
+  k_power_norm<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol64.as<double>(), d.ksf.as<double>(),
+                                       d.x.as<double>(), dos, slots_of<1>(d));
+  k_power_fields<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol64.as<double>(), d.ksf.as<double>(),
+                                         d.nsf.as<double>(), d.x.as<double>(), opt->power, d.phi.as<double>(),
+                                         d.q.as<double>(), d.P.as<double>(), dos, slots_of<2>(d));
+  PGPU_CUDA(cudaGetLastError());
+  PGPU_CUDA(cudaEventRecord(e1, s));
+  if ((st = read_outer(p, os))) return st;
+  float ms = 0.f;
+  PGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  stats->keff = os.k;
+  stats->outer_iterations = outer > opt->max_outer ? opt->max_outer : outer;
+  stats->inner_iterations = inner_total;
+  stats->residual = change;
+  stats->seconds = ms * 1e-3;
+  p->keff = os.k;
+  if (status != PGPU_OK) return fail(status, "power iteration reached max_outer without converging");
+  if (os.negatives > 0) return fail(PGPU_ERR_NEGATIVE_FLUX, "negative values in the scalar-flux solution");
+  return PGPU_OK;
+}
+
+int diffusion_get_flux(pgpu_problem* p, double* phi) {
+  DiffusionData& d = *p->diff;
+  PGPU_CUDA(cudaMemcpyAsync(phi, d.phi.ptr, (size_t)d.n * d.G * 8, cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  return PGPU_OK;
+}
+
+int diffusion_get_power(pgpu_problem* p, double* q, double* P, double* total) {
+  DiffusionData& d = *p->diff;
+  if (q) PGPU_CUDA(cudaMemcpyAsync(q, d.q.ptr, (size_t)d.n * 8, cudaMemcpyDeviceToHost, p->stream));
+  if (P) PGPU_CUDA(cudaMemcpyAsync(P, d.P.ptr, (size_t)d.n * 8, cudaMemcpyDeviceToHost, p->stream));
+  OuterScal os;
+  PGPU_CUDA(cudaMemcpyAsync(&os, d.oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  if (total) *total = os.total_power;
+  return PGPU_OK;
+}
+
+void diffusion_destroy(pgpu_problem* p) {
+  delete p->diff;
+  p->diff = nullptr;
+}
+
+}  // namespace pgpu
+
+extern "C" {
+
+int pgpu_diffusion_create(int device, const pgpu_diffusion_operator* op, pgpu_problem** out) {
+  using namespace pgpu;
+  if (!op || !out) return fail(PGPU_ERR_INVALID, "null argument");
+  *out = nullptr;
+  const int n = op->num_cells, G = op->num_groups, F = op->num_faces, nm = op->num_materials;
+  if (n < 1 || G < 1 || F < 0 || nm < 1) return fail(PGPU_ERR_INVALID, "bad operator sizes");
+  if (G > kMaxGroups) return fail(PGPU_ERR_INVALID, "more than 16 energy groups");
+  if ((long long)n * G >= (1LL << 31)) return fail(PGPU_ERR_INVALID, "operator too large for 32-bit rows");
+  for (int i = 0; i < n; i++)
+    if (op->materials[i] < 0 || op->materials[i] >= nm) return fail(PGPU_ERR_INVALID, "material index out of range");
+  for (long long k = 0; k < (long long)F * n; k++)
+    if (op->neighbors[k] >= n) return fail(PGPU_ERR_INVALID, "neighbour index out of range");
+  PGPU_CUDA(cudaSetDevice(device));
+  pgpu_problem* p = new pgpu_problem();
+  p->kind = 1;
+  p->device = device;
+  p->num_cells = n;
+  p->num_groups = G;
+  p->diff = new DiffusionData();
+  DiffusionData& d = *p->diff;
+  d.n = n;
+  d.G = G;
+  d.F = F;
+  d.nm = nm;
+  const size_t nG = (size_t)n * G;
+  int st = PGPU_OK;
+  auto up = [&](DevBuf& b, const void* h, size_t bytes) {
+    if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes);
+  };
+  auto al = [&](DevBuf& b, size_t bytes) {
+    if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes);
+  };
+  if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "stream");
+  up(d.nbr, op->neighbors, (size_t)F * n * 4);
+  up(d.mat, op->materials, (size_t)n * 4);
+  up(d.off64, op->offdiag, (size_t)F * nG * 8);
+  up(d.diag64, op->diag, nG * 8);
+  up(d.vol64, op->volumes, (size_t)n * 8);
+  up(d.ss64, op->sigma_s, (size_t)nm * G * G * 8);
+  up(d.chi, op->chi, (size_t)nm * G * 8);
+  up(d.nsf, op->nu_sigma_f, (size_t)nm * G * 8);
+  up(d.ksf, op->kappa_sigma_f, (size_t)nm * G * 8);
+  al(d.x, nG * 8);
+  al(d.y, nG * 8);
+  al(d.b, nG * 8);
+  al(d.r64, nG * 8);
+  al(d.phi, nG * 8);
+  al(d.fs, (size_t)n * 8);
+  al(d.fs_old, (size_t)n * 8);
+  al(d.q, (size_t)n * 8);
+  al(d.P, (size_t)n * 8);
+  for (int k = 0; k < 9; k++) al(d.w64[k], nG * 8);
+  al(d.partials, (size_t)4 * kMaxBlocks * 8);
+  al(d.ticket, 64);
+  al(d.bscal, sizeof(BiScal));
+  al(d.oscal, sizeof(OuterScal));
+  if (st == PGPU_OK && cudaMemset(d.ticket.ptr, 0, 64) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "memset");
+  if (st != PGPU_OK) {
+    std::string msg = pgpu_last_error();
+    pgpu_problem_destroy(p);
+    return fail(st, msg);
+  }
+  *out = p;
+  return PGPU_OK;
+}
+
+int pgpu_diffusion_apply(pgpu_problem* p, const double* x, double* y) {
+  using namespace pgpu;
+  if (!p || p->kind != 1) return fail(PGPU_ERR_INVALID, "not a diffusion problem");
+  PGPU_CUDA(cudaSetDevice(p->device));
+  DiffusionData& d = *p->diff;
+  const size_t N = (size_t)d.n * d.G;
+  PGPU_CUDA(cudaMemcpyAsync(d.x.ptr, x, N * 8, cudaMemcpyHostToDevice, p->stream));
+  k_apply<<<grid_for(N), kThreads, 0, p->stream>>>(op64(d), d.x.as<double>(), d.y.as<double>());
+  PGPU_CUDA(cudaGetLastError());
+  PGPU_CUDA(cudaMemcpyAsync(y, d.y.ptr, N * 8, cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  return PGPU_OK;
+}
+
+}  // extern "C"

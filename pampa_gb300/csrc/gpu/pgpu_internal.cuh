@@ -1,0 +1,181 @@
+// Internals shared by the pgpu_* translation units: error state, device buffers,
+// deterministic block reductions and the problem handle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "pampa_gb300.h"
+
+namespace pgpu {
+
+// ---------------------------------------------------------------------------------
+// Errors: a thread-local message plus a PGPU_* code.
+// ---------------------------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+
+#define PGPU_CUDA(call)                                                                 \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return ::pgpu::fail(PGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + \
+                                             " (" __FILE__ ":" + std::to_string(__LINE__) + ")"); \
+  } while (0)
+
+#define PGPU_CHECK(cond, code, msg)                                                     \
+  do {                                                                                  \
+    if (cond) return ::pgpu::fail(code, msg);                                           \
+  } while (0)
+
+// ---------------------------------------------------------------------------------
+// Device buffer (RAII).  Allocations are counted per problem.
+// ---------------------------------------------------------------------------------
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T* as() const { return static_cast<T*>(ptr); }
+};
+
+int dev_alloc(DevBuf& b, size_t bytes, long long* counter);
+int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter);
+
+// ---------------------------------------------------------------------------------
+// Launch geometry.  152 SMs on GB300; grids are capped at a multiple of the SM count
+// and loop grid-stride, so partial-sum arrays have a fixed, small size.
+// ---------------------------------------------------------------------------------
+constexpr int kThreads = 256;
+constexpr int kMaxBlocks = 152 * 8;
+constexpr int kMaxGroups = 16;  // groups per cell handled in registers
+
+inline int grid_for(long long work, int threads = kThreads) {
+  long long b = (work + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > kMaxBlocks) b = kMaxBlocks;
+  return (int)b;
+}
+
+// ---------------------------------------------------------------------------------
+// Deterministic multi-value block reduction.  Each block writes NV partial sums; the
+// last block to finish (ticket counter) adds the partials in block order and calls
+// `finish` with the totals.  The order of additions depends only on the grid size, so
+// results are bitwise reproducible from run to run.
+// ---------------------------------------------------------------------------------
+template <int NV>
+struct ReduceSlots {
+  double* partials;       // [NV][kMaxBlocks]
+  unsigned int* ticket;   // one counter
+};
+
+template <int NV>
+__device__ inline void warp_sum(double (&v)[NV]) {
+#pragma unroll
+  for (int k = 0; k < NV; k++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+}
+
+// Returns true in every thread of the last block, with `tot` filled in thread 0..NV-1's
+// view (all threads see the same totals through shared memory).
+template <int NV>
+__device__ inline bool block_reduce_last(double (&v)[NV], ReduceSlots<NV> slots, double (&tot)[NV]) {
+  __shared__ double sh[NV][32];
+  __shared__ bool last;
+  warp_sum<NV>(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; k++) sh[k][warp] = v[k];
+  __syncthreads();
+  if (warp == 0) {
+    double w[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) w[k] = lane < nw ? sh[k][lane] : 0.0;
+    warp_sum<NV>(w);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < NV; k++) slots.partials[k * kMaxBlocks + blockIdx.x] = w[k];
+      __threadfence();
+      unsigned int t = atomicAdd(slots.ticket, 1u);
+      last = (t == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  // last block: fixed-order sum of the partials
+  double acc[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) acc[k] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; k++) acc[k] += ((volatile double*)slots.partials)[k * kMaxBlocks + b];
+  warp_sum<NV>(acc);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; k++) sh[k][warp] = acc[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double s = 0.0;
+      for (int w2 = 0; w2 < nw; w2++) s += sh[k][w2];
+      sh[k][0] = s;
+    }
+    *slots.ticket = 0u;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; k++) tot[k] = sh[k][0];
+  return true;
+}
+
+// ---------------------------------------------------------------------------------
+// Problem handle.
+// ---------------------------------------------------------------------------------
+struct DiffusionData;
+struct SNData;
+
+}  // namespace pgpu
+
+struct pgpu_problem {
+  int kind = 0;  // 1 diffusion, 2 SN
+  int device = 0;
+  int num_cells = 0, num_groups = 0, num_dirs = 0;
+  long long bytes = 0;
+  cudaStream_t stream = nullptr;
+  bool solved = false;
+  double keff = 0.0;
+  pgpu::DiffusionData* diff = nullptr;
+  pgpu::SNData* sn = nullptr;
+};
+
+namespace pgpu {
+
+// Per-kind entry points implemented in pgpu_diffusion.cu / pgpu_sn.cu.
+int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats);
+int diffusion_get_flux(pgpu_problem* p, double* phi);
+int diffusion_get_power(pgpu_problem* p, double* q, double* P, double* total);
+void diffusion_destroy(pgpu_problem* p);
+
+int sn_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats);
+int sn_get_flux(pgpu_problem* p, double* phi);
+int sn_get_angular(pgpu_problem* p, double* psi);
+int sn_get_power(pgpu_problem* p, double* q, double* P, double* total);
+void sn_destroy(pgpu_problem* p);
+
+}  // namespace pgpu

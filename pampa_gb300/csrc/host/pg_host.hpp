@@ -1,0 +1,225 @@
+// Host-side model of pampa's steady-state neutronics path: input tokens, materials,
+// meshes and the solver classes behind the drop-in C API.  Everything here is plain
+// C++17; the arithmetic of the solve lives in the CUDA kernels behind pgpu_*.
+#pragma once
+
+#include <cstdio>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "pampa_gb300.h"
+
+namespace pg {
+
+// Error convention of the reference (utils.hxx:41-47): print "file:line:func(): error:
+// message." and return 1.
+#define PG_CHECK(cond, msg)                                                              \
+  do {                                                                                   \
+    if (cond) {                                                                          \
+      std::printf("%s:%d:%s(): error: %s.\n", __FILE__, __LINE__, __func__,             \
+                  std::string(msg).c_str());                                             \
+      std::fflush(stdout);                                                               \
+      return 1;                                                                          \
+    }                                                                                    \
+  } while (0)
+
+#define PG_TRY(call, msg) PG_CHECK((call) != 0, msg)
+
+// ----------------------------------------------------------------------------------
+// Tokens: line reader with the semantics of input::get_next_line (input.cxx:4-62).
+// ----------------------------------------------------------------------------------
+class Tokens {
+ public:
+  int open(const std::string& path);
+  std::vector<std::string> next();
+  int read_doubles(std::vector<double>& v, size_t n, double lo, double hi);
+  int read_ints(std::vector<int>& v, size_t n, int lo, int hi);
+  const std::string& path() const { return path_; }
+
+ private:
+  std::string path_;
+  std::vector<std::string> lines_;
+  size_t pos_ = 0;
+};
+
+int to_int(const std::string& s, int lo, int hi, int& out);
+int to_double(const std::string& s, double lo, double hi, double& out);
+int to_bool(const std::string& s, bool& out);
+std::string resolve_path(const std::string& path, const std::string& base_dir);
+
+// ----------------------------------------------------------------------------------
+// Boundary conditions (utils.hxx:96-117).
+// ----------------------------------------------------------------------------------
+enum BCType { BC_NONE = 0, BC_VACUUM, BC_REFLECTIVE, BC_ROBIN, BC_DIRICHLET, BC_ADIABATIC,
+              BC_CONVECTION };
+
+struct BoundaryCondition {
+  BCType type = BC_NONE;
+  std::vector<double> values;  // steady state: value of each function at t = 0
+};
+
+int read_bc(const std::vector<std::string>& line, size_t i, Tokens& tok, BoundaryCondition& bc);
+
+// ----------------------------------------------------------------------------------
+// Materials with constant nuclear data (Material.cxx, ConstantNuclearData.cxx).
+// ----------------------------------------------------------------------------------
+struct Material {
+  std::string name;
+  bool bc = false, split = false, fuel = false, has_nd = false;
+  int num_groups = -1;
+  double beta_total = 0.0;
+  int num_sub = 0;
+  std::vector<double> sigma_t, nu_sigma_f, kappa_sigma_f, sigma_tr, diffusion, chi_prompt,
+      chi_delayed, chi, velocity;
+  std::vector<double> sigma_s;  // [from][to]
+
+  int read(Tokens& tok);
+  int read_file(const std::string& path);
+  int check_for_solver(int G, bool diffusion) const;
+
+ private:
+  int read_nuclear_data(Tokens& tok);
+  int finish_nuclear_data();
+};
+
+// ----------------------------------------------------------------------------------
+// Mesh: cells and padded per-face arrays (row-major cell x face).
+// ----------------------------------------------------------------------------------
+constexpr int NO_FACE = -2147483647;
+
+struct Mesh {
+  int num_dims = 0;
+  int num_cells = 0;
+  int fmax = 0;
+  std::vector<double> volumes;    // n
+  std::vector<double> centroids;  // n*3
+  std::vector<int> materials;     // n
+  std::vector<int> num_faces;     // n
+  std::vector<double> areas;      // n*fmax
+  std::vector<double> fcent;      // n*fmax*3
+  std::vector<double> normals;    // n*fmax*3
+  std::vector<int> neighbors;     // n*fmax: >= 0 cell, < 0 -(boundary+1), NO_FACE pad
+  std::vector<std::string> boundaries;
+  std::map<int, BoundaryCondition> bcs;  // 1-based boundary index
+  bool has_bcs = false;
+
+  int nbr(int i, int f) const { return neighbors[(size_t)i * fmax + f]; }
+  double area(int i, int f) const { return areas[(size_t)i * fmax + f]; }
+  const double* fc(int i, int f) const { return &fcent[((size_t)i * fmax + f) * 3]; }
+  const double* nrm(int i, int f) const { return &normals[((size_t)i * fmax + f) * 3]; }
+  const double* cc(int i) const { return &centroids[(size_t)i * 3]; }
+  void allocate(int n, int F);
+};
+
+int read_cartesian_mesh(const std::string& path, Mesh& mesh);
+int read_unstructured_mesh(const std::string& path, Mesh& mesh);
+int split_materials(Mesh& mesh, std::vector<Material>& materials);
+int remove_bc_materials(const Mesh& in, const std::vector<Material>& materials, Mesh& out);
+
+// ----------------------------------------------------------------------------------
+// Solvers (Solver.hxx:31-98, PhysicsSolver.hxx, NeutronicSolver.hxx).
+// ----------------------------------------------------------------------------------
+struct Field {
+  std::string name;
+  std::vector<double>* vec = nullptr;
+  bool input = false, output = false;
+};
+
+struct RunOptions {
+  pgpu_options gpu;
+  int device = 0;
+  bool verbose = false, silent = false;
+};
+
+class Solver {
+ public:
+  explicit Solver(std::string name) : name_(std::move(name)) {}
+  virtual ~Solver() = default;
+  virtual int read(Tokens& tok, const Mesh& mesh) = 0;
+  virtual int initialize(const Mesh& mesh, const std::vector<Material>& mats,
+                         const RunOptions& opt, bool transient) = 0;
+  virtual int solve(int n, double dt, double t) = 0;
+  virtual int output(int n) const = 0;
+  virtual int finalize() = 0;
+  int getField(double* v, const std::string& name) const;
+  int setField(const double* v, const std::string& name);
+  int fieldSize(const std::string& name, int& size) const;
+  const std::string& name() const { return name_; }
+
+ protected:
+  std::string name_;
+  std::vector<Field> fields_;
+};
+
+class NeutronicSolver : public Solver {
+ public:
+  using Solver::Solver;
+  ~NeutronicSolver() override;
+  int initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
+                 bool transient) override;
+  int solve(int n, double dt, double t) override;
+  int output(int n) const override;
+  int finalize() override;
+  double keff() const { return keff_; }
+  const pgpu_stats& stats() const { return stats_; }
+
+ protected:
+  int readCommon(const std::vector<std::string>& line, Tokens& tok, const Mesh& mesh, bool& used);
+  virtual int buildProblem() = 0;   // assemble and upload the operator
+  virtual int fetchSolution() = 0;  // copy fluxes back after a solve
+  const std::map<int, BoundaryCondition>& boundaryConditions() const;
+
+  const Mesh* mesh_ = nullptr;
+  const std::vector<Material>* mats_ = nullptr;
+  RunOptions opt_;
+  int G_ = -1;
+  double power_ = 1.0;
+  std::map<int, BoundaryCondition> bcs_;
+  bool has_bcs_ = false;
+  double keff_ = -1.0;
+  double total_power_ = 0.0;
+  std::vector<double> T_, S_, phi_, q_, P_;
+  pgpu_problem* problem_ = nullptr;
+  pgpu_stats stats_{};
+};
+
+class DiffusionSolver : public NeutronicSolver {
+ public:
+  DiffusionSolver() : NeutronicSolver("diffusion") {}
+  int read(Tokens& tok, const Mesh& mesh) override;
+
+ protected:
+  int buildProblem() override;
+  int fetchSolution() override;
+};
+
+class SNSolver : public NeutronicSolver {
+ public:
+  SNSolver() : NeutronicSolver("sn") {}
+  int read(Tokens& tok, const Mesh& mesh) override;
+  int initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
+                 bool transient) override;
+
+ protected:
+  int buildProblem() override;
+  int fetchSolution() override;
+  int order_ = -1;
+  double delta_ = 0.1;  // SNSolver.hxx:16
+  bool ls_ = false;
+  int M_ = 0;
+  std::vector<double> psi_;
+};
+
+// Quadrature of AngularQuadratureSet::build (AngularQuadratureSet.cxx:4-209).
+int build_quadrature(int order, std::vector<double>& dirs, std::vector<double>& weights,
+                     std::vector<int>& reflected);
+
+// Host assembly into the GPU operator layouts (exposed for tests through the C API).
+int assemble_diffusion(const Mesh& mesh, const std::vector<Material>& mats, int G,
+                       const std::map<int, BoundaryCondition>& bcs,
+                       std::vector<int>& neighbors, std::vector<double>& offdiag,
+                       std::vector<double>& diag);
+
+}  // namespace pg

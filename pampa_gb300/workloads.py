@@ -1,0 +1,186 @@
+"""Seeded synthetic k-eigenvalue workloads, written as reference-format ``.pmp`` inputs.
+
+Each generator writes ``input.pmp``, ``mesh.pmp`` and ``mat<k>.pmp`` files into a
+directory so the reference parser, the oracle and this library read identical inputs.
+Cross sections are macroscopic (1/cm); the total cross section is written as
+sigma_t = sigma_a + sum of out-scatter (the reference reads sigma_t directly).
+
+Workloads (sizes are the defaults; every generator takes smaller sizes for tests):
+
+* ``diffusion_2d``  -- 2-group diffusion on a 2D Cartesian 34x34 mesh of 5 cm cells,
+  17x17 blocks of 2x2 cells, 4 materials (one non-fissile reflector), vacuum on +x/+y,
+  reflective on -x/-y.
+* ``sn_3d``         -- 2-group S8 discrete ordinates on a 3D Cartesian 64x64x32 mesh of
+  2 cm cells with within-group scattering, pure upwind (mixed-face-interpolation 1.0),
+  no LS boundary correction, vacuum on +x/+y/+z, reflective on -x/-y/-z.
+* ``diffusion_3d_7g`` -- 7-group diffusion on a 3D Cartesian 256x256x128 mesh of 2 cm
+  cells, 6 materials in 8x8x8-cell blocks, down-scatter g->g+1, g->g+2 and up-scatter
+  g->g-1 for the three thermal groups, lognormal entries, chi on groups 1-3.
+"""
+
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+
+# cross-section ranges of the 2-group family (1/cm; D in cm)
+RANGES_2G = dict(D1=(1.2, 1.5), D2=(0.3, 0.4), sa1=(0.008, 0.012), sa2=(0.05, 0.09),
+                 nsf1=(0.0, 0.006), nsf2=(0.0, 0.14), s12=(0.015, 0.025))
+
+
+def _u(rng, lo_hi):
+    lo, hi = lo_hi
+    return float(rng.uniform(lo, hi))
+
+
+def materials_2g(rng, num: int, self_scatter: tuple | None = None, reflector_last: bool = True):
+    """`num` 2-group materials; the last one is a non-fissile reflector."""
+    mats = []
+    for m in range(num):
+        D = [_u(rng, RANGES_2G["D1"]), _u(rng, RANGES_2G["D2"])]
+        sa = [_u(rng, RANGES_2G["sa1"]), _u(rng, RANGES_2G["sa2"])]
+        nsf = [_u(rng, RANGES_2G["nsf1"]), _u(rng, RANGES_2G["nsf2"])]
+        if reflector_last and m == num - 1:
+            nsf = [0.0, 0.0]
+        ss = np.zeros((2, 2))
+        ss[0, 1] = _u(rng, RANGES_2G["s12"])
+        if self_scatter is not None:
+            ss[0, 0] = _u(rng, self_scatter)
+            ss[1, 1] = _u(rng, self_scatter)
+        mats.append(dict(G=2, D=D, sa=sa, nsf=nsf, ss=ss, chi=[1.0, 0.0]))
+    return mats
+
+
+def materials_multigroup(rng, num: int, G: int = 7):
+    """`num` G-group materials for the 7-group family (one non-fissile)."""
+    mats = []
+    t = np.linspace(0.0, 1.0, G)
+    for m in range(num):
+        jitter = rng.uniform(0.9, 1.1, size=G)
+        D = np.exp(np.log(1.35) * (1 - t) + np.log(0.35) * t) * jitter
+        sa = np.exp(np.log(0.010) * (1 - t) + np.log(0.070) * t) * rng.uniform(0.8, 1.2, size=G)
+        nsf = np.exp(np.log(0.003) * (1 - t) + np.log(0.12) * t) * rng.uniform(0.8, 1.2, size=G)
+        if m == num - 1:
+            nsf[:] = 0.0
+        ss = np.zeros((G, G))
+        for g in range(G):
+            for g2, on in ((g + 1, True), (g + 2, True), (g - 1, g >= G - 3)):
+                if on and 0 <= g2 < G:
+                    med = math.exp(rng.uniform(math.log(1e-3), math.log(5e-2)))
+                    ss[g, g2] = med * math.exp(rng.normal(0.0, 0.5))
+        chi = np.zeros(G)
+        chi[:3] = [0.6, 0.3, 0.1]
+        mats.append(dict(G=G, D=list(D), sa=list(sa), nsf=list(nsf), ss=ss, chi=list(chi)))
+    return mats
+
+
+def _fmt(vals) -> str:
+    return " ".join(f"{v:.10g}" for v in vals)
+
+
+def write_material(path: str, mat: dict, diffusion: bool = True):
+    G = mat["G"]
+    ss = np.asarray(mat["ss"])
+    st = [mat["sa"][g] + ss[g].sum() for g in range(G)]
+    lines = ["nuclear-data {", f"   energy-groups {G}", "   sigma-total", "   " + _fmt(st)]
+    if any(v > 0 for v in mat["nsf"]):
+        lines += ["   nu-sigma-fission", "   " + _fmt(mat["nsf"]), "   fission-spectrum",
+                  "   " + _fmt(mat["chi"])]
+    lines += ["   sigma-scattering"] + ["   " + _fmt(ss[g]) for g in range(G)]
+    if diffusion:
+        lines += ["   diffusion-coefficient", "   " + _fmt(mat["D"])]
+    lines += ["}"]
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+
+
+def write_cartesian_mesh(path: str, d: float, nx: int, ny: int, nz: int, layout: np.ndarray,
+                         bcs: dict[str, str]):
+    """layout: (nz, ny, nx) 1-based material indices (0 = void)."""
+    lines = [f"dx -{nx}", f"{d:.6f}", f"dy -{ny}", f"{d:.6f}"]
+    if nz > 0:
+        lines += [f"dz -{nz}", f"{d:.6f}"]
+    lines.append("")
+    for b, t in bcs.items():
+        lines.append(f"bc {b} {t}")
+    lines.append("")
+    ncell = layout.size
+    lines.append(f"materials {ncell}")
+    flat = layout.reshape(-1, nx)
+    for row in flat:
+        lines.append(" ".join(str(int(v)) for v in row))
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+
+
+def _block_layout(rng, shape, block, num_materials) -> np.ndarray:
+    nb = [int(math.ceil(s / b)) for s, b in zip(shape, block)]
+    blocks = rng.integers(1, num_materials + 1, size=nb)
+    lay = blocks
+    for ax, b in enumerate(block):
+        lay = np.repeat(lay, b, axis=ax)
+    return lay[tuple(slice(0, s) for s in shape)]
+
+
+def diffusion_2d(out_dir: str, n: int = 34, cell: float = 5.0, seed: int = 1) -> str:
+    """2-group 2D diffusion (34x34 of 5 cm cells by default)."""
+    os.makedirs(out_dir, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    mats = materials_2g(rng, 4)
+    layout = _block_layout(rng, (1, n, n), (1, 2, 2), 4)
+    write_cartesian_mesh(os.path.join(out_dir, "mesh.pmp"), cell, n, n, 0, layout,
+                         {"-x": "reflective", "+x": "vacuum", "-y": "reflective", "+y": "vacuum"})
+    for k, m in enumerate(mats):
+        write_material(os.path.join(out_dir, f"mat{k + 1}.pmp"), m)
+    lines = ["mesh cartesian mesh.pmp", ""]
+    lines += [f"material mat{k + 1} mat{k + 1}.pmp" for k in range(len(mats))]
+    lines += ["", "solver diffusion {", "   energy-groups 2", "}"]
+    path = os.path.join(out_dir, "input.pmp")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return path
+
+
+def sn_3d(out_dir: str, nx: int = 64, ny: int = 64, nz: int = 32, cell: float = 2.0, order: int = 8,
+          seed: int = 2, block: int = 4) -> str:
+    """2-group S_N on a 3D Cartesian mesh (64x64x32 of 2 cm cells, S8 by default)."""
+    os.makedirs(out_dir, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    mats = materials_2g(rng, 4, self_scatter=(0.2, 0.5))
+    layout = _block_layout(rng, (nz, ny, nx), (block, block, block), 4)
+    write_cartesian_mesh(os.path.join(out_dir, "mesh.pmp"), cell, nx, ny, nz, layout,
+                         {"-x": "reflective", "+x": "vacuum", "-y": "reflective", "+y": "vacuum",
+                          "-z": "reflective", "+z": "vacuum"})
+    for k, m in enumerate(mats):
+        write_material(os.path.join(out_dir, f"mat{k + 1}.pmp"), m, diffusion=False)
+    lines = ["mesh cartesian mesh.pmp", ""]
+    lines += [f"material mat{k + 1} mat{k + 1}.pmp" for k in range(len(mats))]
+    lines += ["", "solver sn {", "   energy-groups 2", f"   order {order}",
+              "   mixed-face-interpolation 1.0", "   least-squares-boundary-interpolation 0", "}"]
+    path = os.path.join(out_dir, "input.pmp")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return path
+
+
+def diffusion_3d_7g(out_dir: str, nx: int = 256, ny: int = 256, nz: int = 128, cell: float = 2.0,
+                    seed: int = 3, block: int = 8, G: int = 7) -> str:
+    """7-group 3D diffusion (256x256x128 of 2 cm cells by default)."""
+    os.makedirs(out_dir, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    mats = materials_multigroup(rng, 6, G)
+    layout = _block_layout(rng, (nz, ny, nx), (block, block, block), 6)
+    write_cartesian_mesh(os.path.join(out_dir, "mesh.pmp"), cell, nx, ny, nz, layout,
+                         {"-x": "reflective", "+x": "vacuum", "-y": "reflective", "+y": "vacuum",
+                          "-z": "reflective", "+z": "vacuum"})
+    for k, m in enumerate(mats):
+        write_material(os.path.join(out_dir, f"mat{k + 1}.pmp"), m)
+    lines = ["mesh cartesian mesh.pmp", ""]
+    lines += [f"material mat{k + 1} mat{k + 1}.pmp" for k in range(len(mats))]
+    lines += ["", "solver diffusion {", f"   energy-groups {G}", "}"]
+    path = os.path.join(out_dir, "input.pmp")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return path

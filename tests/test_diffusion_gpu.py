@@ -1,0 +1,94 @@
+"""GPU parity of the diffusion k-eigenvalue path against the CPU oracle.
+
+Bars: |k_gpu - k_oracle| <= 1e-6 and relative L2 of the normalised scalar flux <= 1e-5
+for the FP64 path; the mixed-precision path must stay within 1 pcm (1e-5) in k and 1e-4
+in flux.  Every test calls through the C-ABI of libpampa_gb300.so.
+"""
+import numpy as np
+import pytest
+
+import pampa_gb300 as pg
+from conftest import known_answers
+from helpers import diffusion_operator_from_oracle, rel_l2
+from oracle import pampa_oracle as po
+
+pytestmark = pytest.mark.gpu
+
+K_TOL = 1e-6
+FLUX_TOL = 1e-5
+
+CASES = ["slabs/reflected-diffusion", "pwr-iaea-benchmark/cartesian-diffusion",
+         "pwr-iaea-benchmark/unstructured-diffusion", "pwr-iaea-benchmark/cartesian-diffusion-3d",
+         "pwr-iaea-benchmark/unstructured-diffusion-3d"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_dropin_diffusion_known_answers(case, case_input):
+    path = case_input(case)
+    ref = po.run_input(path)
+    with pg.Pampa(path, "-silent") as p:
+        p.solve()
+        k = p.keff
+        phi = p.field("scalar-flux")
+        q = p.field("power")
+        P = p.field("production-rate")
+    assert abs(k - ref["keff"]) <= K_TOL, (k, ref["keff"])
+    assert round(k, 6) == pytest.approx(known_answers()[case], abs=1e-12)
+    assert rel_l2(phi, ref["phi"]) <= FLUX_TOL
+    assert rel_l2(q, ref["q"]) <= FLUX_TOL
+    assert rel_l2(P, ref["P"]) <= FLUX_TOL
+    assert q.sum() == pytest.approx(1.0, rel=1e-12)
+
+
+def test_operator_apply_matches_oracle_matrix(case_input):
+    prob = po.read_problem(case_input("pwr-iaea-benchmark/unstructured-diffusion"))
+    R, F = po.assemble_diffusion(prob)
+    with pg.DiffusionProblem(**diffusion_operator_from_oracle(prob, R)) as dp:
+        rng = np.random.default_rng(0)
+        for _ in range(3):
+            x = rng.standard_normal(R.shape[0])
+            y = dp.apply(x)
+            assert rel_l2(y, R @ x) <= 1e-14
+
+
+def test_synthetic_diffusion_2d(tmp_path):
+    from pampa_gb300 import workloads as wl
+    path = wl.diffusion_2d(str(tmp_path))
+    ref = po.run_input(path)
+    with pg.Pampa(path, "-silent") as p:
+        p.solve()
+        assert abs(p.keff - ref["keff"]) <= K_TOL
+        assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= FLUX_TOL
+
+
+def test_mixed_precision_within_one_pcm(case_input):
+    path = case_input("pwr-iaea-benchmark/cartesian-diffusion")
+    ref = po.run_input(path)
+    with pg.Pampa(path, "-silent", "-pgpu_precision", "mixed") as p:
+        p.solve()
+        assert abs(p.keff - ref["keff"]) <= 1e-5
+        assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= 1e-4
+
+
+def test_direct_api_deterministic_and_reusable(case_input):
+    prob = po.read_problem(case_input("pwr-iaea-benchmark/cartesian-diffusion"))
+    R, F = po.assemble_diffusion(prob)
+    with pg.DiffusionProblem(**diffusion_operator_from_oracle(prob, R)) as dp:
+        r1 = dp.solve()
+        phi1 = dp.scalar_flux()
+        r2 = dp.solve()
+        phi2 = dp.scalar_flux()
+        assert r1.keff == r2.keff
+        assert np.array_equal(phi1, phi2)
+        q, P, tot = dp.power()
+        assert tot == pytest.approx(1.0, rel=1e-12)
+
+
+def test_iteration_cap_reports_not_converged(case_input):
+    prob = po.read_problem(case_input("pwr-iaea-benchmark/cartesian-diffusion"))
+    R, F = po.assemble_diffusion(prob)
+    with pg.DiffusionProblem(**diffusion_operator_from_oracle(prob, R)) as dp:
+        with pytest.raises(pg.PampaError, match="not converg|max_outer"):
+            dp.solve(max_outer=1)
+        # the context stays usable after the error
+        assert dp.solve().keff > 0.9
