@@ -71,6 +71,13 @@ void pampa_get_field_size(const char name[], int* size, int* error);
 void pampa_get_solve_stats(int* outer_iterations, int* inner_iterations, double* seconds,
                            int* error);
 
+/* The device-resident problem behind the driver's solver, assembled and uploaded on first
+ * use (no counterpart in the reference).  It stays owned by the driver: do not destroy it.
+ * Lets callers reach the pgpu_* layer (e.g. pgpu_sn_apply) for an input read by the
+ * drop-in parser. */
+typedef struct pgpu_problem pgpu_problem;
+void pampa_get_problem(pgpu_problem** problem, int* error);
+
 /* ------------------------------------------------------------------------------
  * 2. GPU operator API
  * ---------------------------------------------------------------------------- */
@@ -87,7 +94,7 @@ enum {
 
 enum { PGPU_FP64 = 0, PGPU_MIXED = 1 };
 
-typedef struct pgpu_problem pgpu_problem;   /* opaque: operator + iterates on one GPU */
+/* pgpu_problem (declared above) is opaque: operator + iterates on one GPU. */
 
 typedef struct {
   int precision;        /* PGPU_FP64 (default) or PGPU_MIXED (FP32 inner, FP64 outer)  */

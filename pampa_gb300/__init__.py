@@ -82,6 +82,7 @@ SYMBOLS = {
     "pampa_get_keff": (None, [_pd, _pi]),
     "pampa_get_field_size": (None, [C.c_char_p, _pi, _pi]),
     "pampa_get_solve_stats": (None, [_pi, _pi, _pd, _pi]),
+    "pampa_get_problem": (None, [_P(C.c_void_p), _pi]),
     "pgpu_default_options": (None, [_P(pgpu_options)]),
     "pgpu_last_error": (C.c_char_p, []),
     "pgpu_diffusion_create": (C.c_int, [C.c_int, _P(pgpu_diffusion_operator), _P(C.c_void_p)]),
@@ -205,6 +206,27 @@ class Pampa:
         o, i, s, e = C.c_int(0), C.c_int(0), C.c_double(0), C.c_int(0)
         lib().pampa_get_solve_stats(C.byref(o), C.byref(i), C.byref(s), C.byref(e))
         return dict(outer_iterations=o.value, inner_iterations=i.value, seconds=s.value)
+
+    def apply_operator(self, x) -> np.ndarray:
+        """y = R x on the GPU for the operator the driver assembled from the input."""
+        h = C.c_void_p(None)
+        err = C.c_int(0)
+        lib().pampa_get_problem(C.byref(h), C.byref(err))
+        if err.value:
+            raise PampaError(f"pampa_get_problem failed: {last_error()}")
+        x = _f64(x)
+        y = np.zeros_like(x)
+        fn = lib().pgpu_sn_apply if self.field_size("angular-flux") else lib().pgpu_diffusion_apply
+        st = fn(h, _dp(x), _dp(y))
+        if st != PGPU_OK:
+            raise PampaError(f"operator apply failed: {last_error()}")
+        return y
+
+    def field_size(self, name: str) -> int:
+        size = C.c_int(0)
+        err = C.c_int(0)
+        lib().pampa_get_field_size(name.encode(), C.byref(size), C.byref(err))
+        return size.value if err.value == 0 else 0
 
     def finalize(self):
         if self._open:

@@ -1,16 +1,1207 @@
-// Discrete-ordinates k-eigenvalue solve on one GPU (placeholder until the sweep lands).
+// Discrete-ordinates (SN) k-eigenvalue solve on one GPU.
+//
+// Replaces the monolithic assembly + LU + Krylov-Schur of SNSolver (SNSolver.cxx:344-670,
+// petsc.cxx:175-204) with a matrix-free operator and transport sweeps.  The eigenpair is
+// that of the reference's operator R x = (1/k) F x:
+//   R[(i,g,m),(i,g,m)]  = sigma_t V + face terms          (SNSolver.cxx:397, 445-597)
+//   R[(i,g,m),(i,g2,m2)] -= sigma_s(g2->g) w_m2 V         (isotropic scattering, :417-431)
+//   F[(i,g,m),(i,g2,m2)]  = chi_g nu_sigma_f(g2) w_m2 V   (:434-439)
+// Face terms per face f with mu = Omega_m . n_f and area A:
+//   interior: R[l,l] += w_i mu A, R[l,(j,g,m)] += w_j mu A, (w_i, w_j) = Gauss weights by sign(mu)
+//   vacuum:   mu > 0: R[l,l] += mu A, plus the LS boundary correction when enabled
+//   reflective: mu > 0: R[l,l] += mu A; else R[l,(i,g,m')] += mu A, m' the reflected direction.
+//
+// Two solution paths:
+//  * scalar-flux space (pure upwind, no LS): with scattering and fission isotropic, the
+//    eigenproblem closes on phi0 = sum_m w_m psi plus the incoming angular flux at
+//    reflective faces.  One transport sweep inverts the streaming+collision part exactly,
+//    so the inner solves are GMRES on (I - T S) over n*G (+ boundary) unknowns, each
+//    iteration one sweep.  psi itself is rebuilt by one final sweep.
+//  * angular-flux space (general: any Gauss weight delta, LS correction): right-
+//    preconditioned GMRES on R psi = b with the matrix-free R and a sweep over the upwind
+//    part of R as preconditioner.
+// Sweeps follow per-direction upwind level sets built once at setup (Kahn's algorithm
+// over the face graph); directions whose faces see the same upwind pattern share one
+// schedule, so a Cartesian mesh has 8 (one per octant).  All schedules advance together,
+// one kernel launch per level.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
 #include "pgpu_internal.cuh"
 
 namespace pgpu {
-struct SNData {};
-int sn_solve(pgpu_problem*, const pgpu_options*, pgpu_stats*) { return fail(PGPU_ERR_INVALID, "SN not built"); }
-int sn_get_flux(pgpu_problem*, double*) { return fail(PGPU_ERR_INVALID, "SN not built"); }
-int sn_get_angular(pgpu_problem*, double*) { return fail(PGPU_ERR_INVALID, "SN not built"); }
-int sn_get_power(pgpu_problem*, double*, double*, double*) { return fail(PGPU_ERR_INVALID, "SN not built"); }
-void sn_destroy(pgpu_problem* p) { delete p->sn; p->sn = nullptr; }
+
+// ---------------------------------------------------------------------------------
+// Device-side operator description
+// ---------------------------------------------------------------------------------
+template <typename T>
+struct SNOp {
+  int n, G, M, F;
+  int use_ls;
+  const int* __restrict__ nf;        // [n]
+  const int* __restrict__ kind;      // [F][n]
+  const int* __restrict__ nbr;       // [F][n]
+  const T* __restrict__ area;        // [F][n]
+  const T* __restrict__ nrm;         // [F][n][3]
+  const T* __restrict__ gauss;       // [F][n][4]
+  const int* __restrict__ raxis;     // [F][n]
+  const int* __restrict__ rslot;     // [F][n] reflective-face slot or -1
+  const T* __restrict__ lsw;         // [F][n][F] or null
+  const T* __restrict__ lsdiag;      // [F][n] sum of LS weights over physical neighbours
+  const int* __restrict__ mat;       // [n]
+  const T* __restrict__ vol;         // [n]
+  const T* __restrict__ dirs;        // [M][3]
+  const T* __restrict__ w;           // [M]
+  const int* __restrict__ refl;      // [M][3]
+  const T* __restrict__ st;          // [nm][G]
+  const T* __restrict__ ss;          // [nm][G][G]
+};
+
+struct Schedule {
+  int npat = 0, nlev = 0;
+  std::vector<int> pat_dirs_ptr, pat_dirs;      // directions of each pattern
+  std::vector<int> pat_lev_ptr;                 // per pattern: offset into lev_ptr
+  std::vector<int> pat_nlev;
+  std::vector<int> lev_ptr;                     // concatenated level offsets (into order)
+  std::vector<int> order;                       // concatenated cell orders (n per pattern)
+  std::vector<int> grid_x;                      // blocks in x for each global level
+};
+
+struct GmresScal {
+  double beta;
+};
+
+struct SNData {
+  int n = 0, G = 0, M = 0, F = 0, nm = 0;
+  int use_ls = 0;
+  bool upwind = true;       // delta == 1 (no downwind or inflow-side diagonal terms)
+  int nrefl = 0;            // reflective face slots
+  Schedule sched;
+  // operator (FP64 and FP32 copies of the real-valued arrays)
+  DevBuf nf, kind, nbr, raxis, rslot, mat, refl;
+  DevBuf area, nrm, gauss, lsw, lsdiag, vol, dirs, w, st, ss, chi, nsf, ksf;
+  DevBuf area32, nrm32, gauss32, lsw32, lsdiag32, vol32, dirs32, w32, st32, ss32;
+  bool have32 = false;
+  // schedule on device
+  DevBuf d_pat_dirs_ptr, d_pat_dirs, d_pat_lev_ptr, d_pat_nlev, d_lev_ptr, d_order;
+  DevBuf d_slot_cell, d_slot_face;
+  // work arrays
+  DevBuf psi, psi32;          // angular flux [n*G*M]
+  DevBuf phi0, fs, fs_old, phi, q, P, src, src32;  // [n*G] / [n]
+  DevBuf partials, ticket, oscal, hbuf;
+  // Krylov storage: basis [(m+1)][len], plus work vectors
+  DevBuf basis, wvec, xvec, rhs, tmp, scat, phtmp;
+  size_t basis_len = 0;
+  int restart = 0;
+  int krylov_prec = -1;  // element size of the Krylov storage (4 or 8)
+};
+
+struct SNOuter {
+  double k, S, change, p0, total_power;
+  int negatives, nonfinite;
+};
+
+// ---------------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T mu_of(const SNOp<T>& A, int f, int i, int m) {
+  const T* n = A.nrm + ((size_t)f * A.n + i) * 3;
+  const T* d = A.dirs + (size_t)m * 3;
+  return d[0] * n[0] + d[1] * n[1] + d[2] * n[2];
+}
+
+// One level of the sweep for every pattern (blockIdx.y).  Solves each (cell, g, m) row of
+// the upwind part of R: psi = (src - upwind face terms - reflective inflow) / diagonal.
+// src is isotropic ([n*G]) when iso != 0, else angular ([n*G*M]).  bnd holds incoming
+// angular flux at reflective faces ([nrefl][G][M]) or is null (treated as zero).
+template <typename T>
+__global__ void k_sweep_level(SNOp<T> A, int level, const int* __restrict__ pat_dirs_ptr,
+                              const int* __restrict__ pat_dirs, const int* __restrict__ pat_lev_ptr,
+                              const int* __restrict__ pat_nlev, const int* __restrict__ lev_ptr,
+                              const int* __restrict__ order, const T* __restrict__ src, int iso,
+                              const T* __restrict__ bnd, T* psi) {
+  const int p = blockIdx.y;
+  if (level >= pat_nlev[p]) return;
+  const int d0 = pat_dirs_ptr[p], nd = pat_dirs_ptr[p + 1] - d0;
+  const int* lp = lev_ptr + pat_lev_ptr[p];
+  const int c0 = lp[level], nc = lp[level + 1] - c0;
+  const int* ord = order + (size_t)p * A.n;
+  const int G = A.G, M = A.M;
+  const long long items = (long long)nc * G * nd;
+  for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items;
+       it += (long long)gridDim.x * blockDim.x) {
+    const int di = (int)(it % nd);
+    const long long rest = it / nd;
+    const int g = (int)(rest % G);
+    const int ci = (int)(rest / G);
+    const int i = ord[c0 + ci];
+    const int m = pat_dirs[d0 + di];
+    const int mt = A.mat[i];
+    const T V = A.vol[i];
+    T den = A.st[(size_t)mt * G + g] * V;
+    T num = iso ? src[(size_t)i * G + g] : src[((size_t)i * G + g) * M + m];
+    const int nfi = A.nf[i];
+    for (int f = 0; f < nfi; f++) {
+      const size_t o = (size_t)f * A.n + i;
+      const int kd = A.kind[o];
+      const T mu = mu_of(A, f, i, m);
+      const T muA = mu * A.area[o];
+      if (kd == PGPU_FACE_INTERIOR) {
+        const T* c = A.gauss + o * 4;
+        if (mu > T(0)) {
+          den += c[0] * muA;
+        } else {
+          den += c[2] * muA;
+          const int j = A.nbr[o];
+          num -= c[3] * muA * psi[((size_t)j * G + g) * M + m];
+        }
+      } else if (kd == PGPU_FACE_VACUUM) {
+        if (mu > T(0)) {
+          den += muA;
+          if (A.use_ls) den -= A.lsdiag[o] * muA;
+        }
+      } else if (kd == PGPU_FACE_REFLECTIVE) {
+        if (mu > T(0)) {
+          den += muA;
+        } else if (bnd) {
+          const int s = A.rslot[o];
+          num -= muA * bnd[((size_t)s * G + g) * M + m];
+        }
+      }
+    }
+    psi[((size_t)i * G + g) * M + m] = num / den;
+  }
+}
+
+// phi0[i,g] = sum_m w_m psi[i,g,m] (one warp per (i,g) row, fixed order within the warp).
+template <typename T>
+__global__ void k_moment(int rows, int M, const T* __restrict__ w, const T* __restrict__ psi, T* phi0) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = warp; r < rows; r += nwarps) {
+    T s = T(0);
+    for (int m = lane; m < M; m += 32) s += w[m] * psi[r * M + m];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) phi0[r] = s;
+  }
+}
+
+// Isotropic source q[i,g] = V sum_g2 sigma_s(g2->g) phi0[i,g2] (+ b[i,g] when given).
+template <typename T>
+__global__ void k_scatter_source(SNOp<T> A, const T* __restrict__ phi0, const T* __restrict__ b, T* q) {
+  const int G = A.G;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n * G; r += gridDim.x * blockDim.x) {
+    const int i = r / G, g = r - i * G;
+    const T* ssm = A.ss + (size_t)A.mat[i] * G * G;
+    T s = T(0);
+    for (int g2 = 0; g2 < G; g2++) s += ssm[g2 * G + g] * phi0[(size_t)i * G + g2];
+    s *= A.vol[i];
+    if (b) s += b[r];
+    q[r] = s;
+  }
+}
+
+// Angular source q[i,g,m] = V sum_g2 sigma_s(g2->g) phi0[i,g2] (isotropic, broadcast over m).
+template <typename T>
+__global__ void k_broadcast(int rows, int M, const T* __restrict__ qi, T* qa) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < (long long)rows * M;
+       l += (long long)gridDim.x * blockDim.x)
+    qa[l] = qi[l / M];
+}
+
+// Incoming angular flux at reflective faces from the current psi: for slot s (cell i,
+// face f, axis a) and direction m with mu < 0, bnd[s,g,m] = psi[i,g,refl(m,a)].
+template <typename T>
+__global__ void k_reflect_extract(SNOp<T> A, int nrefl, const int* __restrict__ slot_cell,
+                                  const int* __restrict__ slot_face, const T* __restrict__ psi, T* bnd) {
+  const int G = A.G, M = A.M;
+  const long long total = (long long)nrefl * G * M;
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < total;
+       l += (long long)gridDim.x * blockDim.x) {
+    const int m = (int)(l % M);
+    const long long rest = l / M;
+    const int g = (int)(rest % G);
+    const int s = (int)(rest / G);
+    const int i = slot_cell[s], f = slot_face[s];
+    const size_t o = (size_t)f * A.n + i;
+    const T mu = mu_of(A, f, i, m);
+    T v = T(0);
+    if (!(mu > T(0))) v = psi[((size_t)i * G + g) * M + A.refl[m * 3 + A.raxis[o]]];
+    bnd[l] = v;
+  }
+}
+
+// Exact matrix-free R psi (needs phi0 of the same psi).
+template <typename T>
+__global__ void k_apply_R(SNOp<T> A, const T* __restrict__ psi, const T* __restrict__ phi0, T* y) {
+  const int G = A.G, M = A.M;
+  const long long N = (long long)A.n * G * M;
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    const int m = (int)(l % M);
+    const long long r = l / M;
+    const int g = (int)(r % G);
+    const int i = (int)(r / G);
+    const int mt = A.mat[i];
+    const T V = A.vol[i];
+    const T pl = psi[l];
+    T acc = A.st[(size_t)mt * G + g] * V * pl;
+    const T* ssm = A.ss + (size_t)mt * G * G;
+    T sc = T(0);
+    for (int g2 = 0; g2 < G; g2++) sc += ssm[g2 * G + g] * phi0[(size_t)i * G + g2];
+    acc -= V * sc;
+    const int nfi = A.nf[i];
+    for (int f = 0; f < nfi; f++) {
+      const size_t o = (size_t)f * A.n + i;
+      const int kd = A.kind[o];
+      const T mu = mu_of(A, f, i, m);
+      const T muA = mu * A.area[o];
+      if (kd == PGPU_FACE_INTERIOR) {
+        const T* c = A.gauss + o * 4;
+        const int j = A.nbr[o];
+        const T pj = psi[((size_t)j * G + g) * M + m];
+        if (mu > T(0)) acc += c[0] * muA * pl + c[1] * muA * pj;
+        else acc += c[2] * muA * pl + c[3] * muA * pj;
+      } else if (kd == PGPU_FACE_VACUUM) {
+        if (mu > T(0)) {
+          acc += muA * pl;
+          if (A.use_ls) {
+            const T* wl = A.lsw + o * A.F;
+            for (int f2 = 0; f2 < nfi; f2++) {
+              const int j = A.nbr[(size_t)f2 * A.n + i];
+              if (A.kind[(size_t)f2 * A.n + i] == PGPU_FACE_INTERIOR)
+                acc += wl[f2] * muA * (psi[((size_t)j * G + g) * M + m] - pl);
+            }
+          }
+        }
+      } else if (kd == PGPU_FACE_REFLECTIVE) {
+        if (mu > T(0)) acc += muA * pl;
+        else acc += muA * psi[((size_t)i * G + g) * M + A.refl[m * 3 + A.raxis[o]]];
+      }
+    }
+    y[l] = acc;
+  }
+}
+
+// ---- small vector kernels (deterministic reductions) ----
+
+template <typename T>
+__global__ void k_dot_many(long long N, const T* __restrict__ V, long long ld, const T* __restrict__ x,
+                           double* out, double* partials, unsigned int* tickets) {
+  // blockIdx.y = vector index
+  const int k = blockIdx.y;
+  const T* v = V + (size_t)k * ld;
+  double acc[1] = {0.0};
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    acc[0] += (double)v[l] * (double)x[l];
+  ReduceSlots<1> slots{partials + (size_t)k * kMaxBlocks, tickets + k};
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) out[k] = tot[0];
+}
+
+// x -= sum_k h[k] V[k]   (h on device)
+template <typename T>
+__global__ void k_sub_many(long long N, const T* __restrict__ V, long long ld, int nv, const double* __restrict__ h, T* x) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    double s = (double)x[l];
+    for (int k = 0; k < nv; k++) s -= h[k] * (double)V[(size_t)k * ld + l];
+    x[l] = (T)s;
+  }
+}
+
+// x += sum_k y[k] V[k]
+template <typename T>
+__global__ void k_add_many(long long N, const T* __restrict__ V, long long ld, int nv, const double* __restrict__ y, T* x) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    double s = (double)x[l];
+    for (int k = 0; k < nv; k++) s += y[k] * (double)V[(size_t)k * ld + l];
+    x[l] = (T)s;
+  }
+}
+
+template <typename T>
+__global__ void k_scale_to(long long N, const T* __restrict__ a, const double* __restrict__ s, int inv, T* b) {
+  const double f = inv ? 1.0 / *s : *s;
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    b[l] = (T)((double)a[l] * f);
+}
+
+// c = a - b
+template <typename T>
+__global__ void k_sub(long long N, const T* __restrict__ a, const T* __restrict__ b, T* c) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    c[l] = a[l] - b[l];
+}
+
+template <typename T>
+__global__ void k_norm2(long long N, const T* __restrict__ x, double* out, ReduceSlots<1> slots) {
+  double acc[1] = {0.0};
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    acc[0] += (double)x[l] * (double)x[l];
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) *out = sqrt(tot[0]);
+}
+
+template <typename T>
+__global__ void k_fill(long long N, T* a, T v) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    a[l] = v;
+}
+
+// x += u
+template <typename T>
+__global__ void k_add(long long N, const T* __restrict__ u, T* x) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    x[l] += u[l];
+}
+
+template <typename S, typename D>
+__global__ void k_cast(long long N, const S* __restrict__ a, D* b) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    b[l] = (D)a[l];
+}
+
+// ---- outer-iteration kernels (FP64 state) ----
+
+// fs_i = V sum_g nu_sigma_f phi0; S = sum fs; k *= S.
+__global__ void k_sn_fission(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
+                             const double* __restrict__ nsf, const double* __restrict__ phi0, double* fs,
+                             SNOuter* os, ReduceSlots<1> slots) {
+  double acc[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* ns = nsf + (size_t)mat[i] * G;
+    double s = 0.0;
+    for (int g = 0; g < G; g++) s += ns[g] * phi0[(size_t)i * G + g];
+    s *= vol[i];
+    fs[i] = s;
+    acc[0] += s;
+  }
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
+    os->S = tot[0];
+    os->k = os->k * tot[0];
+    os->nonfinite = !(tot[0] == tot[0]) || tot[0] == 0.0;
+  }
+}
+
+// normalise fs by S, change vs fs_old, b = chi fs / k (isotropic, per (i,g)).
+__global__ void k_sn_source(int n, int G, const int* __restrict__ mat, const double* __restrict__ chi,
+                            double* fs, double* fs_old, double* b, SNOuter* os, ReduceSlots<2> slots) {
+  const double invS = 1.0 / os->S, invk = 1.0 / os->k;
+  double acc[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double f = fs[i] * invS;
+    double d = f - fs_old[i];
+    fs_old[i] = f;
+    acc[0] += d * d;
+    acc[1] += f * f;
+    const double* ch = chi + (size_t)mat[i] * G;
+    for (int g = 0; g < G; g++) b[(size_t)i * G + g] = ch[g] * f * invk;
+  }
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) os->change = sqrt(tot[0] / tot[1]);
+}
+
+__global__ void k_sn_power_norm(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
+                                const double* __restrict__ ksf, const double* __restrict__ phi0, SNOuter* os,
+                                ReduceSlots<1> slots) {
+  double acc[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* ks = ksf + (size_t)mat[i] * G;
+    for (int g = 0; g < G; g++) acc[0] += 4.0 * M_PI * phi0[(size_t)i * G + g] * ks[g] * vol[i];
+  }
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) os->p0 = tot[0];
+}
+
+// phi = 4 pi phi0 * power / p0 (SNSolver::calculateScalarFlux + normalizeScalarFlux), q, P.
+__global__ void k_sn_power_fields(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
+                                  const double* __restrict__ ksf, const double* __restrict__ nsf,
+                                  const double* __restrict__ phi0, double power, double* phi, double* q,
+                                  double* P, SNOuter* os, ReduceSlots<2> slots) {
+  const double f = 4.0 * M_PI * power / os->p0;
+  const double k = os->k;
+  double acc[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double* ks = ksf + (size_t)mat[i] * G;
+    const double* ns = nsf + (size_t)mat[i] * G;
+    const double V = vol[i];
+    double qi = 0.0, Pi = 0.0;
+    for (int g = 0; g < G; g++) {
+      double v = phi0[(size_t)i * G + g] * f;
+      phi[(size_t)i * G + g] = v;
+      if (v < 0.0) acc[1] += 1.0;
+      qi += v * ks[g] * V;
+      Pi += v * ns[g] * V / k;
+    }
+    q[i] = qi;
+    P[i] = Pi;
+    acc[0] += qi;
+  }
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
+    os->total_power = tot[0];
+    os->negatives = (int)tot[1];
+  }
+}
+
+// psi *= power / (p0 / 4 pi)  (SNSolver::normalizeAngularFlux); counts negatives.
+__global__ void k_sn_psi_norm(long long N, double* psi, double power, SNOuter* os, ReduceSlots<1> slots) {
+  const double f = 4.0 * M_PI * power / os->p0;
+  double acc[1] = {0.0};
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    double v = psi[l] * f;
+    psi[l] = v;
+    if (v < 0.0) acc[0] += 1.0;
+  }
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) os->negatives += (int)tot[0];
+}
+
+}  // namespace pgpu
+
+// ---------------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------------
+
+namespace pgpu {
+namespace {
+
+struct SlotMaps {
+  std::vector<int> cell, face;
+};
+
+// Upwind level sets.  Directions are grouped by the sign of mu against every distinct
+// face normal of the mesh (or against every face when the mesh has too many distinct
+// normals); each group's dependency graph is ordered by Kahn's algorithm.
+int build_schedule(const pgpu_sn_operator* op, Schedule& S) {
+  const int n = op->num_cells, F = op->num_faces, M = op->num_dirs, G = op->num_groups;
+  auto mu = [&](int f, int i, int m) {
+    const double* nr = op->normals + ((size_t)f * n + i) * 3;
+    const double* d = op->directions + (size_t)m * 3;
+    return d[0] * nr[0] + d[1] * nr[1] + d[2] * nr[2];
+  };
+  // distinct normals of interior faces
+  std::map<std::vector<long long>, int> normal_id;
+  std::vector<int> face_nid((size_t)F * n, -1);
+  for (int i = 0; i < n; i++)
+    for (int f = 0; f < op->num_cell_faces[i]; f++) {
+      const size_t o = (size_t)f * n + i;
+      if (op->face_kind[o] != PGPU_FACE_INTERIOR) continue;
+      const double* nr = op->normals + o * 3;
+      std::vector<long long> key{std::llround(nr[0] * 1e9), std::llround(nr[1] * 1e9), std::llround(nr[2] * 1e9)};
+      auto it = normal_id.find(key);
+      int id = it == normal_id.end() ? (normal_id[key] = (int)normal_id.size()) : it->second;
+      face_nid[o] = id;
+    }
+  const bool by_normal = normal_id.size() <= 4096;
+  std::vector<std::vector<double>> nvec(normal_id.size());
+  for (int i = 0; i < n; i++)
+    for (int f = 0; f < op->num_cell_faces[i]; f++) {
+      const size_t o = (size_t)f * n + i;
+      if (face_nid[o] >= 0 && nvec[face_nid[o]].empty())
+        nvec[face_nid[o]] = {op->normals[o * 3], op->normals[o * 3 + 1], op->normals[o * 3 + 2]};
+    }
+  std::map<std::string, int> pat_of_key;
+  std::vector<std::vector<int>> pat_dirs;
+  for (int m = 0; m < M; m++) {
+    std::string key;
+    if (by_normal) {
+      key.resize(nvec.size());
+      const double* d = op->directions + (size_t)m * 3;
+      for (size_t k = 0; k < nvec.size(); k++)
+        key[k] = (d[0] * nvec[k][0] + d[1] * nvec[k][1] + d[2] * nvec[k][2]) < 0.0 ? '1' : '0';
+    } else {
+      key.resize((size_t)F * n, '0');
+      for (int i = 0; i < n; i++)
+        for (int f = 0; f < op->num_cell_faces[i]; f++)
+          if (op->face_kind[(size_t)f * n + i] == PGPU_FACE_INTERIOR && mu(f, i, m) < 0.0) key[(size_t)f * n + i] = '1';
+    }
+    auto it = pat_of_key.find(key);
+    if (it == pat_of_key.end()) {
+      pat_of_key[key] = (int)pat_dirs.size();
+      pat_dirs.push_back({m});
+    } else {
+      pat_dirs[it->second].push_back(m);
+    }
+  }
+  S = Schedule();
+  S.npat = (int)pat_dirs.size();
+  S.pat_dirs_ptr.push_back(0);
+  for (auto& v : pat_dirs) {
+    for (int m : v) S.pat_dirs.push_back(m);
+    S.pat_dirs_ptr.push_back((int)S.pat_dirs.size());
+  }
+  S.order.resize((size_t)S.npat * n);
+  std::vector<int> indeg(n), head(n + 1), adj;
+  for (int p = 0; p < S.npat; p++) {
+    const int m = pat_dirs[p][0];
+    // edge i -> j when j has an inflow face (mu < 0) whose neighbour is i
+    std::fill(head.begin(), head.end(), 0);
+    std::fill(indeg.begin(), indeg.end(), 0);
+    for (int j = 0; j < n; j++)
+      for (int f = 0; f < op->num_cell_faces[j]; f++) {
+        const size_t o = (size_t)f * n + j;
+        if (op->face_kind[o] == PGPU_FACE_INTERIOR && mu(f, j, m) < 0.0) {
+          head[op->neighbors[o] + 1]++;
+          indeg[j]++;
+        }
+      }
+    for (int i = 0; i < n; i++) head[i + 1] += head[i];
+    adj.assign(head[n], 0);
+    std::vector<int> fill(head.begin(), head.end() - 1);
+    for (int j = 0; j < n; j++)
+      for (int f = 0; f < op->num_cell_faces[j]; f++) {
+        const size_t o = (size_t)f * n + j;
+        if (op->face_kind[o] == PGPU_FACE_INTERIOR && mu(f, j, m) < 0.0) adj[fill[op->neighbors[o]]++] = j;
+      }
+    int* ord = S.order.data() + (size_t)p * n;
+    int cnt = 0;
+    for (int i = 0; i < n; i++)
+      if (indeg[i] == 0) ord[cnt++] = i;
+    S.pat_lev_ptr.push_back((int)S.lev_ptr.size());
+    S.lev_ptr.push_back(0);
+    int lo = 0;
+    while (lo < cnt) {
+      const int hi = cnt;
+      for (int k = lo; k < hi; k++) {
+        const int i = ord[k];
+        for (int e = head[i]; e < head[i + 1]; e++)
+          if (--indeg[adj[e]] == 0) ord[cnt++] = adj[e];
+      }
+      S.lev_ptr.push_back(hi);
+      lo = hi;
+    }
+    if (cnt != n) return fail(PGPU_ERR_INVALID, "the upwind graph of a direction has a cycle; this mesh cannot be swept");
+    S.pat_nlev.push_back((int)S.lev_ptr.size() - S.pat_lev_ptr.back() - 1);
+  }
+  S.nlev = 0;
+  for (int v : S.pat_nlev) S.nlev = std::max(S.nlev, v);
+  S.grid_x.assign(S.nlev, 1);
+  for (int p = 0; p < S.npat; p++) {
+    const int* lp = S.lev_ptr.data() + S.pat_lev_ptr[p];
+    const long long nd = S.pat_dirs_ptr[p + 1] - S.pat_dirs_ptr[p];
+    for (int L = 0; L < S.pat_nlev[p]; L++) {
+      long long items = (long long)(lp[L + 1] - lp[L]) * nd * G;
+      S.grid_x[L] = std::max(S.grid_x[L], grid_for(items));
+    }
+  }
+  return PGPU_OK;
+}
+
+template <typename T>
+SNOp<T> make_op(const SNData& d);
+
+template <>
+SNOp<double> make_op<double>(const SNData& d) {
+  return SNOp<double>{d.n, d.G, d.M, d.F, d.use_ls, d.nf.as<int>(), d.kind.as<int>(), d.nbr.as<int>(),
+                      d.area.as<double>(), d.nrm.as<double>(), d.gauss.as<double>(), d.raxis.as<int>(),
+                      d.rslot.as<int>(), d.lsw.as<double>(), d.lsdiag.as<double>(), d.mat.as<int>(),
+                      d.vol.as<double>(), d.dirs.as<double>(), d.w.as<double>(), d.refl.as<int>(),
+                      d.st.as<double>(), d.ss.as<double>()};
+}
+
+template <>
+SNOp<float> make_op<float>(const SNData& d) {
+  return SNOp<float>{d.n, d.G, d.M, d.F, d.use_ls, d.nf.as<int>(), d.kind.as<int>(), d.nbr.as<int>(),
+                     d.area32.as<float>(), d.nrm32.as<float>(), d.gauss32.as<float>(), d.raxis.as<int>(),
+                     d.rslot.as<int>(), d.lsw32.as<float>(), d.lsdiag32.as<float>(), d.mat.as<int>(),
+                     d.vol32.as<float>(), d.dirs32.as<float>(), d.w32.as<float>(), d.refl.as<int>(),
+                     d.st32.as<float>(), d.ss32.as<float>()};
+}
+
+template <int NV>
+ReduceSlots<NV> sn_slots(SNData& d) {
+  return ReduceSlots<NV>{d.partials.as<double>(), d.ticket.as<unsigned int>()};
+}
+
+int make_fp32(pgpu_problem* p) {
+  SNData& d = *p->sn;
+  if (d.have32) return PGPU_OK;
+  cudaStream_t s = p->stream;
+  auto conv = [&](DevBuf& src, DevBuf& dst) -> int {
+    if (!src.ptr) return PGPU_OK;
+    const long long cnt = (long long)(src.bytes / 8);
+    int st = dev_alloc(dst, (size_t)cnt * 4, &p->bytes);
+    if (st) return st;
+    k_cast<double, float><<<grid_for(cnt), kThreads, 0, s>>>(cnt, src.as<double>(), dst.as<float>());
+    return PGPU_OK;
+  };
+  int st;
+  if ((st = conv(d.area, d.area32)) || (st = conv(d.nrm, d.nrm32)) || (st = conv(d.gauss, d.gauss32)) ||
+      (st = conv(d.lsw, d.lsw32)) || (st = conv(d.lsdiag, d.lsdiag32)) || (st = conv(d.vol, d.vol32)) ||
+      (st = conv(d.dirs, d.dirs32)) || (st = conv(d.w, d.w32)) || (st = conv(d.st, d.st32)) ||
+      (st = conv(d.ss, d.ss32)))
+    return st;
+  PGPU_CUDA(cudaGetLastError());
+  d.have32 = true;
+  return PGPU_OK;
+}
+
+}  // namespace
+}  // namespace pgpu
+
+namespace pgpu {
+namespace {
+
+int sweeps_done = 0;
+
+template <typename T>
+int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd, T* psi) {
+  SNData& d = *p->sn;
+  const Schedule& S = d.sched;
+  for (int L = 0; L < S.nlev; L++) {
+    dim3 grid(S.grid_x[L], S.npat);
+    k_sweep_level<T><<<grid, kThreads, 0, p->stream>>>(
+        A, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
+        d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), src, iso, bnd, psi);
+  }
+  PGPU_CUDA(cudaGetLastError());
+  sweeps_done++;
+  return PGPU_OK;
+}
+
+template <typename T>
+T* psi_work(SNData& d) {
+  return sizeof(T) == 8 ? (T*)d.psi.ptr : (T*)d.psi32.ptr;
+}
+
+
+// y = T(x; b): sweep driven by the scattering source of x's phi0 part (plus b) and the
+// reflective inflow held in x's boundary part; returns [phi0' | inflow'].
+template <typename T>
+int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y) {
+  SNData& d = *p->sn;
+  const int nG = d.n * d.G;
+  T* q = d.scat.as<T>();
+  T* psi = psi_work<T>(d);
+  k_scatter_source<T><<<grid_for(nG), kThreads, 0, p->stream>>>(A, x, b, q);
+  int st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi);
+  if (st) return st;
+  k_moment<T><<<grid_for((long long)nG * 32), kThreads, 0, p->stream>>>(nG, d.M, A.w, psi, y);
+  if (d.nrefl) {
+    const long long nb = (long long)d.nrefl * d.G * d.M;
+    k_reflect_extract<T><<<grid_for(nb), kThreads, 0, p->stream>>>(A, d.nrefl, d.d_slot_cell.as<int>(),
+                                                                   d.d_slot_face.as<int>(), psi, y + nG);
+  }
+  PGPU_CUDA(cudaGetLastError());
+  return PGPU_OK;
+}
+
+// y = R x (angular space), using tmp (>= n*G) for phi0.
+template <typename T>
+int apply_R(pgpu_problem* p, const SNOp<T>& A, const T* x, T* y, T* tmp_phi0) {
+  SNData& d = *p->sn;
+  const int nG = d.n * d.G;
+  const long long N = (long long)nG * d.M;
+  k_moment<T><<<grid_for((long long)nG * 32), kThreads, 0, p->stream>>>(nG, d.M, A.w, x, tmp_phi0);
+  k_apply_R<T><<<grid_for(N), kThreads, 0, p->stream>>>(A, x, tmp_phi0, y);
+  PGPU_CUDA(cudaGetLastError());
+  return PGPU_OK;
+}
+
+int ensure_krylov(pgpu_problem* p, size_t len, int restart, int es) {
+  SNData& d = *p->sn;
+  if (d.basis_len == len && d.restart == restart && d.krylov_prec == es) return PGPU_OK;
+  int st;
+  if ((st = dev_alloc(d.basis, (size_t)(restart + 1) * len * es, &p->bytes))) return st;
+  if ((st = dev_alloc(d.wvec, len * es, &p->bytes))) return st;
+  if ((st = dev_alloc(d.xvec, len * es, &p->bytes))) return st;
+  if ((st = dev_alloc(d.rhs, len * es, &p->bytes))) return st;
+  if ((st = dev_alloc(d.tmp, len * es, &p->bytes))) return st;
+  if ((st = dev_alloc(d.partials, (size_t)(restart + 4) * kMaxBlocks * 8, &p->bytes))) return st;
+  if ((st = dev_alloc(d.ticket, (size_t)(restart + 4) * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.hbuf, (size_t)4 * (restart + 4) * 8, &p->bytes))) return st;
+  if ((st = dev_alloc(d.scat, (size_t)d.n * d.G * es, &p->bytes))) return st;
+  if ((st = dev_alloc(d.phtmp, (size_t)d.n * d.G * es, &p->bytes))) return st;
+  PGPU_CUDA(cudaMemsetAsync(d.ticket.ptr, 0, (size_t)(restart + 4) * 4, p->stream));
+  d.basis_len = len;
+  d.restart = restart;
+  d.krylov_prec = es;
+  return PGPU_OK;
+}
+
+// Restarted GMRES with classical Gram-Schmidt and one re-orthogonalisation (CGS2).
+// residual(r) computes b - A x for the current x; applyA(v, w) computes w = A v;
+// post(u) adds the correction for the Krylov combination u to x.  The small Hessenberg
+// problem is solved on the host with Givens rotations.
+template <typename T, typename Res, typename App, typename Post>
+int gmres(pgpu_problem* p, long long len, Res residual, App applyA, Post post, double tol_abs, int max_it,
+          int* iters, double* res_out) {
+  SNData& d = *p->sn;
+  const int m = d.restart;
+  cudaStream_t s = p->stream;
+  T* V = d.basis.as<T>();
+  T* w = d.wvec.as<T>();
+  T* u = d.tmp.as<T>();
+  double* h1 = d.hbuf.as<double>();
+  double* h2 = h1 + (m + 4);
+  double* hn = h2 + (m + 4);
+  double* yv = hn + (m + 4);
+  const int gx = grid_for(len);
+  std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hh(m + 2), hh2(m + 2);
+  int total = 0, st;
+  double res = 0.0;
+  ReduceSlots<1> nslot{d.partials.as<double>() + (size_t)(m + 2) * kMaxBlocks, d.ticket.as<unsigned int>() + (m + 2)};
+  while (true) {
+    if ((st = residual(V))) return st;
+    k_norm2<T><<<gx, kThreads, 0, s>>>(len, V, hn, nslot);
+    double beta;
+    PGPU_CUDA(cudaMemcpyAsync(&beta, hn, 8, cudaMemcpyDeviceToHost, s));
+    PGPU_CUDA(cudaStreamSynchronize(s));
+    if (!(beta == beta)) return fail(PGPU_ERR_NAN, "NaN in the transport residual");
+    res = beta;
+    if (beta <= tol_abs || total >= max_it) break;
+    k_scale_to<T><<<gx, kThreads, 0, s>>>(len, V, hn, 1, V);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int j = 0;
+    for (; j < m && total < max_it; j++) {
+      T* vj = V + (size_t)j * len;
+      if ((st = applyA(vj, w))) return st;
+      dim3 gd(std::min(gx, 512), j + 1);
+      k_dot_many<T><<<gd, kThreads, 0, s>>>(len, V, len, w, h1, d.partials.as<double>(), d.ticket.as<unsigned int>());
+      k_sub_many<T><<<gx, kThreads, 0, s>>>(len, V, len, j + 1, h1, w);
+      k_dot_many<T><<<gd, kThreads, 0, s>>>(len, V, len, w, h2, d.partials.as<double>(), d.ticket.as<unsigned int>());
+      k_sub_many<T><<<gx, kThreads, 0, s>>>(len, V, len, j + 1, h2, w);
+      k_norm2<T><<<gx, kThreads, 0, s>>>(len, w, hn, nslot);
+      k_scale_to<T><<<gx, kThreads, 0, s>>>(len, w, hn, 1, V + (size_t)(j + 1) * len);
+      PGPU_CUDA(cudaGetLastError());
+      PGPU_CUDA(cudaMemcpyAsync(hh.data(), h1, (j + 1) * 8, cudaMemcpyDeviceToHost, s));
+      PGPU_CUDA(cudaMemcpyAsync(hh2.data(), h2, (j + 1) * 8, cudaMemcpyDeviceToHost, s));
+      double hnext;
+      PGPU_CUDA(cudaMemcpyAsync(&hnext, hn, 8, cudaMemcpyDeviceToHost, s));
+      PGPU_CUDA(cudaStreamSynchronize(s));
+      total++;
+      double* col = &H[(size_t)j * (m + 1)];
+      for (int k = 0; k <= j; k++) col[k] = hh[k] + hh2[k];
+      col[j + 1] = hnext;
+      for (int k = 0; k < j; k++) {
+        double a = cs[k] * col[k] + sn[k] * col[k + 1];
+        double b = -sn[k] * col[k] + cs[k] * col[k + 1];
+        col[k] = a;
+        col[k + 1] = b;
+      }
+      double r = std::hypot(col[j], col[j + 1]);
+      if (r == 0.0 || !(r == r)) {
+        j++;
+        break;
+      }
+      cs[j] = col[j] / r;
+      sn[j] = col[j + 1] / r;
+      col[j] = r;
+      col[j + 1] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      res = std::fabs(g[j + 1]);
+      if (res <= tol_abs || hnext == 0.0) {
+        j++;
+        break;
+      }
+    }
+    // back substitution H y = g
+    std::vector<double> y(j, 0.0);
+    for (int k = j - 1; k >= 0; k--) {
+      double t = g[k];
+      for (int c = k + 1; c < j; c++) t -= H[(size_t)c * (m + 1) + k] * y[c];
+      y[k] = t / H[(size_t)k * (m + 1) + k];
+    }
+    PGPU_CUDA(cudaMemcpyAsync(yv, y.data(), j * 8, cudaMemcpyHostToDevice, s));
+    PGPU_CUDA(cudaMemsetAsync(u, 0, len * sizeof(T), s));
+    k_add_many<T><<<gx, kThreads, 0, s>>>(len, V, len, j, yv, u);
+    PGPU_CUDA(cudaGetLastError());
+    if ((st = post(u))) return st;
+    PGPU_CUDA(cudaStreamSynchronize(s));
+    if (res <= tol_abs || total >= max_it) break;
+  }
+  *iters = total;
+  *res_out = res;
+  return PGPU_OK;
+}
+
+template <typename T>
+int norm_of(pgpu_problem* p, long long len, const T* x, double* out) {
+  SNData& d = *p->sn;
+  double* hn = d.hbuf.as<double>() + 3 * (d.restart + 4);
+  ReduceSlots<1> slot{d.partials.as<double>() + (size_t)(d.restart + 3) * kMaxBlocks, d.ticket.as<unsigned int>() + (d.restart + 3)};
+  k_norm2<T><<<grid_for(len), kThreads, 0, p->stream>>>(len, x, hn, slot);
+  PGPU_CUDA(cudaMemcpyAsync(out, hn, 8, cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  return PGPU_OK;
+}
+
+int read_outer(pgpu_problem* p, SNOuter& os) {
+  PGPU_CUDA(cudaMemcpyAsync(&os, p->sn->oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  return PGPU_OK;
+}
+
+template <typename T>
+int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
+  SNData& d = *p->sn;
+  cudaStream_t s = p->stream;
+  const int n = d.n, G = d.G, M = d.M, nG = n * G;
+  const long long N = (long long)nG * M;
+  const bool phi_space = d.upwind && !d.use_ls;
+  const long long len = phi_space ? (long long)nG + (long long)d.nrefl * G * M : N;
+  const int restart = phi_space ? 30 : 20;
+  int st;
+  if ((st = ensure_krylov(p, (size_t)len, restart, (int)sizeof(T)))) return st;
+  SNOp<T> A = make_op<T>(d);
+  SNOp<double> A64 = make_op<double>(d);
+  SNOuter* dos = d.oscal.as<SNOuter>();
+  T* x = d.xvec.as<T>();
+  T* rhs = d.rhs.as<T>();  // angular-space right-hand side, or the FP32 copy of b
+  double* bsrc = d.src.as<double>();  // FP64 isotropic source b [nG] lives in src
+  double* phi0 = d.phi0.as<double>();
+  ReduceSlots<1> s1{d.partials.as<double>(), d.ticket.as<unsigned int>()};
+  ReduceSlots<2> s2{d.partials.as<double>(), d.ticket.as<unsigned int>()};
+  sweeps_done = 0;
+
+  cudaEvent_t e0, e1;
+  PGPU_CUDA(cudaEventCreate(&e0));
+  PGPU_CUDA(cudaEventCreate(&e1));
+  PGPU_CUDA(cudaEventRecord(e0, s));
+
+  // flat start
+  SNOuter init;
+  std::memset(&init, 0, sizeof(init));
+  init.k = 1.0;
+  PGPU_CUDA(cudaMemcpyAsync(dos, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+  // flat start: phi0 = 1 and x = [1 | 0] (scalar-flux space) or psi = 1 (angular space)
+  k_fill<double><<<grid_for(nG), kThreads, 0, s>>>(nG, phi0, 1.0);
+  PGPU_CUDA(cudaMemsetAsync(x, 0, len * sizeof(T), s));
+  k_fill<T><<<grid_for(phi_space ? nG : N), kThreads, 0, s>>>(phi_space ? nG : N, x, T(1));
+  k_sn_fission<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol.as<double>(), d.nsf.as<double>(), phi0,
+                                                 d.fs.as<double>(), dos, s1);
+  SNOuter os;
+  if ((st = read_outer(p, os))) return st;
+  if (os.nonfinite || os.S <= 0.0) return fail(PGPU_ERR_INVALID, "no fission source in the initial flux");
+  os.k = 1.0;
+  PGPU_CUDA(cudaMemcpyAsync(dos, &os, sizeof(os), cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(cudaMemsetAsync(d.fs_old.ptr, 0, (size_t)n * 8, s));
+  k_sn_source<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.chi.as<double>(), d.fs.as<double>(),
+                                                d.fs_old.as<double>(), bsrc, dos, s2);
+  {
+    double* Sdev = &dos->S;
+    k_scale_to<T><<<grid_for(len), kThreads, 0, s>>>(len, x, Sdev, 1, x);
+  }
+  PGPU_CUDA(cudaGetLastError());
+
+  int outer = 0, inner_total = 0;
+  double change = 1.0, dk = 1.0, k_prev = 1.0;
+  bool converged = false;
+  // b in precision T lives in rhs[0:nG] for the scalar-flux path
+  for (outer = 1; outer <= opt->max_outer; outer++) {
+    const double tol_in = std::fmin(1e-3, std::fmax(1e-12, 0.02 * std::fmin(change, dk * 1e3)));
+    double xnorm = 0.0;
+    if ((st = norm_of<T>(p, len, x, &xnorm))) return st;
+    int it = 0;
+    double res = 0.0;
+    if (phi_space) {
+      T* bt = rhs;
+      k_cast<double, T><<<grid_for(nG), kThreads, 0, s>>>(nG, bsrc, bt);
+      auto residual = [&](T* r) -> int {
+        int e = phi_space_T<T>(p, A, x, bt, r);
+        if (e) return e;
+        k_sub<T><<<grid_for(len), kThreads, 0, s>>>(len, r, x, r);
+        return PGPU_OK;
+      };
+      // w = v - T(v; 0); the sweep output goes to w first
+      auto applyA = [&](const T* v, T* w) -> int {
+        int e = phi_space_T<T>(p, A, v, nullptr, w);
+        if (e) return e;
+        k_sub<T><<<grid_for(len), kThreads, 0, s>>>(len, v, w, w);
+        return PGPU_OK;
+      };
+      auto post_add = [&](T* u) -> int {
+        k_add<T><<<grid_for(len), kThreads, 0, s>>>(len, u, x);
+        return PGPU_OK;
+      };
+      if ((st = gmres<T>(p, len, residual, applyA, post_add, tol_in * xnorm, opt->max_inner, &it, &res))) return st;
+      k_cast<T, double><<<grid_for(nG), kThreads, 0, s>>>(nG, x, phi0);
+    } else {
+      T* z = psi_work<T>(d);
+      T* ph = d.phtmp.as<T>();
+      k_cast<double, T><<<grid_for(nG), kThreads, 0, s>>>(nG, bsrc, ph);
+      k_broadcast<T><<<grid_for(N), kThreads, 0, s>>>(nG, M, ph, rhs);
+      auto residual = [&](T* r) -> int {
+        int e = apply_R<T>(p, A, x, r, ph);
+        if (e) return e;
+        k_sub<T><<<grid_for(len), kThreads, 0, s>>>(len, rhs, r, r);
+        return PGPU_OK;
+      };
+      auto applyA = [&](const T* v, T* w) -> int {
+        int e = sweep<T>(p, A, v, 0, nullptr, z);
+        if (e) return e;
+        return apply_R<T>(p, A, z, w, ph);
+      };
+      auto post_add = [&](T* u) -> int {
+        int e = sweep<T>(p, A, u, 0, nullptr, z);
+        if (e) return e;
+        k_add<T><<<grid_for(len), kThreads, 0, s>>>(len, z, x);
+        return PGPU_OK;
+      };
+      if ((st = gmres<T>(p, len, residual, applyA, post_add, tol_in * xnorm, opt->max_inner, &it, &res))) return st;
+      k_moment<T><<<grid_for((long long)nG * 32), kThreads, 0, s>>>(nG, M, A.w, x, ph);
+      k_cast<T, double><<<grid_for(nG), kThreads, 0, s>>>(nG, ph, phi0);
+    }
+    inner_total += it;
+    k_sn_fission<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol.as<double>(), d.nsf.as<double>(), phi0,
+                                                   d.fs.as<double>(), dos, s1);
+    k_scale_to<T><<<grid_for(len), kThreads, 0, s>>>(len, x, &dos->S, 1, x);
+    k_sn_source<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.chi.as<double>(), d.fs.as<double>(),
+                                                  d.fs_old.as<double>(), bsrc, dos, s2);
+    PGPU_CUDA(cudaGetLastError());
+    if ((st = read_outer(p, os))) return st;
+    if (os.nonfinite || !(os.k == os.k)) return fail(PGPU_ERR_NAN, "non-finite fission source");
+    change = os.change;
+    dk = std::fabs(os.k - k_prev);
+    k_prev = os.k;
+    if (opt->verbose)
+      std::printf("pgpu sn outer %d: k = %.12f  dk = %.3e  source change = %.3e  gmres = %d (res %.2e)\n", outer,
+                  os.k, dk, change, it, res);
+    if (dk < opt->tol_k && change < opt->tol_flux) {
+      converged = true;
+      break;
+    }
+  }
+
+  // psi in FP64 from the converged state
+  double* psi = d.psi.as<double>();
+  if (phi_space) {
+    double* xd = d.phi.as<double>();  // reuse as FP64 copy of [phi0 | inflow] when it fits
+    DevBuf xd_buf;
+    if ((size_t)len * 8 > d.phi.bytes) {
+      if ((st = dev_alloc(xd_buf, (size_t)len * 8, nullptr))) return st;
+      xd = xd_buf.as<double>();
+    }
+    k_cast<T, double><<<grid_for(len), kThreads, 0, s>>>(len, x, xd);
+    double* q = d.q.as<double>();
+    DevBuf qbuf;
+    if ((size_t)nG * 8 > d.q.bytes) {
+      if ((st = dev_alloc(qbuf, (size_t)nG * 8, nullptr))) return st;
+      q = qbuf.as<double>();
+    }
+    k_scatter_source<double><<<grid_for(nG), kThreads, 0, s>>>(A64, xd, bsrc, q);
+    if ((st = sweep<double>(p, A64, q, 1, d.nrefl ? xd + nG : nullptr, psi))) return st;
+    PGPU_CUDA(cudaStreamSynchronize(s));
+  } else {
+    k_cast<T, double><<<grid_for(N), kThreads, 0, s>>>(N, x, psi);
+  }
+  k_moment<double><<<grid_for((long long)nG * 32), kThreads, 0, s>>>(nG, M, d.w.as<double>(), psi, phi0);
+  k_sn_power_norm<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol.as<double>(), d.ksf.as<double>(), phi0,
+                                                    dos, s1);
+  k_sn_power_fields<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol.as<double>(), d.ksf.as<double>(),
+                                                      d.nsf.as<double>(), phi0, opt->power, d.phi.as<double>(),
+                                                      d.q.as<double>(), d.P.as<double>(), dos, s2);
+  k_sn_psi_norm<<<grid_for(N), kThreads, 0, s>>>(N, psi, opt->power, dos, s1);
+  PGPU_CUDA(cudaGetLastError());
+  PGPU_CUDA(cudaEventRecord(e1, s));
+  if ((st = read_outer(p, os))) return st;
+  float ms = 0.f;
+  PGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  stats->keff = os.k;
+  stats->outer_iterations = std::min(outer, opt->max_outer);
+  stats->inner_iterations = inner_total;
+  stats->sweeps = sweeps_done;
+  stats->residual = change;
+  stats->seconds = ms * 1e-3;
+  if (!converged) return fail(PGPU_ERR_NOT_CONVERGED, "SN power iteration reached max_outer without converging");
+  if (os.negatives > 0) return fail(PGPU_ERR_NEGATIVE_FLUX, "negative values in the scalar- or angular-flux solution");
+  return PGPU_OK;
+}
+
+}  // namespace
+
+int sn_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
+  if (opt->precision == PGPU_MIXED) {
+    int st = make_fp32(p);
+    if (st) return st;
+    if (!p->sn->psi32.ptr) {
+      st = dev_alloc(p->sn->psi32, (size_t)p->sn->n * p->sn->G * p->sn->M * 4, &p->bytes);
+      if (st) return st;
+      st = dev_alloc(p->sn->src32, (size_t)p->sn->n * p->sn->G * 4, &p->bytes);
+      if (st) return st;
+    }
+    return solve_T<float>(p, opt, stats);
+  }
+  return solve_T<double>(p, opt, stats);
+}
+
+int sn_get_flux(pgpu_problem* p, double* phi) {
+  SNData& d = *p->sn;
+  PGPU_CUDA(cudaMemcpyAsync(phi, d.phi.ptr, (size_t)d.n * d.G * 8, cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  return PGPU_OK;
+}
+
+int sn_get_angular(pgpu_problem* p, double* psi) {
+  SNData& d = *p->sn;
+  PGPU_CUDA(cudaMemcpyAsync(psi, d.psi.ptr, (size_t)d.n * d.G * d.M * 8, cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  return PGPU_OK;
+}
+
+int sn_get_power(pgpu_problem* p, double* q, double* P, double* total) {
+  SNData& d = *p->sn;
+  if (q) PGPU_CUDA(cudaMemcpyAsync(q, d.q.ptr, (size_t)d.n * 8, cudaMemcpyDeviceToHost, p->stream));
+  if (P) PGPU_CUDA(cudaMemcpyAsync(P, d.P.ptr, (size_t)d.n * 8, cudaMemcpyDeviceToHost, p->stream));
+  SNOuter os;
+  PGPU_CUDA(cudaMemcpyAsync(&os, d.oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  if (total) *total = os.total_power;
+  return PGPU_OK;
+}
+
+void sn_destroy(pgpu_problem* p) {
+  delete p->sn;
+  p->sn = nullptr;
+}
+
 }  // namespace pgpu
 
 extern "C" {
-int pgpu_sn_create(int, const pgpu_sn_operator*, pgpu_problem** out) { *out = nullptr; return pgpu::fail(PGPU_ERR_INVALID, "SN not built"); }
-int pgpu_sn_apply(pgpu_problem*, const double*, double*) { return pgpu::fail(PGPU_ERR_INVALID, "SN not built"); }
+
+int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
+  using namespace pgpu;
+  if (!op || !out) return fail(PGPU_ERR_INVALID, "null argument");
+  *out = nullptr;
+  const int n = op->num_cells, G = op->num_groups, M = op->num_dirs, F = op->num_faces, nm = op->num_materials;
+  if (n < 1 || G < 1 || M < 1 || F < 1 || nm < 1) return fail(PGPU_ERR_INVALID, "bad operator sizes");
+  if ((long long)n * G * M >= (1LL << 40)) return fail(PGPU_ERR_INVALID, "operator too large");
+  if (op->use_ls && !op->ls_weight) return fail(PGPU_ERR_INVALID, "use_ls set without ls_weight");
+  for (int i = 0; i < n; i++) {
+    if (op->materials[i] < 0 || op->materials[i] >= nm) return fail(PGPU_ERR_INVALID, "material index out of range");
+    if (op->num_cell_faces[i] < 0 || op->num_cell_faces[i] > F) return fail(PGPU_ERR_INVALID, "bad face count");
+  }
+  bool upwind = true;
+  std::vector<int> rslot((size_t)F * n, -1), slot_cell, slot_face;
+  std::vector<double> lsdiag((size_t)F * n, 0.0);
+  for (int i = 0; i < n; i++)
+    for (int f = 0; f < op->num_cell_faces[i]; f++) {
+      const size_t o = (size_t)f * n + i;
+      const int k = op->face_kind[o];
+      if (k == PGPU_FACE_INTERIOR) {
+        if (op->neighbors[o] < 0 || op->neighbors[o] >= n) return fail(PGPU_ERR_INVALID, "neighbour index out of range");
+        if (op->gauss[o * 4 + 1] != 0.0 || op->gauss[o * 4 + 2] != 0.0) upwind = false;
+      } else if (k == PGPU_FACE_REFLECTIVE) {
+        if (op->reflect_axis[o] < 0 || op->reflect_axis[o] > 2) return fail(PGPU_ERR_INVALID, "bad reflection axis");
+        rslot[o] = (int)slot_cell.size();
+        slot_cell.push_back(i);
+        slot_face.push_back(f);
+      } else if (k == PGPU_FACE_VACUUM) {
+        if (op->use_ls)
+          for (int f2 = 0; f2 < op->num_cell_faces[i]; f2++)
+            if (op->face_kind[(size_t)f2 * n + i] == PGPU_FACE_INTERIOR) lsdiag[o] += op->ls_weight[o * F + f2];
+      } else if (k != PGPU_FACE_NONE) {
+        return fail(PGPU_ERR_INVALID, "bad face kind");
+      }
+    }
+  for (int m = 0; m < M * 3; m++)
+    if (op->reflected[m] < 0 || op->reflected[m] >= M) return fail(PGPU_ERR_INVALID, "bad reflected direction");
+  Schedule sched;
+  int st = build_schedule(op, sched);
+  if (st) return st;
+  PGPU_CUDA(cudaSetDevice(device));
+  pgpu_problem* p = new pgpu_problem();
+  p->kind = 2;
+  p->device = device;
+  p->num_cells = n;
+  p->num_groups = G;
+  p->num_dirs = M;
+  p->sn = new SNData();
+  SNData& d = *p->sn;
+  d.n = n;
+  d.G = G;
+  d.M = M;
+  d.F = F;
+  d.nm = nm;
+  d.use_ls = op->use_ls;
+  d.upwind = upwind;
+  d.nrefl = (int)slot_cell.size();
+  d.sched = sched;
+  st = PGPU_OK;
+  auto up = [&](DevBuf& b, const void* h, size_t bytes) {
+    if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes);
+  };
+  auto al = [&](DevBuf& b, size_t bytes) {
+    if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes);
+  };
+  if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "stream");
+  const size_t Fn = (size_t)F * n;
+  up(d.nf, op->num_cell_faces, (size_t)n * 4);
+  up(d.kind, op->face_kind, Fn * 4);
+  up(d.nbr, op->neighbors, Fn * 4);
+  up(d.raxis, op->reflect_axis, Fn * 4);
+  up(d.rslot, rslot.data(), Fn * 4);
+  up(d.mat, op->materials, (size_t)n * 4);
+  up(d.refl, op->reflected, (size_t)M * 3 * 4);
+  up(d.area, op->areas, Fn * 8);
+  up(d.nrm, op->normals, Fn * 3 * 8);
+  up(d.gauss, op->gauss, Fn * 4 * 8);
+  if (op->use_ls) up(d.lsw, op->ls_weight, Fn * F * 8);
+  up(d.lsdiag, lsdiag.data(), Fn * 8);
+  up(d.vol, op->volumes, (size_t)n * 8);
+  up(d.dirs, op->directions, (size_t)M * 3 * 8);
+  up(d.w, op->weights, (size_t)M * 8);
+  up(d.st, op->sigma_t, (size_t)nm * G * 8);
+  up(d.ss, op->sigma_s, (size_t)nm * G * G * 8);
+  up(d.chi, op->chi, (size_t)nm * G * 8);
+  up(d.nsf, op->nu_sigma_f, (size_t)nm * G * 8);
+  up(d.ksf, op->kappa_sigma_f, (size_t)nm * G * 8);
+  up(d.d_pat_dirs_ptr, sched.pat_dirs_ptr.data(), sched.pat_dirs_ptr.size() * 4);
+  up(d.d_pat_dirs, sched.pat_dirs.data(), sched.pat_dirs.size() * 4);
+  up(d.d_pat_lev_ptr, sched.pat_lev_ptr.data(), sched.pat_lev_ptr.size() * 4);
+  up(d.d_pat_nlev, sched.pat_nlev.data(), sched.pat_nlev.size() * 4);
+  up(d.d_lev_ptr, sched.lev_ptr.data(), sched.lev_ptr.size() * 4);
+  up(d.d_order, sched.order.data(), sched.order.size() * 4);
+  if (d.nrefl) {
+    up(d.d_slot_cell, slot_cell.data(), slot_cell.size() * 4);
+    up(d.d_slot_face, slot_face.data(), slot_face.size() * 4);
+  }
+  const size_t nG = (size_t)n * G;
+  al(d.psi, nG * M * 8);
+  al(d.phi0, nG * 8);
+  al(d.phi, nG * 8);
+  al(d.src, nG * 8);
+  al(d.fs, (size_t)n * 8);
+  al(d.fs_old, (size_t)n * 8);
+  al(d.q, std::max(nG, (size_t)n) * 8);
+  al(d.P, (size_t)n * 8);
+  al(d.oscal, sizeof(SNOuter));
+  if (st != PGPU_OK) {
+    std::string msg = pgpu_last_error();
+    pgpu_problem_destroy(p);
+    return fail(st, msg);
+  }
+  *out = p;
+  return PGPU_OK;
 }
+
+int pgpu_sn_apply(pgpu_problem* p, const double* x, double* y) {
+  using namespace pgpu;
+  if (!p || p->kind != 2) return fail(PGPU_ERR_INVALID, "not an SN problem");
+  PGPU_CUDA(cudaSetDevice(p->device));
+  SNData& d = *p->sn;
+  const size_t N = (size_t)d.n * d.G * d.M;
+  DevBuf xb, yb;
+  int st;
+  if ((st = dev_alloc(xb, N * 8, nullptr)) || (st = dev_alloc(yb, N * 8, nullptr))) return st;
+  PGPU_CUDA(cudaMemcpyAsync(xb.ptr, x, N * 8, cudaMemcpyHostToDevice, p->stream));
+  if ((st = apply_R<double>(p, make_op<double>(d), xb.as<double>(), yb.as<double>(), d.phi0.as<double>()))) return st;
+  PGPU_CUDA(cudaMemcpyAsync(y, yb.ptr, N * 8, cudaMemcpyDeviceToHost, p->stream));
+  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  return PGPU_OK;
+}
+
+}  // extern "C"

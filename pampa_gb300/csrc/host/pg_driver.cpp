@@ -276,6 +276,12 @@ void pampa_get_field_size(const char name[], int* size, int* error) {
   *error = s ? s->fieldSize(std::string(name), *size) : 1;
 }
 
+void pampa_get_problem(pgpu_problem** problem, int* error) {
+  auto* s = dynamic_cast<pg::NeutronicSolver*>(g_pampa.solver());
+  *error = s ? s->problem(problem) : 1;
+  if (*error > 0) std::printf("Error in pampa_get_problem().\n");
+}
+
 void pampa_get_solve_stats(int* outer, int* inner, double* seconds, int* error) {
   auto* s = dynamic_cast<pg::NeutronicSolver*>(g_pampa.solver());
   *error = s ? 0 : 1;

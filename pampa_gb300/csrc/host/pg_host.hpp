@@ -163,6 +163,7 @@ class NeutronicSolver : public Solver {
   int output(int n) const override;
   int finalize() override;
   double keff() const { return keff_; }
+  int problem(pgpu_problem** out);
   const pgpu_stats& stats() const { return stats_; }
 
  protected:

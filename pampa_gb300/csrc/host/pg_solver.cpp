@@ -141,6 +141,12 @@ int NeutronicSolver::output(int n) const {
   return 0;
 }
 
+int NeutronicSolver::problem(pgpu_problem** out) {
+  if (!problem_) PG_TRY(buildProblem(), "unable to build the coefficient matrices");
+  *out = problem_;
+  return 0;
+}
+
 int NeutronicSolver::finalize() {
   if (problem_) pgpu_problem_destroy(problem_);
   problem_ = nullptr;
