@@ -104,6 +104,7 @@ typedef struct {
   int max_inner;        /* inner Krylov iteration cap per solve      (default 2000)    */
   double power;         /* normalisation target, NeutronicSolver.hxx:17 (default 1.0)  */
   int verbose;          /* print one line per outer iteration when > 0                 */
+  int profile;          /* time the dominant kernel with CUDA events (default 0)       */
 } pgpu_options;
 
 typedef struct {
@@ -114,6 +115,13 @@ typedef struct {
   double residual;       /* final relative eigen-residual estimate                       */
   double seconds;        /* device time of the solve (CUDA events)                       */
   int status;            /* PGPU_* code                                                  */
+  long long launches;    /* kernels launched by the solve                                */
+  /* Dominant kernel (transport sweep for SN, SpMV for diffusion), filled when
+   * options.profile != 0: device seconds inside it (CUDA events on the launching
+   * stream), its launches, and the algorithmic bytes those launches must move. */
+  double kernel_seconds;
+  long long kernel_launches;
+  double kernel_bytes;
 } pgpu_stats;
 
 /* Fill *opt with the defaults listed above. */

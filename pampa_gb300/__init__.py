@@ -38,13 +38,14 @@ class PampaError(RuntimeError):
 class pgpu_options(C.Structure):
     _fields_ = [("precision", C.c_int), ("tol_k", C.c_double), ("tol_flux", C.c_double),
                 ("max_outer", C.c_int), ("max_inner", C.c_int), ("power", C.c_double),
-                ("verbose", C.c_int)]
+                ("verbose", C.c_int), ("profile", C.c_int)]
 
 
 class pgpu_stats(C.Structure):
     _fields_ = [("keff", C.c_double), ("outer_iterations", C.c_int), ("inner_iterations", C.c_int),
                 ("sweeps", C.c_int), ("residual", C.c_double), ("seconds", C.c_double),
-                ("status", C.c_int)]
+                ("status", C.c_int), ("launches", C.c_longlong), ("kernel_seconds", C.c_double),
+                ("kernel_launches", C.c_longlong), ("kernel_bytes", C.c_double)]
 
 
 _P = C.POINTER

@@ -66,9 +66,21 @@ int pgpu_problem_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* sta
   if (!stats) stats = &local;
   std::memset(stats, 0, sizeof(*stats));
   PGPU_CUDA(cudaSetDevice(p->device));
+  p->launches = 0;
+  p->profile = opt->profile != 0;
+  p->prof_bytes = 0.0;
+  p->prof_launches = 0;
   int st = PGPU_ERR_INVALID;
   if (p->kind == 1) st = pgpu::diffusion_solve(p, opt, stats);
   else if (p->kind == 2) st = pgpu::sn_solve(p, opt, stats);
+  cudaStreamSynchronize(p->stream);
+  stats->launches = p->launches;
+  if (p->profile) {
+    stats->kernel_seconds = pgpu::prof_collect(p);
+    stats->kernel_launches = p->prof_launches;
+    stats->kernel_bytes = p->prof_bytes;
+  }
+  p->profile = false;
   stats->status = st;
   p->solved = (st == PGPU_OK);
   if (p->solved) p->keff = stats->keff;

@@ -422,10 +422,10 @@ int make_fp32(pgpu_problem* p) {
   if ((st = dev_alloc(d.vol32, (size_t)d.n * 4, &p->bytes))) return st;
   if ((st = dev_alloc(d.ss32, (size_t)d.nm * d.G * d.G * 4, &p->bytes))) return st;
   cudaStream_t s = p->stream;
-  k_convert<double, float><<<grid_for((long long)d.F * nG), kThreads, 0, s>>>((long long)d.F * nG, d.off64.as<double>(), d.off32.as<float>());
-  k_convert<double, float><<<grid_for(nG), kThreads, 0, s>>>(nG, d.diag64.as<double>(), d.diag32.as<float>());
-  k_convert<double, float><<<grid_for(d.n), kThreads, 0, s>>>(d.n, d.vol64.as<double>(), d.vol32.as<float>());
-  k_convert<double, float><<<1, kThreads, 0, s>>>((long long)d.nm * d.G * d.G, d.ss64.as<double>(), d.ss32.as<float>());
+  launch(p, k_convert<double, float>, grid_for((long long)d.F * nG), kThreads, s, (long long)d.F * nG, d.off64.as<double>(), d.off32.as<float>());
+  launch(p, k_convert<double, float>, grid_for(nG), kThreads, s, nG, d.diag64.as<double>(), d.diag32.as<float>());
+  launch(p, k_convert<double, float>, grid_for(d.n), kThreads, s, d.n, d.vol64.as<double>(), d.vol32.as<float>());
+  launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G * d.G, d.ss64.as<double>(), d.ss32.as<float>());
   for (int k = 0; k < 9; k++)
     if ((st = dev_alloc(d.w32[k], nG * 4, &p->bytes))) return st;
   if ((st = dev_alloc(d.r32, nG * 4, &p->bytes))) return st;
@@ -447,26 +447,38 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
     *s = w[5].as<T>(), *t = w[6].as<T>(), *phat = w[7].as<T>(), *shat = w[8].as<T>();
   BiScal* sc = d.bscal.as<BiScal>();
   cudaStream_t st = p->stream;
-  k_bicg_init<T><<<gN, kThreads, 0, st>>>(N, rin, r, rhat, x, pp, v, sc, slots_of<1>(d), rtol, max_iters);
+  launch(p, k_bicg_init<T>, gN, kThreads, st, N, rin, r, rhat, x, pp, v, sc, slots_of<1>(d), rtol, max_iters);
   PGPU_CUDA(cudaGetLastError());
   BiScal hs;
-  int chunk = 4;
+  // When profiling, iterations go one per chunk so no timed SpMV launch is a no-op.
+  int chunk = p->profile ? 1 : 4;
+  // Algorithmic bytes of one SpMV fused with its dot product: per row the diagonal, the
+  // F face coefficients, x, y and the dot partner (F + 4 values), plus per cell the F
+  // neighbour indices, the material id and the volume.
+  const double sv = (double)sizeof(T);
+  const double spmv_bytes = (double)N * (d.F + 4) * sv + (double)d.n * (4.0 * d.F + 4.0 + sv);
   for (int launched = 0; launched < max_iters; launched += chunk) {
     for (int c = 0; c < chunk; c++) {
-      k_bicg_p<T><<<gC, kThreads, 0, st>>>(A, r, pp, v, phat, sc);
-      k_bicg_v<T><<<gN, kThreads, 0, st>>>(A, phat, v, rhat, sc, slots_of<1>(d));
-      k_bicg_s<T><<<gC, kThreads, 0, st>>>(A, r, v, s, shat, sc);
-      k_bicg_t<T><<<gN, kThreads, 0, st>>>(A, shat, t, s, sc, slots_of<2>(d));
-      k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phat, shat, s, t, rhat, sc, slots_of<2>(d));
+      cudaEvent_t e0;
+      launch(p, k_bicg_p<T>, gC, kThreads, st, A, r, pp, v, phat, sc);
+      prof_begin(p, &e0);
+      launch(p, k_bicg_v<T>, gN, kThreads, st, A, phat, v, rhat, sc, slots_of<1>(d));
+      prof_end(p, e0, 1, 0.0);
+      launch(p, k_bicg_s<T>, gC, kThreads, st, A, r, v, s, shat, sc);
+      prof_begin(p, &e0);
+      launch(p, k_bicg_t<T>, gN, kThreads, st, A, shat, t, s, sc, slots_of<2>(d));
+      prof_end(p, e0, 1, 0.0);
+      launch(p, k_bicg_x<T>, gN, kThreads, st, N, x, r, phat, shat, s, t, rhat, sc, slots_of<2>(d));
     }
     PGPU_CUDA(cudaGetLastError());
     PGPU_CUDA(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, st));
     PGPU_CUDA(cudaStreamSynchronize(st));
     if (hs.converged) break;
-    if (chunk < 16) chunk *= 2;
+    if (chunk < 16 && !p->profile) chunk *= 2;
   }
   PGPU_CUDA(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, st));
   PGPU_CUDA(cudaStreamSynchronize(st));
+  p->prof_bytes += p->profile ? 2.0 * hs.iters * spmv_bytes : 0.0;
   *iters_out = hs.iters;
   if (!(hs.rr == hs.rr)) return fail(PGPU_ERR_NAN, "NaN in the inner Krylov solve");
   return PGPU_OK;
@@ -500,9 +512,9 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   std::memset(&init, 0, sizeof(init));
   init.k = 1.0;
   PGPU_CUDA(cudaMemcpyAsync(dos, &init, sizeof(init), cudaMemcpyHostToDevice, s));
-  k_fill<<<gN, kThreads, 0, s>>>(N, d.y.as<double>(), 1.0);
-  k_fill<<<gC, kThreads, 0, s>>>(n, d.fs_old.as<double>(), 0.0);
-  k_fission_total<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
+  launch(p, k_fill, gN, kThreads, s, N, d.y.as<double>(), 1.0);
+  launch(p, k_fill, gC, kThreads, s, n, d.fs_old.as<double>(), 0.0);
+  launch(p, k_fission_total, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
                                           d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d));
   // the first total only normalises the start vector: keep k = 1
   OuterScal os;
@@ -510,7 +522,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   if (os.nonfinite || os.S <= 0.0) return fail(PGPU_ERR_INVALID, "no fission source in the initial flux");
   os.k = 1.0;
   PGPU_CUDA(cudaMemcpyAsync(dos, &os, sizeof(os), cudaMemcpyHostToDevice, s));
-  k_normalize_source<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.chi.as<double>(), d.y.as<double>(),
+  launch(p, k_normalize_source, gC, kThreads, s, n, G, d.mat.as<int>(), d.chi.as<double>(), d.y.as<double>(),
                                              d.x.as<double>(), d.fs.as<double>(), d.fs_old.as<double>(),
                                              d.b.as<double>(), dos, slots_of<2>(d));
   PGPU_CUDA(cudaGetLastError());
@@ -523,7 +535,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
     // inner solve R y = b by refinement: r = b - R y, correction solve, y += d
     const double tol_in = fmin(1e-3, fmax(1e-13, 0.02 * fmin(change, dk * 1e3)));
     for (int ref = 0; ref < 50; ref++) {
-      k_residual<float><<<gN, kThreads, 0, s>>>(A, d.b.as<double>(), d.y.as<double>(), d.r64.as<double>(),
+      launch(p, k_residual<float>, gN, kThreads, s, A, d.b.as<double>(), d.y.as<double>(), d.r64.as<double>(),
                                                 mixed ? d.r32.as<float>() : (float*)nullptr, dos, slots_of<2>(d));
       if ((st = read_outer(p, os))) return st;
       if (!(os.rr == os.rr)) return fail(PGPU_ERR_NAN, "NaN in the residual");
@@ -535,18 +547,18 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
         DiffOp<float> A32 = op32(d);
         const double rt = fmax(tol_in / rel, 2e-5);
         if ((st = bicgstab<float>(p, A32, d.w32, d.r32.as<float>(), fmin(rt, 0.5), opt->max_inner, &it))) return st;
-        k_axpy_update<float><<<gN, kThreads, 0, s>>>(N, d.y.as<double>(), d.w32[0].as<float>());
+        launch(p, k_axpy_update<float>, gN, kThreads, s, N, d.y.as<double>(), d.w32[0].as<float>());
       } else {
         const double rt = fmax(0.5 * tol_in / rel, 1e-15);
         if ((st = bicgstab<double>(p, A, d.w64, d.r64.as<double>(), fmin(rt, 0.5), opt->max_inner, &it))) return st;
-        k_axpy_update<double><<<gN, kThreads, 0, s>>>(N, d.y.as<double>(), d.w64[0].as<double>());
+        launch(p, k_axpy_update<double>, gN, kThreads, s, N, d.y.as<double>(), d.w64[0].as<double>());
       }
       inner_total += it;
       if (it == 0) break;
     }
-    k_fission_total<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
+    launch(p, k_fission_total, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
                                             d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d));
-    k_normalize_source<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.chi.as<double>(), d.y.as<double>(),
+    launch(p, k_normalize_source, gC, kThreads, s, n, G, d.mat.as<int>(), d.chi.as<double>(), d.y.as<double>(),
                                                d.x.as<double>(), d.fs.as<double>(), d.fs_old.as<double>(),
                                                d.b.as<double>(), dos, slots_of<2>(d));
     PGPU_CUDA(cudaGetLastError());
@@ -568,9 +580,9 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   if (!converged) status = PGPU_ERR_NOT_CONVERGED;
 
   // normalisation and power (NeutronicSolver.cxx:46-116)
-  k_power_norm<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol64.as<double>(), d.ksf.as<double>(),
+  launch(p, k_power_norm, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.ksf.as<double>(),
                                        d.x.as<double>(), dos, slots_of<1>(d));
-  k_power_fields<<<gC, kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol64.as<double>(), d.ksf.as<double>(),
+  launch(p, k_power_fields, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.ksf.as<double>(),
                                          d.nsf.as<double>(), d.x.as<double>(), opt->power, d.phi.as<double>(),
                                          d.q.as<double>(), d.P.as<double>(), dos, slots_of<2>(d));
   PGPU_CUDA(cudaGetLastError());
@@ -691,7 +703,7 @@ int pgpu_diffusion_apply(pgpu_problem* p, const double* x, double* y) {
   DiffusionData& d = *p->diff;
   const size_t N = (size_t)d.n * d.G;
   PGPU_CUDA(cudaMemcpyAsync(d.x.ptr, x, N * 8, cudaMemcpyHostToDevice, p->stream));
-  k_apply<<<grid_for(N), kThreads, 0, p->stream>>>(op64(d), d.x.as<double>(), d.y.as<double>());
+  launch(p, k_apply, grid_for(N), kThreads, p->stream, op64(d), d.x.as<double>(), d.y.as<double>());
   PGPU_CUDA(cudaGetLastError());
   PGPU_CUDA(cudaMemcpyAsync(y, d.y.ptr, N * 8, cudaMemcpyDeviceToHost, p->stream));
   PGPU_CUDA(cudaStreamSynchronize(p->stream));

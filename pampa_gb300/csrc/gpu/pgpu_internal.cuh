@@ -162,9 +162,57 @@ struct pgpu_problem {
   double keff = 0.0;
   pgpu::DiffusionData* diff = nullptr;
   pgpu::SNData* sn = nullptr;
+  // kernel launches issued by this problem (all kernels), and the optional timing of the
+  // dominant kernel (transport sweep for SN, SpMV for diffusion) with CUDA events on the
+  // problem's stream
+  long long launches = 0;
+  bool profile = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
+  double prof_bytes = 0.0;
+  long long prof_launches = 0;
 };
 
 namespace pgpu {
+
+// Launch a kernel on `s` and count it against the problem.
+template <typename... KArgs, typename... Args>
+inline void launch(pgpu_problem* p, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
+                   Args... args) {
+  kernel<<<grid, block, 0, s>>>(args...);
+  p->launches++;
+}
+
+// Record an event pair around a dominant-kernel region when profiling is on.
+inline void prof_begin(pgpu_problem* p, cudaEvent_t* e) {
+  *e = nullptr;
+  if (!p->profile) return;
+  cudaEventCreate(e);
+  cudaEventRecord(*e, p->stream);
+}
+
+inline void prof_end(pgpu_problem* p, cudaEvent_t e0, long long launches, double bytes) {
+  if (!p->profile || !e0) return;
+  cudaEvent_t e1;
+  cudaEventCreate(&e1);
+  cudaEventRecord(e1, p->stream);
+  p->prof_events.push_back({e0, e1});
+  p->prof_launches += launches;
+  p->prof_bytes += bytes;
+}
+
+// Sum the recorded regions (stream must be synchronised) and release the events.
+inline double prof_collect(pgpu_problem* p) {
+  double s = 0.0;
+  for (auto& pr : p->prof_events) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, pr.first, pr.second);
+    s += ms * 1e-3;
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
+  p->prof_events.clear();
+  return s;
+}
 
 // Per-kind entry points implemented in pgpu_diffusion.cu / pgpu_sn.cu.
 int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats);

@@ -96,6 +96,7 @@ struct SNData {
   DevBuf partials, ticket, oscal, hbuf;
   // Krylov storage: basis [(m+1)][len], plus work vectors
   DevBuf basis, wvec, xvec, rhs, tmp, scat, phtmp;
+  DevBuf x64, r64, rhs64;  // FP64 state, residual and right-hand side of the inner system
   size_t basis_len = 0;
   int restart = 0;
   int krylov_prec = -1;  // element size of the Krylov storage (4 or 8)
@@ -104,7 +105,24 @@ struct SNData {
 struct SNOuter {
   double k, S, change, p0, total_power;
   int negatives, nonfinite;
+  unsigned long long amax_phi, amax_psi;  // bit patterns of max |phi0|, max |psi| (>= 0)
 };
+
+// Entries of the converged flux whose exact value is zero (e.g. fast flux in a source-free,
+// non-scattering region) come out of an iterative solve as +-(solver tolerance).  The
+// reference, which factors R exactly, gets exact zeros there and rejects any negative
+// entry.  Entries within kZeroFlush of the maximum are therefore set to zero; anything
+// more negative is a genuine negative flux and is reported.
+constexpr double kZeroFlush = 1e-9;
+
+template <typename T>
+__global__ void k_absmax(long long N, const T* __restrict__ v, unsigned long long* out) {
+  double m = 0.0;
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    m = fmax(m, fabs((double)v[l]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
 
 // ---------------------------------------------------------------------------------
 // Kernels
@@ -355,6 +373,13 @@ __global__ void k_fill(long long N, T* a, T v) {
     a[l] = v;
 }
 
+// x (FP64) += u (precision T)
+template <typename T>
+__global__ void k_add_cast(long long N, const T* __restrict__ u, double* x) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    x[l] += (double)u[l];
+}
+
 // x += u
 template <typename T>
 __global__ void k_add(long long N, const T* __restrict__ u, T* x) {
@@ -428,6 +453,7 @@ __global__ void k_sn_power_fields(int n, int G, const int* __restrict__ mat, con
                                   double* P, SNOuter* os, ReduceSlots<2> slots) {
   const double f = 4.0 * M_PI * power / os->p0;
   const double k = os->k;
+  const double flush = kZeroFlush * __longlong_as_double((long long)os->amax_phi) * fabs(f);
   double acc[2] = {0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double* ks = ksf + (size_t)mat[i] * G;
@@ -436,6 +462,7 @@ __global__ void k_sn_power_fields(int n, int G, const int* __restrict__ mat, con
     double qi = 0.0, Pi = 0.0;
     for (int g = 0; g < G; g++) {
       double v = phi0[(size_t)i * G + g] * f;
+      if (v < 0.0 && v >= -flush) v = 0.0;
       phi[(size_t)i * G + g] = v;
       if (v < 0.0) acc[1] += 1.0;
       qi += v * ks[g] * V;
@@ -455,9 +482,11 @@ __global__ void k_sn_power_fields(int n, int G, const int* __restrict__ mat, con
 // psi *= power / (p0 / 4 pi)  (SNSolver::normalizeAngularFlux); counts negatives.
 __global__ void k_sn_psi_norm(long long N, double* psi, double power, SNOuter* os, ReduceSlots<1> slots) {
   const double f = 4.0 * M_PI * power / os->p0;
+  const double flush = kZeroFlush * __longlong_as_double((long long)os->amax_psi) * fabs(f);
   double acc[1] = {0.0};
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
     double v = psi[l] * f;
+    if (v < 0.0 && v >= -flush) v = 0.0;
     psi[l] = v;
     if (v < 0.0) acc[0] += 1.0;
   }
@@ -631,7 +660,7 @@ int make_fp32(pgpu_problem* p) {
     const long long cnt = (long long)(src.bytes / 8);
     int st = dev_alloc(dst, (size_t)cnt * 4, &p->bytes);
     if (st) return st;
-    k_cast<double, float><<<grid_for(cnt), kThreads, 0, s>>>(cnt, src.as<double>(), dst.as<float>());
+    launch(p, k_cast<double, float>, grid_for(cnt), kThreads, s, cnt, src.as<double>(), dst.as<float>());
     return PGPU_OK;
   };
   int st;
@@ -657,12 +686,21 @@ template <typename T>
 int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd, T* psi) {
   SNData& d = *p->sn;
   const Schedule& S = d.sched;
+  cudaEvent_t e0;
+  prof_begin(p, &e0);
   for (int L = 0; L < S.nlev; L++) {
     dim3 grid(S.grid_x[L], S.npat);
-    k_sweep_level<T><<<grid, kThreads, 0, p->stream>>>(
+    launch(p, k_sweep_level<T>, grid, kThreads, p->stream,
         A, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
         d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), src, iso, bnd, psi);
   }
+  // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
+  // direction update (2 s_v), the source read per cell-group (s_v, or s_v per update for
+  // an angular source), the scalar-flux moment written per cell-group (s_v) and the
+  // material id per cell-group (4 B).
+  const double sv = (double)sizeof(T);
+  const double N = (double)d.n * d.G * d.M, nG = (double)d.n * d.G;
+  prof_end(p, e0, S.nlev, N * 2.0 * sv + nG * (2.0 * sv + 4.0) + (iso ? 0.0 : N * sv));
   PGPU_CUDA(cudaGetLastError());
   sweeps_done++;
   return PGPU_OK;
@@ -682,13 +720,13 @@ int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y)
   const int nG = d.n * d.G;
   T* q = d.scat.as<T>();
   T* psi = psi_work<T>(d);
-  k_scatter_source<T><<<grid_for(nG), kThreads, 0, p->stream>>>(A, x, b, q);
+  launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q);
   int st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi);
   if (st) return st;
-  k_moment<T><<<grid_for((long long)nG * 32), kThreads, 0, p->stream>>>(nG, d.M, A.w, psi, y);
+  launch(p, k_moment<T>, grid_for((long long)nG * 32), kThreads, p->stream, nG, d.M, A.w, psi, y);
   if (d.nrefl) {
     const long long nb = (long long)d.nrefl * d.G * d.M;
-    k_reflect_extract<T><<<grid_for(nb), kThreads, 0, p->stream>>>(A, d.nrefl, d.d_slot_cell.as<int>(),
+    launch(p, k_reflect_extract<T>, grid_for(nb), kThreads, p->stream, A, d.nrefl, d.d_slot_cell.as<int>(),
                                                                    d.d_slot_face.as<int>(), psi, y + nG);
   }
   PGPU_CUDA(cudaGetLastError());
@@ -701,8 +739,8 @@ int apply_R(pgpu_problem* p, const SNOp<T>& A, const T* x, T* y, T* tmp_phi0) {
   SNData& d = *p->sn;
   const int nG = d.n * d.G;
   const long long N = (long long)nG * d.M;
-  k_moment<T><<<grid_for((long long)nG * 32), kThreads, 0, p->stream>>>(nG, d.M, A.w, x, tmp_phi0);
-  k_apply_R<T><<<grid_for(N), kThreads, 0, p->stream>>>(A, x, tmp_phi0, y);
+  launch(p, k_moment<T>, grid_for((long long)nG * 32), kThreads, p->stream, nG, d.M, A.w, x, tmp_phi0);
+  launch(p, k_apply_R<T>, grid_for(N), kThreads, p->stream, A, x, tmp_phi0, y);
   PGPU_CUDA(cudaGetLastError());
   return PGPU_OK;
 }
@@ -719,7 +757,9 @@ int ensure_krylov(pgpu_problem* p, size_t len, int restart, int es) {
   if ((st = dev_alloc(d.partials, (size_t)(restart + 4) * kMaxBlocks * 8, &p->bytes))) return st;
   if ((st = dev_alloc(d.ticket, (size_t)(restart + 4) * 4, &p->bytes))) return st;
   if ((st = dev_alloc(d.hbuf, (size_t)4 * (restart + 4) * 8, &p->bytes))) return st;
-  if ((st = dev_alloc(d.scat, (size_t)d.n * d.G * es, &p->bytes))) return st;
+  // the scattering source is used by FP64 residual sweeps and by correction sweeps in
+  // either precision: size it for FP64
+  if ((st = dev_alloc(d.scat, (size_t)d.n * d.G * 8, &p->bytes))) return st;
   if ((st = dev_alloc(d.phtmp, (size_t)d.n * d.G * es, &p->bytes))) return st;
   PGPU_CUDA(cudaMemsetAsync(d.ticket.ptr, 0, (size_t)(restart + 4) * 4, p->stream));
   d.basis_len = len;
@@ -732,15 +772,18 @@ int ensure_krylov(pgpu_problem* p, size_t len, int restart, int es) {
 // residual(r) computes b - A x for the current x; applyA(v, w) computes w = A v;
 // post(u) adds the correction for the Krylov combination u to x.  The small Hessenberg
 // problem is solved on the host with Givens rotations.
-template <typename T, typename Res, typename App, typename Post>
-int gmres(pgpu_problem* p, long long len, Res residual, App applyA, Post post, double tol_abs, int max_it,
-          int* iters, double* res_out) {
+// GMRES(m) with classical Gram-Schmidt and one re-orthogonalisation (CGS2) for the
+// correction equation A d = r, d starting at zero.  applyA(v, w) computes w = A v.
+// Stops when ||r - A d|| <= max(rtol ||r||, atol) or after max_it Arnoldi steps.  The
+// small Hessenberg least-squares problem is solved on the host with Givens rotations.
+template <typename T, typename App>
+int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, double rtol, double atol,
+          int max_it, int* iters, double* res_out) {
   SNData& d = *p->sn;
   const int m = d.restart;
   cudaStream_t s = p->stream;
   T* V = d.basis.as<T>();
   T* w = d.wvec.as<T>();
-  T* u = d.tmp.as<T>();
   double* h1 = d.hbuf.as<double>();
   double* h2 = h1 + (m + 4);
   double* hn = h2 + (m + 4);
@@ -748,18 +791,29 @@ int gmres(pgpu_problem* p, long long len, Res residual, App applyA, Post post, d
   const int gx = grid_for(len);
   std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hh(m + 2), hh2(m + 2);
   int total = 0, st;
-  double res = 0.0;
+  double res = 0.0, tol = 0.0;
+  bool first = true;
   ReduceSlots<1> nslot{d.partials.as<double>() + (size_t)(m + 2) * kMaxBlocks, d.ticket.as<unsigned int>() + (m + 2)};
+  PGPU_CUDA(cudaMemsetAsync(dvec, 0, len * sizeof(T), s));
   while (true) {
-    if ((st = residual(V))) return st;
-    k_norm2<T><<<gx, kThreads, 0, s>>>(len, V, hn, nslot);
+    if (first) {
+      PGPU_CUDA(cudaMemcpyAsync(V, r, len * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    } else {
+      if ((st = applyA(dvec, w))) return st;
+      launch(p, k_sub<T>, gx, kThreads, s, len, r, (const T*)w, V);
+    }
+    launch(p, k_norm2<T>, gx, kThreads, s, len, (const T*)V, hn, nslot);
     double beta;
     PGPU_CUDA(cudaMemcpyAsync(&beta, hn, 8, cudaMemcpyDeviceToHost, s));
     PGPU_CUDA(cudaStreamSynchronize(s));
-    if (!(beta == beta)) return fail(PGPU_ERR_NAN, "NaN in the transport residual");
+    if (!(beta == beta)) return fail(PGPU_ERR_NAN, "NaN in the transport correction solve");
+    if (first) {
+      tol = std::fmax(rtol * beta, atol);
+      first = false;
+    }
     res = beta;
-    if (beta <= tol_abs || total >= max_it) break;
-    k_scale_to<T><<<gx, kThreads, 0, s>>>(len, V, hn, 1, V);
+    if (beta <= tol || total >= max_it) break;
+    launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)V, (const double*)hn, 1, V);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
@@ -767,12 +821,12 @@ int gmres(pgpu_problem* p, long long len, Res residual, App applyA, Post post, d
       T* vj = V + (size_t)j * len;
       if ((st = applyA(vj, w))) return st;
       dim3 gd(std::min(gx, 512), j + 1);
-      k_dot_many<T><<<gd, kThreads, 0, s>>>(len, V, len, w, h1, d.partials.as<double>(), d.ticket.as<unsigned int>());
-      k_sub_many<T><<<gx, kThreads, 0, s>>>(len, V, len, j + 1, h1, w);
-      k_dot_many<T><<<gd, kThreads, 0, s>>>(len, V, len, w, h2, d.partials.as<double>(), d.ticket.as<unsigned int>());
-      k_sub_many<T><<<gx, kThreads, 0, s>>>(len, V, len, j + 1, h2, w);
-      k_norm2<T><<<gx, kThreads, 0, s>>>(len, w, hn, nslot);
-      k_scale_to<T><<<gx, kThreads, 0, s>>>(len, w, hn, 1, V + (size_t)(j + 1) * len);
+      launch(p, k_dot_many<T>, gd, kThreads, s, len, (const T*)V, len, (const T*)w, h1, d.partials.as<double>(), d.ticket.as<unsigned int>());
+      launch(p, k_sub_many<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, w);
+      launch(p, k_dot_many<T>, gd, kThreads, s, len, (const T*)V, len, (const T*)w, h2, d.partials.as<double>(), d.ticket.as<unsigned int>());
+      launch(p, k_sub_many<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, w);
+      launch(p, k_norm2<T>, gx, kThreads, s, len, (const T*)w, hn, nslot);
+      launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)w, (const double*)hn, 1, V + (size_t)(j + 1) * len);
       PGPU_CUDA(cudaGetLastError());
       PGPU_CUDA(cudaMemcpyAsync(hh.data(), h1, (j + 1) * 8, cudaMemcpyDeviceToHost, s));
       PGPU_CUDA(cudaMemcpyAsync(hh2.data(), h2, (j + 1) * 8, cudaMemcpyDeviceToHost, s));
@@ -789,24 +843,21 @@ int gmres(pgpu_problem* p, long long len, Res residual, App applyA, Post post, d
         col[k] = a;
         col[k + 1] = b;
       }
-      double r = std::hypot(col[j], col[j + 1]);
-      if (r == 0.0 || !(r == r)) {
-        j++;
-        break;
-      }
-      cs[j] = col[j] / r;
-      sn[j] = col[j + 1] / r;
-      col[j] = r;
+      double rr = std::hypot(col[j], col[j + 1]);
+      if (rr == 0.0 || !(rr == rr)) break;
+      cs[j] = col[j] / rr;
+      sn[j] = col[j + 1] / rr;
+      col[j] = rr;
       col[j + 1] = 0.0;
       g[j + 1] = -sn[j] * g[j];
       g[j] = cs[j] * g[j];
       res = std::fabs(g[j + 1]);
-      if (res <= tol_abs || hnext == 0.0) {
+      if (res <= tol || hnext == 0.0) {
         j++;
         break;
       }
     }
-    // back substitution H y = g
+    if (j == 0) break;
     std::vector<double> y(j, 0.0);
     for (int k = j - 1; k >= 0; k--) {
       double t = g[k];
@@ -814,13 +865,11 @@ int gmres(pgpu_problem* p, long long len, Res residual, App applyA, Post post, d
       y[k] = t / H[(size_t)k * (m + 1) + k];
     }
     PGPU_CUDA(cudaMemcpyAsync(yv, y.data(), j * 8, cudaMemcpyHostToDevice, s));
-    PGPU_CUDA(cudaMemsetAsync(u, 0, len * sizeof(T), s));
-    k_add_many<T><<<gx, kThreads, 0, s>>>(len, V, len, j, yv, u);
+    launch(p, k_add_many<T>, gx, kThreads, s, len, (const T*)V, len, j, (const double*)yv, dvec);
     PGPU_CUDA(cudaGetLastError());
-    if ((st = post(u))) return st;
-    PGPU_CUDA(cudaStreamSynchronize(s));
-    if (res <= tol_abs || total >= max_it) break;
+    if (res <= tol || total >= max_it) break;
   }
+  PGPU_CUDA(cudaStreamSynchronize(s));
   *iters = total;
   *res_out = res;
   return PGPU_OK;
@@ -829,9 +878,9 @@ int gmres(pgpu_problem* p, long long len, Res residual, App applyA, Post post, d
 template <typename T>
 int norm_of(pgpu_problem* p, long long len, const T* x, double* out) {
   SNData& d = *p->sn;
-  double* hn = d.hbuf.as<double>() + 3 * (d.restart + 4);
+  double* hn = d.hbuf.as<double>() + 3 * (d.restart + 4) + (d.restart + 2);
   ReduceSlots<1> slot{d.partials.as<double>() + (size_t)(d.restart + 3) * kMaxBlocks, d.ticket.as<unsigned int>() + (d.restart + 3)};
-  k_norm2<T><<<grid_for(len), kThreads, 0, p->stream>>>(len, x, hn, slot);
+  launch(p, k_norm2<T>, grid_for(len), kThreads, p->stream, len, x, hn, slot);
   PGPU_CUDA(cudaMemcpyAsync(out, hn, 8, cudaMemcpyDeviceToHost, p->stream));
   PGPU_CUDA(cudaStreamSynchronize(p->stream));
   return PGPU_OK;
@@ -843,6 +892,13 @@ int read_outer(pgpu_problem* p, SNOuter& os) {
   return PGPU_OK;
 }
 
+// Power iteration on R x = (1/k) F x.  The state x (FP64) is [phi0 | reflective inflow]
+// in scalar-flux space or psi in angular space.  Every outer iteration evaluates the FP64
+// residual of the inner system, solves the correction equation in precision T (FP64, or
+// FP32 for mixed precision: iterative refinement), updates x, and renormalises the
+// fission source.  The correction solve reduces the FP64 residual by kEta.
+constexpr double kEta = 0.02;
+
 template <typename T>
 int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   SNData& d = *p->sn;
@@ -851,18 +907,29 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   const long long N = (long long)nG * M;
   const bool phi_space = d.upwind && !d.use_ls;
   const long long len = phi_space ? (long long)nG + (long long)d.nrefl * G * M : N;
-  const int restart = phi_space ? 30 : 20;
+  const int restart = 30;
   int st;
   if ((st = ensure_krylov(p, (size_t)len, restart, (int)sizeof(T)))) return st;
+  if (d.x64.bytes < (size_t)len * 8) {
+    if ((st = dev_alloc(d.x64, (size_t)len * 8, &p->bytes)) || (st = dev_alloc(d.r64, (size_t)len * 8, &p->bytes)) ||
+        (st = dev_alloc(d.rhs64, (size_t)len * 8, &p->bytes)))
+      return st;
+  }
   SNOp<T> A = make_op<T>(d);
   SNOp<double> A64 = make_op<double>(d);
   SNOuter* dos = d.oscal.as<SNOuter>();
-  T* x = d.xvec.as<T>();
-  T* rhs = d.rhs.as<T>();  // angular-space right-hand side, or the FP32 copy of b
-  double* bsrc = d.src.as<double>();  // FP64 isotropic source b [nG] lives in src
+  double* x64 = d.x64.as<double>();
+  double* r64 = d.r64.as<double>();
+  double* rhs64 = d.rhs64.as<double>();
+  T* rT = d.rhs.as<T>();    // correction right-hand side in precision T
+  T* dT = d.tmp.as<T>();    // correction in precision T
+  T* phT = d.phtmp.as<T>();
+  double* bsrc = d.src.as<double>();  // isotropic fission source b = chi fs / k, [n*G]
   double* phi0 = d.phi0.as<double>();
+  double* ph64 = d.phi.as<double>();  // FP64 scratch [n*G] until the final fields
   ReduceSlots<1> s1{d.partials.as<double>(), d.ticket.as<unsigned int>()};
   ReduceSlots<2> s2{d.partials.as<double>(), d.ticket.as<unsigned int>()};
+  const int gl = grid_for(len), gn = grid_for(n), gG = grid_for(nG);
   sweeps_done = 0;
 
   cudaEvent_t e0, e1;
@@ -870,95 +937,89 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   PGPU_CUDA(cudaEventCreate(&e1));
   PGPU_CUDA(cudaEventRecord(e0, s));
 
-  // flat start
+  // flat start: phi0 = 1; x = [1 | 0] or psi = 1; k = 1
   SNOuter init;
   std::memset(&init, 0, sizeof(init));
   init.k = 1.0;
   PGPU_CUDA(cudaMemcpyAsync(dos, &init, sizeof(init), cudaMemcpyHostToDevice, s));
-  // flat start: phi0 = 1 and x = [1 | 0] (scalar-flux space) or psi = 1 (angular space)
-  k_fill<double><<<grid_for(nG), kThreads, 0, s>>>(nG, phi0, 1.0);
-  PGPU_CUDA(cudaMemsetAsync(x, 0, len * sizeof(T), s));
-  k_fill<T><<<grid_for(phi_space ? nG : N), kThreads, 0, s>>>(phi_space ? nG : N, x, T(1));
-  k_sn_fission<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol.as<double>(), d.nsf.as<double>(), phi0,
-                                                 d.fs.as<double>(), dos, s1);
+  launch(p, k_fill<double>, gG, kThreads, s, (long long)nG, phi0, 1.0);
+  PGPU_CUDA(cudaMemsetAsync(x64, 0, len * 8, s));
+  launch(p, k_fill<double>, grid_for(phi_space ? nG : N), kThreads, s, phi_space ? (long long)nG : N, x64, 1.0);
+  launch(p, k_sn_fission, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.vol.as<double>(),
+         (const double*)d.nsf.as<double>(), (const double*)phi0, d.fs.as<double>(), dos, s1);
   SNOuter os;
   if ((st = read_outer(p, os))) return st;
   if (os.nonfinite || os.S <= 0.0) return fail(PGPU_ERR_INVALID, "no fission source in the initial flux");
   os.k = 1.0;
   PGPU_CUDA(cudaMemcpyAsync(dos, &os, sizeof(os), cudaMemcpyHostToDevice, s));
   PGPU_CUDA(cudaMemsetAsync(d.fs_old.ptr, 0, (size_t)n * 8, s));
-  k_sn_source<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.chi.as<double>(), d.fs.as<double>(),
-                                                d.fs_old.as<double>(), bsrc, dos, s2);
-  {
-    double* Sdev = &dos->S;
-    k_scale_to<T><<<grid_for(len), kThreads, 0, s>>>(len, x, Sdev, 1, x);
-  }
+  launch(p, k_sn_source, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.chi.as<double>(),
+         d.fs.as<double>(), d.fs_old.as<double>(), bsrc, dos, s2);
+  launch(p, k_scale_to<double>, gl, kThreads, s, len, (const double*)x64, (const double*)&dos->S, 1, x64);
   PGPU_CUDA(cudaGetLastError());
 
-  int outer = 0, inner_total = 0;
-  double change = 1.0, dk = 1.0, k_prev = 1.0;
-  bool converged = false;
-  // b in precision T lives in rhs[0:nG] for the scalar-flux path
-  for (outer = 1; outer <= opt->max_outer; outer++) {
-    const double tol_in = std::fmin(1e-3, std::fmax(1e-12, 0.02 * std::fmin(change, dk * 1e3)));
-    double xnorm = 0.0;
-    if ((st = norm_of<T>(p, len, x, &xnorm))) return st;
-    int it = 0;
-    double res = 0.0;
+  // correction operators in precision T
+  T* zT = psi_work<T>(d);
+  auto applyA = [&](const T* v, T* w) -> int {
+    int e;
     if (phi_space) {
-      T* bt = rhs;
-      k_cast<double, T><<<grid_for(nG), kThreads, 0, s>>>(nG, bsrc, bt);
-      auto residual = [&](T* r) -> int {
-        int e = phi_space_T<T>(p, A, x, bt, r);
-        if (e) return e;
-        k_sub<T><<<grid_for(len), kThreads, 0, s>>>(len, r, x, r);
-        return PGPU_OK;
-      };
-      // w = v - T(v; 0); the sweep output goes to w first
-      auto applyA = [&](const T* v, T* w) -> int {
-        int e = phi_space_T<T>(p, A, v, nullptr, w);
-        if (e) return e;
-        k_sub<T><<<grid_for(len), kThreads, 0, s>>>(len, v, w, w);
-        return PGPU_OK;
-      };
-      auto post_add = [&](T* u) -> int {
-        k_add<T><<<grid_for(len), kThreads, 0, s>>>(len, u, x);
-        return PGPU_OK;
-      };
-      if ((st = gmres<T>(p, len, residual, applyA, post_add, tol_in * xnorm, opt->max_inner, &it, &res))) return st;
-      k_cast<T, double><<<grid_for(nG), kThreads, 0, s>>>(nG, x, phi0);
+      if ((e = phi_space_T<T>(p, A, v, nullptr, w))) return e;  // w = T_s v
+      launch(p, k_sub<T>, gl, kThreads, s, len, v, (const T*)w, w);  // w = v - T_s v
+      return PGPU_OK;
+    }
+    if ((e = sweep<T>(p, A, v, 0, nullptr, zT))) return e;  // z = P^-1 v
+    return apply_R<T>(p, A, zT, w, phT);                     // w = R z
+  };
+
+  int outer = 0, inner_total = 0;
+  double change = 1.0, dk = 1.0, k_prev = 1.0, res = 0.0;
+  bool converged = false;
+  for (outer = 1; outer <= opt->max_outer; outer++) {
+    // FP64 residual of the inner system for the current fission source
+    double scale = 0.0;
+    if (phi_space) {
+      if ((st = phi_space_T<double>(p, A64, x64, bsrc, r64))) return st;  // T(x; b)
+      launch(p, k_sub<double>, gl, kThreads, s, len, (const double*)r64, (const double*)x64, r64);
+      if ((st = norm_of<double>(p, len, x64, &scale))) return st;
     } else {
-      T* z = psi_work<T>(d);
-      T* ph = d.phtmp.as<T>();
-      k_cast<double, T><<<grid_for(nG), kThreads, 0, s>>>(nG, bsrc, ph);
-      k_broadcast<T><<<grid_for(N), kThreads, 0, s>>>(nG, M, ph, rhs);
-      auto residual = [&](T* r) -> int {
-        int e = apply_R<T>(p, A, x, r, ph);
-        if (e) return e;
-        k_sub<T><<<grid_for(len), kThreads, 0, s>>>(len, rhs, r, r);
-        return PGPU_OK;
-      };
-      auto applyA = [&](const T* v, T* w) -> int {
-        int e = sweep<T>(p, A, v, 0, nullptr, z);
-        if (e) return e;
-        return apply_R<T>(p, A, z, w, ph);
-      };
-      auto post_add = [&](T* u) -> int {
-        int e = sweep<T>(p, A, u, 0, nullptr, z);
-        if (e) return e;
-        k_add<T><<<grid_for(len), kThreads, 0, s>>>(len, z, x);
-        return PGPU_OK;
-      };
-      if ((st = gmres<T>(p, len, residual, applyA, post_add, tol_in * xnorm, opt->max_inner, &it, &res))) return st;
-      k_moment<T><<<grid_for((long long)nG * 32), kThreads, 0, s>>>(nG, M, A.w, x, ph);
-      k_cast<T, double><<<grid_for(nG), kThreads, 0, s>>>(nG, ph, phi0);
+      launch(p, k_broadcast<double>, grid_for(N), kThreads, s, nG, M, (const double*)bsrc, rhs64);
+      if ((st = apply_R<double>(p, A64, x64, r64, ph64))) return st;
+      launch(p, k_sub<double>, gl, kThreads, s, len, (const double*)rhs64, (const double*)r64, r64);
+      if ((st = norm_of<double>(p, len, rhs64, &scale))) return st;
+    }
+    double rnorm = 0.0;
+    if ((st = norm_of<double>(p, len, r64, &rnorm))) return st;
+    int it = 0;
+    const double atol = 1e-14 * scale;
+    if (rnorm > atol) {
+      const T* rin;
+      if (sizeof(T) == 8) {
+        rin = (const T*)r64;
+      } else {
+        launch(p, k_cast<double, T>, gl, kThreads, s, len, (const double*)r64, rT);
+        rin = rT;
+      }
+      if ((st = gmres<T>(p, len, applyA, rin, dT, kEta, sizeof(T) == 8 ? atol : 0.0, opt->max_inner, &it, &res))) return st;
+      if (phi_space) {
+        launch(p, k_add_cast<T>, gl, kThreads, s, len, (const T*)dT, x64);
+      } else {
+        if ((st = sweep<T>(p, A, dT, 0, nullptr, zT))) return st;  // x += P^-1 d
+        launch(p, k_add_cast<T>, gl, kThreads, s, len, (const T*)zT, x64);
+      }
     }
     inner_total += it;
-    k_sn_fission<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol.as<double>(), d.nsf.as<double>(), phi0,
-                                                   d.fs.as<double>(), dos, s1);
-    k_scale_to<T><<<grid_for(len), kThreads, 0, s>>>(len, x, &dos->S, 1, x);
-    k_sn_source<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.chi.as<double>(), d.fs.as<double>(),
-                                                  d.fs_old.as<double>(), bsrc, dos, s2);
+    // fission source, k and normalisation (FP64)
+    if (phi_space) {
+      PGPU_CUDA(cudaMemcpyAsync(phi0, x64, (size_t)nG * 8, cudaMemcpyDeviceToDevice, s));
+    } else {
+      launch(p, k_moment<double>, grid_for((long long)nG * 32), kThreads, s, nG, M, (const double*)d.w.as<double>(),
+             (const double*)x64, phi0);
+    }
+    launch(p, k_sn_fission, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.vol.as<double>(),
+           (const double*)d.nsf.as<double>(), (const double*)phi0, d.fs.as<double>(), dos, s1);
+    launch(p, k_scale_to<double>, gl, kThreads, s, len, (const double*)x64, (const double*)&dos->S, 1, x64);
+    launch(p, k_sn_source, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.chi.as<double>(),
+           d.fs.as<double>(), d.fs_old.as<double>(), bsrc, dos, s2);
     PGPU_CUDA(cudaGetLastError());
     if ((st = read_outer(p, os))) return st;
     if (os.nonfinite || !(os.k == os.k)) return fail(PGPU_ERR_NAN, "non-finite fission source");
@@ -966,43 +1027,33 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
     dk = std::fabs(os.k - k_prev);
     k_prev = os.k;
     if (opt->verbose)
-      std::printf("pgpu sn outer %d: k = %.12f  dk = %.3e  source change = %.3e  gmres = %d (res %.2e)\n", outer,
-                  os.k, dk, change, it, res);
+      std::printf("pgpu sn outer %d: k = %.12f  dk = %.3e  source change = %.3e  |r|/scale = %.2e  gmres = %d\n",
+                  outer, os.k, dk, change, scale > 0 ? rnorm / scale : 0.0, it);
     if (dk < opt->tol_k && change < opt->tol_flux) {
       converged = true;
       break;
     }
   }
 
-  // psi in FP64 from the converged state
+  // psi in FP64 from the converged state (one more sweep in scalar-flux space)
   double* psi = d.psi.as<double>();
   if (phi_space) {
-    double* xd = d.phi.as<double>();  // reuse as FP64 copy of [phi0 | inflow] when it fits
-    DevBuf xd_buf;
-    if ((size_t)len * 8 > d.phi.bytes) {
-      if ((st = dev_alloc(xd_buf, (size_t)len * 8, nullptr))) return st;
-      xd = xd_buf.as<double>();
-    }
-    k_cast<T, double><<<grid_for(len), kThreads, 0, s>>>(len, x, xd);
-    double* q = d.q.as<double>();
-    DevBuf qbuf;
-    if ((size_t)nG * 8 > d.q.bytes) {
-      if ((st = dev_alloc(qbuf, (size_t)nG * 8, nullptr))) return st;
-      q = qbuf.as<double>();
-    }
-    k_scatter_source<double><<<grid_for(nG), kThreads, 0, s>>>(A64, xd, bsrc, q);
-    if ((st = sweep<double>(p, A64, q, 1, d.nrefl ? xd + nG : nullptr, psi))) return st;
-    PGPU_CUDA(cudaStreamSynchronize(s));
+    launch(p, k_scatter_source<double>, gG, kThreads, s, A64, (const double*)x64, (const double*)bsrc, ph64);
+    if ((st = sweep<double>(p, A64, ph64, 1, d.nrefl ? x64 + nG : nullptr, psi))) return st;
   } else {
-    k_cast<T, double><<<grid_for(N), kThreads, 0, s>>>(N, x, psi);
+    PGPU_CUDA(cudaMemcpyAsync(psi, x64, (size_t)N * 8, cudaMemcpyDeviceToDevice, s));
   }
-  k_moment<double><<<grid_for((long long)nG * 32), kThreads, 0, s>>>(nG, M, d.w.as<double>(), psi, phi0);
-  k_sn_power_norm<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol.as<double>(), d.ksf.as<double>(), phi0,
-                                                    dos, s1);
-  k_sn_power_fields<<<grid_for(n), kThreads, 0, s>>>(n, G, d.mat.as<int>(), d.vol.as<double>(), d.ksf.as<double>(),
-                                                      d.nsf.as<double>(), phi0, opt->power, d.phi.as<double>(),
-                                                      d.q.as<double>(), d.P.as<double>(), dos, s2);
-  k_sn_psi_norm<<<grid_for(N), kThreads, 0, s>>>(N, psi, opt->power, dos, s1);
+  launch(p, k_moment<double>, grid_for((long long)nG * 32), kThreads, s, nG, M, (const double*)d.w.as<double>(),
+         (const double*)psi, phi0);
+  PGPU_CUDA(cudaMemsetAsync(&dos->amax_phi, 0, 2 * sizeof(unsigned long long), s));
+  launch(p, k_absmax<double>, gG, kThreads, s, (long long)nG, (const double*)phi0, &dos->amax_phi);
+  launch(p, k_absmax<double>, grid_for(N), kThreads, s, N, (const double*)psi, &dos->amax_psi);
+  launch(p, k_sn_power_norm, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.vol.as<double>(),
+         (const double*)d.ksf.as<double>(), (const double*)phi0, dos, s1);
+  launch(p, k_sn_power_fields, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.vol.as<double>(),
+         (const double*)d.ksf.as<double>(), (const double*)d.nsf.as<double>(), (const double*)phi0, opt->power,
+         d.phi.as<double>(), d.q.as<double>(), d.P.as<double>(), dos, s2);
+  launch(p, k_sn_psi_norm, grid_for(N), kThreads, s, N, psi, opt->power, dos, s1);
   PGPU_CUDA(cudaGetLastError());
   PGPU_CUDA(cudaEventRecord(e1, s));
   if ((st = read_outer(p, os))) return st;
@@ -1029,8 +1080,6 @@ int sn_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
     if (st) return st;
     if (!p->sn->psi32.ptr) {
       st = dev_alloc(p->sn->psi32, (size_t)p->sn->n * p->sn->G * p->sn->M * 4, &p->bytes);
-      if (st) return st;
-      st = dev_alloc(p->sn->src32, (size_t)p->sn->n * p->sn->G * 4, &p->bytes);
       if (st) return st;
     }
     return solve_T<float>(p, opt, stats);
