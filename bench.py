@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""k-eigenvalue solves/s of the GB300 hot path, one JSON line on stdout (rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+A step is one complete k-eigenvalue solve (flat start to convergence, |dk| < 1e-10,
+fission-source change < 1e-9) of the workload's synthetic input, generated from a fixed
+seed in the reference's .pmp format.  Default workload: 2-group S8 (80 directions)
+discrete ordinates on a 3D Cartesian 64x64x32 mesh of 2 cm cells in FP64 (~21M angular
+unknowns), pure upwind, reflective -x/-y/-z, vacuum +x/+y/+z.
+
+* value: solves/s with the operator and iterates already resident in HBM, device time
+  from CUDA events on the library's launching stream, max over ranks; the L2 is flushed
+  (256 MB write) between timed solves.
+* e2e: the same metric through the drop-in C API with host buffers: pampa_initialize
+  (parse + host assembly) + pampa_solve (upload + solve) + pampa_get_field of the scalar
+  flux, angular flux and power + pampa_finalize, wall-clock per step.
+* roofline: the transport-sweep kernel, algorithmic bytes (psi written and read once per
+  cell-group-direction update, source, moment and material id per cell-group) over its
+  CUDA-event time inside the timed solves; peak = measured HBM copy bandwidth.
+* cpu_baseline: oracle/cpu_sweep.c (C + OpenMP restatement of the same upwind sweep) on
+  the host cores for a bounded sample of sweeps, scaled by the sweeps one solve takes.
+* --impl reference: the CPU restatement alone (the reference's own LU + Krylov-Schur on
+  this operator would need ~82 GB of AIJ storage and is not buildable here).
+
+Multi-GPU: the path does not shard (one solve is one GPU); --gpus N under torchrun runs N
+independent replicas and value is the total over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "sn_s8_64x64x32_g2": dict(kind="sn", args=dict(), precision="fp64", dtype="f64",
+                               desc="2-group S8 SN k-eigenvalue, 3D Cartesian 64x64x32 (2 cm), ~21M angular unknowns"),
+    "sn_s8_64x64x32_g2_mixed": dict(kind="sn", args=dict(), precision="mixed", dtype="f32+f64",
+                                     desc="same, FP32 sweeps/GMRES with FP64 residual refinement"),
+    "diffusion_2d_34x34_g2": dict(kind="diffusion2d", args=dict(), precision="fp64", dtype="f64",
+                                  desc="2-group diffusion k-eigenvalue, 2D Cartesian 34x34 (5 cm)"),
+}
+DEFAULT = "sn_s8_64x64x32_g2"
+SOLVE_STATS = os.path.join(ROOT, "profiles", "solve_stats.json")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_input(name: str, out_dir: str) -> str:
+    from pampa_gb300 import workloads as wl
+    w = WORKLOADS[name]
+    if w["kind"] == "sn":
+        return wl.sn_3d(out_dir, **w["args"])
+    return wl.diffusion_2d(out_dir, **w["args"])
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return dict(hbm_gbs=float(d["hbm_gbs"]), source="measured")
+    return dict(hbm_gbs=6800.0, source="fallback")
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not os.path.exists(self.path):
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=["nvidia-smi unavailable"])
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(smax) if smax else None,
+                    reasons=sorted(reasons), samples=len(sm))
+
+
+def load_solve_stats() -> dict:
+    if os.path.exists(SOLVE_STATS):
+        with open(SOLVE_STATS) as fh:
+            return json.load(fh)
+    return {}
+
+
+def cpu_baseline(input_path: str, sweeps_per_solve: float, budget_s: float = 20.0) -> dict:
+    """Time the oracle's C sweep on the host cores; scale to solves/s."""
+    from oracle import pampa_oracle as po, sn_cpu
+    prob = po.read_problem(input_path)
+    inp = sn_cpu.sweep_inputs(prob)
+    t1, threads = sn_cpu.time_sweeps(inp, 1)
+    nsw = max(1, min(50, int(budget_s / max(t1, 1e-6))))
+    t, threads = sn_cpu.time_sweeps(inp, nsw, threads)
+    per_solve = t * sweeps_per_solve
+    return dict(value=1.0 / per_solve, unit="solves/s", cores=threads, kind="port",
+                sample=(f"{nsw} upwind sweeps + scalar-flux moments of this workload with oracle/cpu_sweep.c "
+                        f"({threads} OpenMP threads, {t * 1e3:.1f} ms/sweep), scaled by the "
+                        f"{sweeps_per_solve:.0f} sweeps one GPU k-eigenvalue solve of the same algorithm takes"),
+                seconds_per_sweep=t)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    w = WORKLOADS[args.workload]
+    if w["kind"] != "sn":
+        print(json.dumps({"impl": "reference", "unavailable": "CPU reference arm is implemented for the SN workloads"}))
+        return 0
+    stats = load_solve_stats().get(args.workload)
+    if not stats:
+        print(json.dumps({"impl": "reference", "unavailable": "no recorded sweeps-per-solve for this workload "
+                          "(run bench.py --impl ours once to record profiles/solve_stats.json)"}))
+        return 0
+    with tempfile.TemporaryDirectory() as d:
+        path = make_input(args.workload, d)
+        from oracle import pampa_oracle as po, sn_cpu
+        prob = po.read_problem(path)
+        inp = sn_cpu.sweep_inputs(prob)
+        per = []
+        threads = None
+        for i in range(args.warmup + args.steps):
+            t, threads = sn_cpu.time_sweeps(inp, 1, threads)
+            if i >= args.warmup:
+                per.append(t)
+    t = statistics.mean(per)
+    value = 1.0 / (t * stats["sweeps"])
+    cpu = dict(value=value, unit="solves/s", cores=threads, kind="port",
+               sample=f"one upwind sweep + moment per step ({t * 1e3:.1f} ms) with oracle/cpu_sweep.c, "
+                      f"scaled by {stats['sweeps']} sweeps per solve")
+    line = dict(metric="k-eigen solves/s", value=value, unit="solves/s", n_gpus=world, steps=args.steps,
+                warmup=args.warmup, ms_per_step=1e3 * t * stats["sweeps"], higher_is_better=True, scaling="weak",
+                vs_baseline=None, dtype="f64", data="synthetic (seeded generator, reference .pmp format)",
+                config=dict(workload=args.workload, description=w["desc"]), impl="reference", cpu_baseline=cpu,
+                e2e=dict(value=value, unit="solves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args, rank, world, local):
+    import ctypes as C
+    import numpy as np
+    import torch
+    import pampa_gb300 as pg
+
+    dev = local
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    w = WORKLOADS[args.workload]
+    tmp = tempfile.mkdtemp(prefix=f"bench_r{rank}_")
+    path = make_input(args.workload, tmp)
+    prec = ["-pgpu_precision", w["precision"]]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    # ---- device-resident solves ---------------------------------------------------
+    p = pg.Pampa(path, "-silent", "-pgpu_device", str(dev), *prec)
+    h = C.c_void_p(None)
+    err = C.c_int(0)
+    pg.lib().pampa_get_problem(C.byref(h), C.byref(err))
+    if err.value:
+        raise RuntimeError(pg.last_error())
+    opts = pg.default_options(precision=pg.PGPU_MIXED if w["precision"] == "mixed" else pg.PGPU_FP64)
+    stats = pg.pgpu_stats()
+
+    def solve(profile: int):
+        opts.profile = profile
+        st = pg.lib().pgpu_problem_solve(h, C.byref(opts), C.byref(stats))
+        if st != pg.PGPU_OK:
+            raise RuntimeError(f"solve failed: {pg.last_error()}")
+        return {k: getattr(stats, k) for k, _ in pg.pgpu_stats._fields_}
+
+    for _ in range(args.warmup):
+        solve(0)
+    results = []
+    torch.cuda.synchronize()
+    barrier()
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            results.append(solve(1))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier()
+    dev_time = sum(r["seconds"] for r in results)
+    if dist is not None:
+        tt = torch.tensor([dev_time], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_time = float(tt.item())
+    keff = results[-1]["keff"]
+    kern_s = sum(r["kernel_seconds"] for r in results)
+    kern_b = sum(r["kernel_bytes"] for r in results)
+    kern_n = sum(r["kernel_launches"] for r in results)
+    launches = sum(r["launches"] for r in results)
+    sweeps = results[-1]["sweeps"]
+    upload = int(pg.lib().pgpu_problem_upload_bytes(h))
+    n_phi = p.field_size("scalar-flux")
+    n_psi = p.field_size("angular-flux")
+    n_cells = p.field_size("power")
+    p.finalize()
+
+    # ---- end-to-end through the drop-in API -------------------------------------
+    e2e_times = []
+    for i in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        q = pg.Pampa(path, "-silent", "-pgpu_device", str(dev), *prec)
+        q.solve()
+        q.field("scalar-flux")
+        if n_psi:
+            q.field("angular-flux")
+        q.field("power")
+        q.finalize()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t1)
+    e2e_t = statistics.mean(e2e_times)
+    if dist is not None:
+        tt = torch.tensor([e2e_t], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+
+    peaks = measured_peaks()
+    achieved = kern_b / kern_s / 1e9 if kern_s > 0 else None
+    roof = dict(bound="hbm", kernel="k_sweep_level" if w["kind"] == "sn" else "k_bicg_v/k_bicg_t (SpMV)",
+                achieved=achieved, peak=peaks["hbm_gbs"], unit="GB/s",
+                frac=(achieved / peaks["hbm_gbs"]) if achieved else None, peak_source=peaks["source"],
+                traffic=None, launches=kern_n,
+                kernel_share_of_solve=kern_s / dev_time if dev_time > 0 else None)
+    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as fh:
+            roof["traffic"] = json.load(fh).get(args.workload)
+
+    line = dict(metric="k-eigen solves/s", value=world * args.steps / dev_time, unit="solves/s", n_gpus=world,
+                steps=args.steps, warmup=args.warmup, ms_per_step=1e3 * dev_time / args.steps,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype=w["dtype"],
+                data="synthetic (seeded generator, reference .pmp format)",
+                config=dict(workload=args.workload, description=w["desc"], keff=keff,
+                            sweeps_per_solve=sweeps, outer_iterations=results[-1]["outer_iterations"],
+                            gmres_iterations=results[-1]["inner_iterations"], l2="flushed (256 MB write) between steps",
+                            parallelism=f"replicas x{world}" if world > 1 else "1 GPU",
+                            wall_ms_per_step=1e3 * wall / args.steps),
+                e2e=dict(value=world / e2e_t, unit="solves/s", h2d_bytes_per_step=upload,
+                         d2h_bytes_per_step=8 * (n_phi + n_psi + n_cells),
+                         note="drop-in pampa_* API: parse + host assembly + upload + solve + field reads; "
+                              "host buffers are pageable"),
+                gpu_launches=launches, roofline=roof, clocks=clk.summary())
+    if rank == 0 and world == 1 and w["kind"] == "sn" and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(path, sweeps)
+        except Exception as e:  # the baseline never decides the GPU result
+            line["cpu_baseline"] = dict(value=None, unavailable=str(e))
+    if rank == 0:
+        rec = load_solve_stats()
+        rec[args.workload] = dict(sweeps=sweeps, outer_iterations=results[-1]["outer_iterations"],
+                                  gmres_iterations=results[-1]["inner_iterations"], keff=keff)
+        if args.record:
+            os.makedirs(os.path.dirname(SOLVE_STATS), exist_ok=True)
+            with open(SOLVE_STATS, "w") as fh:
+                json.dump(rec, fh, indent=1, sort_keys=True)
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--record", action="store_true", help="write profiles/solve_stats.json")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    import pampa_gb300.build as b
+    b.build()
+    return run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -215,6 +215,9 @@ int pgpu_problem_get_power(pgpu_problem* p, double* q, double* P, double* total_
 /* Device memory held by the problem, in bytes. */
 long long pgpu_problem_device_bytes(pgpu_problem* p);
 
+/* Bytes copied host-to-device when the problem was created (the operator). */
+long long pgpu_problem_upload_bytes(pgpu_problem* p);
+
 void pgpu_problem_destroy(pgpu_problem* p);
 
 #ifdef __cplusplus

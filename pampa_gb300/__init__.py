@@ -96,6 +96,7 @@ SYMBOLS = {
     "pgpu_problem_get_angular_flux": (C.c_int, [C.c_void_p, _pd]),
     "pgpu_problem_get_power": (C.c_int, [C.c_void_p, _pd, _pd, _pd]),
     "pgpu_problem_device_bytes": (C.c_longlong, [C.c_void_p]),
+    "pgpu_problem_upload_bytes": (C.c_longlong, [C.c_void_p]),
     "pgpu_problem_destroy": (None, [C.c_void_p]),
 }
 

@@ -115,6 +115,8 @@ int pgpu_problem_get_power(pgpu_problem* p, double* q, double* P, double* total)
 
 long long pgpu_problem_device_bytes(pgpu_problem* p) { return p ? p->bytes : 0; }
 
+long long pgpu_problem_upload_bytes(pgpu_problem* p) { return p ? p->uploaded : 0; }
+
 void pgpu_problem_destroy(pgpu_problem* p) {
   if (!p) return;
   cudaSetDevice(p->device);

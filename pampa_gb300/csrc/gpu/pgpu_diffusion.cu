@@ -658,6 +658,7 @@ int pgpu_diffusion_create(int device, const pgpu_diffusion_operator* op, pgpu_pr
   int st = PGPU_OK;
   auto up = [&](DevBuf& b, const void* h, size_t bytes) {
     if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes);
+    p->uploaded += (long long)bytes;
   };
   auto al = [&](DevBuf& b, size_t bytes) {
     if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes);

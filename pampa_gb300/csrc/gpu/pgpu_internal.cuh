@@ -156,7 +156,8 @@ struct pgpu_problem {
   int kind = 0;  // 1 diffusion, 2 SN
   int device = 0;
   int num_cells = 0, num_groups = 0, num_dirs = 0;
-  long long bytes = 0;
+  long long bytes = 0;     // device memory held
+  long long uploaded = 0;  // host-to-device bytes copied at creation
   cudaStream_t stream = nullptr;
   bool solved = false;
   double keff = 0.0;

@@ -1182,6 +1182,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
   st = PGPU_OK;
   auto up = [&](DevBuf& b, const void* h, size_t bytes) {
     if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes);
+    p->uploaded += (long long)bytes;
   };
   auto al = [&](DevBuf& b, size_t bytes) {
     if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes);
