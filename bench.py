@@ -223,10 +223,13 @@ def run_ours(args, rank, world, local):
     opts = pg.default_options(precision=pg.PGPU_MIXED if w["precision"] == "mixed" else pg.PGPU_FP64)
     stats = pg.pgpu_stats()
 
+    if args.profile_outer:
+        opts.max_outer = args.profile_outer
+
     def solve(profile: int):
         opts.profile = profile
         st = pg.lib().pgpu_problem_solve(h, C.byref(opts), C.byref(stats))
-        if st != pg.PGPU_OK:
+        if st != pg.PGPU_OK and not (args.profile_outer and st == pg.PGPU_ERR_NOT_CONVERGED):
             raise RuntimeError(f"solve failed: {pg.last_error()}")
         return {k: getattr(stats, k) for k, _ in pg.pgpu_stats._fields_}
 
@@ -264,7 +267,7 @@ def run_ours(args, rank, world, local):
 
     # ---- end-to-end through the drop-in API -------------------------------------
     e2e_times = []
-    for i in range(max(1, min(args.steps, 3))):
+    for i in range(0 if args.profile_outer else max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         q = pg.Pampa(path, "-silent", "-pgpu_device", str(dev), *prec)
@@ -276,7 +279,7 @@ def run_ours(args, rank, world, local):
         q.finalize()
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t1)
-    e2e_t = statistics.mean(e2e_times)
+    e2e_t = statistics.mean(e2e_times) if e2e_times else float("inf")
     if dist is not None:
         tt = torch.tensor([e2e_t], device=f"cuda:{dev}", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -308,7 +311,9 @@ def run_ours(args, rank, world, local):
                          note="drop-in pampa_* API: parse + host assembly + upload + solve + field reads; "
                               "host buffers are pageable"),
                 gpu_launches=launches, roofline=roof, clocks=clk.summary())
-    if rank == 0 and world == 1 and w["kind"] == "sn" and not args.no_cpu:
+    if args.profile_outer:
+        line["profile_run"] = f"solves capped at {args.profile_outer} outer iterations; not a benchmark result"
+    if rank == 0 and world == 1 and w["kind"] == "sn" and not args.no_cpu and not args.profile_outer:
         try:
             line["cpu_baseline"] = cpu_baseline(path, sweeps)
         except Exception as e:  # the baseline never decides the GPU result
@@ -317,7 +322,7 @@ def run_ours(args, rank, world, local):
         rec = load_solve_stats()
         rec[args.workload] = dict(sweeps=sweeps, outer_iterations=results[-1]["outer_iterations"],
                                   gmres_iterations=results[-1]["inner_iterations"], keff=keff)
-        if args.record:
+        if args.record and not args.profile_outer:
             os.makedirs(os.path.dirname(SOLVE_STATS), exist_ok=True)
             with open(SOLVE_STATS, "w") as fh:
                 json.dump(rec, fh, indent=1, sort_keys=True)
@@ -336,6 +341,9 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--record", action="store_true", help="write profiles/solve_stats.json")
+    ap.add_argument("--profile-outer", type=int, default=0,
+                    help="profiling runs under ncu only: cap every solve at this many outer iterations, "
+                         "skip the e2e and CPU legs; the printed line is not a benchmark result")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -60,6 +60,8 @@ struct SNOp {
   const int* __restrict__ refl;      // [M][3]
   const T* __restrict__ st;          // [nm][G]
   const T* __restrict__ ss;          // [nm][G][G]
+  const T* __restrict__ chi;         // [nm][G]
+  const T* __restrict__ nsf;         // [nm][G]
 };
 
 struct Schedule {
@@ -85,7 +87,10 @@ struct SNData {
   // operator (FP64 and FP32 copies of the real-valued arrays)
   DevBuf nf, kind, nbr, raxis, rslot, mat, refl;
   DevBuf area, nrm, gauss, lsw, lsdiag, vol, dirs, w, st, ss, chi, nsf, ksf;
-  DevBuf area32, nrm32, gauss32, lsw32, lsdiag32, vol32, dirs32, w32, st32, ss32;
+  DevBuf area32, nrm32, gauss32, lsw32, lsdiag32, vol32, dirs32, w32, st32, ss32, chi32, nsf32;
+  // sweep face weights (SweepFaces)
+  DevBuf cls, mutab, wout, windiag, win, mutab32, wout32, windiag32, win32;
+  bool use_tab = false;
   bool have32 = false;
   // schedule on device
   DevBuf d_pat_dirs_ptr, d_pat_dirs, d_pat_lev_ptr, d_pat_nlev, d_lev_ptr, d_order;
@@ -139,8 +144,25 @@ __device__ __forceinline__ T mu_of(const SNOp<T>& A, int f, int i, int m) {
 // the upwind part of R: psi = (src - upwind face terms - reflective inflow) / diagonal.
 // src is isotropic ([n*G]) when iso != 0, else angular ([n*G*M]).  bnd holds incoming
 // angular flux at reflective faces ([nrefl][G][M]) or is null (treated as zero).
+// Per-face sweep weights, precomputed at setup so a face costs one or two FP64 operations
+// (GB300's FP64 rate is 1/64 of FP32, and the sweep is FP64-bound):
+//   outflow (mu > 0):  den += mu * wout   (interior: Gauss weight c0 * A; vacuum: A, minus the
+//                                          LS diagonal share; reflective: A)
+//   inflow  (mu <= 0): den += mu * windiag (interior, delta < 1: c2 * A)
+//                      num -= mu * win * psi_upwind (interior: c3 * A) or * inflow (reflective: A)
+// mu comes from a table over the mesh's distinct face normals when there are at most 255.
 template <typename T>
-__global__ void k_sweep_level(SNOp<T> A, int level, const int* __restrict__ pat_dirs_ptr,
+struct SweepFaces {
+  const unsigned char* __restrict__ cls;  // [F][n] normal class, or null: mu from the normals
+  const T* __restrict__ mutab;            // [ncls][M]
+  const T* __restrict__ wout;             // [F][n]
+  const T* __restrict__ windiag;          // [F][n]
+  const T* __restrict__ win;              // [F][n]
+  int upwind;                             // windiag == 0 everywhere
+};
+
+template <typename T>
+__global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* __restrict__ pat_dirs_ptr,
                               const int* __restrict__ pat_dirs, const int* __restrict__ pat_lev_ptr,
                               const int* __restrict__ pat_nlev, const int* __restrict__ lev_ptr,
                               const int* __restrict__ order, const T* __restrict__ src, int iso,
@@ -151,46 +173,31 @@ __global__ void k_sweep_level(SNOp<T> A, int level, const int* __restrict__ pat_
   const int* lp = lev_ptr + pat_lev_ptr[p];
   const int c0 = lp[level], nc = lp[level + 1] - c0;
   const int* ord = order + (size_t)p * A.n;
-  const int G = A.G, M = A.M;
-  const long long items = (long long)nc * G * nd;
-  for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items;
-       it += (long long)gridDim.x * blockDim.x) {
-    const int di = (int)(it % nd);
-    const long long rest = it / nd;
-    const int g = (int)(rest % G);
-    const int ci = (int)(rest / G);
+  const int G = A.G, M = A.M, n = A.n;
+  const int items = nc * G * nd;  // < 2^31 (checked at setup)
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < items; it += gridDim.x * blockDim.x) {
+    const int rest = it / nd;
+    const int di = it - rest * nd;
+    const int ci = rest / G;
+    const int g = rest - ci * G;
     const int i = ord[c0 + ci];
     const int m = pat_dirs[d0 + di];
     const int mt = A.mat[i];
-    const T V = A.vol[i];
-    T den = A.st[(size_t)mt * G + g] * V;
+    T den = A.st[mt * G + g] * A.vol[i];
     T num = iso ? src[(size_t)i * G + g] : src[((size_t)i * G + g) * M + m];
     const int nfi = A.nf[i];
     for (int f = 0; f < nfi; f++) {
-      const size_t o = (size_t)f * A.n + i;
-      const int kd = A.kind[o];
-      const T mu = mu_of(A, f, i, m);
-      const T muA = mu * A.area[o];
-      if (kd == PGPU_FACE_INTERIOR) {
-        const T* c = A.gauss + o * 4;
-        if (mu > T(0)) {
-          den += c[0] * muA;
-        } else {
-          den += c[2] * muA;
-          const int j = A.nbr[o];
-          num -= c[3] * muA * psi[((size_t)j * G + g) * M + m];
-        }
-      } else if (kd == PGPU_FACE_VACUUM) {
-        if (mu > T(0)) {
-          den += muA;
-          if (A.use_ls) den -= A.lsdiag[o] * muA;
-        }
-      } else if (kd == PGPU_FACE_REFLECTIVE) {
-        if (mu > T(0)) {
-          den += muA;
-        } else if (bnd) {
-          const int s = A.rslot[o];
-          num -= muA * bnd[((size_t)s * G + g) * M + m];
+      const size_t o = (size_t)f * n + i;
+      const T mu = W.cls ? W.mutab[W.cls[o] * M + m] : mu_of(A, f, i, m);
+      if (mu > T(0)) {
+        den += mu * W.wout[o];
+      } else {
+        if (!W.upwind) den += mu * W.windiag[o];
+        const int kd = A.kind[o];
+        if (kd == PGPU_FACE_INTERIOR) {
+          num -= (mu * W.win[o]) * psi[((size_t)A.nbr[o] * G + g) * M + m];
+        } else if (kd == PGPU_FACE_REFLECTIVE && bnd) {
+          num -= (mu * W.win[o]) * bnd[((size_t)A.rslot[o] * G + g) * M + m];
         }
       }
     }
@@ -212,15 +219,24 @@ __global__ void k_moment(int rows, int M, const T* __restrict__ w, const T* __re
   }
 }
 
-// Isotropic source q[i,g] = V sum_g2 sigma_s(g2->g) phi0[i,g2] (+ b[i,g] when given).
+// Isotropic source q[i,g] = V sum_g2 (sigma_s(g2->g) + lam_s chi_g nu_sigma_f(g2)) phi0[i,g2]
+// (+ b[i,g] when given).  lam_s is the Wielandt shift (0 for plain power iteration).
 template <typename T>
-__global__ void k_scatter_source(SNOp<T> A, const T* __restrict__ phi0, const T* __restrict__ b, T* q) {
+__global__ void k_scatter_source(SNOp<T> A, const T* __restrict__ phi0, const T* __restrict__ b, T* q,
+                                 double lam_s) {
   const int G = A.G;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n * G; r += gridDim.x * blockDim.x) {
     const int i = r / G, g = r - i * G;
-    const T* ssm = A.ss + (size_t)A.mat[i] * G * G;
+    const int mt = A.mat[i];
+    const T* ssm = A.ss + (size_t)mt * G * G;
     T s = T(0);
     for (int g2 = 0; g2 < G; g2++) s += ssm[g2 * G + g] * phi0[(size_t)i * G + g2];
+    if (lam_s != 0.0) {
+      const T* ns = A.nsf + (size_t)mt * G;
+      T f = T(0);
+      for (int g2 = 0; g2 < G; g2++) f += ns[g2] * phi0[(size_t)i * G + g2];
+      s += (T)lam_s * A.chi[(size_t)mt * G + g] * f;
+    }
     s *= A.vol[i];
     if (b) s += b[r];
     q[r] = s;
@@ -368,6 +384,12 @@ __global__ void k_norm2(long long N, const T* __restrict__ x, double* out, Reduc
 }
 
 template <typename T>
+__global__ void k_mul(long long N, T* a, double f) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    a[l] = (T)((double)a[l] * f);
+}
+
+template <typename T>
 __global__ void k_fill(long long N, T* a, T v) {
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
     a[l] = v;
@@ -395,10 +417,12 @@ __global__ void k_cast(long long N, const S* __restrict__ a, D* b) {
 
 // ---- outer-iteration kernels (FP64 state) ----
 
-// fs_i = V sum_g nu_sigma_f phi0; S = sum fs; k *= S.
+// fs_i = V sum_g nu_sigma_f phi0; S = sum fs.  The inner solve of a (shifted) power
+// iteration step maps a fission source of total 1 to y, so lambda = lam_s + 1/S and
+// k = 1/lambda (lam_s = 0: k = S).
 __global__ void k_sn_fission(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
                              const double* __restrict__ nsf, const double* __restrict__ phi0, double* fs,
-                             SNOuter* os, ReduceSlots<1> slots) {
+                             SNOuter* os, ReduceSlots<1> slots, double lam_s) {
   double acc[1] = {0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double* ns = nsf + (size_t)mat[i] * G;
@@ -411,15 +435,15 @@ __global__ void k_sn_fission(int n, int G, const int* __restrict__ mat, const do
   double tot[1];
   if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
     os->S = tot[0];
-    os->k = os->k * tot[0];
+    os->k = 1.0 / (lam_s + 1.0 / tot[0]);
     os->nonfinite = !(tot[0] == tot[0]) || tot[0] == 0.0;
   }
 }
 
-// normalise fs by S, change vs fs_old, b = chi fs / k (isotropic, per (i,g)).
+// normalise fs by S, change vs fs_old, b = chi fs (isotropic, per (i,g); total 1).
 __global__ void k_sn_source(int n, int G, const int* __restrict__ mat, const double* __restrict__ chi,
                             double* fs, double* fs_old, double* b, SNOuter* os, ReduceSlots<2> slots) {
-  const double invS = 1.0 / os->S, invk = 1.0 / os->k;
+  const double invS = 1.0 / os->S, invk = 1.0;
   double acc[2] = {0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double f = fs[i] * invS;
@@ -634,7 +658,7 @@ SNOp<double> make_op<double>(const SNData& d) {
                       d.area.as<double>(), d.nrm.as<double>(), d.gauss.as<double>(), d.raxis.as<int>(),
                       d.rslot.as<int>(), d.lsw.as<double>(), d.lsdiag.as<double>(), d.mat.as<int>(),
                       d.vol.as<double>(), d.dirs.as<double>(), d.w.as<double>(), d.refl.as<int>(),
-                      d.st.as<double>(), d.ss.as<double>()};
+                      d.st.as<double>(), d.ss.as<double>(), d.chi.as<double>(), d.nsf.as<double>()};
 }
 
 template <>
@@ -643,7 +667,7 @@ SNOp<float> make_op<float>(const SNData& d) {
                      d.area32.as<float>(), d.nrm32.as<float>(), d.gauss32.as<float>(), d.raxis.as<int>(),
                      d.rslot.as<int>(), d.lsw32.as<float>(), d.lsdiag32.as<float>(), d.mat.as<int>(),
                      d.vol32.as<float>(), d.dirs32.as<float>(), d.w32.as<float>(), d.refl.as<int>(),
-                     d.st32.as<float>(), d.ss32.as<float>()};
+                     d.st32.as<float>(), d.ss32.as<float>(), d.chi32.as<float>(), d.nsf32.as<float>()};
 }
 
 template <int NV>
@@ -667,11 +691,28 @@ int make_fp32(pgpu_problem* p) {
   if ((st = conv(d.area, d.area32)) || (st = conv(d.nrm, d.nrm32)) || (st = conv(d.gauss, d.gauss32)) ||
       (st = conv(d.lsw, d.lsw32)) || (st = conv(d.lsdiag, d.lsdiag32)) || (st = conv(d.vol, d.vol32)) ||
       (st = conv(d.dirs, d.dirs32)) || (st = conv(d.w, d.w32)) || (st = conv(d.st, d.st32)) ||
-      (st = conv(d.ss, d.ss32)))
+      (st = conv(d.ss, d.ss32)) || (st = conv(d.chi, d.chi32)) || (st = conv(d.nsf, d.nsf32)) ||
+      (st = conv(d.mutab, d.mutab32)) || (st = conv(d.wout, d.wout32)) || (st = conv(d.windiag, d.windiag32)) ||
+      (st = conv(d.win, d.win32)))
     return st;
   PGPU_CUDA(cudaGetLastError());
   d.have32 = true;
   return PGPU_OK;
+}
+
+template <typename T>
+SweepFaces<T> make_faces(const SNData& d);
+
+template <>
+SweepFaces<double> make_faces<double>(const SNData& d) {
+  return SweepFaces<double>{d.use_tab ? d.cls.as<unsigned char>() : nullptr, d.mutab.as<double>(),
+                            d.wout.as<double>(), d.windiag.as<double>(), d.win.as<double>(), d.upwind ? 1 : 0};
+}
+
+template <>
+SweepFaces<float> make_faces<float>(const SNData& d) {
+  return SweepFaces<float>{d.use_tab ? d.cls.as<unsigned char>() : nullptr, d.mutab32.as<float>(),
+                           d.wout32.as<float>(), d.windiag32.as<float>(), d.win32.as<float>(), d.upwind ? 1 : 0};
 }
 
 }  // namespace
@@ -686,12 +727,13 @@ template <typename T>
 int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd, T* psi) {
   SNData& d = *p->sn;
   const Schedule& S = d.sched;
+  const SweepFaces<T> W = make_faces<T>(d);
   cudaEvent_t e0;
   prof_begin(p, &e0);
   for (int L = 0; L < S.nlev; L++) {
     dim3 grid(S.grid_x[L], S.npat);
     launch(p, k_sweep_level<T>, grid, kThreads, p->stream,
-        A, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
+        A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
         d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), src, iso, bnd, psi);
   }
   // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
@@ -712,15 +754,15 @@ T* psi_work(SNData& d) {
 }
 
 
-// y = T(x; b): sweep driven by the scattering source of x's phi0 part (plus b) and the
-// reflective inflow held in x's boundary part; returns [phi0' | inflow'].
+// y = T(x; b): sweep driven by the scattering (+ lam_s-shifted fission) source of x's phi0
+// part plus b, and the reflective inflow held in x's boundary part; returns [phi0' | inflow'].
 template <typename T>
-int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y) {
+int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y, double lam_s) {
   SNData& d = *p->sn;
   const int nG = d.n * d.G;
   T* q = d.scat.as<T>();
   T* psi = psi_work<T>(d);
-  launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q);
+  launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q, lam_s);
   int st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi);
   if (st) return st;
   launch(p, k_moment<T>, grid_for((long long)nG * 32), kThreads, p->stream, nG, d.M, A.w, psi, y);
@@ -898,6 +940,13 @@ int read_outer(pgpu_problem* p, SNOuter& os) {
 // FP32 for mixed precision: iterative refinement), updates x, and renormalises the
 // fission source.  The correction solve reduces the FP64 residual by kEta.
 constexpr double kEta = 0.02;
+// Wielandt shift: lambda_s = 1 / (k + kShiftDk) once at least kShiftAfter outer iterations
+// have run and |dk| < kShiftWhenDk.  The inner operator I - T (S + lambda_s F) stays
+// nonsingular while k + kShiftDk is above the fundamental k; the shifted iteration's
+// dominance ratio is (1/k1 - lambda_s) / (1/k2 - lambda_s).
+constexpr double kShiftDk = 0.05;
+constexpr int kShiftAfter = 3;
+constexpr double kShiftWhenDk = 1e-3;
 
 template <typename T>
 int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
@@ -946,7 +995,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   PGPU_CUDA(cudaMemsetAsync(x64, 0, len * 8, s));
   launch(p, k_fill<double>, grid_for(phi_space ? nG : N), kThreads, s, phi_space ? (long long)nG : N, x64, 1.0);
   launch(p, k_sn_fission, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.vol.as<double>(),
-         (const double*)d.nsf.as<double>(), (const double*)phi0, d.fs.as<double>(), dos, s1);
+         (const double*)d.nsf.as<double>(), (const double*)phi0, d.fs.as<double>(), dos, s1, 0.0);
   SNOuter os;
   if ((st = read_outer(p, os))) return st;
   if (os.nonfinite || os.S <= 0.0) return fail(PGPU_ERR_INVALID, "no fission source in the initial flux");
@@ -958,12 +1007,16 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   launch(p, k_scale_to<double>, gl, kThreads, s, len, (const double*)x64, (const double*)&dos->S, 1, x64);
   PGPU_CUDA(cudaGetLastError());
 
+  // Wielandt shift lam_s = 1/(k + kShiftDk), switched on once k has settled (scalar-flux
+  // space only); 0 means plain power iteration.
+  double lam_s = 0.0;
+
   // correction operators in precision T
   T* zT = psi_work<T>(d);
   auto applyA = [&](const T* v, T* w) -> int {
     int e;
     if (phi_space) {
-      if ((e = phi_space_T<T>(p, A, v, nullptr, w))) return e;  // w = T_s v
+      if ((e = phi_space_T<T>(p, A, v, nullptr, w, lam_s))) return e;  // w = T (S + lam_s F) v
       launch(p, k_sub<T>, gl, kThreads, s, len, v, (const T*)w, w);  // w = v - T_s v
       return PGPU_OK;
     }
@@ -975,10 +1028,13 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   double change = 1.0, dk = 1.0, k_prev = 1.0, res = 0.0;
   bool converged = false;
   for (outer = 1; outer <= opt->max_outer; outer++) {
+    // initial guess of the inner solution: an eigenvector x with fission total 1 maps to
+    // x / (lambda - lam_s)
+    launch(p, k_mul<double>, gl, kThreads, s, len, x64, 1.0 / (1.0 / k_prev - lam_s));
     // FP64 residual of the inner system for the current fission source
     double scale = 0.0;
     if (phi_space) {
-      if ((st = phi_space_T<double>(p, A64, x64, bsrc, r64))) return st;  // T(x; b)
+      if ((st = phi_space_T<double>(p, A64, x64, bsrc, r64, lam_s))) return st;  // T((S + lam_s F) x + b)
       launch(p, k_sub<double>, gl, kThreads, s, len, (const double*)r64, (const double*)x64, r64);
       if ((st = norm_of<double>(p, len, x64, &scale))) return st;
     } else {
@@ -1016,29 +1072,32 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
              (const double*)x64, phi0);
     }
     launch(p, k_sn_fission, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.vol.as<double>(),
-           (const double*)d.nsf.as<double>(), (const double*)phi0, d.fs.as<double>(), dos, s1);
+           (const double*)d.nsf.as<double>(), (const double*)phi0, d.fs.as<double>(), dos, s1, lam_s);
     launch(p, k_scale_to<double>, gl, kThreads, s, len, (const double*)x64, (const double*)&dos->S, 1, x64);
     launch(p, k_sn_source, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.chi.as<double>(),
            d.fs.as<double>(), d.fs_old.as<double>(), bsrc, dos, s2);
     PGPU_CUDA(cudaGetLastError());
     if ((st = read_outer(p, os))) return st;
-    if (os.nonfinite || !(os.k == os.k)) return fail(PGPU_ERR_NAN, "non-finite fission source");
+    if (os.nonfinite || !(os.k == os.k) || !(os.k > 0.0)) return fail(PGPU_ERR_NAN, "non-finite fission source");
     change = os.change;
     dk = std::fabs(os.k - k_prev);
     k_prev = os.k;
     if (opt->verbose)
-      std::printf("pgpu sn outer %d: k = %.12f  dk = %.3e  source change = %.3e  |r|/scale = %.2e  gmres = %d\n",
-                  outer, os.k, dk, change, scale > 0 ? rnorm / scale : 0.0, it);
+      std::printf("pgpu sn outer %d: k = %.12f  dk = %.3e  source change = %.3e  |r|/scale = %.2e  gmres = %d  lam_s = %.6f\n",
+                  outer, os.k, dk, change, scale > 0 ? rnorm / scale : 0.0, it, lam_s);
     if (dk < opt->tol_k && change < opt->tol_flux) {
       converged = true;
       break;
     }
+    if (phi_space && outer >= kShiftAfter && dk < kShiftWhenDk) lam_s = 1.0 / (os.k + kShiftDk);
   }
 
   // psi in FP64 from the converged state (one more sweep in scalar-flux space)
   double* psi = d.psi.as<double>();
   if (phi_space) {
-    launch(p, k_scatter_source<double>, gG, kThreads, s, A64, (const double*)x64, (const double*)bsrc, ph64);
+    // source of the eigen-equation: (S + F / k) phi0
+    launch(p, k_scatter_source<double>, gG, kThreads, s, A64, (const double*)x64, (const double*)nullptr, ph64,
+           1.0 / k_prev);
     if ((st = sweep<double>(p, A64, ph64, 1, d.nrefl ? x64 + nG : nullptr, psi))) return st;
   } else {
     PGPU_CUDA(cudaMemcpyAsync(psi, x64, (size_t)N * 8, cudaMemcpyDeviceToDevice, s));
@@ -1158,6 +1217,51 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
     }
   for (int m = 0; m < M * 3; m++)
     if (op->reflected[m] < 0 || op->reflected[m] >= M) return fail(PGPU_ERR_INVALID, "bad reflected direction");
+  if ((long long)n * G * M >= (1LL << 31)) return fail(PGPU_ERR_INVALID, "more than 2^31 angular unknowns");
+  // sweep face weights and the table of mu over distinct face normals (SweepFaces)
+  std::vector<double> wout((size_t)F * n, 0.0), windiag((size_t)F * n, 0.0), winw((size_t)F * n, 0.0);
+  std::vector<unsigned char> cls((size_t)F * n, 0);
+  std::map<std::vector<long long>, int> cls_of;
+  std::vector<const double*> cls_nrm;
+  bool use_tab = true;
+  for (int i = 0; i < n; i++)
+    for (int f = 0; f < op->num_cell_faces[i]; f++) {
+      const size_t o = (size_t)f * n + i;
+      const double A = op->areas[o];
+      const int k = op->face_kind[o];
+      if (k == PGPU_FACE_INTERIOR) {
+        wout[o] = op->gauss[o * 4 + 0] * A;
+        windiag[o] = op->gauss[o * 4 + 2] * A;
+        winw[o] = op->gauss[o * 4 + 3] * A;
+      } else if (k == PGPU_FACE_VACUUM) {
+        wout[o] = A * (1.0 - lsdiag[o]);
+      } else if (k == PGPU_FACE_REFLECTIVE) {
+        wout[o] = A;
+        winw[o] = A;
+      }
+      const double* nr = op->normals + o * 3;
+      std::vector<long long> key{std::llround(nr[0] * 1e12), std::llround(nr[1] * 1e12), std::llround(nr[2] * 1e12)};
+      auto it = cls_of.find(key);
+      int id;
+      if (it == cls_of.end()) {
+        id = (int)cls_nrm.size();
+        cls_of[key] = id;
+        cls_nrm.push_back(nr);
+      } else {
+        id = it->second;
+      }
+      if (id > 255) use_tab = false;
+      cls[o] = (unsigned char)(id & 255);
+    }
+  std::vector<double> mutab;
+  if (use_tab) {
+    mutab.assign(cls_nrm.size() * M, 0.0);
+    for (size_t c = 0; c < cls_nrm.size(); c++)
+      for (int m = 0; m < M; m++) {
+        const double* d0 = op->directions + (size_t)m * 3;
+        mutab[c * M + m] = d0[0] * cls_nrm[c][0] + d0[1] * cls_nrm[c][1] + d0[2] * cls_nrm[c][2];
+      }
+  }
   Schedule sched;
   int st = build_schedule(op, sched);
   if (st) return st;
@@ -1215,6 +1319,12 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
   up(d.d_pat_nlev, sched.pat_nlev.data(), sched.pat_nlev.size() * 4);
   up(d.d_lev_ptr, sched.lev_ptr.data(), sched.lev_ptr.size() * 4);
   up(d.d_order, sched.order.data(), sched.order.size() * 4);
+  d.use_tab = use_tab;
+  up(d.cls, cls.data(), Fn);
+  if (use_tab) up(d.mutab, mutab.data(), mutab.size() * 8);
+  up(d.wout, wout.data(), Fn * 8);
+  up(d.windiag, windiag.data(), Fn * 8);
+  up(d.win, winw.data(), Fn * 8);
   if (d.nrefl) {
     up(d.d_slot_cell, slot_cell.data(), slot_cell.size() * 4);
     up(d.d_slot_face, slot_face.data(), slot_face.size() * 4);
