@@ -32,6 +32,9 @@ struct DiffOp {
   const int* __restrict__ mat;  // [n]
   const T* __restrict__ vol;    // [n]
   const T* __restrict__ ss;     // [nm][G][G]
+  const T* __restrict__ chi;    // [nm][G]
+  const T* __restrict__ nsf;    // [nm][G]
+  T lam_s;                      // Wielandt shift: the operator is R - lam_s F
 };
 
 // Device-resident BiCGStab state; every scalar of the iteration stays on the GPU.
@@ -51,7 +54,7 @@ struct OuterScal {
 struct DiffusionData {
   int n = 0, G = 0, F = 0, nm = 0;
   DevBuf nbr, mat, off64, diag64, vol64, ss64, chi, nsf, ksf;
-  DevBuf off32, diag32, vol32, ss32;
+  DevBuf off32, diag32, vol32, ss32, chi32, nsf32;
   DevBuf x, y, b, r64, r32, fs, fs_old, phi, q, P;
   DevBuf w64[9];  // BiCGStab vectors for FP64
   DevBuf w32[9];  // BiCGStab vectors for FP32
@@ -74,6 +77,12 @@ __device__ __forceinline__ T apply_row(const DiffOp<T>& A, const T* __restrict__
   T sc = T(0);
   for (int g2 = 0; g2 < G; g2++)
     if (g2 != g) sc += ssm[g2 * G + g] * x[(size_t)i * G + g2];
+  if (A.lam_s != T(0)) {
+    const T* ns = A.nsf + (size_t)m * G;
+    T f = T(0);
+    for (int g2 = 0; g2 < G; g2++) f += ns[g2] * x[(size_t)i * G + g2];
+    sc += A.lam_s * A.chi[(size_t)m * G + g] * f;
+  }
   acc -= A.vol[i] * sc;
   const size_t nG = (size_t)A.n * G;
   for (int f = 0; f < A.F; f++) {
@@ -282,10 +291,11 @@ __global__ void k_axpy_update(int N, double* y, const T* __restrict__ d) {
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) y[l] += (double)d[l];
 }
 
-// fs_i = V_i sum_g nu_sigma_f x_ig; S = sum_i fs_i; k_new = k * S.
+// fs_i = V_i sum_g nu_sigma_f y_ig; S = sum_i fs_i.  One (shifted) power-iteration step maps
+// a fission source of total 1 to y, so 1/k = lam_s + 1/S (lam_s = 0: k = S).
 __global__ void k_fission_total(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
                                 const double* __restrict__ nsf, const double* __restrict__ y,
-                                double* fs, OuterScal* os, ReduceSlots<1> slots) {
+                                double* fs, OuterScal* os, ReduceSlots<1> slots, double lam_s) {
   double acc[1] = {0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double* ns = nsf + (size_t)mat[i] * G;
@@ -299,17 +309,18 @@ __global__ void k_fission_total(int n, int G, const int* __restrict__ mat, const
   if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
     os->S = tot[0];
     os->k_old = os->k;
-    os->k = os->k * tot[0];
+    os->k = 1.0 / (lam_s + 1.0 / tot[0]);
     os->nonfinite = !(tot[0] == tot[0]) || tot[0] == 0.0;
   }
 }
 
-// x = y / S; fs normalised; change = |fs - fs_old| / |fs|; b = chi fs / k.
+// x = y / S; fs normalised; change = |fs - fs_old| / |fs|; b = chi fs (fission source of
+// total 1).
 __global__ void k_normalize_source(int n, int G, const int* __restrict__ mat, const double* __restrict__ chi,
                                    const double* __restrict__ y, double* x, double* fs, double* fs_old,
                                    double* b, OuterScal* os, ReduceSlots<2> slots) {
   const double invS = 1.0 / os->S;
-  const double invk = 1.0 / os->k;
+  const double invk = 1.0;
   double acc[2] = {0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     for (int g = 0; g < G; g++) x[(size_t)i * G + g] = y[(size_t)i * G + g] * invS;
@@ -323,6 +334,16 @@ __global__ void k_normalize_source(int n, int G, const int* __restrict__ mat, co
   }
   double tot[2];
   if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) os->change = sqrt(tot[0] / tot[1]);
+}
+
+// Wielandt shift schedule (see diffusion_solve).
+constexpr double kShiftDk = 0.05;
+constexpr int kShiftAfter = 3;
+constexpr double kShiftWhenDk = 1e-3;
+
+// y = f x
+__global__ void k_scale_copy(int N, const double* __restrict__ x, double f, double* y) {
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) y[l] = f * x[l];
 }
 
 // Initial flat flux: x = y = 1, fission source and b for k = 1.
@@ -397,14 +418,16 @@ __global__ void k_convert(long long N, const S* __restrict__ a, D* b) {
 
 namespace {
 
-DiffOp<double> op64(const DiffusionData& d) {
+DiffOp<double> op64(const DiffusionData& d, double lam_s = 0.0) {
   return DiffOp<double>{d.n, d.G, d.F, d.nbr.as<int>(), d.off64.as<double>(), d.diag64.as<double>(),
-                        d.mat.as<int>(), d.vol64.as<double>(), d.ss64.as<double>()};
+                        d.mat.as<int>(), d.vol64.as<double>(), d.ss64.as<double>(), d.chi.as<double>(),
+                        d.nsf.as<double>(), lam_s};
 }
 
-DiffOp<float> op32(const DiffusionData& d) {
+DiffOp<float> op32(const DiffusionData& d, double lam_s = 0.0) {
   return DiffOp<float>{d.n, d.G, d.F, d.nbr.as<int>(), d.off32.as<float>(), d.diag32.as<float>(),
-                       d.mat.as<int>(), d.vol32.as<float>(), d.ss32.as<float>()};
+                       d.mat.as<int>(), d.vol32.as<float>(), d.ss32.as<float>(), d.chi32.as<float>(),
+                       d.nsf32.as<float>(), (float)lam_s};
 }
 
 template <int NV>
@@ -426,6 +449,10 @@ int make_fp32(pgpu_problem* p) {
   launch(p, k_convert<double, float>, grid_for(nG), kThreads, s, nG, d.diag64.as<double>(), d.diag32.as<float>());
   launch(p, k_convert<double, float>, grid_for(d.n), kThreads, s, d.n, d.vol64.as<double>(), d.vol32.as<float>());
   launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G * d.G, d.ss64.as<double>(), d.ss32.as<float>());
+  if ((st = dev_alloc(d.chi32, (size_t)d.nm * d.G * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.nsf32, (size_t)d.nm * d.G * 4, &p->bytes))) return st;
+  launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G, d.chi.as<double>(), d.chi32.as<float>());
+  launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G, d.nsf.as<double>(), d.nsf32.as<float>());
   for (int k = 0; k < 9; k++)
     if ((st = dev_alloc(d.w32[k], nG * 4, &p->bytes))) return st;
   if ((st = dev_alloc(d.r32, nG * 4, &p->bytes))) return st;
@@ -515,7 +542,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   launch(p, k_fill, gN, kThreads, s, N, d.y.as<double>(), 1.0);
   launch(p, k_fill, gC, kThreads, s, n, d.fs_old.as<double>(), 0.0);
   launch(p, k_fission_total, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
-                                          d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d));
+                                          d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d), 0.0);
   // the first total only normalises the start vector: keep k = 1
   OuterScal os;
   if ((st = read_outer(p, os))) return st;
@@ -531,8 +558,14 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   double change = 1.0, dk = 1.0, k_prev = 1.0;
   bool converged = false;
   int status = PGPU_OK;
+  // Wielandt shift lam_s = 1/(k + kShiftDk) once k has settled; the inner operator is
+  // R - lam_s F, whose solve maps the normalised fission source to x / (1/k - lam_s).
+  double lam_s = 0.0;
   for (outer = 1; outer <= opt->max_outer; outer++) {
-    // inner solve R y = b by refinement: r = b - R y, correction solve, y += d
+    A = op64(d, lam_s);
+    launch(p, k_scale_copy, gN, kThreads, s, N, (const double*)d.x.as<double>(), 1.0 / (1.0 / k_prev - lam_s),
+           d.y.as<double>());
+    // inner solve (R - lam_s F) y = b by refinement: r = b - A y, correction solve, y += d
     const double tol_in = fmin(1e-3, fmax(1e-13, 0.02 * fmin(change, dk * 1e3)));
     for (int ref = 0; ref < 50; ref++) {
       launch(p, k_residual<float>, gN, kThreads, s, A, d.b.as<double>(), d.y.as<double>(), d.r64.as<double>(),
@@ -544,7 +577,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       int it = 0;
       if (mixed) {
         // FP32 correction solve on the FP32 copy of the FP64 residual
-        DiffOp<float> A32 = op32(d);
+        DiffOp<float> A32 = op32(d, lam_s);
         const double rt = fmax(tol_in / rel, 2e-5);
         if ((st = bicgstab<float>(p, A32, d.w32, d.r32.as<float>(), fmin(rt, 0.5), opt->max_inner, &it))) return st;
         launch(p, k_axpy_update<float>, gN, kThreads, s, N, d.y.as<double>(), d.w32[0].as<float>());
@@ -557,25 +590,24 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       if (it == 0) break;
     }
     launch(p, k_fission_total, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
-                                            d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d));
+                                            d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d), lam_s);
     launch(p, k_normalize_source, gC, kThreads, s, n, G, d.mat.as<int>(), d.chi.as<double>(), d.y.as<double>(),
                                                d.x.as<double>(), d.fs.as<double>(), d.fs_old.as<double>(),
                                                d.b.as<double>(), dos, slots_of<2>(d));
     PGPU_CUDA(cudaGetLastError());
     if ((st = read_outer(p, os))) return st;
-    if (os.nonfinite || !(os.k == os.k)) return fail(PGPU_ERR_NAN, "non-finite fission source");
+    if (os.nonfinite || !(os.k == os.k) || !(os.k > 0.0)) return fail(PGPU_ERR_NAN, "non-finite fission source");
     change = os.change;
     dk = fabs(os.k - k_prev);
     k_prev = os.k;
     if (opt->verbose)
-      std::printf("pgpu diffusion outer %d: k = %.12f  dk = %.3e  source change = %.3e  inner = %d\n",
-                  outer, os.k, dk, change, inner_total);
-    // y keeps the unnormalised iterate; restart the next inner solve from x
-    PGPU_CUDA(cudaMemcpyAsync(d.y.ptr, d.x.ptr, (size_t)N * 8, cudaMemcpyDeviceToDevice, s));
+      std::printf("pgpu diffusion outer %d: k = %.12f  dk = %.3e  source change = %.3e  inner = %d  lam_s = %.6f\n",
+                  outer, os.k, dk, change, inner_total, lam_s);
     if (dk < opt->tol_k && change < opt->tol_flux) {
       converged = true;
       break;
     }
+    if (outer >= kShiftAfter && dk < kShiftWhenDk) lam_s = 1.0 / (os.k + kShiftDk);
   }
   if (!converged) status = PGPU_ERR_NOT_CONVERGED;
 
