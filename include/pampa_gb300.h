@@ -220,6 +220,26 @@ long long pgpu_problem_upload_bytes(pgpu_problem* p);
 
 void pgpu_problem_destroy(pgpu_problem* p);
 
+/* Flux normalisation and power fields that allocate nothing (no counterpart in the
+ * reference; it is the normalisation its NeutronicSolver::normalizeScalarFlux and
+ * calculatePowerAndProductionRate apply).  For callers that cannot call cudaMalloc --
+ * their device memory belongs to another allocator, or they must not grow the device
+ * footprint after start-up.  Every pointer is a caller-owned device buffer:
+ *   in:  materials[n], volumes[n], kappa_sigma_f[nm*G], nu_sigma_f[nm*G], phi[n*G]
+ *   out: phi_out[n*G] = phi * power / p0 with p0 = sum phi kappa_sigma_f V,
+ *        q[n] (cell power), P[n] (production rate, divided by keff),
+ *        total_power[1] and negatives[1] (may be NULL)
+ * Work goes into `stream` (a cudaStream_t; NULL = legacy default stream).  The scratch
+ * is a fixed __device__ array inside the library holding at most 1,048,576 cells;
+ * larger num_cells is rejected with PGPU_ERR_INVALID.  The first call on a device looks
+ * up that array's device address (cudaGetSymbolAddress) and must happen before any
+ * stream capture.  All calls share the one array and it keeps the previous call's
+ * contents: calls that overlap on the GPU (different streams, no ordering) race. */
+int pgpu_normalize_power_noalloc(int num_cells, int num_groups, const int* materials, const double* volumes,
+                                 const double* kappa_sigma_f, const double* nu_sigma_f, const double* phi,
+                                 double power, double keff, double* phi_out, double* q, double* P,
+                                 double* total_power, int* negatives, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -98,6 +98,8 @@ SYMBOLS = {
     "pgpu_problem_device_bytes": (C.c_longlong, [C.c_void_p]),
     "pgpu_problem_upload_bytes": (C.c_longlong, [C.c_void_p]),
     "pgpu_problem_destroy": (None, [C.c_void_p]),
+    "pgpu_normalize_power_noalloc": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 5 + [C.c_double, C.c_double]
+                                     + [C.c_void_p] * 6),
 }
 
 
