@@ -90,6 +90,14 @@ struct SNData {
   DevBuf area32, nrm32, gauss32, lsw32, lsdiag32, vol32, dirs32, w32, st32, ss32, chi32, nsf32;
   // sweep face weights (SweepFaces)
   DevBuf cls, mutab, wout, windiag, win, mutab32, wout32, windiag32, win32;
+  DevBuf rden, rden32;  // reciprocal sweep diagonals [n*G*M], built on first sweep
+  DevBuf sweep_ptrs;    // SweepPtrs block read by the level kernels
+  cudaGraphExec_t sweep_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][iso]
+  ~SNData() {
+    for (auto& row : sweep_graph)
+      for (auto& g : row)
+        if (g) cudaGraphExecDestroy(g);
+  }
   bool use_tab = false;
   bool have32 = false;
   // schedule on device
@@ -159,16 +167,60 @@ struct SweepFaces {
   const T* __restrict__ windiag;          // [F][n]
   const T* __restrict__ win;              // [F][n]
   int upwind;                             // windiag == 0 everywhere
+  const T* __restrict__ rden;             // [n*G*M] 1 / diagonal, precomputed (or null)
 };
+
+template <typename T>
+__device__ __forceinline__ T sweep_mu(const SNOp<T>& A, const SweepFaces<T>& W, int f, int i, int m) {
+  return W.cls ? W.mutab[W.cls[(size_t)f * A.n + i] * A.M + m] : mu_of(A, f, i, m);
+}
+
+// The sweep's diagonal, sigma_t V + outflow terms + inflow-side diagonal terms, depends on
+// the operator only; its reciprocal is stored once per (cell, group, direction) so a sweep
+// does no FP64 division and skips the outflow faces.
+template <typename T>
+__global__ void k_sweep_rden(SNOp<T> A, SweepFaces<T> W, T* rden) {
+  const int G = A.G, M = A.M, n = A.n;
+  const long long N = (long long)n * G * M;
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    const int m = (int)(l % M);
+    const int r = (int)(l / M);
+    const int i = r / G, g = r - i * G;
+    T den = A.st[A.mat[i] * G + g] * A.vol[i];
+    for (int f = 0; f < A.nf[i]; f++) {
+      const size_t o = (size_t)f * n + i;
+      const T mu = sweep_mu(A, W, f, i, m);
+      if (mu > T(0)) den += mu * W.wout[o];
+      else if (!W.upwind) den += mu * W.windiag[o];
+    }
+    rden[l] = T(1) / den;
+  }
+}
+
+// Buffers of one sweep, read by every level kernel from device memory so that the level
+// launches can be captured once in a CUDA graph and replayed for any buffers.
+struct SweepPtrs {
+  const void* src;
+  const void* bnd;
+  void* psi;
+};
+
+__global__ void k_set_sweep_ptrs(SweepPtrs* P, const void* src, const void* bnd, void* psi) {
+  P->src = src;
+  P->bnd = bnd;
+  P->psi = psi;
+}
 
 template <typename T>
 __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* __restrict__ pat_dirs_ptr,
                               const int* __restrict__ pat_dirs, const int* __restrict__ pat_lev_ptr,
                               const int* __restrict__ pat_nlev, const int* __restrict__ lev_ptr,
-                              const int* __restrict__ order, const T* __restrict__ src, int iso,
-                              const T* __restrict__ bnd, T* psi) {
+                              const int* __restrict__ order, const SweepPtrs* __restrict__ P, int iso) {
   const int p = blockIdx.y;
   if (level >= pat_nlev[p]) return;
+  const T* __restrict__ src = static_cast<const T*>(P->src);
+  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
+  T* psi = static_cast<T*>(P->psi);
   const int d0 = pat_dirs_ptr[p], nd = pat_dirs_ptr[p + 1] - d0;
   const int* lp = lev_ptr + pat_lev_ptr[p];
   const int c0 = lp[level], nc = lp[level + 1] - c0;
@@ -182,13 +234,28 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
     const int g = rest - ci * G;
     const int i = ord[c0 + ci];
     const int m = pat_dirs[d0 + di];
-    const int mt = A.mat[i];
-    T den = A.st[mt * G + g] * A.vol[i];
-    T num = iso ? src[(size_t)i * G + g] : src[((size_t)i * G + g) * M + m];
+    const size_t l = ((size_t)i * G + g) * M + m;
+    T num = iso ? src[(size_t)i * G + g] : src[l];
     const int nfi = A.nf[i];
+    if (W.rden) {
+      for (int f = 0; f < nfi; f++) {
+        const T mu = sweep_mu(A, W, f, i, m);
+        if (mu > T(0)) continue;
+        const size_t o = (size_t)f * n + i;
+        const int kd = A.kind[o];
+        if (kd == PGPU_FACE_INTERIOR) {
+          num -= (mu * W.win[o]) * psi[((size_t)A.nbr[o] * G + g) * M + m];
+        } else if (kd == PGPU_FACE_REFLECTIVE && bnd) {
+          num -= (mu * W.win[o]) * bnd[((size_t)A.rslot[o] * G + g) * M + m];
+        }
+      }
+      psi[l] = num * W.rden[l];
+      continue;
+    }
+    T den = A.st[A.mat[i] * G + g] * A.vol[i];
     for (int f = 0; f < nfi; f++) {
       const size_t o = (size_t)f * n + i;
-      const T mu = W.cls ? W.mutab[W.cls[o] * M + m] : mu_of(A, f, i, m);
+      const T mu = sweep_mu(A, W, f, i, m);
       if (mu > T(0)) {
         den += mu * W.wout[o];
       } else {
@@ -201,7 +268,7 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
         }
       }
     }
-    psi[((size_t)i * G + g) * M + m] = num / den;
+    psi[l] = num / den;
   }
 }
 
@@ -706,13 +773,30 @@ SweepFaces<T> make_faces(const SNData& d);
 template <>
 SweepFaces<double> make_faces<double>(const SNData& d) {
   return SweepFaces<double>{d.use_tab ? d.cls.as<unsigned char>() : nullptr, d.mutab.as<double>(),
-                            d.wout.as<double>(), d.windiag.as<double>(), d.win.as<double>(), d.upwind ? 1 : 0};
+                            d.wout.as<double>(), d.windiag.as<double>(), d.win.as<double>(), d.upwind ? 1 : 0,
+                            d.rden.as<double>()};
 }
 
 template <>
 SweepFaces<float> make_faces<float>(const SNData& d) {
   return SweepFaces<float>{d.use_tab ? d.cls.as<unsigned char>() : nullptr, d.mutab32.as<float>(),
-                           d.wout32.as<float>(), d.windiag32.as<float>(), d.win32.as<float>(), d.upwind ? 1 : 0};
+                           d.wout32.as<float>(), d.windiag32.as<float>(), d.win32.as<float>(), d.upwind ? 1 : 0,
+                           d.rden32.as<float>()};
+}
+
+// Reciprocal sweep diagonals in precision T, computed on first use.
+template <typename T>
+int ensure_rden(pgpu_problem* p, const SNOp<T>& A) {
+  SNData& d = *p->sn;
+  DevBuf& buf = sizeof(T) == 8 ? d.rden : d.rden32;
+  if (buf.ptr) return PGPU_OK;
+  const long long N = (long long)d.n * d.G * d.M;
+  SweepFaces<T> W = make_faces<T>(d);  // rden still null here
+  int st = dev_alloc(buf, (size_t)N * sizeof(T), &p->bytes);
+  if (st) return st;
+  launch(p, k_sweep_rden<T>, grid_for(N), kThreads, p->stream, A, W, buf.as<T>());
+  PGPU_CUDA(cudaGetLastError());
+  return PGPU_OK;
 }
 
 }  // namespace
@@ -727,15 +811,36 @@ template <typename T>
 int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd, T* psi) {
   SNData& d = *p->sn;
   const Schedule& S = d.sched;
+  int rst = ensure_rden<T>(p, A);
+  if (rst) return rst;
   const SweepFaces<T> W = make_faces<T>(d);
+  if (!d.sweep_ptrs.ptr && (rst = dev_alloc(d.sweep_ptrs, sizeof(SweepPtrs), &p->bytes))) return rst;
+  SweepPtrs* P = d.sweep_ptrs.as<SweepPtrs>();
+  // the level launches are captured once per (precision, source kind) and replayed; the
+  // buffers of this sweep go through the device-side pointer block
+  launch(p, k_set_sweep_ptrs, 1, 1, p->stream, P, (const void*)src, (const void*)bnd, (void*)psi);
+  cudaGraphExec_t& gx = d.sweep_graph[sizeof(T) == 8 ? 0 : 1][iso ? 1 : 0];
+  if (!gx) {
+    cudaGraph_t graph;
+    PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    for (int L = 0; L < S.nlev; L++) {
+      dim3 grid(S.grid_x[L], S.npat);
+      k_sweep_level<T><<<grid, kThreads, 0, p->stream>>>(
+          A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
+          d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
+    }
+    PGPU_CUDA(cudaStreamEndCapture(p->stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&gx, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      gx = nullptr;
+      return fail(PGPU_ERR_CUDA, std::string("sweep graph instantiation: ") + cudaGetErrorString(e));
+    }
+  }
   cudaEvent_t e0;
   prof_begin(p, &e0);
-  for (int L = 0; L < S.nlev; L++) {
-    dim3 grid(S.grid_x[L], S.npat);
-    launch(p, k_sweep_level<T>, grid, kThreads, p->stream,
-        A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
-        d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), src, iso, bnd, psi);
-  }
+  PGPU_CUDA(cudaGraphLaunch(gx, p->stream));
+  p->launches += S.nlev;
   // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
   // direction update (2 s_v), the source read per cell-group (s_v, or s_v per update for
   // an angular source), the scalar-flux moment written per cell-group (s_v) and the
