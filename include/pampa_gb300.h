@@ -192,6 +192,10 @@ typedef struct {
   const double* chi;
   const double* nu_sigma_f;
   const double* kappa_sigma_f;
+  /* Optional: the mesh is a full nx*ny*nz Cartesian box in the reference's cell order
+   * (x fastest, faces -y,+x,+y,-x,-z,+z).  Set all three to 0 otherwise.  When given and
+   * verified, sweeps use tiles of 4x4x4 cells instead of per-cell upwind levels. */
+  int cart_nx, cart_ny, cart_nz;
 } pgpu_sn_operator;
 
 /* Upload an SN operator; builds the per-direction upwind sweep schedule. */

@@ -67,7 +67,8 @@ class pgpu_sn_operator(C.Structure):
                 ("normals", _pd), ("gauss", _pd), ("reflect_axis", _pi), ("ls_weight", _pd),
                 ("materials", _pi), ("volumes", _pd), ("directions", _pd), ("weights", _pd),
                 ("reflected", _pi), ("sigma_t", _pd), ("sigma_s", _pd), ("chi", _pd),
-                ("nu_sigma_f", _pd), ("kappa_sigma_f", _pd)]
+                ("nu_sigma_f", _pd), ("kappa_sigma_f", _pd), ("cart_nx", C.c_int), ("cart_ny", C.c_int),
+                ("cart_nz", C.c_int)]
 
 
 # Every C symbol declared in include/pampa_gb300.h, with its ctypes signature.

@@ -92,6 +92,11 @@ struct SNData {
   DevBuf cls, mutab, wout, windiag, win, mutab32, wout32, windiag32, win32;
   DevBuf rden, rden32;  // reciprocal sweep diagonals [n*G*M], built on first sweep
   DevBuf sweep_ptrs;    // SweepPtrs block read by the level kernels
+  // tiled sweep of a full Cartesian box (k_sweep_kba), when the operator qualifies
+  bool kba = false;
+  int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_ndiag = 0, kba_nd = 0;
+  std::vector<int> kba_grid_x;
+  DevBuf d_tdiag_ptr, d_tiles, d_pat_sign;
   cudaGraphExec_t sweep_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][iso]
   ~SNData() {
     for (auto& row : sweep_graph)
@@ -269,6 +274,101 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
       }
     }
     psi[l] = num / den;
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Tiled sweep for a full Cartesian box (KBA-style wavefront over tiles).
+//
+// The box is cut into kTile^3-cell tiles.  For octant pattern p the tiles are visited in
+// diagonals of the octant-oriented tile index (tx' + ty' + tz' = D), one launch per D for
+// all patterns at once (blockIdx.y); a CTA sweeps one tile for all directions of its
+// pattern and all groups through the tile's own 3*(kTile-1)+1 cell diagonals, keeping
+// the tile's angular flux in shared memory.  Inflow from the upwind tile comes from the
+// global psi written by the previous launch.  Same arithmetic as k_sweep_level: psi =
+// (src - sum_inflow mu * w_in * psi_up) * rden.
+// ---------------------------------------------------------------------------------
+constexpr int kTile = 4;
+constexpr int kTileCells = kTile * kTile * kTile;
+constexpr int kTileDiags = 3 * (kTile - 1) + 1;
+
+// oriented local cells of a tile (lx | ly << 2 | lz << 4) sorted by lx + ly + lz
+__constant__ unsigned char c_tile_cell[kTileCells];
+__constant__ int c_tile_dptr[kTileDiags + 1];
+
+struct KbaGeom {
+  int nx, ny, ntx, nty, ntz;
+  const int* __restrict__ tdiag_ptr;  // [ndiag + 1]
+  const int* __restrict__ tiles;      // [ntiles][3] oriented tile coordinates, by diagonal
+  const int* __restrict__ pat_sign;   // [npat][3]: +1 sweeps towards +axis, -1 towards -axis
+  const int* __restrict__ pat_dirs_ptr;
+  const int* __restrict__ pat_dirs;
+};
+
+template <typename T>
+__device__ __forceinline__ void kba_inflow(const SNOp<T>& A, const SweepFaces<T>& W, const T* __restrict__ psi,
+                                           const T* __restrict__ bnd, const T* tpsi, bool in_tile, int tidx,
+                                           int f, int i, int g, int m, T om, T& num) {
+  const T mu = om > T(0) ? -om : om;  // Omega . n of the inflow face of an axis-aligned cell
+  const size_t o = (size_t)f * A.n + i;
+  if (in_tile) {
+    num -= (mu * W.win[o]) * tpsi[tidx];
+    return;
+  }
+  const int kd = A.kind[o];
+  if (kd == PGPU_FACE_INTERIOR)
+    num -= (mu * W.win[o]) * psi[((size_t)A.nbr[o] * A.G + g) * A.M + m];
+  else if (kd == PGPU_FACE_REFLECTIVE && bnd)
+    num -= (mu * W.win[o]) * bnd[((size_t)A.rslot[o] * A.G + g) * A.M + m];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_sweep_kba(SNOp<T> A, SweepFaces<T> W, KbaGeom K, int diag,
+                                                  const SweepPtrs* __restrict__ P, int iso) {
+  extern __shared__ unsigned char kba_smem[];
+  T* tpsi = reinterpret_cast<T*>(kba_smem);
+  const int p = blockIdx.y;
+  const int t0 = K.tdiag_ptr[diag];
+  if ((int)blockIdx.x >= K.tdiag_ptr[diag + 1] - t0) return;  // uniform per block
+  const T* __restrict__ src = static_cast<const T*>(P->src);
+  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
+  T* psi = static_cast<T*>(P->psi);
+  const int sx = K.pat_sign[p * 3], sy = K.pat_sign[p * 3 + 1], sz = K.pat_sign[p * 3 + 2];
+  const int d0 = K.pat_dirs_ptr[p], nd = K.pat_dirs_ptr[p + 1] - d0;
+  const int* tc = K.tiles + 3 * (t0 + blockIdx.x);
+  const int bx = (sx > 0 ? tc[0] : K.ntx - 1 - tc[0]) * kTile;
+  const int by = (sy > 0 ? tc[1] : K.nty - 1 - tc[1]) * kTile;
+  const int bz = (sz > 0 ? tc[2] : K.ntz - 1 - tc[2]) * kTile;
+  const int G = A.G, M = A.M, ndG = nd * G, nx = K.nx, nxy = K.nx * K.ny;
+  for (int dd = 0; dd < kTileDiags; dd++) {
+    const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
+    for (int it = threadIdx.x; it < cn * ndG; it += blockDim.x) {
+      const int c = it / ndG;
+      const int r = it - c * ndG;
+      const int g = r / nd;
+      const int di = r - g * nd;
+      const int pk = c_tile_cell[cb + c];
+      const int lx = pk & 3, ly = (pk >> 2) & 3, lz = (pk >> 4) & 3;
+      const int x = bx + (sx > 0 ? lx : kTile - 1 - lx);
+      const int y = by + (sy > 0 ? ly : kTile - 1 - ly);
+      const int z = bz + (sz > 0 ? lz : kTile - 1 - lz);
+      const int i = x + nx * y + nxy * z;
+      const int m = K.pat_dirs[d0 + di];
+      const size_t l = ((size_t)i * G + g) * M + m;
+      const T* om = A.dirs + (size_t)m * 3;
+      const int slot = g * nd + di;
+      T num = iso ? src[(size_t)i * G + g] : src[l];
+      kba_inflow(A, W, psi, bnd, tpsi, lx > 0, (((lz * kTile + ly) * kTile + lx - 1) * ndG) + slot,
+                 sx > 0 ? 3 : 1, i, g, m, om[0], num);
+      kba_inflow(A, W, psi, bnd, tpsi, ly > 0, (((lz * kTile + ly - 1) * kTile + lx) * ndG) + slot,
+                 sy > 0 ? 0 : 2, i, g, m, om[1], num);
+      kba_inflow(A, W, psi, bnd, tpsi, lz > 0, ((((lz - 1) * kTile + ly) * kTile + lx) * ndG) + slot,
+                 sz > 0 ? 4 : 5, i, g, m, om[2], num);
+      const T v = num * W.rden[l];
+      psi[l] = v;
+      tpsi[(((lz * kTile + ly) * kTile + lx) * ndG) + slot] = v;
+    }
+    __syncthreads();
   }
 }
 
@@ -820,14 +920,26 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   // buffers of this sweep go through the device-side pointer block
   launch(p, k_set_sweep_ptrs, 1, 1, p->stream, P, (const void*)src, (const void*)bnd, (void*)psi);
   cudaGraphExec_t& gx = d.sweep_graph[sizeof(T) == 8 ? 0 : 1][iso ? 1 : 0];
+  const int nlaunch = d.kba ? d.kba_ndiag : S.nlev;
   if (!gx) {
     cudaGraph_t graph;
     PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
-    for (int L = 0; L < S.nlev; L++) {
-      dim3 grid(S.grid_x[L], S.npat);
-      k_sweep_level<T><<<grid, kThreads, 0, p->stream>>>(
-          A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
-          d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
+    if (d.kba) {
+      const KbaGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, d.d_tdiag_ptr.as<int>(),
+                      d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_pat_dirs_ptr.as<int>(),
+                      d.d_pat_dirs.as<int>()};
+      const size_t smem = (size_t)kTileCells * d.kba_nd * d.G * sizeof(T);
+      for (int D = 0; D < d.kba_ndiag; D++) {
+        dim3 grid(d.kba_grid_x[D], S.npat);
+        k_sweep_kba<T><<<grid, kThreads, smem, p->stream>>>(A, W, K, D, P, iso);
+      }
+    } else {
+      for (int L = 0; L < S.nlev; L++) {
+        dim3 grid(S.grid_x[L], S.npat);
+        k_sweep_level<T><<<grid, kThreads, 0, p->stream>>>(
+            A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
+            d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
+      }
     }
     PGPU_CUDA(cudaStreamEndCapture(p->stream, &graph));
     cudaError_t e = cudaGraphInstantiate(&gx, graph, 0);
@@ -840,14 +952,14 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   cudaEvent_t e0;
   prof_begin(p, &e0);
   PGPU_CUDA(cudaGraphLaunch(gx, p->stream));
-  p->launches += S.nlev;
+  p->launches += nlaunch;
   // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
   // direction update (2 s_v), the source read per cell-group (s_v, or s_v per update for
   // an angular source), the scalar-flux moment written per cell-group (s_v) and the
   // material id per cell-group (4 B).
   const double sv = (double)sizeof(T);
   const double N = (double)d.n * d.G * d.M, nG = (double)d.n * d.G;
-  prof_end(p, e0, S.nlev, N * 2.0 * sv + nG * (2.0 * sv + 4.0) + (iso ? 0.0 : N * sv));
+  prof_end(p, e0, nlaunch, N * 2.0 * sv + nG * (2.0 * sv + 4.0) + (iso ? 0.0 : N * sv));
   PGPU_CUDA(cudaGetLastError());
   sweeps_done++;
   return PGPU_OK;
@@ -1281,6 +1393,88 @@ void sn_destroy(pgpu_problem* p) {
   p->sn = nullptr;
 }
 
+// Plan of the tiled sweep: verifies that the operator is a full Cartesian box in the
+// reference's cell and face order, with sides that are multiples of kTile and one sign per
+// axis for every sweep pattern; returns false (level sweeps are used) otherwise.
+struct KbaPlan {
+  int ntx, nty, ntz, ndiag, nd;
+  std::vector<int> tdiag_ptr, tiles, pat_sign, grid_x;
+};
+
+static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) {
+  const int nx = op->cart_nx, ny = op->cart_ny, nz = op->cart_nz, n = op->num_cells;
+  if (nx <= 0 || ny <= 0 || nz <= 0 || (long long)nx * ny * nz != n || op->num_faces != 6) return false;
+  if (nx % kTile || ny % kTile || nz % kTile) return false;
+  // face f: normal and neighbour offset in the reference's order -y, +x, +y, -x, -z, +z
+  const int nrm[6][3] = {{0, -1, 0}, {1, 0, 0}, {0, 1, 0}, {-1, 0, 0}, {0, 0, -1}, {0, 0, 1}};
+  for (int z = 0, i = 0; z < nz; z++)
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++, i++) {
+        if (op->num_cell_faces[i] != 6) return false;
+        for (int f = 0; f < 6; f++) {
+          const size_t o = (size_t)f * n + i;
+          for (int a = 0; a < 3; a++)
+            if (op->normals[o * 3 + a] != (double)nrm[f][a]) return false;
+          const int x2 = x + nrm[f][0], y2 = y + nrm[f][1], z2 = z + nrm[f][2];
+          const bool inside = x2 >= 0 && x2 < nx && y2 >= 0 && y2 < ny && z2 >= 0 && z2 < nz;
+          if (inside != (op->face_kind[o] == PGPU_FACE_INTERIOR)) return false;
+          if (inside && op->neighbors[o] != x2 + nx * (y2 + ny * z2)) return false;
+        }
+      }
+  K.nd = 0;
+  for (int p = 0; p < S.npat; p++) {
+    int sg[3] = {0, 0, 0};
+    for (int k = S.pat_dirs_ptr[p]; k < S.pat_dirs_ptr[p + 1]; k++) {
+      const double* d = op->directions + (size_t)S.pat_dirs[k] * 3;
+      for (int a = 0; a < 3; a++) {
+        const int s = d[a] > 0.0 ? 1 : (d[a] < 0.0 ? -1 : 0);
+        if (s == 0 || (sg[a] != 0 && sg[a] != s)) return false;
+        sg[a] = s;
+      }
+    }
+    for (int a = 0; a < 3; a++) K.pat_sign.push_back(sg[a]);
+    K.nd = std::max(K.nd, S.pat_dirs_ptr[p + 1] - S.pat_dirs_ptr[p]);
+  }
+  if ((size_t)kTileCells * K.nd * op->num_groups * sizeof(double) > 48 * 1024) return false;
+  K.ntx = nx / kTile;
+  K.nty = ny / kTile;
+  K.ntz = nz / kTile;
+  K.ndiag = K.ntx + K.nty + K.ntz - 2;
+  K.tdiag_ptr.assign(1, 0);
+  for (int D = 0; D < K.ndiag; D++) {
+    int cnt = 0;
+    for (int tz = 0; tz < K.ntz; tz++)
+      for (int ty = 0; ty < K.nty; ty++) {
+        const int tx = D - ty - tz;
+        if (tx < 0 || tx >= K.ntx) continue;
+        K.tiles.push_back(tx);
+        K.tiles.push_back(ty);
+        K.tiles.push_back(tz);
+        cnt++;
+      }
+    K.tdiag_ptr.push_back(K.tdiag_ptr.back() + cnt);
+    K.grid_x.push_back(cnt);
+  }
+  return true;
+}
+
+static int kba_tables() {
+  unsigned char cells[kTileCells];
+  int dptr[kTileDiags + 1];
+  int k = 0;
+  for (int dd = 0; dd < kTileDiags; dd++) {
+    dptr[dd] = k;
+    for (int lz = 0; lz < kTile; lz++)
+      for (int ly = 0; ly < kTile; ly++)
+        for (int lx = 0; lx < kTile; lx++)
+          if (lx + ly + lz == dd) cells[k++] = (unsigned char)(lx | (ly << 2) | (lz << 4));
+  }
+  dptr[kTileDiags] = k;
+  PGPU_CUDA(cudaMemcpyToSymbol(c_tile_cell, cells, sizeof(cells)));
+  PGPU_CUDA(cudaMemcpyToSymbol(c_tile_dptr, dptr, sizeof(dptr)));
+  return PGPU_OK;
+}
+
 }  // namespace pgpu
 
 extern "C" {
@@ -1430,6 +1624,23 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
   up(d.wout, wout.data(), Fn * 8);
   up(d.windiag, windiag.data(), Fn * 8);
   up(d.win, winw.data(), Fn * 8);
+  KbaPlan kp;
+  if (st == PGPU_OK && kba_plan(op, sched, kp)) {
+    if ((st = kba_tables()) == PGPU_OK) {
+      d.kba = true;
+      d.kba_nx = op->cart_nx;
+      d.kba_ny = op->cart_ny;
+      d.kba_ntx = kp.ntx;
+      d.kba_nty = kp.nty;
+      d.kba_ntz = kp.ntz;
+      d.kba_ndiag = kp.ndiag;
+      d.kba_nd = kp.nd;
+      d.kba_grid_x = kp.grid_x;
+      up(d.d_tdiag_ptr, kp.tdiag_ptr.data(), kp.tdiag_ptr.size() * 4);
+      up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
+      up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
+    }
+  }
   if (d.nrefl) {
     up(d.d_slot_cell, slot_cell.data(), slot_cell.size() * 4);
     up(d.d_slot_face, slot_face.data(), slot_face.size() * 4);

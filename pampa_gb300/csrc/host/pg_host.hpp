@@ -93,6 +93,7 @@ struct Mesh {
   int num_dims = 0;
   int num_cells = 0;
   int fmax = 0;
+  int cart_nx = 0, cart_ny = 0, cart_nz = 0;  // full Cartesian box without void cells, else 0
   std::vector<double> volumes;    // n
   std::vector<double> centroids;  // n*3
   std::vector<int> materials;     // n

@@ -134,6 +134,11 @@ int read_cartesian_mesh(const std::string& path, Mesh& mesh) {
   mesh.boundaries = boundaries;
   mesh.bcs = bcs;
   mesh.has_bcs = has_bcs;
+  if (n == nx * NY * NZ && nz > 0) {  // full 3D box: the GPU may sweep it in tiles
+    mesh.cart_nx = nx;
+    mesh.cart_ny = NY;
+    mesh.cart_nz = NZ;
+  }
   std::vector<std::string> dirs{"-x", "+x"};
   if (ny > 0) { dirs.push_back("-y"); dirs.push_back("+y"); }
   if (nz > 0) { dirs.push_back("-z"); dirs.push_back("+z"); }

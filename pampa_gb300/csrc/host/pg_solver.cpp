@@ -541,6 +541,9 @@ int SNSolver::buildProblem() {
   op.chi = chi.data();
   op.nu_sigma_f = nsf.data();
   op.kappa_sigma_f = ksf.data();
+  op.cart_nx = mesh.cart_nx;
+  op.cart_ny = mesh.cart_ny;
+  op.cart_nz = mesh.cart_nz;
   int code = pgpu_sn_create(opt_.device, &op, &problem_);
   PG_CHECK(code != PGPU_OK, std::string("unable to upload the SN operator: ") + pgpu_last_error());
   return 0;

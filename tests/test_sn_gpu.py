@@ -50,7 +50,9 @@ def test_dropin_sn_known_answers(case, case_input):
     assert q.sum() == pytest.approx(1.0, rel=1e-12)
 
 
-@pytest.mark.parametrize("shape,order", [((6, 6, 4), 4), ((4, 4, 3), 8)])
+@pytest.mark.parametrize("shape,order", [((6, 6, 4), 4), ((4, 4, 3), 8),     # level-set sweeps
+                                         ((8, 8, 4), 4), ((4, 4, 4), 8),     # tiled (4^3) sweeps
+                                         ((12, 8, 8), 2)])
 def test_synthetic_sn_3d_reflective(shape, order, tmp_path):
     from pampa_gb300 import workloads as wl
     nx, ny, nz = shape
