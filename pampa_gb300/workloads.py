@@ -184,3 +184,84 @@ def diffusion_3d_7g(out_dir: str, nx: int = 256, ny: int = 256, nz: int = 128, c
     with open(path, "w") as fh:
         fh.write("\n".join(lines) + "\n")
     return path
+
+
+def materials_4g(rng, num: int):
+    """`num` 4-group materials (isotropic scattering, one non-fissile) from the 2-group ranges,
+    log-interpolated between the fast and thermal values."""
+    mats = []
+    G = 4
+    t = np.linspace(0.0, 1.0, G)
+    for m in range(num):
+        D1, D2 = _u(rng, RANGES_2G["D1"]), _u(rng, RANGES_2G["D2"])
+        a1, a2 = _u(rng, RANGES_2G["sa1"]), _u(rng, RANGES_2G["sa2"])
+        f1, f2 = _u(rng, (0.001, 0.006)), _u(rng, (0.02, 0.14))
+        D = list(np.exp(np.log(D1) * (1 - t) + np.log(D2) * t))
+        sa = list(np.exp(np.log(a1) * (1 - t) + np.log(a2) * t))
+        nsf = list(np.exp(np.log(f1) * (1 - t) + np.log(f2) * t))
+        if m == num - 1:
+            nsf = [0.0] * G
+        ss = np.zeros((G, G))
+        for g in range(G):
+            ss[g, g] = _u(rng, (0.2, 0.5))
+            if g + 1 < G:
+                ss[g, g + 1] = _u(rng, RANGES_2G["s12"])
+        chi = [0.8, 0.2, 0.0, 0.0]
+        mats.append(dict(G=G, D=D, sa=sa, nsf=nsf, ss=ss, chi=chi))
+    return mats
+
+
+def write_hex_prism_mesh(path: str, nq: int, nr: int, pitch: float, nz: int, dz: float, layout: np.ndarray):
+    """Unstructured extruded mesh of an nq x nr lattice of flat-topped hexagons (flat-to-flat
+    = pitch), CCW points, every lateral boundary edge on the default boundary 'exterior'
+    (declared before dz so the default boundary keeps its own index), vacuum everywhere.
+    layout: (nz, nr, nq) 1-based material indices."""
+    s = pitch / math.sqrt(3.0)           # side length
+    pts: dict = {}
+    coords = []
+    cells = []
+
+    def pid(x, y):
+        key = (round(x, 9), round(y, 9))
+        if key not in pts:
+            pts[key] = len(coords)
+            coords.append((x, y))
+        return pts[key]
+
+    for r in range(nr):
+        for q in range(nq):
+            cx = 1.5 * s * q
+            cy = pitch * (r + 0.5 * (q & 1))
+            ids = [pid(cx + s * math.cos(math.radians(60 * k)), cy + s * math.sin(math.radians(60 * k)))
+                   for k in range(6)]
+            cells.append(ids)
+    lines = [f"points {len(coords)}"] + [f"{x:.9f} {y:.9f}" for x, y in coords]
+    lines += [f"cells {len(cells)} {6 * len(cells)}"] + [" ".join(str(i) for i in c) for c in cells]
+    lines += ["boundary exterior 0", f"dz -{nz}", f"{dz:.6f}", "",
+              "bc exterior vacuum", "bc -z vacuum", "bc +z vacuum", ""]
+    lines.append(f"materials {layout.size}")
+    for row in layout.reshape(nz, -1):
+        lines.append(" ".join(str(int(v)) for v in row))
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+
+
+def sn_hex(out_dir: str, nq: int = 200, nr: int = 200, nz: int = 40, pitch: float = 2.0, dz: float = 2.0,
+           order: int = 8, seed: int = 5, block: int = 10) -> str:
+    """4-group S_N on a hexagonal-prism lattice (200 x 200 hexagons x 40 layers by default,
+    1.6M cells), 5 materials in blocks of `block` hexagons, vacuum boundaries."""
+    os.makedirs(out_dir, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    mats = materials_4g(rng, 5)
+    layout = _block_layout(rng, (nz, nr, nq), (max(1, nz // 4), block, block), 5)
+    write_hex_prism_mesh(os.path.join(out_dir, "mesh.pmp"), nq, nr, pitch, nz, dz, layout)
+    for k, m in enumerate(mats):
+        write_material(os.path.join(out_dir, f"mat{k + 1}.pmp"), m, diffusion=False)
+    lines = ["mesh unstructured mesh.pmp", ""]
+    lines += [f"material mat{k + 1} mat{k + 1}.pmp" for k in range(len(mats))]
+    lines += ["", "solver sn {", "   energy-groups 4", f"   order {order}",
+              "   mixed-face-interpolation 1.0", "   least-squares-boundary-interpolation 0", "}"]
+    path = os.path.join(out_dir, "input.pmp")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return path

@@ -105,3 +105,16 @@ def test_sn_default_delta_negative_flux_is_an_error(tmp_path, capfd):
     with pg.Pampa(path, "-silent") as p:
         with pytest.raises(pg.PampaError, match="negative"):
             p.solve()
+
+
+@pytest.mark.parametrize("order", [4, 8])
+def test_hex_prism_lattice(order, tmp_path):
+    """Unstructured extruded hexagonal prisms (level-set sweeps over 8-face cells)."""
+    from pampa_gb300 import workloads as wl
+    path = wl.sn_hex(str(tmp_path), nq=5, nr=4, nz=3, order=order, block=2)
+    ref = po.run_input(path)
+    with pg.Pampa(path, "-silent") as p:
+        p.solve()
+        assert abs(p.keff - ref["keff"]) <= K_TOL, (p.keff, ref["keff"])
+        assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= FLUX_TOL
+        assert rel_l2(p.field("angular-flux"), ref["psi"]) <= FLUX_TOL
