@@ -287,7 +287,9 @@ def run_ours(args, rank, world, local):
 
     peaks = measured_peaks()
     achieved = kern_b / kern_s / 1e9 if kern_s > 0 else None
-    roof = dict(bound="hbm", kernel="k_sweep_level" if w["kind"] == "sn" else "k_bicg_v/k_bicg_t (SpMV)",
+    kname = results[-1]["kernel_name"]
+    kname = kname.decode() if isinstance(kname, bytes) else str(kname)
+    roof = dict(bound="hbm", kernel=kname,
                 achieved=achieved, peak=peaks["hbm_gbs"], unit="GB/s",
                 frac=(achieved / peaks["hbm_gbs"]) if achieved else None, peak_source=peaks["source"],
                 traffic=None, launches=kern_n,

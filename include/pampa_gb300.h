@@ -89,7 +89,9 @@ enum {
   PGPU_ERR_NOT_CONVERGED = 3,  /* an iteration cap was reached                      */
   PGPU_ERR_NEGATIVE_FLUX = 4,  /* normalised flux has negative entries              */
   PGPU_ERR_NAN = 5,            /* a reduction produced NaN/Inf                       */
-  PGPU_ERR_NO_MEMORY = 6       /* device memory budget exceeded                     */
+  PGPU_ERR_NO_MEMORY = 6,      /* device memory budget exceeded                     */
+  PGPU_ERR_TIMEOUT = 7         /* a bounded device-side wait ran out; the kernel     */
+                               /* returned early and the results are not valid       */
 };
 
 enum { PGPU_FP64 = 0, PGPU_MIXED = 1 };
@@ -122,6 +124,7 @@ typedef struct {
   double kernel_seconds;
   long long kernel_launches;
   double kernel_bytes;
+  char kernel_name[32];  /* name of that kernel (NUL-terminated)                         */
 } pgpu_stats;
 
 /* Fill *opt with the defaults listed above. */

@@ -24,7 +24,7 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libpampa_gb300.so")
 
 PGPU_OK, PGPU_ERR_INVALID, PGPU_ERR_CUDA, PGPU_ERR_NOT_CONVERGED, PGPU_ERR_NEGATIVE_FLUX, \
-    PGPU_ERR_NAN, PGPU_ERR_NO_MEMORY = range(7)
+    PGPU_ERR_NAN, PGPU_ERR_NO_MEMORY, PGPU_ERR_TIMEOUT = range(8)
 PGPU_FP64, PGPU_MIXED = 0, 1
 FACE_INTERIOR, FACE_VACUUM, FACE_REFLECTIVE, FACE_NONE = range(4)
 
@@ -45,7 +45,8 @@ class pgpu_stats(C.Structure):
     _fields_ = [("keff", C.c_double), ("outer_iterations", C.c_int), ("inner_iterations", C.c_int),
                 ("sweeps", C.c_int), ("residual", C.c_double), ("seconds", C.c_double),
                 ("status", C.c_int), ("launches", C.c_longlong), ("kernel_seconds", C.c_double),
-                ("kernel_launches", C.c_longlong), ("kernel_bytes", C.c_double)]
+                ("kernel_launches", C.c_longlong), ("kernel_bytes", C.c_double),
+                ("kernel_name", C.c_char * 32)]
 
 
 _P = C.POINTER

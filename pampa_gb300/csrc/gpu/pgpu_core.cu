@@ -79,6 +79,7 @@ int pgpu_problem_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* sta
     stats->kernel_seconds = pgpu::prof_collect(p);
     stats->kernel_launches = p->prof_launches;
     stats->kernel_bytes = p->prof_bytes;
+    std::snprintf(stats->kernel_name, sizeof(stats->kernel_name), "%s", p->prof_name);
   }
   p->profile = false;
   stats->status = st;

@@ -479,6 +479,7 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   BiScal hs;
   // When profiling, iterations go one per chunk so no timed SpMV launch is a no-op.
   int chunk = p->profile ? 1 : 4;
+  p->prof_name = "k_bicg_v+k_bicg_t";
   // Algorithmic bytes of one SpMV fused with its dot product: per row the diagonal, the
   // F face coefficients, x, y and the dot partner (F + 4 values), plus per cell the F
   // neighbour indices, the material id and the volume.

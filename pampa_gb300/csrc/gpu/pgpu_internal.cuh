@@ -171,6 +171,7 @@ struct pgpu_problem {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   double prof_bytes = 0.0;
   long long prof_launches = 0;
+  const char* prof_name = "";
 };
 
 namespace pgpu {

@@ -92,11 +92,12 @@ struct SNData {
   DevBuf cls, mutab, wout, windiag, win, mutab32, wout32, windiag32, win32;
   DevBuf rden, rden32;  // reciprocal sweep diagonals [n*G*M], built on first sweep
   DevBuf sweep_ptrs;    // SweepPtrs block read by the level kernels
-  // tiled sweep of a full Cartesian box (k_sweep_kba), when the operator qualifies
+  // dataflow tiled sweep of a full Cartesian box (k_sweep_flow), when the operator qualifies
   bool kba = false;
-  int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_ndiag = 0, kba_nd = 0;
-  std::vector<int> kba_grid_x;
-  DevBuf d_tdiag_ptr, d_tiles, d_pat_sign;
+  int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_nd = 0, kba_ntasks = 0;
+  int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
+  int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
+  DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
   cudaGraphExec_t sweep_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][iso]
   ~SNData() {
     for (auto& row : sweep_graph)
@@ -184,6 +185,18 @@ __device__ __forceinline__ T sweep_mu(const SNOp<T>& A, const SweepFaces<T>& W, 
 // the operator only; its reciprocal is stored once per (cell, group, direction) so a sweep
 // does no FP64 division and skips the outflow faces.
 template <typename T>
+__device__ __forceinline__ T sweep_den(const SNOp<T>& A, const SweepFaces<T>& W, int i, int g, int m) {
+  T den = A.st[A.mat[i] * A.G + g] * A.vol[i];
+  for (int f = 0; f < A.nf[i]; f++) {
+    const size_t o = (size_t)f * A.n + i;
+    const T mu = sweep_mu(A, W, f, i, m);
+    if (mu > T(0)) den += mu * W.wout[o];
+    else if (!W.upwind) den += mu * W.windiag[o];
+  }
+  return den;
+}
+
+template <typename T>
 __global__ void k_sweep_rden(SNOp<T> A, SweepFaces<T> W, T* rden) {
   const int G = A.G, M = A.M, n = A.n;
   const long long N = (long long)n * G * M;
@@ -191,14 +204,7 @@ __global__ void k_sweep_rden(SNOp<T> A, SweepFaces<T> W, T* rden) {
     const int m = (int)(l % M);
     const int r = (int)(l / M);
     const int i = r / G, g = r - i * G;
-    T den = A.st[A.mat[i] * G + g] * A.vol[i];
-    for (int f = 0; f < A.nf[i]; f++) {
-      const size_t o = (size_t)f * n + i;
-      const T mu = sweep_mu(A, W, f, i, m);
-      if (mu > T(0)) den += mu * W.wout[o];
-      else if (!W.upwind) den += mu * W.windiag[o];
-    }
-    rden[l] = T(1) / den;
+    rden[l] = T(1) / sweep_den(A, W, i, g, m);
   }
 }
 
@@ -278,97 +284,214 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 }
 
 // ---------------------------------------------------------------------------------
-// Tiled sweep for a full Cartesian box (KBA-style wavefront over tiles).
+// Dataflow tiled sweep for a full Cartesian box (one persistent launch per sweep).
 //
-// The box is cut into kTile^3-cell tiles.  For octant pattern p the tiles are visited in
-// diagonals of the octant-oriented tile index (tx' + ty' + tz' = D), one launch per D for
-// all patterns at once (blockIdx.y); a CTA sweeps one tile for all directions of its
-// pattern and all groups through the tile's own 3*(kTile-1)+1 cell diagonals, keeping
-// the tile's angular flux in shared memory.  Inflow from the upwind tile comes from the
-// global psi written by the previous launch.  Same arithmetic as k_sweep_level: psi =
-// (src - sum_inflow mu * w_in * psi_up) * rden.
+// The box is cut into kTile^3-cell tiles; a task is one tile for one octant pattern (all
+// the pattern's directions and all groups).  Tasks are numbered tile diagonal by tile
+// diagonal of the octant-oriented tile index (tx' + ty' + tz' = D), so the upwind tasks
+// of a task -- (tx'-1, ty', tz'), (tx', ty'-1, tz'), (tx', ty', tz'-1) of the same
+// pattern -- always come earlier.  Each CTA takes the next task from an atomic counter,
+// waits until the flags of its upwind tasks hold this sweep's epoch, sweeps the tile
+// through its 3*(kTile-1)+1 cell diagonals with the tile's angular flux in shared memory,
+// writes psi and publishes its own flag.  A task is taken only by a running CTA, and only
+// after every earlier task was taken by a running CTA, so every wait ends; the waits are
+// bounded all the same (kFlowSpinLimit): a wait that runs out sets the error word, every
+// later wait then returns at once, and the host reports PGPU_ERR_TIMEOUT.
+//
+// Arithmetic per (cell, group, direction): psi = rd * src + sum over the three inflow
+// faces of a_f * psi_upwind, with rd = 1 / diagonal and a_f = -(mu_f * w_in,f) * rd.
+// (rd, a_x, a_y, a_z) depend on the cell only through its material, volume and face
+// weights, so cells are grouped into classes with equal values and the coefficients are
+// read from a small per-class table; a mesh with too many classes uses the per-row
+// reciprocal diagonal instead (psi = (src - sum mu_f w_in,f psi_upwind) * rden).
 // ---------------------------------------------------------------------------------
 constexpr int kTile = 4;
 constexpr int kTileCells = kTile * kTile * kTile;
 constexpr int kTileDiags = 3 * (kTile - 1) + 1;
+constexpr int kFlowThreads = 128;
+constexpr unsigned int kFlowSpinLimit = 1u << 22;  // ~0.4 s of polling at 100 ns
 
 // oriented local cells of a tile (lx | ly << 2 | lz << 4) sorted by lx + ly + lz
 __constant__ unsigned char c_tile_cell[kTileCells];
 __constant__ int c_tile_dptr[kTileDiags + 1];
 
-struct KbaGeom {
-  int nx, ny, ntx, nty, ntz;
-  const int* __restrict__ tdiag_ptr;  // [ndiag + 1]
-  const int* __restrict__ tiles;      // [ntiles][3] oriented tile coordinates, by diagonal
-  const int* __restrict__ pat_sign;   // [npat][3]: +1 sweeps towards +axis, -1 towards -axis
-  const int* __restrict__ pat_dirs_ptr;
-  const int* __restrict__ pat_dirs;
+struct FlowSync {
+  unsigned int next;   // task counter of the running sweep
+  unsigned int epoch;  // sweep number; a task's flag holds it once the task is done
+  unsigned int error;  // set when a wait ran out
+  unsigned int pad;
 };
 
-template <typename T>
-__device__ __forceinline__ void kba_inflow(const SNOp<T>& A, const SweepFaces<T>& W, const T* __restrict__ psi,
-                                           const T* __restrict__ bnd, const T* tpsi, bool in_tile, int tidx,
-                                           int f, int i, int g, int m, T om, T& num) {
-  const T mu = om > T(0) ? -om : om;  // Omega . n of the inflow face of an axis-aligned cell
-  const size_t o = (size_t)f * A.n + i;
-  if (in_tile) {
-    num -= (mu * W.win[o]) * tpsi[tidx];
-    return;
-  }
-  const int kd = A.kind[o];
-  if (kd == PGPU_FACE_INTERIOR)
-    num -= (mu * W.win[o]) * psi[((size_t)A.nbr[o] * A.G + g) * A.M + m];
-  else if (kd == PGPU_FACE_REFLECTIVE && bnd)
-    num -= (mu * W.win[o]) * bnd[((size_t)A.rslot[o] * A.G + g) * A.M + m];
+struct FlowGeom {
+  int nx, ny, ntx, nty, ntz, npat, nd, ntasks;
+  const int* __restrict__ tiles;         // [ntiles][3] oriented tile coordinates, by diagonal
+  const int* __restrict__ pat_sign;      // [npat][3]: +1 sweeps towards +axis, -1 towards -axis
+  const int* __restrict__ pat_dirs_ptr;  // [npat + 1]
+  const int* __restrict__ pat_dirs;
+  const unsigned short* __restrict__ ccls;  // [n] cell class, or null (per-row rden)
+  const void* coef;                         // [ncls][G][M][4] (rd, a_x, a_y, a_z) in T
+  FlowSync* sync;
+  unsigned int* flags;  // [npat][ntz][nty][ntx] by oriented tile coordinates
+};
+
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 
+__device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits until *flag == epoch; returns without waiting once any wait of the sweep ran out.
+__device__ __forceinline__ void flow_wait(const unsigned int* flag, unsigned int epoch, unsigned int* error) {
+  for (unsigned int it = 0;; it++) {
+    if (ld_acquire_gpu(flag) == epoch) return;
+    if (*(volatile unsigned int*)error) return;
+    if (it >= kFlowSpinLimit) {
+      atomicExch(error, 1u);
+      return;
+    }
+    __nanosleep(100);
+  }
+}
+
+__global__ void k_flow_begin(FlowSync* s) {
+  s->next = 0u;
+  s->epoch = s->epoch + 1u;
+}
+
+// Upwind value along one axis for a cell whose upwind neighbour lies outside the tile:
+// the neighbour's psi (written by an earlier task, read through L2), the reflective
+// inflow, or nothing at a vacuum face.  Returns false when there is no inflow.
 template <typename T>
-__global__ void __launch_bounds__(256) k_sweep_kba(SNOp<T> A, SweepFaces<T> W, KbaGeom K, int diag,
-                                                  const SweepPtrs* __restrict__ P, int iso) {
-  extern __shared__ unsigned char kba_smem[];
-  T* tpsi = reinterpret_cast<T*>(kba_smem);
-  const int p = blockIdx.y;
-  const int t0 = K.tdiag_ptr[diag];
-  if ((int)blockIdx.x >= K.tdiag_ptr[diag + 1] - t0) return;  // uniform per block
+__device__ __forceinline__ bool flow_outside(const SNOp<T>& A, const T* psi, const T* __restrict__ bnd,
+                                             bool in_box, int nb, int f, int i, int g, int m, T& up) {
+  if (in_box) {
+    up = __ldcg(psi + ((size_t)nb * A.G + g) * A.M + m);
+    return true;
+  }
+  const size_t o = (size_t)f * A.n + i;
+  if (A.kind[o] == PGPU_FACE_REFLECTIVE && bnd) {
+    up = bnd[((size_t)A.rslot[o] * A.G + g) * A.M + m];
+    return true;
+  }
+  return false;
+}
+
+template <typename T, bool kClass>
+__global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFaces<T> W, FlowGeom K,
+                                                             const SweepPtrs* __restrict__ P, int iso) {
+  extern __shared__ __align__(16) unsigned char flow_smem[];
+  T* tpsi = reinterpret_cast<T*>(flow_smem);
+  __shared__ int s_task;
   const T* __restrict__ src = static_cast<const T*>(P->src);
   const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
   T* psi = static_cast<T*>(P->psi);
-  const int sx = K.pat_sign[p * 3], sy = K.pat_sign[p * 3 + 1], sz = K.pat_sign[p * 3 + 2];
-  const int d0 = K.pat_dirs_ptr[p], nd = K.pat_dirs_ptr[p + 1] - d0;
-  const int* tc = K.tiles + 3 * (t0 + blockIdx.x);
-  const int bx = (sx > 0 ? tc[0] : K.ntx - 1 - tc[0]) * kTile;
-  const int by = (sy > 0 ? tc[1] : K.nty - 1 - tc[1]) * kTile;
-  const int bz = (sz > 0 ? tc[2] : K.ntz - 1 - tc[2]) * kTile;
-  const int G = A.G, M = A.M, ndG = nd * G, nx = K.nx, nxy = K.nx * K.ny;
-  for (int dd = 0; dd < kTileDiags; dd++) {
-    const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
-    for (int it = threadIdx.x; it < cn * ndG; it += blockDim.x) {
-      const int c = it / ndG;
-      const int r = it - c * ndG;
-      const int g = r / nd;
-      const int di = r - g * nd;
-      const int pk = c_tile_cell[cb + c];
-      const int lx = pk & 3, ly = (pk >> 2) & 3, lz = (pk >> 4) & 3;
-      const int x = bx + (sx > 0 ? lx : kTile - 1 - lx);
-      const int y = by + (sy > 0 ? ly : kTile - 1 - ly);
-      const int z = bz + (sz > 0 ? lz : kTile - 1 - lz);
-      const int i = x + nx * y + nxy * z;
-      const int m = K.pat_dirs[d0 + di];
-      const size_t l = ((size_t)i * G + g) * M + m;
-      const T* om = A.dirs + (size_t)m * 3;
-      const int slot = g * nd + di;
-      T num = iso ? src[(size_t)i * G + g] : src[l];
-      kba_inflow(A, W, psi, bnd, tpsi, lx > 0, (((lz * kTile + ly) * kTile + lx - 1) * ndG) + slot,
-                 sx > 0 ? 3 : 1, i, g, m, om[0], num);
-      kba_inflow(A, W, psi, bnd, tpsi, ly > 0, (((lz * kTile + ly - 1) * kTile + lx) * ndG) + slot,
-                 sy > 0 ? 0 : 2, i, g, m, om[1], num);
-      kba_inflow(A, W, psi, bnd, tpsi, lz > 0, ((((lz - 1) * kTile + ly) * kTile + lx) * ndG) + slot,
-                 sz > 0 ? 4 : 5, i, g, m, om[2], num);
-      const T v = num * W.rden[l];
-      psi[l] = v;
-      tpsi[(((lz * kTile + ly) * kTile + lx) * ndG) + slot] = v;
+  const T* __restrict__ coef = static_cast<const T*>(K.coef);
+  const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
+  const int G = A.G, M = A.M, n = A.n, ndG = K.nd * G;
+  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
+  const int slot = threadIdx.x % ndG, cl = threadIdx.x / ndG, ncl = blockDim.x / ndG;
+  const int g = slot / K.nd, di = slot - g * K.nd;
+  for (;;) {
+    if (threadIdx.x == 0) s_task = (int)atomicAdd(&K.sync->next, 1u);
+    __syncthreads();
+    const int t = s_task;
+    if (t >= K.ntasks) return;  // uniform over the CTA
+    const int j = t / K.npat, p = t - j * K.npat;
+    const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
+    unsigned int* pflags = K.flags + (size_t)p * ntiles;
+    if (threadIdx.x < 3) {
+      const int a = threadIdx.x;
+      const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
+      if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
     }
     __syncthreads();
+    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
+    const int bx = (sx > 0 ? tx : K.ntx - 1 - tx) * kTile;
+    const int by = (sy > 0 ? ty : K.nty - 1 - ty) * kTile;
+    const int bz = (sz > 0 ? tz : K.ntz - 1 - tz) * kTile;
+    const int d0 = K.pat_dirs_ptr[p];
+    const bool active = cl < ncl && di < K.pat_dirs_ptr[p + 1] - d0;
+    const int m = active ? K.pat_dirs[d0 + di] : 0;
+    // inflow faces (reference order -y, +x, +y, -x, -z, +z) and their mu (general path)
+    const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
+    T mux = T(0), muy = T(0), muz = T(0);
+    if (!kClass && active) {
+      mux = -fabs(A.dirs[(size_t)m * 3]);
+      muy = -fabs(A.dirs[(size_t)m * 3 + 1]);
+      muz = -fabs(A.dirs[(size_t)m * 3 + 2]);
+    }
+    for (int dd = 0; dd < kTileDiags; dd++) {
+      const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
+      if (active) {
+        for (int c = cl; c < cn; c += ncl) {
+          const int pk = c_tile_cell[cb + c];
+          const int lx = pk & 3, ly = (pk >> 2) & 3, lz = (pk >> 4) & 3;
+          const int x = bx + (sx > 0 ? lx : kTile - 1 - lx);
+          const int y = by + (sy > 0 ? ly : kTile - 1 - ly);
+          const int z = bz + (sz > 0 ? lz : kTile - 1 - lz);
+          const int i = x + nx * y + nxy * z;
+          const size_t l = ((size_t)i * G + g) * M + m;
+          const int tl = ((lz * kTile + ly) * kTile + lx) * ndG + slot;
+          const T s = iso ? src[(size_t)i * G + g] : src[l];
+          T ux = T(0), uy = T(0), uz = T(0);
+          bool hx = true, hy = true, hz = true;
+          if (lx > 0) ux = tpsi[tl - ndG];
+          else hx = flow_outside(A, psi, bnd, sx > 0 ? x > 0 : x < nx - 1, i - sx, fx, i, g, m, ux);
+          if (ly > 0) uy = tpsi[tl - kTile * ndG];
+          else hy = flow_outside(A, psi, bnd, sy > 0 ? y > 0 : y < K.ny - 1, i - sy * nx, fy, i, g, m, uy);
+          if (lz > 0) uz = tpsi[tl - kTile * kTile * ndG];
+          else hz = flow_outside(A, psi, bnd, sz > 0 ? z > 0 : z < A.n / nxy - 1, i - sz * nxy, fz, i, g, m, uz);
+          T v;
+          if (kClass) {
+            const T* cf = coef + (((size_t)K.ccls[i] * G + g) * M + m) * 4;
+            v = cf[0] * s;
+            if (hx) v += cf[1] * ux;
+            if (hy) v += cf[2] * uy;
+            if (hz) v += cf[3] * uz;
+          } else {
+            T num = s;
+            if (hx) num -= (mux * W.win[(size_t)fx * n + i]) * ux;
+            if (hy) num -= (muy * W.win[(size_t)fy * n + i]) * uy;
+            if (hz) num -= (muz * W.win[(size_t)fz * n + i]) * uz;
+            v = num * W.rden[l];
+          }
+          psi[l] = v;
+          tpsi[tl] = v;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
+    }
+  }
+}
+
+// Per-class sweep coefficients (rd, a_x, a_y, a_z) for every (class, group, direction),
+// evaluated on a representative cell of the class with the same diagonal as k_sweep_rden.
+template <typename T>
+__global__ void k_sweep_coef(SNOp<T> A, SweepFaces<T> W, int ncls, const int* __restrict__ rep, T* coef) {
+  const int G = A.G, M = A.M;
+  const long long N = (long long)ncls * G * M;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < N; r += (long long)gridDim.x * blockDim.x) {
+    const int m = (int)(r % M);
+    const int cg = (int)(r / M);
+    const int c = cg / G, g = cg - c * G;
+    const int i = rep[c];
+    const T rd = T(1) / sweep_den(A, W, i, g, m);
+    coef[r * 4] = rd;
+    // inflow face of axis a: the -a face when Omega_a > 0, the +a face otherwise
+    const int fminus[3] = {3, 0, 4}, fplus[3] = {1, 2, 5};
+    for (int a = 0; a < 3; a++) {
+      const int f = A.dirs[(size_t)m * 3 + a] > T(0) ? fminus[a] : fplus[a];
+      const T mu = sweep_mu(A, W, f, i, m);
+      coef[r * 4 + 1 + a] = -(mu * W.win[(size_t)f * A.n + i]) * rd;
+    }
   }
 }
 
@@ -907,36 +1030,77 @@ namespace {
 
 int sweeps_done = 0;
 
+// Per-class sweep coefficients in precision T (dataflow sweep with cell classes), computed
+// on first use.
+template <typename T>
+int ensure_coef(pgpu_problem* p, const SNOp<T>& A) {
+  SNData& d = *p->sn;
+  DevBuf& buf = sizeof(T) == 8 ? d.coef : d.coef32;
+  if (buf.ptr) return PGPU_OK;
+  const long long N = (long long)d.ncls * d.G * d.M;
+  SweepFaces<T> W = make_faces<T>(d);
+  int st = dev_alloc(buf, (size_t)N * 4 * sizeof(T), &p->bytes);
+  if (st) return st;
+  launch(p, k_sweep_coef<T>, grid_for(N), kThreads, p->stream, A, W, d.ncls, (const int*)d.d_crep.as<int>(),
+         buf.as<T>());
+  PGPU_CUDA(cudaGetLastError());
+  return PGPU_OK;
+}
+
+// Persistent grid of the dataflow sweep: every CTA that fits on the device at once, at
+// most one per task.
+template <typename T, bool kClass>
+int flow_grid(SNData& d, size_t smem) {
+  int& grid = d.flow_grid[sizeof(T) == 8 ? 0 : 1];
+  if (grid) return grid;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_flow<T, kClass>, kFlowThreads, smem) != cudaSuccess ||
+      per_sm < 1)
+    return 0;
+  grid = std::min(d.kba_ntasks, sms * per_sm);
+  return grid;
+}
+
 template <typename T>
 int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd, T* psi) {
   SNData& d = *p->sn;
   const Schedule& S = d.sched;
-  int rst = ensure_rden<T>(p, A);
+  const bool cls = d.kba && d.ncls > 0;
+  int rst = cls ? ensure_coef<T>(p, A) : ensure_rden<T>(p, A);
   if (rst) return rst;
   const SweepFaces<T> W = make_faces<T>(d);
   if (!d.sweep_ptrs.ptr && (rst = dev_alloc(d.sweep_ptrs, sizeof(SweepPtrs), &p->bytes))) return rst;
   SweepPtrs* P = d.sweep_ptrs.as<SweepPtrs>();
-  // the level launches are captured once per (precision, source kind) and replayed; the
+  // the sweep's launches are captured once per (precision, source kind) and replayed; the
   // buffers of this sweep go through the device-side pointer block
   launch(p, k_set_sweep_ptrs, 1, 1, p->stream, P, (const void*)src, (const void*)bnd, (void*)psi);
   cudaGraphExec_t& gx = d.sweep_graph[sizeof(T) == 8 ? 0 : 1][iso ? 1 : 0];
-  const int nlaunch = d.kba ? d.kba_ndiag : S.nlev;
+  const int nlaunch = d.kba ? 2 : S.nlev;
   if (!gx) {
+    int grid = 0;
+    const size_t smem = (size_t)kTileCells * d.kba_nd * d.G * sizeof(T);
+    if (d.kba) {
+      grid = cls ? flow_grid<T, true>(d, smem) : flow_grid<T, false>(d, smem);
+      if (grid < 1) return fail(PGPU_ERR_CUDA, "occupancy query of the dataflow sweep failed");
+    }
     cudaGraph_t graph;
     PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     if (d.kba) {
-      const KbaGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, d.d_tdiag_ptr.as<int>(),
-                      d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_pat_dirs_ptr.as<int>(),
-                      d.d_pat_dirs.as<int>()};
-      const size_t smem = (size_t)kTileCells * d.kba_nd * d.G * sizeof(T);
-      for (int D = 0; D < d.kba_ndiag; D++) {
-        dim3 grid(d.kba_grid_x[D], S.npat);
-        k_sweep_kba<T><<<grid, kThreads, smem, p->stream>>>(A, W, K, D, P, iso);
-      }
+      const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, S.npat, d.kba_nd, d.kba_ntasks,
+                       d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(),
+                       cls ? d.d_ccls.as<unsigned short>() : nullptr,
+                       cls ? (sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr) : nullptr, d.flow_sync.as<FlowSync>(),
+                       d.flow_flags.as<unsigned int>()};
+      k_flow_begin<<<1, 1, 0, p->stream>>>(K.sync);
+      if (cls)
+        k_sweep_flow<T, true><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
+      else
+        k_sweep_flow<T, false><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
     } else {
       for (int L = 0; L < S.nlev; L++) {
-        dim3 grid(S.grid_x[L], S.npat);
-        k_sweep_level<T><<<grid, kThreads, 0, p->stream>>>(
+        dim3 g(S.grid_x[L], S.npat);
+        k_sweep_level<T><<<g, kThreads, 0, p->stream>>>(
             A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
             d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
       }
@@ -953,6 +1117,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   prof_begin(p, &e0);
   PGPU_CUDA(cudaGraphLaunch(gx, p->stream));
   p->launches += nlaunch;
+  p->prof_name = d.kba ? "k_sweep_flow" : "k_sweep_level";
   // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
   // direction update (2 s_v), the source read per cell-group (s_v, or s_v per update for
   // an angular source), the scalar-flux moment written per cell-group (s_v) and the
@@ -1146,8 +1311,12 @@ int norm_of(pgpu_problem* p, long long len, const T* x, double* out) {
 }
 
 int read_outer(pgpu_problem* p, SNOuter& os) {
-  PGPU_CUDA(cudaMemcpyAsync(&os, p->sn->oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
+  SNData& d = *p->sn;
+  FlowSync fs{0u, 0u, 0u, 0u};
+  PGPU_CUDA(cudaMemcpyAsync(&os, d.oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
+  if (d.kba) PGPU_CUDA(cudaMemcpyAsync(&fs, d.flow_sync.ptr, sizeof(fs), cudaMemcpyDeviceToHost, p->stream));
   PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  if (fs.error) return fail(PGPU_ERR_TIMEOUT, "sweep: a wait for an upwind tile ran out (kernel returned early)");
   return PGPU_OK;
 }
 
@@ -1208,6 +1377,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   std::memset(&init, 0, sizeof(init));
   init.k = 1.0;
   PGPU_CUDA(cudaMemcpyAsync(dos, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+  if (d.kba) PGPU_CUDA(cudaMemsetAsync(&d.flow_sync.as<FlowSync>()->error, 0, sizeof(unsigned int), s));
   launch(p, k_fill<double>, gG, kThreads, s, (long long)nG, phi0, 1.0);
   PGPU_CUDA(cudaMemsetAsync(x64, 0, len * 8, s));
   launch(p, k_fill<double>, grid_for(phi_space ? nG : N), kThreads, s, phi_space ? (long long)nG : N, x64, 1.0);
@@ -1397,8 +1567,8 @@ void sn_destroy(pgpu_problem* p) {
 // reference's cell and face order, with sides that are multiples of kTile and one sign per
 // axis for every sweep pattern; returns false (level sweeps are used) otherwise.
 struct KbaPlan {
-  int ntx, nty, ntz, ndiag, nd;
-  std::vector<int> tdiag_ptr, tiles, pat_sign, grid_x;
+  int ntx, nty, ntz, nd, ntasks;
+  std::vector<int> tiles, pat_sign;
 };
 
 static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) {
@@ -1436,13 +1606,13 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
     K.nd = std::max(K.nd, S.pat_dirs_ptr[p + 1] - S.pat_dirs_ptr[p]);
   }
   if ((size_t)kTileCells * K.nd * op->num_groups * sizeof(double) > 48 * 1024) return false;
+  if (K.nd * op->num_groups > kFlowThreads) return false;
   K.ntx = nx / kTile;
   K.nty = ny / kTile;
   K.ntz = nz / kTile;
-  K.ndiag = K.ntx + K.nty + K.ntz - 2;
-  K.tdiag_ptr.assign(1, 0);
-  for (int D = 0; D < K.ndiag; D++) {
-    int cnt = 0;
+  // tiles in oriented coordinates, tile diagonal by tile diagonal
+  const int ndiag = K.ntx + K.nty + K.ntz - 2;
+  for (int D = 0; D < ndiag; D++)
     for (int tz = 0; tz < K.ntz; tz++)
       for (int ty = 0; ty < K.nty; ty++) {
         const int tx = D - ty - tz;
@@ -1450,10 +1620,56 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
         K.tiles.push_back(tx);
         K.tiles.push_back(ty);
         K.tiles.push_back(tz);
-        cnt++;
       }
-    K.tdiag_ptr.push_back(K.tdiag_ptr.back() + cnt);
-    K.grid_x.push_back(cnt);
+  const long long ntasks = (long long)K.ntx * K.nty * K.ntz * S.npat;
+  if (ntasks >= (1LL << 31)) return false;
+  K.ntasks = (int)ntasks;
+  return true;
+}
+
+// Cell classes of the dataflow sweep's coefficient table: cells with the same material,
+// volume and, per face, kind, normal class and sweep weights have the same (rd, a_x, a_y,
+// a_z) for every group and direction.  Returns false when the table would hold more than
+// kMaxClassTable bytes in FP64 (the per-row reciprocal diagonal is used instead).
+constexpr size_t kMaxClassTable = 8u << 20;
+
+static bool kba_classes(const pgpu_sn_operator* op, const std::vector<unsigned char>& ncls,
+                        const std::vector<double>& wout, const std::vector<double>& windiag,
+                        const std::vector<double>& win, std::vector<unsigned short>& ccls, std::vector<int>& rep) {
+  const int n = op->num_cells, F = op->num_faces, G = op->num_groups, M = op->num_dirs;
+  const size_t per_class = (size_t)G * M * 4 * sizeof(double);
+  std::map<std::vector<unsigned long long>, int> ids;
+  std::vector<unsigned long long> key((size_t)2 + (size_t)F * 5);
+  auto bits = [](double v) {
+    unsigned long long u;
+    std::memcpy(&u, &v, sizeof(u));
+    return u;
+  };
+  ccls.assign(n, 0);
+  rep.clear();
+  for (int i = 0; i < n; i++) {
+    key[0] = (unsigned long long)op->materials[i];
+    key[1] = bits(op->volumes[i]);
+    for (int f = 0; f < F; f++) {
+      const size_t o = (size_t)f * n + i;
+      unsigned long long* k = key.data() + 2 + (size_t)f * 5;
+      k[0] = (unsigned long long)(unsigned)op->face_kind[o];
+      k[1] = ncls[o];
+      k[2] = bits(wout[o]);
+      k[3] = bits(windiag[o]);
+      k[4] = bits(win[o]);
+    }
+    auto it = ids.find(key);
+    int id;
+    if (it == ids.end()) {
+      id = (int)rep.size();
+      if (id > 65535 || (size_t)(id + 1) * per_class > kMaxClassTable) return false;
+      ids.emplace(key, id);
+      rep.push_back(i);
+    } else {
+      id = it->second;
+    }
+    ccls[i] = (unsigned short)id;
   }
   return true;
 }
@@ -1633,12 +1849,22 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       d.kba_ntx = kp.ntx;
       d.kba_nty = kp.nty;
       d.kba_ntz = kp.ntz;
-      d.kba_ndiag = kp.ndiag;
       d.kba_nd = kp.nd;
-      d.kba_grid_x = kp.grid_x;
-      up(d.d_tdiag_ptr, kp.tdiag_ptr.data(), kp.tdiag_ptr.size() * 4);
+      d.kba_ntasks = kp.ntasks;
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
       up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
+      std::vector<unsigned short> ccls;
+      std::vector<int> crep;
+      if (kba_classes(op, cls, wout, windiag, winw, ccls, crep)) {
+        d.ncls = (int)crep.size();
+        up(d.d_ccls, ccls.data(), ccls.size() * 2);
+        up(d.d_crep, crep.data(), crep.size() * 4);
+      }
+      al(d.flow_sync, sizeof(FlowSync));
+      al(d.flow_flags, (size_t)kp.ntasks * 4);
+      if (st == PGPU_OK && (cudaMemsetAsync(d.flow_sync.ptr, 0, sizeof(FlowSync), p->stream) != cudaSuccess ||
+                            cudaMemsetAsync(d.flow_flags.ptr, 0, (size_t)kp.ntasks * 4, p->stream) != cudaSuccess))
+        st = fail(PGPU_ERR_CUDA, "clearing the sweep flags");
     }
   }
   if (d.nrefl) {
