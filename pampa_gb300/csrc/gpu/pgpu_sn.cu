@@ -98,6 +98,7 @@ struct SNData {
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
+  DevBuf mom;  // per-pattern scalar-flux moments of the dataflow sweep [npat][n*G]
   cudaGraphExec_t sweep_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][iso]
   ~SNData() {
     for (auto& row : sweep_graph)
@@ -214,12 +215,14 @@ struct SweepPtrs {
   const void* src;
   const void* bnd;
   void* psi;
+  void* mom;  // dataflow sweep: per-pattern scalar-flux moments [npat][n*G], or null
 };
 
-__global__ void k_set_sweep_ptrs(SweepPtrs* P, const void* src, const void* bnd, void* psi) {
+__global__ void k_set_sweep_ptrs(SweepPtrs* P, const void* src, const void* bnd, void* psi, void* mom) {
   P->src = src;
   P->bnd = bnd;
   P->psi = psi;
+  P->mom = mom;
 }
 
 template <typename T>
@@ -309,6 +312,7 @@ constexpr int kTile = 4;
 constexpr int kTileCells = kTile * kTile * kTile;
 constexpr int kTileDiags = 3 * (kTile - 1) + 1;
 constexpr int kFlowThreads = 128;
+constexpr size_t kFlowMaxSmem = 160u << 10;  // dynamic shared memory of one CTA
 constexpr unsigned int kFlowSpinLimit = 1u << 22;  // ~0.4 s of polling at 100 ns
 
 // oriented local cells of a tile (lx | ly << 2 | lz << 4) sorted by lx + ly + lz
@@ -334,9 +338,9 @@ struct FlowGeom {
   unsigned int* flags;  // [npat][ntz][nty][ntx] by oriented tile coordinates
 };
 
-__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+__device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
   unsigned int v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
@@ -344,17 +348,19 @@ __device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) 
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Waits until *flag == epoch; returns without waiting once any wait of the sweep ran out.
+// Waits until *flag == epoch (relaxed polling, then one fence for acquire); returns
+// without waiting once any wait of the sweep ran out.
 __device__ __forceinline__ void flow_wait(const unsigned int* flag, unsigned int epoch, unsigned int* error) {
   for (unsigned int it = 0;; it++) {
-    if (ld_acquire_gpu(flag) == epoch) return;
-    if (*(volatile unsigned int*)error) return;
+    if (ld_relaxed_gpu(flag) == epoch) break;
+    if (*(volatile unsigned int*)error) break;
     if (it >= kFlowSpinLimit) {
       atomicExch(error, 1u);
-      return;
+      break;
     }
     __nanosleep(100);
   }
+  __threadfence();
 }
 
 __global__ void k_flow_begin(FlowSync* s) {
@@ -362,37 +368,39 @@ __global__ void k_flow_begin(FlowSync* s) {
   s->epoch = s->epoch + 1u;
 }
 
-// Upwind value along one axis for a cell whose upwind neighbour lies outside the tile:
-// the neighbour's psi (written by an earlier task, read through L2), the reflective
-// inflow, or nothing at a vacuum face.  Returns false when there is no inflow.
+// Global cell index of the tile cell with oriented local coordinates (lx, ly, lz).
+struct FlowTile {
+  int bx, by, bz, sx, sy, sz;
+  __device__ __forceinline__ int x(int lx) const { return bx + (sx > 0 ? lx : kTile - 1 - lx); }
+  __device__ __forceinline__ int y(int ly) const { return by + (sy > 0 ? ly : kTile - 1 - ly); }
+  __device__ __forceinline__ int z(int lz) const { return bz + (sz > 0 ? lz : kTile - 1 - lz); }
+};
+
+// Shared memory of one task: the tile's angular flux, the inflow on its three upwind
+// faces, the isotropic source and the cell classes of its cells.
 template <typename T>
-__device__ __forceinline__ bool flow_outside(const SNOp<T>& A, const T* psi, const T* __restrict__ bnd,
-                                             bool in_box, int nb, int f, int i, int g, int m, T& up) {
-  if (in_box) {
-    up = __ldcg(psi + ((size_t)nb * A.G + g) * A.M + m);
-    return true;
-  }
-  const size_t o = (size_t)f * A.n + i;
-  if (A.kind[o] == PGPU_FACE_REFLECTIVE && bnd) {
-    up = bnd[((size_t)A.rslot[o] * A.G + g) * A.M + m];
-    return true;
-  }
-  return false;
+__host__ __device__ constexpr size_t flow_smem_bytes(int ndG, int G) {
+  return ((size_t)kTileCells * ndG + (size_t)3 * kTile * kTile * ndG + (size_t)kTileCells * G) * sizeof(T) +
+         (size_t)kTileCells * sizeof(int);
 }
 
 template <typename T, bool kClass>
 __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFaces<T> W, FlowGeom K,
                                                              const SweepPtrs* __restrict__ P, int iso) {
   extern __shared__ __align__(16) unsigned char flow_smem[];
-  T* tpsi = reinterpret_cast<T*>(flow_smem);
+  const int G = A.G, M = A.M, n = A.n, ndG = K.nd * G;
+  T* tpsi = reinterpret_cast<T*>(flow_smem);               // [64][ndG]
+  T* tin = tpsi + kTileCells * ndG;                         // [3][16][ndG]
+  T* tsrc = tin + 3 * kTile * kTile * ndG;                  // [64][G]
+  int* tcls = reinterpret_cast<int*>(tsrc + kTileCells * G);  // [64]
   __shared__ int s_task;
   const T* __restrict__ src = static_cast<const T*>(P->src);
   const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
   T* psi = static_cast<T*>(P->psi);
+  T* mom = static_cast<T*>(P->mom);
   const T* __restrict__ coef = static_cast<const T*>(K.coef);
   const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
-  const int G = A.G, M = A.M, n = A.n, ndG = K.nd * G;
-  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
+  const int nx = K.nx, ny = K.ny, nxy = K.nx * K.ny, nz = n / nxy, ntiles = K.ntx * K.nty * K.ntz;
   const int slot = threadIdx.x % ndG, cl = threadIdx.x / ndG, ncl = blockDim.x / ndG;
   const int g = slot / K.nd, di = slot - g * K.nd;
   for (;;) {
@@ -402,21 +410,57 @@ __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFac
     if (t >= K.ntasks) return;  // uniform over the CTA
     const int j = t / K.npat, p = t - j * K.npat;
     const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
+    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
+    const FlowTile tile{(sx > 0 ? tx : K.ntx - 1 - tx) * kTile, (sy > 0 ? ty : K.nty - 1 - ty) * kTile,
+                        (sz > 0 ? tz : K.ntz - 1 - tz) * kTile, sx, sy, sz};
+    const int d0 = K.pat_dirs_ptr[p], ndp = K.pat_dirs_ptr[p + 1] - d0;
     unsigned int* pflags = K.flags + (size_t)p * ntiles;
+    // 1. data that does not depend on the upwind tiles, loaded while they finish
+    if (iso)
+      for (int r = threadIdx.x; r < kTileCells * G; r += blockDim.x) {
+        const int c = r / G, gg = r - c * G;
+        const int i = tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4);
+        tsrc[r] = src[(size_t)i * G + gg];
+      }
+    if (kClass)
+      for (int c = threadIdx.x; c < kTileCells; c += blockDim.x)
+        tcls[c] = K.ccls[tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4)];
+    // 2. wait for the upwind tiles of this pattern
     if (threadIdx.x < 3) {
       const int a = threadIdx.x;
       const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
       if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
     }
     __syncthreads();
-    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
-    const int bx = (sx > 0 ? tx : K.ntx - 1 - tx) * kTile;
-    const int by = (sy > 0 ? ty : K.nty - 1 - ty) * kTile;
-    const int bz = (sz > 0 ? tz : K.ntz - 1 - tz) * kTile;
-    const int d0 = K.pat_dirs_ptr[p];
-    const bool active = cl < ncl && di < K.pat_dirs_ptr[p + 1] - d0;
+    // 3. inflow on the three upwind faces: upwind tile's psi (through L2), reflective
+    //    inflow, or zero at a vacuum face; face a, position (u, v) -> tin[(a*16 + u + 4v)][slot]
+    for (int r = threadIdx.x; r < 3 * kTile * kTile * ndG; r += blockDim.x) {
+      const int fs = r / ndG, sl = r - fs * ndG;
+      const int a = fs >> 4, u = fs & 3, v = (fs >> 2) & 3;
+      const int gg = sl / K.nd, dj = sl - gg * K.nd;
+      T val = T(0);
+      if (dj < ndp) {
+        const int m = K.pat_dirs[d0 + dj];
+        const int lx = a == 0 ? 0 : u, ly = a == 0 ? u : (a == 1 ? 0 : v), lz = a == 2 ? 0 : v;
+        const int x = tile.x(lx), y = tile.y(ly), z = tile.z(lz);
+        const int i = x + nx * y + nxy * z;
+        const int s = a == 0 ? sx : (a == 1 ? sy : sz);
+        const int c = a == 0 ? x : (a == 1 ? y : z), cmax = a == 0 ? nx : (a == 1 ? ny : nz);
+        if (s > 0 ? c > 0 : c < cmax - 1) {
+          const int nb = i - s * (a == 0 ? 1 : (a == 1 ? nx : nxy));
+          val = __ldcg(psi + ((size_t)nb * G + gg) * M + m);
+        } else if (bnd) {
+          const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
+          const size_t o = (size_t)f * n + i;
+          if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd[((size_t)A.rslot[o] * G + gg) * M + m];
+        }
+      }
+      tin[r] = val;
+    }
+    __syncthreads();
+    // 4. the tile's cell diagonals
+    const bool active = cl < ncl && di < ndp;
     const int m = active ? K.pat_dirs[d0 + di] : 0;
-    // inflow faces (reference order -y, +x, +y, -x, -z, +z) and their mu (general path)
     const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
     T mux = T(0), muy = T(0), muz = T(0);
     if (!kClass && active) {
@@ -430,33 +474,25 @@ __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFac
         for (int c = cl; c < cn; c += ncl) {
           const int pk = c_tile_cell[cb + c];
           const int lx = pk & 3, ly = (pk >> 2) & 3, lz = (pk >> 4) & 3;
-          const int x = bx + (sx > 0 ? lx : kTile - 1 - lx);
-          const int y = by + (sy > 0 ? ly : kTile - 1 - ly);
-          const int z = bz + (sz > 0 ? lz : kTile - 1 - lz);
-          const int i = x + nx * y + nxy * z;
+          const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
           const size_t l = ((size_t)i * G + g) * M + m;
-          const int tl = ((lz * kTile + ly) * kTile + lx) * ndG + slot;
-          const T s = iso ? src[(size_t)i * G + g] : src[l];
-          T ux = T(0), uy = T(0), uz = T(0);
-          bool hx = true, hy = true, hz = true;
-          if (lx > 0) ux = tpsi[tl - ndG];
-          else hx = flow_outside(A, psi, bnd, sx > 0 ? x > 0 : x < nx - 1, i - sx, fx, i, g, m, ux);
-          if (ly > 0) uy = tpsi[tl - kTile * ndG];
-          else hy = flow_outside(A, psi, bnd, sy > 0 ? y > 0 : y < K.ny - 1, i - sy * nx, fy, i, g, m, uy);
-          if (lz > 0) uz = tpsi[tl - kTile * kTile * ndG];
-          else hz = flow_outside(A, psi, bnd, sz > 0 ? z > 0 : z < A.n / nxy - 1, i - sz * nxy, fz, i, g, m, uz);
+          const int tl = pk * ndG + slot;
+          const T s = iso ? tsrc[pk * G + g] : src[l];
+          const T ux = lx > 0 ? tpsi[tl - ndG] : tin[(ly + 4 * lz) * ndG + slot];
+          const T uy = ly > 0 ? tpsi[tl - kTile * ndG] : tin[(16 + lx + 4 * lz) * ndG + slot];
+          const T uz = lz > 0 ? tpsi[tl - kTile * kTile * ndG] : tin[(32 + lx + 4 * ly) * ndG + slot];
           T v;
           if (kClass) {
-            const T* cf = coef + (((size_t)K.ccls[i] * G + g) * M + m) * 4;
+            const T* cf = coef + (((size_t)tcls[pk] * G + g) * M + m) * 4;
             v = cf[0] * s;
-            if (hx) v += cf[1] * ux;
-            if (hy) v += cf[2] * uy;
-            if (hz) v += cf[3] * uz;
+            v += cf[1] * ux;
+            v += cf[2] * uy;
+            v += cf[3] * uz;
           } else {
             T num = s;
-            if (hx) num -= (mux * W.win[(size_t)fx * n + i]) * ux;
-            if (hy) num -= (muy * W.win[(size_t)fy * n + i]) * uy;
-            if (hz) num -= (muz * W.win[(size_t)fz * n + i]) * uz;
+            num -= (mux * W.win[(size_t)fx * n + i]) * ux;
+            num -= (muy * W.win[(size_t)fy * n + i]) * uy;
+            num -= (muz * W.win[(size_t)fz * n + i]) * uz;
             v = num * W.rden[l];
           }
           psi[l] = v;
@@ -465,10 +501,30 @@ __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFac
       }
       __syncthreads();
     }
+    // 5. publish the tile, then its scalar-flux moment over this pattern's directions
     if (threadIdx.x == 0) {
       __threadfence();
       st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
     }
+    if (mom) {
+      for (int r = threadIdx.x; r < kTileCells * G; r += blockDim.x) {
+        const int c = r / G, gg = r - c * G;
+        T acc = T(0);
+        for (int dj = 0; dj < ndp; dj++) acc += A.w[K.pat_dirs[d0 + dj]] * tpsi[c * ndG + gg * K.nd + dj];
+        const int i = tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4);
+        mom[(size_t)p * n * G + (size_t)i * G + gg] = acc;
+      }
+    }
+  }
+}
+
+// phi0[r] = sum over the sweep patterns of their moments, in pattern order.
+template <typename T>
+__global__ void k_mom_reduce(long long rows, int npat, const T* __restrict__ mom, T* phi0) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x) {
+    T s = T(0);
+    for (int p = 0; p < npat; p++) s += mom[(size_t)p * rows + r];
+    phi0[r] = s;
   }
 }
 
@@ -1054,6 +1110,9 @@ int flow_grid(SNData& d, size_t smem) {
   int& grid = d.flow_grid[sizeof(T) == 8 ? 0 : 1];
   if (grid) return grid;
   int dev = 0, sms = 0, per_sm = 0;
+  if (smem > 48u * 1024u &&
+      cudaFuncSetAttribute(k_sweep_flow<T, kClass>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_flow<T, kClass>, kFlowThreads, smem) != cudaSuccess ||
       per_sm < 1)
@@ -1063,7 +1122,7 @@ int flow_grid(SNData& d, size_t smem) {
 }
 
 template <typename T>
-int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd, T* psi) {
+int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd, T* psi, T* mom = nullptr) {
   SNData& d = *p->sn;
   const Schedule& S = d.sched;
   const bool cls = d.kba && d.ncls > 0;
@@ -1074,12 +1133,13 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   SweepPtrs* P = d.sweep_ptrs.as<SweepPtrs>();
   // the sweep's launches are captured once per (precision, source kind) and replayed; the
   // buffers of this sweep go through the device-side pointer block
-  launch(p, k_set_sweep_ptrs, 1, 1, p->stream, P, (const void*)src, (const void*)bnd, (void*)psi);
+  launch(p, k_set_sweep_ptrs, 1, 1, p->stream, P, (const void*)src, (const void*)bnd, (void*)psi,
+         (void*)(d.kba ? mom : nullptr));
   cudaGraphExec_t& gx = d.sweep_graph[sizeof(T) == 8 ? 0 : 1][iso ? 1 : 0];
   const int nlaunch = d.kba ? 2 : S.nlev;
   if (!gx) {
     int grid = 0;
-    const size_t smem = (size_t)kTileCells * d.kba_nd * d.G * sizeof(T);
+    const size_t smem = flow_smem_bytes<T>(d.kba_nd * d.G, d.G);
     if (d.kba) {
       grid = cls ? flow_grid<T, true>(d, smem) : flow_grid<T, false>(d, smem);
       if (grid < 1) return fail(PGPU_ERR_CUDA, "occupancy query of the dataflow sweep failed");
@@ -1145,9 +1205,17 @@ int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y,
   T* q = d.scat.as<T>();
   T* psi = psi_work<T>(d);
   launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q, lam_s);
-  int st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi);
-  if (st) return st;
-  launch(p, k_moment<T>, grid_for((long long)nG * 32), kThreads, p->stream, nG, d.M, A.w, psi, y);
+  int st;
+  if (d.kba) {
+    // the dataflow sweep writes per-pattern moments; they are summed in pattern order
+    if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)d.sched.npat * nG * sizeof(double), &p->bytes))) return st;
+    T* mom = d.mom.as<T>();
+    if ((st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi, mom))) return st;
+    launch(p, k_mom_reduce<T>, grid_for(nG), kThreads, p->stream, (long long)nG, d.sched.npat, (const T*)mom, y);
+  } else {
+    if ((st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi))) return st;
+    launch(p, k_moment<T>, grid_for((long long)nG * 32), kThreads, p->stream, nG, d.M, A.w, psi, y);
+  }
   if (d.nrefl) {
     const long long nb = (long long)d.nrefl * d.G * d.M;
     launch(p, k_reflect_extract<T>, grid_for(nb), kThreads, p->stream, A, d.nrefl, d.d_slot_cell.as<int>(),
@@ -1605,8 +1673,8 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
     for (int a = 0; a < 3; a++) K.pat_sign.push_back(sg[a]);
     K.nd = std::max(K.nd, S.pat_dirs_ptr[p + 1] - S.pat_dirs_ptr[p]);
   }
-  if ((size_t)kTileCells * K.nd * op->num_groups * sizeof(double) > 48 * 1024) return false;
   if (K.nd * op->num_groups > kFlowThreads) return false;
+  if (flow_smem_bytes<double>(K.nd * op->num_groups, op->num_groups) > kFlowMaxSmem) return false;
   K.ntx = nx / kTile;
   K.nty = ny / kTile;
   K.ntz = nz / kTile;

@@ -107,11 +107,11 @@ def test_sn_default_delta_negative_flux_is_an_error(tmp_path, capfd):
             p.solve()
 
 
-@pytest.mark.parametrize("order", [4, 8])
-def test_hex_prism_lattice(order, tmp_path):
+@pytest.mark.parametrize("nq,nr,nz,order", [(5, 4, 3, 2), (5, 4, 3, 4), (3, 2, 2, 8)])
+def test_hex_prism_lattice(nq, nr, nz, order, tmp_path):
     """Unstructured extruded hexagonal prisms (level-set sweeps over 8-face cells)."""
     from pampa_gb300 import workloads as wl
-    path = wl.sn_hex(str(tmp_path), nq=5, nr=4, nz=3, order=order, block=2)
+    path = wl.sn_hex(str(tmp_path), nq=nq, nr=nr, nz=nz, order=order, block=2)
     ref = po.run_input(path)
     with pg.Pampa(path, "-silent") as p:
         p.solve()
