@@ -368,6 +368,23 @@ __global__ void k_flow_begin(FlowSync* s) {
   s->epoch = s->epoch + 1u;
 }
 
+__device__ __forceinline__ void flow_load4(const double* __restrict__ p, double (&o)[4]) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = b.x;
+  o[3] = b.y;
+}
+
+__device__ __forceinline__ void flow_load4(const float* __restrict__ p, float (&o)[4]) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = a.z;
+  o[3] = a.w;
+}
+
 // Global cell index of the tile cell with oriented local coordinates (lx, ly, lz).
 struct FlowTile {
   int bx, by, bz, sx, sy, sz;
@@ -461,45 +478,82 @@ __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFac
     // 4. the tile's cell diagonals
     const bool active = cl < ncl && di < ndp;
     const int m = active ? K.pat_dirs[d0 + di] : 0;
+    // one (cell, group, direction) update from the staged inflow and the coefficients
+    auto update = [&](int pk, const T (&cf)[4]) {
+      const int lx = pk & 3, ly = (pk >> 2) & 3, lz = (pk >> 4) & 3;
+      const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
+      const size_t l = ((size_t)i * G + g) * M + m;
+      const int tl = pk * ndG + slot;
+      const T s = iso ? tsrc[pk * G + g] : src[l];
+      const T ux = lx > 0 ? tpsi[tl - ndG] : tin[(ly + 4 * lz) * ndG + slot];
+      const T uy = ly > 0 ? tpsi[tl - kTile * ndG] : tin[(16 + lx + 4 * lz) * ndG + slot];
+      const T uz = lz > 0 ? tpsi[tl - kTile * kTile * ndG] : tin[(32 + lx + 4 * ly) * ndG + slot];
+      T v;
+      if (kClass) {
+        v = cf[0] * s;
+        v += cf[1] * ux;
+        v += cf[2] * uy;
+        v += cf[3] * uz;
+      } else {
+        // cf = (rden, -mu_x w_x, -mu_y w_y, -mu_z w_z) of this row
+        T num = s;
+        num += cf[1] * ux;
+        num += cf[2] * uy;
+        num += cf[3] * uz;
+        v = num * cf[0];
+      }
+      psi[l] = v;
+      tpsi[tl] = v;
+    };
+    // coefficients of one update: the class table, or the row's reciprocal diagonal and
+    // face weights
     const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
     T mux = T(0), muy = T(0), muz = T(0);
     if (!kClass && active) {
-      mux = -fabs(A.dirs[(size_t)m * 3]);
-      muy = -fabs(A.dirs[(size_t)m * 3 + 1]);
-      muz = -fabs(A.dirs[(size_t)m * 3 + 2]);
+      mux = fabs(A.dirs[(size_t)m * 3]);
+      muy = fabs(A.dirs[(size_t)m * 3 + 1]);
+      muz = fabs(A.dirs[(size_t)m * 3 + 2]);
     }
+    auto fetch = [&](int pk, T (&cf)[4]) {
+      if (kClass) {
+        flow_load4(coef + (((size_t)tcls[pk] * G + g) * M + m) * 4, cf);
+      } else {
+        const int i = tile.x(pk & 3) + nx * tile.y((pk >> 2) & 3) + nxy * tile.z(pk >> 4);
+        cf[0] = W.rden[((size_t)i * G + g) * M + m];
+        cf[1] = mux * W.win[(size_t)fx * n + i];
+        cf[2] = muy * W.win[(size_t)fy * n + i];
+        cf[3] = muz * W.win[(size_t)fz * n + i];
+      }
+    };
+    // a thread's first two cells of each diagonal take their coefficients from registers
+    // loaded one diagonal ahead, so the loads overlap the previous diagonal
+    T cur[2][4] = {}, nxt[2][4] = {};
+    auto fetch_diag = [&](int dd, T (&dst)[2][4]) {
+      if (!active || dd >= kTileDiags) return;
+      const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
+#pragma unroll
+      for (int q = 0; q < 2; q++)
+        if (cl + q * ncl < cn) fetch(c_tile_cell[cb + cl + q * ncl], dst[q]);
+    };
+    fetch_diag(0, cur);
     for (int dd = 0; dd < kTileDiags; dd++) {
       const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
+      fetch_diag(dd + 1, nxt);
       if (active) {
-        for (int c = cl; c < cn; c += ncl) {
-          const int pk = c_tile_cell[cb + c];
-          const int lx = pk & 3, ly = (pk >> 2) & 3, lz = (pk >> 4) & 3;
-          const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
-          const size_t l = ((size_t)i * G + g) * M + m;
-          const int tl = pk * ndG + slot;
-          const T s = iso ? tsrc[pk * G + g] : src[l];
-          const T ux = lx > 0 ? tpsi[tl - ndG] : tin[(ly + 4 * lz) * ndG + slot];
-          const T uy = ly > 0 ? tpsi[tl - kTile * ndG] : tin[(16 + lx + 4 * lz) * ndG + slot];
-          const T uz = lz > 0 ? tpsi[tl - kTile * kTile * ndG] : tin[(32 + lx + 4 * ly) * ndG + slot];
-          T v;
-          if (kClass) {
-            const T* cf = coef + (((size_t)tcls[pk] * G + g) * M + m) * 4;
-            v = cf[0] * s;
-            v += cf[1] * ux;
-            v += cf[2] * uy;
-            v += cf[3] * uz;
-          } else {
-            T num = s;
-            num -= (mux * W.win[(size_t)fx * n + i]) * ux;
-            num -= (muy * W.win[(size_t)fy * n + i]) * uy;
-            num -= (muz * W.win[(size_t)fz * n + i]) * uz;
-            v = num * W.rden[l];
-          }
-          psi[l] = v;
-          tpsi[tl] = v;
+#pragma unroll
+        for (int q = 0; q < 2; q++)
+          if (cl + q * ncl < cn) update(c_tile_cell[cb + cl + q * ncl], cur[q]);
+        for (int c = cl + 2 * ncl; c < cn; c += ncl) {  // more than two cells per thread
+          T cf[4];
+          fetch(c_tile_cell[cb + c], cf);
+          update(c_tile_cell[cb + c], cf);
         }
       }
       __syncthreads();
+#pragma unroll
+      for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) cur[q][k] = nxt[q][k];
     }
     // 5. publish the tile, then its scalar-flux moment over this pattern's directions
     if (threadIdx.x == 0) {
