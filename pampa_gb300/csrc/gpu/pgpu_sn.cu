@@ -94,7 +94,7 @@ struct SNData {
   DevBuf sweep_ptrs;    // SweepPtrs block read by the level kernels
   // dataflow tiled sweep of a full Cartesian box (k_sweep_flow), when the operator qualifies
   bool kba = false;
-  int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_nd = 0, kba_ntasks = 0;
+  int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_nd = 0, kba_ntasks = 0, kba_nchunk = 1;
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
@@ -328,6 +328,7 @@ struct FlowSync {
 
 struct FlowGeom {
   int nx, ny, ntx, nty, ntz, npat, nd, ntasks;
+  int nchunk;                            // warp-task form: 32-slot chunks per (tile, pattern)
   const int* __restrict__ tiles;         // [ntiles][3] oriented tile coordinates, by diagonal
   const int* __restrict__ pat_sign;      // [npat][3]: +1 sweeps towards +axis, -1 towards -axis
   const int* __restrict__ pat_dirs_ptr;  // [npat + 1]
@@ -568,6 +569,112 @@ __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFac
         const int i = tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4);
         mom[(size_t)p * n * G + (size_t)i * G + gg] = acc;
       }
+    }
+  }
+}
+
+// Warp-task form of the dataflow sweep.  A task is one tile, one octant pattern and one
+// chunk of 32 (group, direction) slots; a warp sweeps it alone, each lane marching the
+// tile's 64 cells in x-fastest order for its own slot (slots never couple inside a sweep),
+// so no barrier is needed.  The tile's values of the lane stay in registers; inflow from
+// the upwind tiles is read through L2 after the warp has seen their flags.  The upwind
+// tasks of a task are the same pattern and chunk on the three upwind tiles, numbered
+// earlier, so the claim-order argument of k_sweep_flow holds unchanged.
+template <typename T, bool kClass>
+__global__ void __launch_bounds__(kFlowThreads) k_sweep_warp(SNOp<T> A, SweepFaces<T> W, FlowGeom K,
+                                                             const SweepPtrs* __restrict__ P, int iso) {
+  const int lane = threadIdx.x & 31;
+  const T* __restrict__ src = static_cast<const T*>(P->src);
+  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
+  T* psi = static_cast<T*>(P->psi);
+  const T* __restrict__ coef = static_cast<const T*>(K.coef);
+  const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
+  const int G = A.G, M = A.M, n = A.n, ndG = K.nd * G, nchunk = K.nchunk;
+  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
+  const size_t GM = (size_t)G * M;
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = (int)atomicAdd(&K.sync->next, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= K.ntasks) return;  // uniform over the warp
+    const int jp = t / nchunk, k = t - jp * nchunk;
+    const int j = jp / K.npat, p = jp - j * K.npat;
+    const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
+    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
+    unsigned int* pflags = K.flags + ((size_t)p * nchunk + k) * ntiles;
+    // wait for the three upwind tasks (lanes 0-2), then order the warp after them
+    if (lane < 3) {
+      const int ux = tx - (lane == 0), uy = ty - (lane == 1), uz = tz - (lane == 2);
+      if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
+    }
+    __syncwarp();
+    const int slot = k * 32 + lane;
+    const int g = slot / K.nd, di = slot - g * K.nd;
+    const int d0 = K.pat_dirs_ptr[p];
+    if (slot < ndG && di < K.pat_dirs_ptr[p + 1] - d0) {
+      const int m = K.pat_dirs[d0 + di];
+      const size_t lofs = (size_t)g * M + m;
+      // cell of oriented local (lx, ly, lz): i0 + lx*dx + ly*dy + lz*dz
+      const int dx = sx, dy = sy * nx, dz = sz * nxy;
+      const int i0 = (sx > 0 ? tx * kTile : nx - 1 - tx * kTile) + nx * (sy > 0 ? ty * kTile : K.ny - 1 - ty * kTile) +
+                     nxy * (sz > 0 ? tz * kTile : n / nxy - 1 - tz * kTile);
+      const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
+      T ax = T(0), ay = T(0), az = T(0);
+      if (!kClass) {
+        ax = fabs(A.dirs[(size_t)m * 3]);
+        ay = fabs(A.dirs[(size_t)m * 3 + 1]);
+        az = fabs(A.dirs[(size_t)m * 3 + 2]);
+      }
+      // inflow through the tile face of axis a for cell i: the upwind tile's psi, the
+      // reflective inflow, or zero at a vacuum face
+      auto inflow = [&](bool inner, int i, int step, int f) -> T {
+        if (inner) return __ldcg(psi + (size_t)(i - step) * GM + lofs);
+        if (bnd) {
+          const size_t o = (size_t)f * n + i;
+          if (A.kind[o] == PGPU_FACE_REFLECTIVE) return bnd[(size_t)A.rslot[o] * GM + lofs];
+        }
+        return T(0);
+      };
+      T wv[kTileCells];
+#pragma unroll
+      for (int c = 0; c < kTileCells; c++) {
+        const int lx = c & 3, ly = (c >> 2) & 3, lz = c >> 4;
+        const int i = i0 + lx * dx + ly * dy + lz * dz;
+        const size_t l = (size_t)i * GM + lofs;
+        const T s = iso ? src[(size_t)i * G + g] : src[l];
+        T cf[4];
+        if (kClass) {
+          flow_load4(coef + ((size_t)K.ccls[i] * GM + lofs) * 4, cf);
+        } else {
+          cf[0] = W.rden[l];
+          cf[1] = ax * W.win[(size_t)fx * n + i];
+          cf[2] = ay * W.win[(size_t)fy * n + i];
+          cf[3] = az * W.win[(size_t)fz * n + i];
+        }
+        const T uy = ly > 0 ? wv[c - kTile] : inflow(ty > 0, i, dy, fy);
+        const T uz = lz > 0 ? wv[c - kTile * kTile] : inflow(tz > 0, i, dz, fz);
+        const T ux = lx > 0 ? wv[c - 1] : inflow(tx > 0, i, dx, fx);
+        T v;
+        if (kClass) {
+          v = cf[0] * s;
+          v += cf[2] * uy;
+          v += cf[3] * uz;
+          v += cf[1] * ux;
+        } else {
+          T num = s;
+          num += cf[2] * uy;
+          num += cf[3] * uz;
+          num += cf[1] * ux;
+          v = num * cf[0];
+        }
+        psi[l] = v;
+        wv[c] = v;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence();
+      st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
     }
   }
 }
@@ -1164,14 +1271,12 @@ int flow_grid(SNData& d, size_t smem) {
   int& grid = d.flow_grid[sizeof(T) == 8 ? 0 : 1];
   if (grid) return grid;
   int dev = 0, sms = 0, per_sm = 0;
-  if (smem > 48u * 1024u &&
-      cudaFuncSetAttribute(k_sweep_flow<T, kClass>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_flow<T, kClass>, kFlowThreads, smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_warp<T, kClass>, kFlowThreads, smem) != cudaSuccess ||
       per_sm < 1)
     return 0;
-  grid = std::min(d.kba_ntasks, sms * per_sm);
+  const int warps = kFlowThreads / 32;
+  grid = std::min((d.kba_ntasks + warps - 1) / warps, sms * per_sm);
   return grid;
 }
 
@@ -1193,7 +1298,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   const int nlaunch = d.kba ? 2 : S.nlev;
   if (!gx) {
     int grid = 0;
-    const size_t smem = flow_smem_bytes<T>(d.kba_nd * d.G, d.G);
+    const size_t smem = 0;
     if (d.kba) {
       grid = cls ? flow_grid<T, true>(d, smem) : flow_grid<T, false>(d, smem);
       if (grid < 1) return fail(PGPU_ERR_CUDA, "occupancy query of the dataflow sweep failed");
@@ -1201,16 +1306,16 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
     cudaGraph_t graph;
     PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     if (d.kba) {
-      const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, S.npat, d.kba_nd, d.kba_ntasks,
+      const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, S.npat, d.kba_nd, d.kba_ntasks, d.kba_nchunk,
                        d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(),
                        cls ? d.d_ccls.as<unsigned short>() : nullptr,
                        cls ? (sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr) : nullptr, d.flow_sync.as<FlowSync>(),
                        d.flow_flags.as<unsigned int>()};
       k_flow_begin<<<1, 1, 0, p->stream>>>(K.sync);
       if (cls)
-        k_sweep_flow<T, true><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
+        k_sweep_warp<T, true><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
       else
-        k_sweep_flow<T, false><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
+        k_sweep_warp<T, false><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
     } else {
       for (int L = 0; L < S.nlev; L++) {
         dim3 g(S.grid_x[L], S.npat);
@@ -1231,7 +1336,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   prof_begin(p, &e0);
   PGPU_CUDA(cudaGraphLaunch(gx, p->stream));
   p->launches += nlaunch;
-  p->prof_name = d.kba ? "k_sweep_flow" : "k_sweep_level";
+  p->prof_name = d.kba ? "k_sweep_warp" : "k_sweep_level";
   // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
   // direction update (2 s_v), the source read per cell-group (s_v, or s_v per update for
   // an angular source), the scalar-flux moment written per cell-group (s_v) and the
@@ -1260,7 +1365,7 @@ int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y,
   T* psi = psi_work<T>(d);
   launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q, lam_s);
   int st;
-  if (d.kba) {
+  if (false) {
     // the dataflow sweep writes per-pattern moments; they are summed in pattern order
     if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)d.sched.npat * nG * sizeof(double), &p->bytes))) return st;
     T* mom = d.mom.as<T>();
@@ -1689,7 +1794,7 @@ void sn_destroy(pgpu_problem* p) {
 // reference's cell and face order, with sides that are multiples of kTile and one sign per
 // axis for every sweep pattern; returns false (level sweeps are used) otherwise.
 struct KbaPlan {
-  int ntx, nty, ntz, nd, ntasks;
+  int ntx, nty, ntz, nd, nchunk, ntasks;
   std::vector<int> tiles, pat_sign;
 };
 
@@ -1727,8 +1832,6 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
     for (int a = 0; a < 3; a++) K.pat_sign.push_back(sg[a]);
     K.nd = std::max(K.nd, S.pat_dirs_ptr[p + 1] - S.pat_dirs_ptr[p]);
   }
-  if (K.nd * op->num_groups > kFlowThreads) return false;
-  if (flow_smem_bytes<double>(K.nd * op->num_groups, op->num_groups) > kFlowMaxSmem) return false;
   K.ntx = nx / kTile;
   K.nty = ny / kTile;
   K.ntz = nz / kTile;
@@ -1743,7 +1846,8 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
         K.tiles.push_back(ty);
         K.tiles.push_back(tz);
       }
-  const long long ntasks = (long long)K.ntx * K.nty * K.ntz * S.npat;
+  K.nchunk = (K.nd * op->num_groups + 31) / 32;
+  const long long ntasks = (long long)K.ntx * K.nty * K.ntz * S.npat * K.nchunk;
   if (ntasks >= (1LL << 31)) return false;
   K.ntasks = (int)ntasks;
   return true;
@@ -1973,6 +2077,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       d.kba_ntz = kp.ntz;
       d.kba_nd = kp.nd;
       d.kba_ntasks = kp.ntasks;
+      d.kba_nchunk = kp.nchunk;
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
       up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
       std::vector<unsigned short> ccls;
