@@ -94,7 +94,7 @@ struct SNData {
   DevBuf sweep_ptrs;    // SweepPtrs block read by the level kernels
   // dataflow tiled sweep of a full Cartesian box (k_sweep_flow), when the operator qualifies
   bool kba = false;
-  int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_nd = 0, kba_ntasks = 0, kba_nchunk = 1;
+  int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_nd = 0, kba_ntasks = 0, kba_nchunk = 1, kba_gchunk = 1;
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
@@ -289,17 +289,20 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 // ---------------------------------------------------------------------------------
 // Dataflow tiled sweep for a full Cartesian box (one persistent launch per sweep).
 //
-// The box is cut into kTile^3-cell tiles; a task is one tile for one octant pattern (all
-// the pattern's directions and all groups).  Tasks are numbered tile diagonal by tile
-// diagonal of the octant-oriented tile index (tx' + ty' + tz' = D), so the upwind tasks
-// of a task -- (tx'-1, ty', tz'), (tx', ty'-1, tz'), (tx', ty', tz'-1) of the same
-// pattern -- always come earlier.  Each CTA takes the next task from an atomic counter,
-// waits until the flags of its upwind tasks hold this sweep's epoch, sweeps the tile
-// through its 3*(kTile-1)+1 cell diagonals with the tile's angular flux in shared memory,
-// writes psi and publishes its own flag.  A task is taken only by a running CTA, and only
-// after every earlier task was taken by a running CTA, so every wait ends; the waits are
-// bounded all the same (kFlowSpinLimit): a wait that runs out sets the error word, every
-// later wait then returns at once, and the host reports PGPU_ERR_TIMEOUT.
+// The box is cut into kTile^3-cell tiles.  A task is one tile, one octant pattern and one
+// chunk of energy groups (all the pattern's directions for those groups; groups never
+// couple inside a sweep).  Tasks are numbered tile diagonal by tile diagonal of the
+// octant-oriented tile index (tx' + ty' + tz' = D), so the upwind tasks of a task --
+// (tx'-1, ty', tz'), (tx', ty'-1, tz'), (tx', ty', tz'-1), same pattern and chunk --
+// always come earlier.  Each CTA takes the next task from an atomic counter, stages the
+// tile's source and cell classes in shared memory, waits until the flags of its upwind
+// tasks hold this sweep's epoch, loads the inflow on the tile's three upwind faces,
+// sweeps the tile through its 3*(kTile-1)+1 cell diagonals with the tile's angular flux
+// in shared memory, writes psi, publishes its own flag and writes its pattern's share of
+// the scalar-flux moment.  A task is taken only by a running CTA, and only after every
+// earlier task was taken by a running CTA, so every wait ends; the waits are bounded all
+// the same (kFlowSpinLimit): a wait that runs out sets the error word, every later wait
+// then returns at once, and the host reports PGPU_ERR_TIMEOUT.
 //
 // Arithmetic per (cell, group, direction): psi = rd * src + sum over the three inflow
 // faces of a_f * psi_upwind, with rd = 1 / diagonal and a_f = -(mu_f * w_in,f) * rd.
@@ -312,7 +315,7 @@ constexpr int kTile = 4;
 constexpr int kTileCells = kTile * kTile * kTile;
 constexpr int kTileDiags = 3 * (kTile - 1) + 1;
 constexpr int kFlowThreads = 128;
-constexpr size_t kFlowMaxSmem = 160u << 10;  // dynamic shared memory of one CTA
+constexpr int kFlowSlots = 10;  // (group, direction) slots of one task at most
 constexpr unsigned int kFlowSpinLimit = 1u << 22;  // ~0.4 s of polling at 100 ns
 
 // oriented local cells of a tile (lx | ly << 2 | lz << 4) sorted by lx + ly + lz
@@ -328,7 +331,7 @@ struct FlowSync {
 
 struct FlowGeom {
   int nx, ny, ntx, nty, ntz, npat, nd, ntasks;
-  int nchunk;                            // warp-task form: 32-slot chunks per (tile, pattern)
+  int gchunk, nchunk;                    // groups per task, group chunks per (tile, pattern)
   const int* __restrict__ tiles;         // [ntiles][3] oriented tile coordinates, by diagonal
   const int* __restrict__ pat_sign;      // [npat][3]: +1 sweeps towards +axis, -1 towards -axis
   const int* __restrict__ pat_dirs_ptr;  // [npat + 1]
@@ -336,7 +339,7 @@ struct FlowGeom {
   const unsigned short* __restrict__ ccls;  // [n] cell class, or null (per-row rden)
   const void* coef;                         // [ncls][G][M][4] (rd, a_x, a_y, a_z) in T
   FlowSync* sync;
-  unsigned int* flags;  // [npat][ntz][nty][ntx] by oriented tile coordinates
+  unsigned int* flags;  // [npat][nchunk][ntz][nty][ntx] by oriented tile coordinates
 };
 
 __device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
@@ -394,23 +397,23 @@ struct FlowTile {
   __device__ __forceinline__ int z(int lz) const { return bz + (sz > 0 ? lz : kTile - 1 - lz); }
 };
 
-// Shared memory of one task: the tile's angular flux, the inflow on its three upwind
-// faces, the isotropic source and the cell classes of its cells.
+// Shared memory of one task with S slots and Gc groups: the tile's angular flux, the
+// inflow on its three upwind faces, the isotropic source and the cells' classes.
 template <typename T>
-__host__ __device__ constexpr size_t flow_smem_bytes(int ndG, int G) {
-  return ((size_t)kTileCells * ndG + (size_t)3 * kTile * kTile * ndG + (size_t)kTileCells * G) * sizeof(T) +
+__host__ __device__ constexpr size_t flow_smem_bytes(int S, int Gc) {
+  return ((size_t)kTileCells * S + (size_t)3 * kTile * kTile * S + (size_t)kTileCells * Gc) * sizeof(T) +
          (size_t)kTileCells * sizeof(int);
 }
 
 template <typename T, bool kClass>
-__global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFaces<T> W, FlowGeom K,
+__global__ void __launch_bounds__(kFlowThreads, 8) k_sweep_flow(SNOp<T> A, SweepFaces<T> W, FlowGeom K,
                                                              const SweepPtrs* __restrict__ P, int iso) {
   extern __shared__ __align__(16) unsigned char flow_smem[];
-  const int G = A.G, M = A.M, n = A.n, ndG = K.nd * G;
-  T* tpsi = reinterpret_cast<T*>(flow_smem);               // [64][ndG]
-  T* tin = tpsi + kTileCells * ndG;                         // [3][16][ndG]
-  T* tsrc = tin + 3 * kTile * kTile * ndG;                  // [64][G]
-  int* tcls = reinterpret_cast<int*>(tsrc + kTileCells * G);  // [64]
+  const int G = A.G, M = A.M, n = A.n, Gc = K.gchunk, nd = K.nd, S = nd * Gc;
+  T* tpsi = reinterpret_cast<T*>(flow_smem);               // [64][S]
+  T* tin = tpsi + kTileCells * S;                           // [3][16][S]
+  T* tsrc = tin + 3 * kTile * kTile * S;                    // [64][Gc]
+  int* tcls = reinterpret_cast<int*>(tsrc + kTileCells * Gc);  // [64]
   __shared__ int s_task;
   const T* __restrict__ src = static_cast<const T*>(P->src);
   const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
@@ -419,95 +422,64 @@ __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFac
   const T* __restrict__ coef = static_cast<const T*>(K.coef);
   const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
   const int nx = K.nx, ny = K.ny, nxy = K.nx * K.ny, nz = n / nxy, ntiles = K.ntx * K.nty * K.ntz;
-  const int slot = threadIdx.x % ndG, cl = threadIdx.x / ndG, ncl = blockDim.x / ndG;
-  const int g = slot / K.nd, di = slot - g * K.nd;
+  // fixed thread -> (slot, cell lane) map; slot = local group * nd + direction index
+  const int slot = threadIdx.x % S, cl = threadIdx.x / S, ncl = blockDim.x / S;
+  const int gl = slot / nd, di = slot - gl * nd;
   for (;;) {
     if (threadIdx.x == 0) s_task = (int)atomicAdd(&K.sync->next, 1u);
     __syncthreads();
     const int t = s_task;
     if (t >= K.ntasks) return;  // uniform over the CTA
-    const int j = t / K.npat, p = t - j * K.npat;
+    const int jp = t / K.nchunk, ch = t - jp * K.nchunk;
+    const int j = jp / K.npat, p = jp - j * K.npat;
+    const int g0 = ch * Gc, gn = min(Gc, G - g0);
     const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
     const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
     const FlowTile tile{(sx > 0 ? tx : K.ntx - 1 - tx) * kTile, (sy > 0 ? ty : K.nty - 1 - ty) * kTile,
                         (sz > 0 ? tz : K.ntz - 1 - tz) * kTile, sx, sy, sz};
     const int d0 = K.pat_dirs_ptr[p], ndp = K.pat_dirs_ptr[p + 1] - d0;
-    unsigned int* pflags = K.flags + (size_t)p * ntiles;
+    unsigned int* pflags = K.flags + ((size_t)p * K.nchunk + ch) * ntiles;
     // 1. data that does not depend on the upwind tiles, loaded while they finish
     if (iso)
-      for (int r = threadIdx.x; r < kTileCells * G; r += blockDim.x) {
-        const int c = r / G, gg = r - c * G;
-        const int i = tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4);
-        tsrc[r] = src[(size_t)i * G + gg];
+      for (int r = threadIdx.x; r < kTileCells * Gc; r += blockDim.x) {
+        const int c = r / Gc, gg = r - c * Gc;
+        if (gg < gn) tsrc[r] = src[(size_t)(tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4)) * G + g0 + gg];
       }
     if (kClass)
       for (int c = threadIdx.x; c < kTileCells; c += blockDim.x)
         tcls[c] = K.ccls[tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4)];
-    // 2. wait for the upwind tiles of this pattern
+    // 2. wait for the upwind tiles of this pattern and chunk
     if (threadIdx.x < 3) {
       const int a = threadIdx.x;
       const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
       if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
     }
     __syncthreads();
+    const bool active = cl < ncl && gl < gn && di < ndp;
+    const int g = g0 + gl;
+    const int m = active ? K.pat_dirs[d0 + di] : 0;
     // 3. inflow on the three upwind faces: upwind tile's psi (through L2), reflective
     //    inflow, or zero at a vacuum face; face a, position (u, v) -> tin[(a*16 + u + 4v)][slot]
-    for (int r = threadIdx.x; r < 3 * kTile * kTile * ndG; r += blockDim.x) {
-      const int fs = r / ndG, sl = r - fs * ndG;
+    for (int fs = cl; fs < 3 * kTile * kTile; fs += ncl) {
+      if (!active) break;
       const int a = fs >> 4, u = fs & 3, v = (fs >> 2) & 3;
-      const int gg = sl / K.nd, dj = sl - gg * K.nd;
+      const int lx = a == 0 ? 0 : u, ly = a == 0 ? u : (a == 1 ? 0 : v), lz = a == 2 ? 0 : v;
+      const int x = tile.x(lx), y = tile.y(ly), z = tile.z(lz);
+      const int i = x + nx * y + nxy * z;
+      const int s = a == 0 ? sx : (a == 1 ? sy : sz);
+      const int c = a == 0 ? x : (a == 1 ? y : z), cmax = a == 0 ? nx : (a == 1 ? ny : nz);
       T val = T(0);
-      if (dj < ndp) {
-        const int m = K.pat_dirs[d0 + dj];
-        const int lx = a == 0 ? 0 : u, ly = a == 0 ? u : (a == 1 ? 0 : v), lz = a == 2 ? 0 : v;
-        const int x = tile.x(lx), y = tile.y(ly), z = tile.z(lz);
-        const int i = x + nx * y + nxy * z;
-        const int s = a == 0 ? sx : (a == 1 ? sy : sz);
-        const int c = a == 0 ? x : (a == 1 ? y : z), cmax = a == 0 ? nx : (a == 1 ? ny : nz);
-        if (s > 0 ? c > 0 : c < cmax - 1) {
-          const int nb = i - s * (a == 0 ? 1 : (a == 1 ? nx : nxy));
-          val = __ldcg(psi + ((size_t)nb * G + gg) * M + m);
-        } else if (bnd) {
-          const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
-          const size_t o = (size_t)f * n + i;
-          if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd[((size_t)A.rslot[o] * G + gg) * M + m];
-        }
+      if (s > 0 ? c > 0 : c < cmax - 1) {
+        const int nb = i - s * (a == 0 ? 1 : (a == 1 ? nx : nxy));
+        val = __ldcg(psi + ((size_t)nb * G + g) * M + m);
+      } else if (bnd) {
+        const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
+        const size_t o = (size_t)f * n + i;
+        if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd[((size_t)A.rslot[o] * G + g) * M + m];
       }
-      tin[r] = val;
+      tin[fs * S + slot] = val;
     }
-    __syncthreads();
     // 4. the tile's cell diagonals
-    const bool active = cl < ncl && di < ndp;
-    const int m = active ? K.pat_dirs[d0 + di] : 0;
-    // one (cell, group, direction) update from the staged inflow and the coefficients
-    auto update = [&](int pk, const T (&cf)[4]) {
-      const int lx = pk & 3, ly = (pk >> 2) & 3, lz = (pk >> 4) & 3;
-      const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
-      const size_t l = ((size_t)i * G + g) * M + m;
-      const int tl = pk * ndG + slot;
-      const T s = iso ? tsrc[pk * G + g] : src[l];
-      const T ux = lx > 0 ? tpsi[tl - ndG] : tin[(ly + 4 * lz) * ndG + slot];
-      const T uy = ly > 0 ? tpsi[tl - kTile * ndG] : tin[(16 + lx + 4 * lz) * ndG + slot];
-      const T uz = lz > 0 ? tpsi[tl - kTile * kTile * ndG] : tin[(32 + lx + 4 * ly) * ndG + slot];
-      T v;
-      if (kClass) {
-        v = cf[0] * s;
-        v += cf[1] * ux;
-        v += cf[2] * uy;
-        v += cf[3] * uz;
-      } else {
-        // cf = (rden, -mu_x w_x, -mu_y w_y, -mu_z w_z) of this row
-        T num = s;
-        num += cf[1] * ux;
-        num += cf[2] * uy;
-        num += cf[3] * uz;
-        v = num * cf[0];
-      }
-      psi[l] = v;
-      tpsi[tl] = v;
-    };
-    // coefficients of one update: the class table, or the row's reciprocal diagonal and
-    // face weights
     const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
     T mux = T(0), muy = T(0), muz = T(0);
     if (!kClass && active) {
@@ -515,46 +487,80 @@ __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFac
       muy = fabs(A.dirs[(size_t)m * 3 + 1]);
       muz = fabs(A.dirs[(size_t)m * 3 + 2]);
     }
-    auto fetch = [&](int pk, T (&cf)[4]) {
+    // coefficients of one update, with the source term folded in: (rd * src, a_x, a_y,
+    // a_z) from the class table, or (src, w_x, w_y, w_z, rden) from the row
+    auto fetch = [&](int pk, T (&cf)[4], T& rd) {
+      const T s = iso ? tsrc[pk * Gc + gl] : T(0);
       if (kClass) {
         flow_load4(coef + (((size_t)tcls[pk] * G + g) * M + m) * 4, cf);
+        rd = T(1);
+        cf[0] = iso ? cf[0] * s : cf[0];
       } else {
         const int i = tile.x(pk & 3) + nx * tile.y((pk >> 2) & 3) + nxy * tile.z(pk >> 4);
-        cf[0] = W.rden[((size_t)i * G + g) * M + m];
+        rd = W.rden[((size_t)i * G + g) * M + m];
+        cf[0] = s;
         cf[1] = mux * W.win[(size_t)fx * n + i];
         cf[2] = muy * W.win[(size_t)fy * n + i];
         cf[3] = muz * W.win[(size_t)fz * n + i];
       }
     };
+    auto update = [&](int pk, const T (&cf)[4], T rd) {
+      const int lx = pk & 3, ly = (pk >> 2) & 3, lz = pk >> 4;
+      const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
+      const size_t l = ((size_t)i * G + g) * M + m;
+      const int tl = pk * S + slot;
+      const T ux = lx > 0 ? tpsi[tl - S] : tin[(ly + 4 * lz) * S + slot];
+      const T uy = ly > 0 ? tpsi[tl - kTile * S] : tin[(16 + lx + 4 * lz) * S + slot];
+      const T uz = lz > 0 ? tpsi[tl - kTile * kTile * S] : tin[(32 + lx + 4 * ly) * S + slot];
+      T v;
+      if (kClass) {
+        // angular source: rd * src[l]; isotropic: rd * src folded in at fetch time
+        v = iso ? cf[0] : cf[0] * src[l];
+        v += cf[3] * uz;
+        v += cf[2] * uy;
+        v += cf[1] * ux;
+      } else {
+        T num = iso ? cf[0] : src[l];
+        num += cf[3] * uz;
+        num += cf[2] * uy;
+        num += cf[1] * ux;
+        v = num * rd;
+      }
+      psi[l] = v;
+      tpsi[tl] = v;
+    };
     // a thread's first two cells of each diagonal take their coefficients from registers
     // loaded one diagonal ahead, so the loads overlap the previous diagonal
-    T cur[2][4] = {}, nxt[2][4] = {};
-    auto fetch_diag = [&](int dd, T (&dst)[2][4]) {
+    T cur[2][4] = {}, nxt[2][4] = {}, rcur[2] = {}, rnxt[2] = {};
+    auto fetch_diag = [&](int dd, T (&dst)[2][4], T (&rdst)[2]) {
       if (!active || dd >= kTileDiags) return;
       const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
 #pragma unroll
       for (int q = 0; q < 2; q++)
-        if (cl + q * ncl < cn) fetch(c_tile_cell[cb + cl + q * ncl], dst[q]);
+        if (cl + q * ncl < cn) fetch(c_tile_cell[cb + cl + q * ncl], dst[q], rdst[q]);
     };
-    fetch_diag(0, cur);
+    fetch_diag(0, cur, rcur);
+    __syncthreads();
     for (int dd = 0; dd < kTileDiags; dd++) {
       const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
-      fetch_diag(dd + 1, nxt);
+      fetch_diag(dd + 1, nxt, rnxt);
       if (active) {
 #pragma unroll
         for (int q = 0; q < 2; q++)
-          if (cl + q * ncl < cn) update(c_tile_cell[cb + cl + q * ncl], cur[q]);
+          if (cl + q * ncl < cn) update(c_tile_cell[cb + cl + q * ncl], cur[q], rcur[q]);
         for (int c = cl + 2 * ncl; c < cn; c += ncl) {  // more than two cells per thread
-          T cf[4];
-          fetch(c_tile_cell[cb + c], cf);
-          update(c_tile_cell[cb + c], cf);
+          T cf[4], rd;
+          fetch(c_tile_cell[cb + c], cf, rd);
+          update(c_tile_cell[cb + c], cf, rd);
         }
       }
       __syncthreads();
 #pragma unroll
-      for (int q = 0; q < 2; q++)
+      for (int q = 0; q < 2; q++) {
+        rcur[q] = rnxt[q];
 #pragma unroll
         for (int k = 0; k < 4; k++) cur[q][k] = nxt[q][k];
+      }
     }
     // 5. publish the tile, then its scalar-flux moment over this pattern's directions
     if (threadIdx.x == 0) {
@@ -562,119 +568,13 @@ __global__ void __launch_bounds__(kFlowThreads) k_sweep_flow(SNOp<T> A, SweepFac
       st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
     }
     if (mom) {
-      for (int r = threadIdx.x; r < kTileCells * G; r += blockDim.x) {
-        const int c = r / G, gg = r - c * G;
+      for (int r = threadIdx.x; r < kTileCells * gn; r += blockDim.x) {
+        const int c = r / gn, gg = r - c * gn;
         T acc = T(0);
-        for (int dj = 0; dj < ndp; dj++) acc += A.w[K.pat_dirs[d0 + dj]] * tpsi[c * ndG + gg * K.nd + dj];
+        for (int dj = 0; dj < ndp; dj++) acc += A.w[K.pat_dirs[d0 + dj]] * tpsi[c * S + gg * nd + dj];
         const int i = tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4);
-        mom[(size_t)p * n * G + (size_t)i * G + gg] = acc;
+        mom[(size_t)p * n * G + (size_t)i * G + g0 + gg] = acc;
       }
-    }
-  }
-}
-
-// Warp-task form of the dataflow sweep.  A task is one tile, one octant pattern and one
-// chunk of 32 (group, direction) slots; a warp sweeps it alone, each lane marching the
-// tile's 64 cells in x-fastest order for its own slot (slots never couple inside a sweep),
-// so no barrier is needed.  The tile's values of the lane stay in registers; inflow from
-// the upwind tiles is read through L2 after the warp has seen their flags.  The upwind
-// tasks of a task are the same pattern and chunk on the three upwind tiles, numbered
-// earlier, so the claim-order argument of k_sweep_flow holds unchanged.
-template <typename T, bool kClass>
-__global__ void __launch_bounds__(kFlowThreads) k_sweep_warp(SNOp<T> A, SweepFaces<T> W, FlowGeom K,
-                                                             const SweepPtrs* __restrict__ P, int iso) {
-  const int lane = threadIdx.x & 31;
-  const T* __restrict__ src = static_cast<const T*>(P->src);
-  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
-  T* psi = static_cast<T*>(P->psi);
-  const T* __restrict__ coef = static_cast<const T*>(K.coef);
-  const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
-  const int G = A.G, M = A.M, n = A.n, ndG = K.nd * G, nchunk = K.nchunk;
-  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
-  const size_t GM = (size_t)G * M;
-  for (;;) {
-    int t = 0;
-    if (lane == 0) t = (int)atomicAdd(&K.sync->next, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= K.ntasks) return;  // uniform over the warp
-    const int jp = t / nchunk, k = t - jp * nchunk;
-    const int j = jp / K.npat, p = jp - j * K.npat;
-    const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
-    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
-    unsigned int* pflags = K.flags + ((size_t)p * nchunk + k) * ntiles;
-    // wait for the three upwind tasks (lanes 0-2), then order the warp after them
-    if (lane < 3) {
-      const int ux = tx - (lane == 0), uy = ty - (lane == 1), uz = tz - (lane == 2);
-      if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
-    }
-    __syncwarp();
-    const int slot = k * 32 + lane;
-    const int g = slot / K.nd, di = slot - g * K.nd;
-    const int d0 = K.pat_dirs_ptr[p];
-    if (slot < ndG && di < K.pat_dirs_ptr[p + 1] - d0) {
-      const int m = K.pat_dirs[d0 + di];
-      const size_t lofs = (size_t)g * M + m;
-      // cell of oriented local (lx, ly, lz): i0 + lx*dx + ly*dy + lz*dz
-      const int dx = sx, dy = sy * nx, dz = sz * nxy;
-      const int i0 = (sx > 0 ? tx * kTile : nx - 1 - tx * kTile) + nx * (sy > 0 ? ty * kTile : K.ny - 1 - ty * kTile) +
-                     nxy * (sz > 0 ? tz * kTile : n / nxy - 1 - tz * kTile);
-      const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
-      T ax = T(0), ay = T(0), az = T(0);
-      if (!kClass) {
-        ax = fabs(A.dirs[(size_t)m * 3]);
-        ay = fabs(A.dirs[(size_t)m * 3 + 1]);
-        az = fabs(A.dirs[(size_t)m * 3 + 2]);
-      }
-      // inflow through the tile face of axis a for cell i: the upwind tile's psi, the
-      // reflective inflow, or zero at a vacuum face
-      auto inflow = [&](bool inner, int i, int step, int f) -> T {
-        if (inner) return __ldcg(psi + (size_t)(i - step) * GM + lofs);
-        if (bnd) {
-          const size_t o = (size_t)f * n + i;
-          if (A.kind[o] == PGPU_FACE_REFLECTIVE) return bnd[(size_t)A.rslot[o] * GM + lofs];
-        }
-        return T(0);
-      };
-      T wv[kTileCells];
-#pragma unroll
-      for (int c = 0; c < kTileCells; c++) {
-        const int lx = c & 3, ly = (c >> 2) & 3, lz = c >> 4;
-        const int i = i0 + lx * dx + ly * dy + lz * dz;
-        const size_t l = (size_t)i * GM + lofs;
-        const T s = iso ? src[(size_t)i * G + g] : src[l];
-        T cf[4];
-        if (kClass) {
-          flow_load4(coef + ((size_t)K.ccls[i] * GM + lofs) * 4, cf);
-        } else {
-          cf[0] = W.rden[l];
-          cf[1] = ax * W.win[(size_t)fx * n + i];
-          cf[2] = ay * W.win[(size_t)fy * n + i];
-          cf[3] = az * W.win[(size_t)fz * n + i];
-        }
-        const T uy = ly > 0 ? wv[c - kTile] : inflow(ty > 0, i, dy, fy);
-        const T uz = lz > 0 ? wv[c - kTile * kTile] : inflow(tz > 0, i, dz, fz);
-        const T ux = lx > 0 ? wv[c - 1] : inflow(tx > 0, i, dx, fx);
-        T v;
-        if (kClass) {
-          v = cf[0] * s;
-          v += cf[2] * uy;
-          v += cf[3] * uz;
-          v += cf[1] * ux;
-        } else {
-          T num = s;
-          num += cf[2] * uy;
-          num += cf[3] * uz;
-          num += cf[1] * ux;
-          v = num * cf[0];
-        }
-        psi[l] = v;
-        wv[c] = v;
-      }
-    }
-    __syncwarp();
-    if (lane == 0) {
-      __threadfence();
-      st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
     }
   }
 }
@@ -855,6 +755,73 @@ __global__ void k_sub_many(long long N, const T* __restrict__ V, long long ld, i
     for (int k = 0; k < nv; k++) s -= h[k] * (double)V[(size_t)k * ld + l];
     x[l] = (T)s;
   }
+}
+
+// Gram-Schmidt passes of the GMRES Arnoldi step over nv <= kGsMax basis vectors V_k
+// (stride ld): all nv products with w come out of one pass over the basis, and the
+// subtraction of one pass is fused with the products (or the norm) of the next.
+constexpr int kGsMax = 32;
+
+// out[k] = <V_k, w>
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_gs_dot(long long N, const T* __restrict__ V, long long ld, int nv,
+                                                    const T* __restrict__ w, double* out, ReduceSlots<kGsMax> slots) {
+  double acc[kGsMax];
+#pragma unroll
+  for (int k = 0; k < kGsMax; k++) acc[k] = 0.0;
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    const double x = (double)w[l];
+#pragma unroll
+    for (int k = 0; k < kGsMax; k++)
+      if (k < nv) acc[k] += (double)V[(size_t)k * ld + l] * x;
+  }
+  double tot[kGsMax];
+  if (block_reduce_last<kGsMax>(acc, slots, tot) && threadIdx.x == 0)
+    for (int k = 0; k < nv; k++) out[k] = tot[k];
+}
+
+// w -= sum_k h[k] V_k, then out[k] = <V_k, w> (second Gram-Schmidt pass)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_gs_sub_dot(long long N, const T* __restrict__ V, long long ld, int nv,
+                                                        const double* __restrict__ h, T* w, double* out,
+                                                        ReduceSlots<kGsMax> slots) {
+  double acc[kGsMax];
+#pragma unroll
+  for (int k = 0; k < kGsMax; k++) acc[k] = 0.0;
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    double s = (double)w[l];
+#pragma unroll
+    for (int k = 0; k < kGsMax; k++)
+      if (k < nv) s -= h[k] * (double)V[(size_t)k * ld + l];
+    const T sw = (T)s;
+    w[l] = sw;
+    const double x = (double)sw;
+#pragma unroll
+    for (int k = 0; k < kGsMax; k++)
+      if (k < nv) acc[k] += (double)V[(size_t)k * ld + l] * x;
+  }
+  double tot[kGsMax];
+  if (block_reduce_last<kGsMax>(acc, slots, tot) && threadIdx.x == 0)
+    for (int k = 0; k < nv; k++) out[k] = tot[k];
+}
+
+// w -= sum_k h[k] V_k, then *out = ||w||
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_gs_sub_norm(long long N, const T* __restrict__ V, long long ld, int nv,
+                                                         const double* __restrict__ h, T* w, double* out,
+                                                         ReduceSlots<1> slots) {
+  double acc[1] = {0.0};
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    double s = (double)w[l];
+#pragma unroll
+    for (int k = 0; k < kGsMax; k++)
+      if (k < nv) s -= h[k] * (double)V[(size_t)k * ld + l];
+    const T sw = (T)s;
+    w[l] = sw;
+    acc[0] += (double)sw * (double)sw;
+  }
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) *out = sqrt(tot[0]);
 }
 
 // x += sum_k y[k] V[k]
@@ -1272,11 +1239,10 @@ int flow_grid(SNData& d, size_t smem) {
   if (grid) return grid;
   int dev = 0, sms = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_warp<T, kClass>, kFlowThreads, smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_flow<T, kClass>, kFlowThreads, smem) != cudaSuccess ||
       per_sm < 1)
     return 0;
-  const int warps = kFlowThreads / 32;
-  grid = std::min((d.kba_ntasks + warps - 1) / warps, sms * per_sm);
+  grid = std::min(d.kba_ntasks, sms * per_sm);
   return grid;
 }
 
@@ -1298,7 +1264,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   const int nlaunch = d.kba ? 2 : S.nlev;
   if (!gx) {
     int grid = 0;
-    const size_t smem = 0;
+    const size_t smem = flow_smem_bytes<T>(d.kba_nd * d.kba_gchunk, d.kba_gchunk);
     if (d.kba) {
       grid = cls ? flow_grid<T, true>(d, smem) : flow_grid<T, false>(d, smem);
       if (grid < 1) return fail(PGPU_ERR_CUDA, "occupancy query of the dataflow sweep failed");
@@ -1306,16 +1272,16 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
     cudaGraph_t graph;
     PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     if (d.kba) {
-      const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, S.npat, d.kba_nd, d.kba_ntasks, d.kba_nchunk,
+      const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, S.npat, d.kba_nd, d.kba_ntasks, d.kba_gchunk, d.kba_nchunk,
                        d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(),
                        cls ? d.d_ccls.as<unsigned short>() : nullptr,
                        cls ? (sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr) : nullptr, d.flow_sync.as<FlowSync>(),
                        d.flow_flags.as<unsigned int>()};
       k_flow_begin<<<1, 1, 0, p->stream>>>(K.sync);
       if (cls)
-        k_sweep_warp<T, true><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
+        k_sweep_flow<T, true><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
       else
-        k_sweep_warp<T, false><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
+        k_sweep_flow<T, false><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
     } else {
       for (int L = 0; L < S.nlev; L++) {
         dim3 g(S.grid_x[L], S.npat);
@@ -1336,7 +1302,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   prof_begin(p, &e0);
   PGPU_CUDA(cudaGraphLaunch(gx, p->stream));
   p->launches += nlaunch;
-  p->prof_name = d.kba ? "k_sweep_warp" : "k_sweep_level";
+  p->prof_name = d.kba ? "k_sweep_flow" : "k_sweep_level";
   // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
   // direction update (2 s_v), the source read per cell-group (s_v, or s_v per update for
   // an angular source), the scalar-flux moment written per cell-group (s_v) and the
@@ -1365,7 +1331,7 @@ int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y,
   T* psi = psi_work<T>(d);
   launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q, lam_s);
   int st;
-  if (false) {
+  if (d.kba) {
     // the dataflow sweep writes per-pattern moments; they are summed in pattern order
     if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)d.sched.npat * nG * sizeof(double), &p->bytes))) return st;
     T* mom = d.mom.as<T>();
@@ -1419,10 +1385,6 @@ int ensure_krylov(pgpu_problem* p, size_t len, int restart, int es) {
   return PGPU_OK;
 }
 
-// Restarted GMRES with classical Gram-Schmidt and one re-orthogonalisation (CGS2).
-// residual(r) computes b - A x for the current x; applyA(v, w) computes w = A v;
-// post(u) adds the correction for the Krylov combination u to x.  The small Hessenberg
-// problem is solved on the host with Givens rotations.
 // GMRES(m) with classical Gram-Schmidt and one re-orthogonalisation (CGS2) for the
 // correction equation A d = r, d starting at zero.  applyA(v, w) computes w = A v.
 // Stops when ||r - A d|| <= max(rtol ||r||, atol) or after max_it Arnoldi steps.  The
@@ -1445,6 +1407,8 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
   double res = 0.0, tol = 0.0;
   bool first = true;
   ReduceSlots<1> nslot{d.partials.as<double>() + (size_t)(m + 2) * kMaxBlocks, d.ticket.as<unsigned int>() + (m + 2)};
+  ReduceSlots<kGsMax> gslot{d.partials.as<double>(), d.ticket.as<unsigned int>()};
+  if (m + 1 > kGsMax) return fail(PGPU_ERR_INVALID, "GMRES restart length above the Gram-Schmidt kernels' limit");
   PGPU_CUDA(cudaMemsetAsync(dvec, 0, len * sizeof(T), s));
   while (true) {
     if (first) {
@@ -1471,12 +1435,10 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
     for (; j < m && total < max_it; j++) {
       T* vj = V + (size_t)j * len;
       if ((st = applyA(vj, w))) return st;
-      dim3 gd(std::min(gx, 512), j + 1);
-      launch(p, k_dot_many<T>, gd, kThreads, s, len, (const T*)V, len, (const T*)w, h1, d.partials.as<double>(), d.ticket.as<unsigned int>());
-      launch(p, k_sub_many<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, w);
-      launch(p, k_dot_many<T>, gd, kThreads, s, len, (const T*)V, len, (const T*)w, h2, d.partials.as<double>(), d.ticket.as<unsigned int>());
-      launch(p, k_sub_many<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, w);
-      launch(p, k_norm2<T>, gx, kThreads, s, len, (const T*)w, hn, nslot);
+      // CGS2: h1 = V^T w; w -= V h1 and h2 = V^T w; w -= V h2 and ||w||
+      launch(p, k_gs_dot<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const T*)w, h1, gslot);
+      launch(p, k_gs_sub_dot<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, w, h2, gslot);
+      launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, w, hn, nslot);
       launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)w, (const double*)hn, 1, V + (size_t)(j + 1) * len);
       PGPU_CUDA(cudaGetLastError());
       PGPU_CUDA(cudaMemcpyAsync(hh.data(), h1, (j + 1) * 8, cudaMemcpyDeviceToHost, s));
@@ -1794,7 +1756,7 @@ void sn_destroy(pgpu_problem* p) {
 // reference's cell and face order, with sides that are multiples of kTile and one sign per
 // axis for every sweep pattern; returns false (level sweeps are used) otherwise.
 struct KbaPlan {
-  int ntx, nty, ntz, nd, nchunk, ntasks;
+  int ntx, nty, ntz, nd, gchunk, nchunk, ntasks;
   std::vector<int> tiles, pat_sign;
 };
 
@@ -1846,7 +1808,10 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
         K.tiles.push_back(ty);
         K.tiles.push_back(tz);
       }
-  K.nchunk = (K.nd * op->num_groups + 31) / 32;
+  // groups per task: as many as fit in kFlowSlots (group, direction) slots
+  K.gchunk = std::max(1, std::min(op->num_groups, kFlowSlots / std::max(1, K.nd)));
+  K.nchunk = (op->num_groups + K.gchunk - 1) / K.gchunk;
+  if (K.nd * K.gchunk > kFlowThreads) return false;
   const long long ntasks = (long long)K.ntx * K.nty * K.ntz * S.npat * K.nchunk;
   if (ntasks >= (1LL << 31)) return false;
   K.ntasks = (int)ntasks;
@@ -2078,6 +2043,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       d.kba_nd = kp.nd;
       d.kba_ntasks = kp.ntasks;
       d.kba_nchunk = kp.nchunk;
+      d.kba_gchunk = kp.gchunk;
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
       up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
       std::vector<unsigned short> ccls;
