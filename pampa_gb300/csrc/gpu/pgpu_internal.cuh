@@ -120,9 +120,11 @@ __device__ inline bool block_reduce_last(double (&v)[NV], ReduceSlots<NV> slots,
   double acc[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) acc[k] = 0.0;
+  // partials of the other blocks are read through L2 (ld.global.cg), which also lets the
+  // loads of one thread overlap
   for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
 #pragma unroll
-    for (int k = 0; k < NV; k++) acc[k] += ((volatile double*)slots.partials)[k * kMaxBlocks + b];
+    for (int k = 0; k < NV; k++) acc[k] += __ldcg(slots.partials + k * kMaxBlocks + b);
   warp_sum<NV>(acc);
   __syncthreads();
   if (lane == 0)

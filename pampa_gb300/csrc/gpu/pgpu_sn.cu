@@ -1436,8 +1436,11 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
       T* vj = V + (size_t)j * len;
       if ((st = applyA(vj, w))) return st;
       // CGS2: h1 = V^T w; w -= V h1 and h2 = V^T w; w -= V h2 and ||w||
-      launch(p, k_gs_dot<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const T*)w, h1, gslot);
-      launch(p, k_gs_sub_dot<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, w, h2, gslot);
+      // (the 32-product kernels run one 256-thread block per SM at a time: two per SM
+      // keep the partials short)
+      const int gg = std::min(gx, kMaxBlocks / 4);
+      launch(p, k_gs_dot<T>, gg, kThreads, s, len, (const T*)V, len, j + 1, (const T*)w, h1, gslot);
+      launch(p, k_gs_sub_dot<T>, gg, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, w, h2, gslot);
       launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, w, hn, nslot);
       launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)w, (const double*)hn, 1, V + (size_t)(j + 1) * len);
       PGPU_CUDA(cudaGetLastError());
