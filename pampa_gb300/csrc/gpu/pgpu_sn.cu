@@ -95,6 +95,7 @@ struct SNData {
   // dataflow tiled sweep of a full Cartesian box (k_sweep_flow), when the operator qualifies
   bool kba = false;
   int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_nd = 0, kba_ntasks = 0, kba_nchunk = 1, kba_gchunk = 1;
+  int kba_t[3] = {4, 4, 4};                // tile shape (4x4x4 or 8x8x4)
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
@@ -120,6 +121,7 @@ struct SNData {
   size_t basis_len = 0;
   int restart = 0;
   int krylov_prec = -1;  // element size of the Krylov storage (4 or 8)
+  int sweeps = 0;        // sweeps of the running solve
 };
 
 struct SNOuter {
@@ -289,7 +291,7 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 // ---------------------------------------------------------------------------------
 // Dataflow tiled sweep for a full Cartesian box (one persistent launch per sweep).
 //
-// The box is cut into kTile^3-cell tiles.  A task is one tile, one octant pattern and one
+// The box is cut into tiles (4x4x4 or 8x8x4 cells).  A task is one tile, one octant and one
 // chunk of energy groups (all the pattern's directions for those groups; groups never
 // couple inside a sweep).  Tasks are numbered tile diagonal by tile diagonal of the
 // octant-oriented tile index (tx' + ty' + tz' = D), so the upwind tasks of a task --
@@ -297,7 +299,7 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 // always come earlier.  Each CTA takes the next task from an atomic counter, stages the
 // tile's source and cell classes in shared memory, waits until the flags of its upwind
 // tasks hold this sweep's epoch, loads the inflow on the tile's three upwind faces,
-// sweeps the tile through its 3*(kTile-1)+1 cell diagonals with the tile's angular flux
+// sweeps the tile through its TX+TY+TZ-2 cell diagonals with the tile's angular flux
 // in shared memory, writes psi, publishes its own flag and writes its pattern's share of
 // the scalar-flux moment.  A task is taken only by a running CTA, and only after every
 // earlier task was taken by a running CTA, so every wait ends; the waits are bounded all
@@ -311,16 +313,32 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 // read from a small per-class table; a mesh with too many classes uses the per-row
 // reciprocal diagonal instead (psi = (src - sum mu_f w_in,f psi_upwind) * rden).
 // ---------------------------------------------------------------------------------
-constexpr int kTile = 4;
-constexpr int kTileCells = kTile * kTile * kTile;
-constexpr int kTileDiags = 3 * (kTile - 1) + 1;
-constexpr int kFlowThreads = 128;
 constexpr int kFlowSlots = 10;  // (group, direction) slots of one task at most
-constexpr unsigned int kFlowSpinLimit = 1u << 22;  // ~0.4 s of polling at 100 ns
+constexpr unsigned int kFlowSpinLimit = 1u << 23;  // ~0.3-0.5 s of polling
 
-// oriented local cells of a tile (lx | ly << 2 | lz << 4) sorted by lx + ly + lz
-__constant__ unsigned char c_tile_cell[kTileCells];
-__constant__ int c_tile_dptr[kTileDiags + 1];
+// Tile shapes: 4x4x4 cells (128 threads) for small boxes, 8x8x4 (256 threads) for large
+// ones, where fewer tile hops per sweep pay for the longer in-tile diagonals.  Local
+// cell c = lx + TX*(ly + TY*lz); the tables list the cells diagonal by diagonal
+// (lx + ly + lz), with the offset of each diagonal.
+__constant__ unsigned char c_cell444[64];
+__constant__ int c_dptr444[11];
+__constant__ unsigned char c_cell884[256];
+__constant__ int c_dptr884[19];
+
+template <int TX, int TY, int TZ>
+struct TileShape;
+template <>
+struct TileShape<4, 4, 4> {
+  static constexpr int kThreads = 128;
+  __device__ static __forceinline__ int cell(int k) { return c_cell444[k]; }
+  __device__ static __forceinline__ int dptr(int d) { return c_dptr444[d]; }
+};
+template <>
+struct TileShape<8, 8, 4> {
+  static constexpr int kThreads = 256;
+  __device__ static __forceinline__ int cell(int k) { return c_cell884[k]; }
+  __device__ static __forceinline__ int dptr(int d) { return c_dptr884[d]; }
+};
 
 struct FlowSync {
   unsigned int next;   // task counter of the running sweep
@@ -348,23 +366,29 @@ __device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
   return v;
 }
 
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Waits until *flag == epoch (relaxed polling, then one fence for acquire); returns
-// without waiting once any wait of the sweep ran out.
+// Waits until *flag == epoch (relaxed polling, then one acquire load of the flag);
+// returns without waiting once any wait of the sweep ran out.
 __device__ __forceinline__ void flow_wait(const unsigned int* flag, unsigned int epoch, unsigned int* error) {
   for (unsigned int it = 0;; it++) {
     if (ld_relaxed_gpu(flag) == epoch) break;
-    if (*(volatile unsigned int*)error) break;
+    if (*(volatile unsigned int*)error) return;
     if (it >= kFlowSpinLimit) {
       atomicExch(error, 1u);
-      break;
+      return;
     }
-    __nanosleep(100);
+    __nanosleep(32);
   }
-  __threadfence();
+  (void)ld_acquire_gpu(flag);
 }
 
 __global__ void k_flow_begin(FlowSync* s) {
@@ -389,31 +413,36 @@ __device__ __forceinline__ void flow_load4(const float* __restrict__ p, float (&
   o[3] = a.w;
 }
 
-// Global cell index of the tile cell with oriented local coordinates (lx, ly, lz).
+// Global coordinates of the tile cell with oriented local coordinates (lx, ly, lz).
+template <int TX, int TY, int TZ>
 struct FlowTile {
   int bx, by, bz, sx, sy, sz;
-  __device__ __forceinline__ int x(int lx) const { return bx + (sx > 0 ? lx : kTile - 1 - lx); }
-  __device__ __forceinline__ int y(int ly) const { return by + (sy > 0 ? ly : kTile - 1 - ly); }
-  __device__ __forceinline__ int z(int lz) const { return bz + (sz > 0 ? lz : kTile - 1 - lz); }
+  __device__ __forceinline__ int x(int lx) const { return bx + (sx > 0 ? lx : TX - 1 - lx); }
+  __device__ __forceinline__ int y(int ly) const { return by + (sy > 0 ? ly : TY - 1 - ly); }
+  __device__ __forceinline__ int z(int lz) const { return bz + (sz > 0 ? lz : TZ - 1 - lz); }
 };
 
 // Shared memory of one task with S slots and Gc groups: the tile's angular flux, the
 // inflow on its three upwind faces, the isotropic source and the cells' classes.
 template <typename T>
-__host__ __device__ constexpr size_t flow_smem_bytes(int S, int Gc) {
-  return ((size_t)kTileCells * S + (size_t)3 * kTile * kTile * S + (size_t)kTileCells * Gc) * sizeof(T) +
-         (size_t)kTileCells * sizeof(int);
+__host__ __device__ constexpr size_t flow_smem_bytes(int TX, int TY, int TZ, int S, int Gc) {
+  return ((size_t)TX * TY * TZ * S + (size_t)(TY * TZ + TX * TZ + TX * TY) * S + (size_t)TX * TY * TZ * Gc) *
+             sizeof(T) +
+         (size_t)TX * TY * TZ * sizeof(int);
 }
 
-template <typename T, bool kClass>
-__global__ void __launch_bounds__(kFlowThreads, 8) k_sweep_flow(SNOp<T> A, SweepFaces<T> W, FlowGeom K,
-                                                             const SweepPtrs* __restrict__ P, int iso) {
+template <typename T, bool kClass, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileShape<TX, TY, TZ>::kThreads)
+    k_sweep_flow(SNOp<T> A, SweepFaces<T> W, FlowGeom K, const SweepPtrs* __restrict__ P, int iso) {
+  using Shape = TileShape<TX, TY, TZ>;
+  constexpr int kCells = TX * TY * TZ, kDiags = TX + TY + TZ - 2;
+  constexpr int kFx = TY * TZ, kFy = TX * TZ, kFz = TX * TY;  // upwind face cells per axis
   extern __shared__ __align__(16) unsigned char flow_smem[];
   const int G = A.G, M = A.M, n = A.n, Gc = K.gchunk, nd = K.nd, S = nd * Gc;
-  T* tpsi = reinterpret_cast<T*>(flow_smem);               // [64][S]
-  T* tin = tpsi + kTileCells * S;                           // [3][16][S]
-  T* tsrc = tin + 3 * kTile * kTile * S;                    // [64][Gc]
-  int* tcls = reinterpret_cast<int*>(tsrc + kTileCells * Gc);  // [64]
+  T* tpsi = reinterpret_cast<T*>(flow_smem);                 // [kCells][S]
+  T* tin = tpsi + kCells * S;                                 // [kFx + kFy + kFz][S]
+  T* tsrc = tin + (kFx + kFy + kFz) * S;                      // [kCells][Gc]
+  int* tcls = reinterpret_cast<int*>(tsrc + kCells * Gc);     // [kCells]
   __shared__ int s_task;
   const T* __restrict__ src = static_cast<const T*>(P->src);
   const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
@@ -435,19 +464,21 @@ __global__ void __launch_bounds__(kFlowThreads, 8) k_sweep_flow(SNOp<T> A, Sweep
     const int g0 = ch * Gc, gn = min(Gc, G - g0);
     const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
     const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
-    const FlowTile tile{(sx > 0 ? tx : K.ntx - 1 - tx) * kTile, (sy > 0 ? ty : K.nty - 1 - ty) * kTile,
-                        (sz > 0 ? tz : K.ntz - 1 - tz) * kTile, sx, sy, sz};
+    const FlowTile<TX, TY, TZ> tile{(sx > 0 ? tx : K.ntx - 1 - tx) * TX, (sy > 0 ? ty : K.nty - 1 - ty) * TY,
+                                    (sz > 0 ? tz : K.ntz - 1 - tz) * TZ, sx, sy, sz};
+    auto cell_index = [&](int c) {
+      return tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY));
+    };
     const int d0 = K.pat_dirs_ptr[p], ndp = K.pat_dirs_ptr[p + 1] - d0;
     unsigned int* pflags = K.flags + ((size_t)p * K.nchunk + ch) * ntiles;
     // 1. data that does not depend on the upwind tiles, loaded while they finish
     if (iso)
-      for (int r = threadIdx.x; r < kTileCells * Gc; r += blockDim.x) {
+      for (int r = threadIdx.x; r < kCells * Gc; r += blockDim.x) {
         const int c = r / Gc, gg = r - c * Gc;
-        if (gg < gn) tsrc[r] = src[(size_t)(tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4)) * G + g0 + gg];
+        if (gg < gn) tsrc[r] = src[(size_t)cell_index(c) * G + g0 + gg];
       }
     if (kClass)
-      for (int c = threadIdx.x; c < kTileCells; c += blockDim.x)
-        tcls[c] = K.ccls[tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4)];
+      for (int c = threadIdx.x; c < kCells; c += blockDim.x) tcls[c] = K.ccls[cell_index(c)];
     // 2. wait for the upwind tiles of this pattern and chunk
     if (threadIdx.x < 3) {
       const int a = threadIdx.x;
@@ -459,11 +490,18 @@ __global__ void __launch_bounds__(kFlowThreads, 8) k_sweep_flow(SNOp<T> A, Sweep
     const int g = g0 + gl;
     const int m = active ? K.pat_dirs[d0 + di] : 0;
     // 3. inflow on the three upwind faces: upwind tile's psi (through L2), reflective
-    //    inflow, or zero at a vacuum face; face a, position (u, v) -> tin[(a*16 + u + 4v)][slot]
-    for (int fs = cl; fs < 3 * kTile * kTile; fs += ncl) {
+    //    inflow, or zero at a vacuum face.  x face: (ly, lz) -> ly + TY lz; y face:
+    //    (lx, lz) -> kFx + lx + TX lz; z face: (lx, ly) -> kFx + kFy + lx + TX ly.
+    for (int fs = cl; fs < kFx + kFy + kFz; fs += ncl) {
       if (!active) break;
-      const int a = fs >> 4, u = fs & 3, v = (fs >> 2) & 3;
-      const int lx = a == 0 ? 0 : u, ly = a == 0 ? u : (a == 1 ? 0 : v), lz = a == 2 ? 0 : v;
+      int a, lx, ly, lz;
+      if (fs < kFx) {
+        a = 0, lx = 0, ly = fs % TY, lz = fs / TY;
+      } else if (fs < kFx + kFy) {
+        a = 1, lx = (fs - kFx) % TX, ly = 0, lz = (fs - kFx) / TX;
+      } else {
+        a = 2, lx = (fs - kFx - kFy) % TX, ly = (fs - kFx - kFy) / TX, lz = 0;
+      }
       const int x = tile.x(lx), y = tile.y(ly), z = tile.z(lz);
       const int i = x + nx * y + nxy * z;
       const int s = a == 0 ? sx : (a == 1 ? sy : sz);
@@ -489,14 +527,14 @@ __global__ void __launch_bounds__(kFlowThreads, 8) k_sweep_flow(SNOp<T> A, Sweep
     }
     // coefficients of one update, with the source term folded in: (rd * src, a_x, a_y,
     // a_z) from the class table, or (src, w_x, w_y, w_z, rden) from the row
-    auto fetch = [&](int pk, T (&cf)[4], T& rd) {
-      const T s = iso ? tsrc[pk * Gc + gl] : T(0);
+    auto fetch = [&](int c, T (&cf)[4], T& rd) {
+      const T s = iso ? tsrc[c * Gc + gl] : T(0);
       if (kClass) {
-        flow_load4(coef + (((size_t)tcls[pk] * G + g) * M + m) * 4, cf);
+        flow_load4(coef + (((size_t)tcls[c] * G + g) * M + m) * 4, cf);
         rd = T(1);
         cf[0] = iso ? cf[0] * s : cf[0];
       } else {
-        const int i = tile.x(pk & 3) + nx * tile.y((pk >> 2) & 3) + nxy * tile.z(pk >> 4);
+        const int i = cell_index(c);
         rd = W.rden[((size_t)i * G + g) * M + m];
         cf[0] = s;
         cf[1] = mux * W.win[(size_t)fx * n + i];
@@ -504,14 +542,14 @@ __global__ void __launch_bounds__(kFlowThreads, 8) k_sweep_flow(SNOp<T> A, Sweep
         cf[3] = muz * W.win[(size_t)fz * n + i];
       }
     };
-    auto update = [&](int pk, const T (&cf)[4], T rd) {
-      const int lx = pk & 3, ly = (pk >> 2) & 3, lz = pk >> 4;
+    auto update = [&](int c, const T (&cf)[4], T rd) {
+      const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
       const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
       const size_t l = ((size_t)i * G + g) * M + m;
-      const int tl = pk * S + slot;
-      const T ux = lx > 0 ? tpsi[tl - S] : tin[(ly + 4 * lz) * S + slot];
-      const T uy = ly > 0 ? tpsi[tl - kTile * S] : tin[(16 + lx + 4 * lz) * S + slot];
-      const T uz = lz > 0 ? tpsi[tl - kTile * kTile * S] : tin[(32 + lx + 4 * ly) * S + slot];
+      const int tl = c * S + slot;
+      const T ux = lx > 0 ? tpsi[tl - S] : tin[(ly + TY * lz) * S + slot];
+      const T uy = ly > 0 ? tpsi[tl - TX * S] : tin[(kFx + lx + TX * lz) * S + slot];
+      const T uz = lz > 0 ? tpsi[tl - TX * TY * S] : tin[(kFx + kFy + lx + TX * ly) * S + slot];
       T v;
       if (kClass) {
         // angular source: rd * src[l]; isotropic: rd * src folded in at fetch time
@@ -533,25 +571,25 @@ __global__ void __launch_bounds__(kFlowThreads, 8) k_sweep_flow(SNOp<T> A, Sweep
     // loaded one diagonal ahead, so the loads overlap the previous diagonal
     T cur[2][4] = {}, nxt[2][4] = {}, rcur[2] = {}, rnxt[2] = {};
     auto fetch_diag = [&](int dd, T (&dst)[2][4], T (&rdst)[2]) {
-      if (!active || dd >= kTileDiags) return;
-      const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
+      if (!active || dd >= kDiags) return;
+      const int cb = Shape::dptr(dd), cn = Shape::dptr(dd + 1) - cb;
 #pragma unroll
       for (int q = 0; q < 2; q++)
-        if (cl + q * ncl < cn) fetch(c_tile_cell[cb + cl + q * ncl], dst[q], rdst[q]);
+        if (cl + q * ncl < cn) fetch(Shape::cell(cb + cl + q * ncl), dst[q], rdst[q]);
     };
     fetch_diag(0, cur, rcur);
     __syncthreads();
-    for (int dd = 0; dd < kTileDiags; dd++) {
-      const int cb = c_tile_dptr[dd], cn = c_tile_dptr[dd + 1] - cb;
+    for (int dd = 0; dd < kDiags; dd++) {
+      const int cb = Shape::dptr(dd), cn = Shape::dptr(dd + 1) - cb;
       fetch_diag(dd + 1, nxt, rnxt);
       if (active) {
 #pragma unroll
         for (int q = 0; q < 2; q++)
-          if (cl + q * ncl < cn) update(c_tile_cell[cb + cl + q * ncl], cur[q], rcur[q]);
+          if (cl + q * ncl < cn) update(Shape::cell(cb + cl + q * ncl), cur[q], rcur[q]);
         for (int c = cl + 2 * ncl; c < cn; c += ncl) {  // more than two cells per thread
           T cf[4], rd;
-          fetch(c_tile_cell[cb + c], cf, rd);
-          update(c_tile_cell[cb + c], cf, rd);
+          fetch(Shape::cell(cb + c), cf, rd);
+          update(Shape::cell(cb + c), cf, rd);
         }
       }
       __syncthreads();
@@ -568,12 +606,11 @@ __global__ void __launch_bounds__(kFlowThreads, 8) k_sweep_flow(SNOp<T> A, Sweep
       st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
     }
     if (mom) {
-      for (int r = threadIdx.x; r < kTileCells * gn; r += blockDim.x) {
+      for (int r = threadIdx.x; r < kCells * gn; r += blockDim.x) {
         const int c = r / gn, gg = r - c * gn;
         T acc = T(0);
         for (int dj = 0; dj < ndp; dj++) acc += A.w[K.pat_dirs[d0 + dj]] * tpsi[c * S + gg * nd + dj];
-        const int i = tile.x(c & 3) + nx * tile.y((c >> 2) & 3) + nxy * tile.z(c >> 4);
-        mom[(size_t)p * n * G + (size_t)i * G + g0 + gg] = acc;
+        mom[(size_t)p * n * G + (size_t)cell_index(c) * G + g0 + gg] = acc;
       }
     }
   }
@@ -1212,7 +1249,6 @@ int ensure_rden(pgpu_problem* p, const SNOp<T>& A) {
 namespace pgpu {
 namespace {
 
-int sweeps_done = 0;
 
 // Per-class sweep coefficients in precision T (dataflow sweep with cell classes), computed
 // on first use.
@@ -1231,19 +1267,45 @@ int ensure_coef(pgpu_problem* p, const SNOp<T>& A) {
   return PGPU_OK;
 }
 
-// Persistent grid of the dataflow sweep: every CTA that fits on the device at once, at
-// most one per task.
-template <typename T, bool kClass>
-int flow_grid(SNData& d, size_t smem) {
-  int& grid = d.flow_grid[sizeof(T) == 8 ? 0 : 1];
-  if (grid) return grid;
+// The dataflow sweep for the problem's tile shape runs on a persistent grid: every CTA
+// that fits on the device at once, at most one per task.  flow_prepare sizes it (before
+// the launch is captured in the sweep graph), flow_launch enqueues it.
+template <typename T, bool kClass, int TX, int TY, int TZ>
+int flow_prepare(SNData& d) {
+  constexpr int nt = TileShape<TX, TY, TZ>::kThreads;
+  const size_t smem = flow_smem_bytes<T>(TX, TY, TZ, d.kba_nd * d.kba_gchunk, d.kba_gchunk);
   int dev = 0, sms = 0, per_sm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_flow<T, kClass>, kFlowThreads, smem) != cudaSuccess ||
-      per_sm < 1)
-    return 0;
-  grid = std::min(d.kba_ntasks, sms * per_sm);
-  return grid;
+  if (smem > 48u * 1024u)
+    PGPU_CUDA(cudaFuncSetAttribute(k_sweep_flow<T, kClass, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  PGPU_CUDA(cudaGetDevice(&dev));
+  PGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_flow<T, kClass, TX, TY, TZ>, nt, smem));
+  if (per_sm < 1) return fail(PGPU_ERR_CUDA, "the dataflow sweep does not fit on an SM");
+  d.flow_grid[sizeof(T) == 8 ? 0 : 1] = std::min(d.kba_ntasks, sms * per_sm);
+  return PGPU_OK;
+}
+
+template <typename T, bool kClass, int TX, int TY, int TZ>
+void flow_launch(SNData& d, cudaStream_t s, const SNOp<T>& A, const SweepFaces<T>& W, const FlowGeom& K,
+                 const SweepPtrs* P, int iso) {
+  constexpr int nt = TileShape<TX, TY, TZ>::kThreads;
+  const size_t smem = flow_smem_bytes<T>(TX, TY, TZ, d.kba_nd * d.kba_gchunk, d.kba_gchunk);
+  k_sweep_flow<T, kClass, TX, TY, TZ><<<d.flow_grid[sizeof(T) == 8 ? 0 : 1], nt, smem, s>>>(A, W, K, P, iso);
+}
+
+template <typename T, bool kClass>
+int flow_prepare(SNData& d) {
+  return d.kba_t[0] == 8 ? flow_prepare<T, kClass, 8, 8, 4>(d) : flow_prepare<T, kClass, 4, 4, 4>(d);
+}
+
+template <typename T, bool kClass>
+void flow_launch(SNData& d, cudaStream_t s, const SNOp<T>& A, const SweepFaces<T>& W, const FlowGeom& K,
+                 const SweepPtrs* P, int iso) {
+  if (d.kba_t[0] == 8)
+    flow_launch<T, kClass, 8, 8, 4>(d, s, A, W, K, P, iso);
+  else
+    flow_launch<T, kClass, 4, 4, 4>(d, s, A, W, K, P, iso);
 }
 
 template <typename T>
@@ -1263,12 +1325,9 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   cudaGraphExec_t& gx = d.sweep_graph[sizeof(T) == 8 ? 0 : 1][iso ? 1 : 0];
   const int nlaunch = d.kba ? 2 : S.nlev;
   if (!gx) {
-    int grid = 0;
-    const size_t smem = flow_smem_bytes<T>(d.kba_nd * d.kba_gchunk, d.kba_gchunk);
-    if (d.kba) {
-      grid = cls ? flow_grid<T, true>(d, smem) : flow_grid<T, false>(d, smem);
-      if (grid < 1) return fail(PGPU_ERR_CUDA, "occupancy query of the dataflow sweep failed");
-    }
+    if (d.kba && !d.flow_grid[sizeof(T) == 8 ? 0 : 1] &&
+        (rst = cls ? flow_prepare<T, true>(d) : flow_prepare<T, false>(d)))
+      return rst;
     cudaGraph_t graph;
     PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     if (d.kba) {
@@ -1279,9 +1338,9 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
                        d.flow_flags.as<unsigned int>()};
       k_flow_begin<<<1, 1, 0, p->stream>>>(K.sync);
       if (cls)
-        k_sweep_flow<T, true><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
+        flow_launch<T, true>(d, p->stream, A, W, K, P, iso);
       else
-        k_sweep_flow<T, false><<<grid, kFlowThreads, smem, p->stream>>>(A, W, K, P, iso);
+        flow_launch<T, false>(d, p->stream, A, W, K, P, iso);
     } else {
       for (int L = 0; L < S.nlev; L++) {
         dim3 g(S.grid_x[L], S.npat);
@@ -1311,7 +1370,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   const double N = (double)d.n * d.G * d.M, nG = (double)d.n * d.G;
   prof_end(p, e0, nlaunch, N * 2.0 * sv + nG * (2.0 * sv + 4.0) + (iso ? 0.0 : N * sv));
   PGPU_CUDA(cudaGetLastError());
-  sweeps_done++;
+  d.sweeps++;
   return PGPU_OK;
 }
 
@@ -1557,7 +1616,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   ReduceSlots<1> s1{d.partials.as<double>(), d.ticket.as<unsigned int>()};
   ReduceSlots<2> s2{d.partials.as<double>(), d.ticket.as<unsigned int>()};
   const int gl = grid_for(len), gn = grid_for(n), gG = grid_for(nG);
-  sweeps_done = 0;
+  d.sweeps = 0;
 
   cudaEvent_t e0, e1;
   PGPU_CUDA(cudaEventCreate(&e0));
@@ -1702,7 +1761,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   stats->keff = os.k;
   stats->outer_iterations = std::min(outer, opt->max_outer);
   stats->inner_iterations = inner_total;
-  stats->sweeps = sweeps_done;
+  stats->sweeps = d.sweeps;
   stats->residual = change;
   stats->seconds = ms * 1e-3;
   if (!converged) return fail(PGPU_ERR_NOT_CONVERGED, "SN power iteration reached max_outer without converging");
@@ -1756,9 +1815,10 @@ void sn_destroy(pgpu_problem* p) {
 }
 
 // Plan of the tiled sweep: verifies that the operator is a full Cartesian box in the
-// reference's cell and face order, with sides that are multiples of kTile and one sign per
+// reference's cell and face order, with sides that are multiples of 4 and one sign per
 // axis for every sweep pattern; returns false (level sweeps are used) otherwise.
 struct KbaPlan {
+  int t[3];  // tile shape
   int ntx, nty, ntz, nd, gchunk, nchunk, ntasks;
   std::vector<int> tiles, pat_sign;
 };
@@ -1766,7 +1826,7 @@ struct KbaPlan {
 static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) {
   const int nx = op->cart_nx, ny = op->cart_ny, nz = op->cart_nz, n = op->num_cells;
   if (nx <= 0 || ny <= 0 || nz <= 0 || (long long)nx * ny * nz != n || op->num_faces != 6) return false;
-  if (nx % kTile || ny % kTile || nz % kTile) return false;
+  if (nx % 4 || ny % 4 || nz % 4) return false;
   // face f: normal and neighbour offset in the reference's order -y, +x, +y, -x, -z, +z
   const int nrm[6][3] = {{0, -1, 0}, {1, 0, 0}, {0, 1, 0}, {-1, 0, 0}, {0, 0, -1}, {0, 0, 1}};
   for (int z = 0, i = 0; z < nz; z++)
@@ -1797,9 +1857,18 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
     for (int a = 0; a < 3; a++) K.pat_sign.push_back(sg[a]);
     K.nd = std::max(K.nd, S.pat_dirs_ptr[p + 1] - S.pat_dirs_ptr[p]);
   }
-  K.ntx = nx / kTile;
-  K.nty = ny / kTile;
-  K.ntz = nz / kTile;
+  // groups per task: as many as fit in kFlowSlots (group, direction) slots
+  K.gchunk = std::max(1, std::min(op->num_groups, kFlowSlots / std::max(1, K.nd)));
+  K.nchunk = (op->num_groups + K.gchunk - 1) / K.gchunk;
+  // 8x8x4 tiles when the box divides into them, 4x4x4 otherwise
+  const bool big = nx % 8 == 0 && ny % 8 == 0;
+  K.t[0] = big ? 8 : 4;
+  K.t[1] = big ? 8 : 4;
+  K.t[2] = 4;
+  if (K.nd * K.gchunk > (big ? 256 : 128)) return false;
+  K.ntx = nx / K.t[0];
+  K.nty = ny / K.t[1];
+  K.ntz = nz / K.t[2];
   // tiles in oriented coordinates, tile diagonal by tile diagonal
   const int ndiag = K.ntx + K.nty + K.ntz - 2;
   for (int D = 0; D < ndiag; D++)
@@ -1811,10 +1880,6 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
         K.tiles.push_back(ty);
         K.tiles.push_back(tz);
       }
-  // groups per task: as many as fit in kFlowSlots (group, direction) slots
-  K.gchunk = std::max(1, std::min(op->num_groups, kFlowSlots / std::max(1, K.nd)));
-  K.nchunk = (op->num_groups + K.gchunk - 1) / K.gchunk;
-  if (K.nd * K.gchunk > kFlowThreads) return false;
   const long long ntasks = (long long)K.ntx * K.nty * K.ntz * S.npat * K.nchunk;
   if (ntasks >= (1LL << 31)) return false;
   K.ntasks = (int)ntasks;
@@ -1868,20 +1933,28 @@ static bool kba_classes(const pgpu_sn_operator* op, const std::vector<unsigned c
   return true;
 }
 
-static int kba_tables() {
-  unsigned char cells[kTileCells];
-  int dptr[kTileDiags + 1];
+// Cell order of the two tile shapes, diagonal by diagonal (local cell lx + TX*(ly + TY*lz)).
+static void tile_order(int TX, int TY, int TZ, unsigned char* cells, int* dptr) {
   int k = 0;
-  for (int dd = 0; dd < kTileDiags; dd++) {
+  for (int dd = 0; dd < TX + TY + TZ - 2; dd++) {
     dptr[dd] = k;
-    for (int lz = 0; lz < kTile; lz++)
-      for (int ly = 0; ly < kTile; ly++)
-        for (int lx = 0; lx < kTile; lx++)
-          if (lx + ly + lz == dd) cells[k++] = (unsigned char)(lx | (ly << 2) | (lz << 4));
+    for (int lz = 0; lz < TZ; lz++)
+      for (int ly = 0; ly < TY; ly++)
+        for (int lx = 0; lx < TX; lx++)
+          if (lx + ly + lz == dd) cells[k++] = (unsigned char)(lx + TX * (ly + TY * lz));
   }
-  dptr[kTileDiags] = k;
-  PGPU_CUDA(cudaMemcpyToSymbol(c_tile_cell, cells, sizeof(cells)));
-  PGPU_CUDA(cudaMemcpyToSymbol(c_tile_dptr, dptr, sizeof(dptr)));
+  dptr[TX + TY + TZ - 2] = k;
+}
+
+static int kba_tables() {
+  unsigned char c444[64], c884[256];
+  int d444[11], d884[19];
+  tile_order(4, 4, 4, c444, d444);
+  tile_order(8, 8, 4, c884, d884);
+  PGPU_CUDA(cudaMemcpyToSymbol(c_cell444, c444, sizeof(c444)));
+  PGPU_CUDA(cudaMemcpyToSymbol(c_dptr444, d444, sizeof(d444)));
+  PGPU_CUDA(cudaMemcpyToSymbol(c_cell884, c884, sizeof(c884)));
+  PGPU_CUDA(cudaMemcpyToSymbol(c_dptr884, d884, sizeof(d884)));
   return PGPU_OK;
 }
 
@@ -2047,6 +2120,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       d.kba_ntasks = kp.ntasks;
       d.kba_nchunk = kp.nchunk;
       d.kba_gchunk = kp.gchunk;
+      for (int a = 0; a < 3; a++) d.kba_t[a] = kp.t[a];
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
       up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
       std::vector<unsigned short> ccls;

@@ -51,8 +51,9 @@ def test_dropin_sn_known_answers(case, case_input):
 
 
 @pytest.mark.parametrize("shape,order", [((6, 6, 4), 4), ((4, 4, 3), 8),     # level-set sweeps
-                                         ((8, 8, 4), 4), ((4, 4, 4), 8),     # tiled (4^3) sweeps
-                                         ((12, 8, 8), 2)])
+                                         ((4, 4, 4), 8), ((12, 8, 8), 2),    # dataflow, 4x4x4 tiles
+                                         ((8, 8, 4), 4), ((16, 8, 4), 4),    # dataflow, 8x8x4 tiles
+                                         ((16, 16, 8), 2)])
 def test_synthetic_sn_3d_reflective(shape, order, tmp_path):
     from pampa_gb300 import workloads as wl
     nx, ny, nz = shape
