@@ -100,6 +100,7 @@ struct SNData {
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
   DevBuf mom;  // per-pattern scalar-flux moments of the dataflow sweep [npat][n*G]
+  DevBuf d_tile_cls, d_tile_ncls, d_cell_lcls;  // per-tile class lists (FlowGeom)
   cudaGraphExec_t sweep_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][iso]
   ~SNData() {
     for (auto& row : sweep_graph)
@@ -314,6 +315,7 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 // reciprocal diagonal instead (psi = (src - sum mu_f w_in,f psi_upwind) * rden).
 // ---------------------------------------------------------------------------------
 constexpr int kFlowSlots = 10;  // (group, direction) slots of one task at most
+constexpr int kTileClasses = 16;  // cell classes of a tile whose coefficients are staged
 constexpr unsigned int kFlowSpinLimit = 1u << 23;  // ~0.3-0.5 s of polling
 
 // Tile shapes: 4x4x4 cells (128 threads) for small boxes, 8x8x4 (256 threads) for large
@@ -356,6 +358,9 @@ struct FlowGeom {
   const int* __restrict__ pat_dirs;
   const unsigned short* __restrict__ ccls;  // [n] cell class, or null (per-row rden)
   const void* coef;                         // [ncls][G][M][4] (rd, a_x, a_y, a_z) in T
+  const int* __restrict__ tile_cls;         // [ntiles][kTileClasses] classes of a tile (absolute index)
+  const int* __restrict__ tile_ncls;        // [ntiles] their count, > kTileClasses: not staged
+  const unsigned char* __restrict__ cell_lcls;  // [n] a cell's index in its tile's class list
   FlowSync* sync;
   unsigned int* flags;  // [npat][nchunk][ntz][nty][ntx] by oriented tile coordinates
 };
@@ -426,7 +431,8 @@ struct FlowTile {
 // inflow on its three upwind faces, the isotropic source and the cells' classes.
 template <typename T>
 __host__ __device__ constexpr size_t flow_smem_bytes(int TX, int TY, int TZ, int S, int Gc) {
-  return ((size_t)TX * TY * TZ * S + (size_t)(TY * TZ + TX * TZ + TX * TY) * S + (size_t)TX * TY * TZ * Gc) *
+  return ((size_t)TX * TY * TZ * S + (size_t)(TY * TZ + TX * TZ + TX * TY) * S + (size_t)TX * TY * TZ * Gc +
+          (size_t)kTileClasses * S * 4) *
              sizeof(T) +
          (size_t)TX * TY * TZ * sizeof(int);
 }
@@ -439,10 +445,11 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
   constexpr int kFx = TY * TZ, kFy = TX * TZ, kFz = TX * TY;  // upwind face cells per axis
   extern __shared__ __align__(16) unsigned char flow_smem[];
   const int G = A.G, M = A.M, n = A.n, Gc = K.gchunk, nd = K.nd, S = nd * Gc;
-  T* tpsi = reinterpret_cast<T*>(flow_smem);                 // [kCells][S]
+  T* tcoef = reinterpret_cast<T*>(flow_smem);                 // [kTileClasses][S][4]
+  T* tpsi = tcoef + kTileClasses * S * 4;                     // [kCells][S]
   T* tin = tpsi + kCells * S;                                 // [kFx + kFy + kFz][S]
   T* tsrc = tin + (kFx + kFy + kFz) * S;                      // [kCells][Gc]
-  int* tcls = reinterpret_cast<int*>(tsrc + kCells * Gc);     // [kCells]
+  int* tcls = reinterpret_cast<int*>(tsrc + kCells * Gc);     // [kCells] class (local or global)
   __shared__ int s_task;
   const T* __restrict__ src = static_cast<const T*>(P->src);
   const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
@@ -464,37 +471,40 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     const int g0 = ch * Gc, gn = min(Gc, G - g0);
     const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
     const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
-    const FlowTile<TX, TY, TZ> tile{(sx > 0 ? tx : K.ntx - 1 - tx) * TX, (sy > 0 ? ty : K.nty - 1 - ty) * TY,
-                                    (sz > 0 ? tz : K.ntz - 1 - tz) * TZ, sx, sy, sz};
+    const int atx = sx > 0 ? tx : K.ntx - 1 - tx, aty = sy > 0 ? ty : K.nty - 1 - ty, atz = sz > 0 ? tz : K.ntz - 1 - tz;
+    const FlowTile<TX, TY, TZ> tile{atx * TX, aty * TY, atz * TZ, sx, sy, sz};
     auto cell_index = [&](int c) {
       return tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY));
     };
     const int d0 = K.pat_dirs_ptr[p], ndp = K.pat_dirs_ptr[p + 1] - d0;
+    const bool active = cl < ncl && gl < gn && di < ndp;
+    const int g = g0 + gl;
+    const int m = active ? K.pat_dirs[d0 + di] : 0;
     unsigned int* pflags = K.flags + ((size_t)p * K.nchunk + ch) * ntiles;
-    // 1. data that does not depend on the upwind tiles, loaded while they finish
+    const int tb = (atz * K.nty + aty) * K.ntx + atx;
+    const int nk = kClass ? K.tile_ncls[tb] : 0;
+    const bool staged = kClass && nk <= kTileClasses;
+    // 1. data that does not depend on the upwind tiles, loaded while they finish: the
+    //    source, the cells' classes and the coefficients of the tile's classes, and the
+    //    inflow on upwind faces that lie on the box boundary
     if (iso)
       for (int r = threadIdx.x; r < kCells * Gc; r += blockDim.x) {
         const int c = r / Gc, gg = r - c * Gc;
         if (gg < gn) tsrc[r] = src[(size_t)cell_index(c) * G + g0 + gg];
       }
-    if (kClass)
-      for (int c = threadIdx.x; c < kCells; c += blockDim.x) tcls[c] = K.ccls[cell_index(c)];
-    // 2. wait for the upwind tiles of this pattern and chunk
-    if (threadIdx.x < 3) {
-      const int a = threadIdx.x;
-      const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
-      if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
+    if (kClass) {
+      for (int c = threadIdx.x; c < kCells; c += blockDim.x) {
+        const int i = cell_index(c);
+        tcls[c] = staged ? (int)K.cell_lcls[i] : (int)K.ccls[i];
+      }
+      if (staged && active)
+        for (int k = cl; k < nk; k += ncl)
+          flow_load4(coef + (((size_t)K.tile_cls[(size_t)tb * kTileClasses + k] * G + g) * M + m) * 4,
+                     *reinterpret_cast<T(*)[4]>(tcoef + (k * S + slot) * 4));
     }
-    __syncthreads();
-    const bool active = cl < ncl && gl < gn && di < ndp;
-    const int g = g0 + gl;
-    const int m = active ? K.pat_dirs[d0 + di] : 0;
-    // 3. inflow on the three upwind faces: upwind tile's psi (through L2), reflective
-    //    inflow, or zero at a vacuum face.  x face: (ly, lz) -> ly + TY lz; y face:
-    //    (lx, lz) -> kFx + lx + TX lz; z face: (lx, ly) -> kFx + kFy + lx + TX ly.
-    for (int fs = cl; fs < kFx + kFy + kFz; fs += ncl) {
-      if (!active) break;
-      int a, lx, ly, lz;
+    // face a, position (u, v): x face (ly, lz) -> ly + TY lz; y face (lx, lz) -> kFx + lx +
+    // TX lz; z face (lx, ly) -> kFx + kFy + lx + TX ly
+    auto face_cell = [&](int fs, int& a, int& lx, int& ly, int& lz) {
       if (fs < kFx) {
         a = 0, lx = 0, ly = fs % TY, lz = fs / TY;
       } else if (fs < kFx + kFy) {
@@ -502,21 +512,39 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
       } else {
         a = 2, lx = (fs - kFx - kFy) % TX, ly = (fs - kFx - kFy) / TX, lz = 0;
       }
-      const int x = tile.x(lx), y = tile.y(ly), z = tile.z(lz);
-      const int i = x + nx * y + nxy * z;
-      const int s = a == 0 ? sx : (a == 1 ? sy : sz);
-      const int c = a == 0 ? x : (a == 1 ? y : z), cmax = a == 0 ? nx : (a == 1 ? ny : nz);
-      T val = T(0);
-      if (s > 0 ? c > 0 : c < cmax - 1) {
-        const int nb = i - s * (a == 0 ? 1 : (a == 1 ? nx : nxy));
-        val = __ldcg(psi + ((size_t)nb * G + g) * M + m);
-      } else if (bnd) {
-        const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
-        const size_t o = (size_t)f * n + i;
-        if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd[((size_t)A.rslot[o] * G + g) * M + m];
+    };
+    const int inner = (tx > 0) | (ty > 0) << 1 | (tz > 0) << 2;  // upwind faces inside the box
+    if (active)
+      for (int fs = cl; fs < kFx + kFy + kFz; fs += ncl) {
+        int a, lx, ly, lz;
+        face_cell(fs, a, lx, ly, lz);
+        if ((inner >> a) & 1) continue;
+        T val = T(0);
+        if (bnd) {
+          const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
+          const size_t o = (size_t)f * n + (tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz));
+          if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd[((size_t)A.rslot[o] * G + g) * M + m];
+        }
+        tin[fs * S + slot] = val;
       }
-      tin[fs * S + slot] = val;
+    // 2. wait for the upwind tiles of this pattern and chunk
+    if (threadIdx.x < 3) {
+      const int a = threadIdx.x;
+      const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
+      if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
     }
+    __syncthreads();
+    // 3. inflow from the upwind tiles (through L2)
+    if (active)
+      for (int fs = cl; fs < kFx + kFy + kFz; fs += ncl) {
+        int a, lx, ly, lz;
+        face_cell(fs, a, lx, ly, lz);
+        if (!((inner >> a) & 1)) continue;
+        const int s = a == 0 ? sx : (a == 1 ? sy : sz);
+        const int nb = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz) - s * (a == 0 ? 1 : (a == 1 ? nx : nxy));
+        tin[fs * S + slot] = __ldcg(psi + ((size_t)nb * G + g) * M + m);
+      }
+    __syncthreads();
     // 4. the tile's cell diagonals
     const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
     T mux = T(0), muy = T(0), muz = T(0);
@@ -525,80 +553,43 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
       muy = fabs(A.dirs[(size_t)m * 3 + 1]);
       muz = fabs(A.dirs[(size_t)m * 3 + 2]);
     }
-    // coefficients of one update, with the source term folded in: (rd * src, a_x, a_y,
-    // a_z) from the class table, or (src, w_x, w_y, w_z, rden) from the row
-    auto fetch = [&](int c, T (&cf)[4], T& rd) {
-      const T s = iso ? tsrc[c * Gc + gl] : T(0);
-      if (kClass) {
-        flow_load4(coef + (((size_t)tcls[c] * G + g) * M + m) * 4, cf);
-        rd = T(1);
-        cf[0] = iso ? cf[0] * s : cf[0];
-      } else {
-        const int i = cell_index(c);
-        rd = W.rden[((size_t)i * G + g) * M + m];
-        cf[0] = s;
-        cf[1] = mux * W.win[(size_t)fx * n + i];
-        cf[2] = muy * W.win[(size_t)fy * n + i];
-        cf[3] = muz * W.win[(size_t)fz * n + i];
-      }
-    };
-    auto update = [&](int c, const T (&cf)[4], T rd) {
-      const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
-      const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
-      const size_t l = ((size_t)i * G + g) * M + m;
-      const int tl = c * S + slot;
-      const T ux = lx > 0 ? tpsi[tl - S] : tin[(ly + TY * lz) * S + slot];
-      const T uy = ly > 0 ? tpsi[tl - TX * S] : tin[(kFx + lx + TX * lz) * S + slot];
-      const T uz = lz > 0 ? tpsi[tl - TX * TY * S] : tin[(kFx + kFy + lx + TX * ly) * S + slot];
-      T v;
-      if (kClass) {
-        // angular source: rd * src[l]; isotropic: rd * src folded in at fetch time
-        v = iso ? cf[0] : cf[0] * src[l];
-        v += cf[3] * uz;
-        v += cf[2] * uy;
-        v += cf[1] * ux;
-      } else {
-        T num = iso ? cf[0] : src[l];
-        num += cf[3] * uz;
-        num += cf[2] * uy;
-        num += cf[1] * ux;
-        v = num * rd;
-      }
-      psi[l] = v;
-      tpsi[tl] = v;
-    };
-    // a thread's first two cells of each diagonal take their coefficients from registers
-    // loaded one diagonal ahead, so the loads overlap the previous diagonal
-    T cur[2][4] = {}, nxt[2][4] = {}, rcur[2] = {}, rnxt[2] = {};
-    auto fetch_diag = [&](int dd, T (&dst)[2][4], T (&rdst)[2]) {
-      if (!active || dd >= kDiags) return;
-      const int cb = Shape::dptr(dd), cn = Shape::dptr(dd + 1) - cb;
-#pragma unroll
-      for (int q = 0; q < 2; q++)
-        if (cl + q * ncl < cn) fetch(Shape::cell(cb + cl + q * ncl), dst[q], rdst[q]);
-    };
-    fetch_diag(0, cur, rcur);
-    __syncthreads();
     for (int dd = 0; dd < kDiags; dd++) {
       const int cb = Shape::dptr(dd), cn = Shape::dptr(dd + 1) - cb;
-      fetch_diag(dd + 1, nxt, rnxt);
-      if (active) {
-#pragma unroll
-        for (int q = 0; q < 2; q++)
-          if (cl + q * ncl < cn) update(Shape::cell(cb + cl + q * ncl), cur[q], rcur[q]);
-        for (int c = cl + 2 * ncl; c < cn; c += ncl) {  // more than two cells per thread
-          T cf[4], rd;
-          fetch(Shape::cell(cb + c), cf, rd);
-          update(Shape::cell(cb + c), cf, rd);
+      if (active)
+        for (int q = cl; q < cn; q += ncl) {
+          const int c = Shape::cell(cb + q);
+          const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
+          const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
+          const size_t l = ((size_t)i * G + g) * M + m;
+          const int tl = c * S + slot;
+          const T ux = lx > 0 ? tpsi[tl - S] : tin[(ly + TY * lz) * S + slot];
+          const T uy = ly > 0 ? tpsi[tl - TX * S] : tin[(kFx + lx + TX * lz) * S + slot];
+          const T uz = lz > 0 ? tpsi[tl - TX * TY * S] : tin[(kFx + kFy + lx + TX * ly) * S + slot];
+          const T s = iso ? tsrc[c * Gc + gl] : src[l];
+          T v;
+          if (kClass) {
+            T cf[4];
+            if (staged) {
+              const T* sc = tcoef + (tcls[c] * S + slot) * 4;
+              cf[0] = sc[0], cf[1] = sc[1], cf[2] = sc[2], cf[3] = sc[3];
+            } else {
+              flow_load4(coef + (((size_t)tcls[c] * G + g) * M + m) * 4, cf);
+            }
+            v = cf[0] * s;
+            v += cf[3] * uz;
+            v += cf[2] * uy;
+            v += cf[1] * ux;
+          } else {
+            T num = s;
+            num += (muz * W.win[(size_t)fz * n + i]) * uz;
+            num += (muy * W.win[(size_t)fy * n + i]) * uy;
+            num += (mux * W.win[(size_t)fx * n + i]) * ux;
+            v = num * W.rden[l];
+          }
+          psi[l] = v;
+          tpsi[tl] = v;
         }
-      }
       __syncthreads();
-#pragma unroll
-      for (int q = 0; q < 2; q++) {
-        rcur[q] = rnxt[q];
-#pragma unroll
-        for (int k = 0; k < 4; k++) cur[q][k] = nxt[q][k];
-      }
     }
     // 5. publish the tile, then its scalar-flux moment over this pattern's directions
     if (threadIdx.x == 0) {
@@ -770,20 +761,6 @@ __global__ void k_apply_R(SNOp<T> A, const T* __restrict__ psi, const T* __restr
 
 // ---- small vector kernels (deterministic reductions) ----
 
-template <typename T>
-__global__ void k_dot_many(long long N, const T* __restrict__ V, long long ld, const T* __restrict__ x,
-                           double* out, double* partials, unsigned int* tickets) {
-  // blockIdx.y = vector index
-  const int k = blockIdx.y;
-  const T* v = V + (size_t)k * ld;
-  double acc[1] = {0.0};
-  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
-    acc[0] += (double)v[l] * (double)x[l];
-  ReduceSlots<1> slots{partials + (size_t)k * kMaxBlocks, tickets + k};
-  double tot[1];
-  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) out[k] = tot[0];
-}
-
 // x -= sum_k h[k] V[k]   (h on device)
 template <typename T>
 __global__ void k_sub_many(long long N, const T* __restrict__ V, long long ld, int nv, const double* __restrict__ h, T* x) {
@@ -795,51 +772,30 @@ __global__ void k_sub_many(long long N, const T* __restrict__ V, long long ld, i
 }
 
 // Gram-Schmidt passes of the GMRES Arnoldi step over nv <= kGsMax basis vectors V_k
-// (stride ld): all nv products with w come out of one pass over the basis, and the
-// subtraction of one pass is fused with the products (or the norm) of the next.
+// (stride ld).  Products: each block row (blockIdx.y) takes kGsChunk vectors, so w is
+// read once per chunk instead of once per vector, with few registers per thread.
 constexpr int kGsMax = 32;
+constexpr int kGsChunk = 8;
 
-// out[k] = <V_k, w>
+// out[k] = <V_k, w> for k < nv; reduction slots of chunk y at partials + y*kGsChunk*kMaxBlocks
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_gs_dot(long long N, const T* __restrict__ V, long long ld, int nv,
-                                                    const T* __restrict__ w, double* out, ReduceSlots<kGsMax> slots) {
-  double acc[kGsMax];
+__global__ void k_gs_dot(long long N, const T* __restrict__ V, long long ld, int nv, const T* __restrict__ w,
+                         double* out, double* partials, unsigned int* tickets) {
+  const int k0 = blockIdx.y * kGsChunk;
+  const int nk = min(kGsChunk, nv - k0);
+  double acc[kGsChunk];
 #pragma unroll
-  for (int k = 0; k < kGsMax; k++) acc[k] = 0.0;
+  for (int k = 0; k < kGsChunk; k++) acc[k] = 0.0;
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
     const double x = (double)w[l];
 #pragma unroll
-    for (int k = 0; k < kGsMax; k++)
-      if (k < nv) acc[k] += (double)V[(size_t)k * ld + l] * x;
+    for (int k = 0; k < kGsChunk; k++)
+      if (k < nk) acc[k] += (double)V[(size_t)(k0 + k) * ld + l] * x;
   }
-  double tot[kGsMax];
-  if (block_reduce_last<kGsMax>(acc, slots, tot) && threadIdx.x == 0)
-    for (int k = 0; k < nv; k++) out[k] = tot[k];
-}
-
-// w -= sum_k h[k] V_k, then out[k] = <V_k, w> (second Gram-Schmidt pass)
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_gs_sub_dot(long long N, const T* __restrict__ V, long long ld, int nv,
-                                                        const double* __restrict__ h, T* w, double* out,
-                                                        ReduceSlots<kGsMax> slots) {
-  double acc[kGsMax];
-#pragma unroll
-  for (int k = 0; k < kGsMax; k++) acc[k] = 0.0;
-  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
-    double s = (double)w[l];
-#pragma unroll
-    for (int k = 0; k < kGsMax; k++)
-      if (k < nv) s -= h[k] * (double)V[(size_t)k * ld + l];
-    const T sw = (T)s;
-    w[l] = sw;
-    const double x = (double)sw;
-#pragma unroll
-    for (int k = 0; k < kGsMax; k++)
-      if (k < nv) acc[k] += (double)V[(size_t)k * ld + l] * x;
-  }
-  double tot[kGsMax];
-  if (block_reduce_last<kGsMax>(acc, slots, tot) && threadIdx.x == 0)
-    for (int k = 0; k < nv; k++) out[k] = tot[k];
+  ReduceSlots<kGsChunk> slots{partials + (size_t)blockIdx.y * kGsChunk * kMaxBlocks, tickets + blockIdx.y};
+  double tot[kGsChunk];
+  if (block_reduce_last<kGsChunk>(acc, slots, tot) && threadIdx.x == 0)
+    for (int k = 0; k < nk; k++) out[k0 + k] = tot[k];
 }
 
 // w -= sum_k h[k] V_k, then *out = ||w||
@@ -850,9 +806,7 @@ __global__ void __launch_bounds__(kThreads) k_gs_sub_norm(long long N, const T* 
   double acc[1] = {0.0};
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
     double s = (double)w[l];
-#pragma unroll
-    for (int k = 0; k < kGsMax; k++)
-      if (k < nv) s -= h[k] * (double)V[(size_t)k * ld + l];
+    for (int k = 0; k < nv; k++) s -= h[k] * (double)V[(size_t)k * ld + l];
     const T sw = (T)s;
     w[l] = sw;
     acc[0] += (double)sw * (double)sw;
@@ -1334,7 +1288,8 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
       const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, S.npat, d.kba_nd, d.kba_ntasks, d.kba_gchunk, d.kba_nchunk,
                        d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(),
                        cls ? d.d_ccls.as<unsigned short>() : nullptr,
-                       cls ? (sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr) : nullptr, d.flow_sync.as<FlowSync>(),
+                       cls ? (sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr) : nullptr, d.d_tile_cls.as<int>(),
+                       d.d_tile_ncls.as<int>(), d.d_cell_lcls.as<unsigned char>(), d.flow_sync.as<FlowSync>(),
                        d.flow_flags.as<unsigned int>()};
       k_flow_begin<<<1, 1, 0, p->stream>>>(K.sync);
       if (cls)
@@ -1466,7 +1421,6 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
   double res = 0.0, tol = 0.0;
   bool first = true;
   ReduceSlots<1> nslot{d.partials.as<double>() + (size_t)(m + 2) * kMaxBlocks, d.ticket.as<unsigned int>() + (m + 2)};
-  ReduceSlots<kGsMax> gslot{d.partials.as<double>(), d.ticket.as<unsigned int>()};
   if (m + 1 > kGsMax) return fail(PGPU_ERR_INVALID, "GMRES restart length above the Gram-Schmidt kernels' limit");
   PGPU_CUDA(cudaMemsetAsync(dvec, 0, len * sizeof(T), s));
   while (true) {
@@ -1494,12 +1448,13 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
     for (; j < m && total < max_it; j++) {
       T* vj = V + (size_t)j * len;
       if ((st = applyA(vj, w))) return st;
-      // CGS2: h1 = V^T w; w -= V h1 and h2 = V^T w; w -= V h2 and ||w||
-      // (the 32-product kernels run one 256-thread block per SM at a time: two per SM
-      // keep the partials short)
-      const int gg = std::min(gx, kMaxBlocks / 4);
-      launch(p, k_gs_dot<T>, gg, kThreads, s, len, (const T*)V, len, j + 1, (const T*)w, h1, gslot);
-      launch(p, k_gs_sub_dot<T>, gg, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, w, h2, gslot);
+      // CGS2: h1 = V^T w; w -= V h1; h2 = V^T w; w -= V h2 and ||w||
+      const dim3 gd(std::min(gx, kMaxBlocks / 2), (j + 1 + kGsChunk - 1) / kGsChunk);
+      double* part = d.partials.as<double>();
+      unsigned int* tick = d.ticket.as<unsigned int>();
+      launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)w, h1, part, tick);
+      launch(p, k_sub_many<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, w);
+      launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)w, h2, part, tick);
       launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, w, hn, nslot);
       launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)w, (const double*)hn, 1, V + (size_t)(j + 1) * len);
       PGPU_CUDA(cudaGetLastError());
@@ -2129,6 +2084,25 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
         d.ncls = (int)crep.size();
         up(d.d_ccls, ccls.data(), ccls.size() * 2);
         up(d.d_crep, crep.data(), crep.size() * 4);
+        // per tile: its distinct classes (first kTileClasses) and each cell's index there
+        const int ntl = kp.ntx * kp.nty * kp.ntz, nx = op->cart_nx, ny = op->cart_ny;
+        std::vector<int> tcl((size_t)ntl * kTileClasses, -1), tnc(ntl, 0);
+        std::vector<unsigned char> lcl(n, 0);
+        for (int i = 0; i < n; i++) {
+          const int x = i % nx, y = (i / nx) % ny, z = i / (nx * ny);
+          const int tb = ((z / kp.t[2]) * kp.nty + y / kp.t[1]) * kp.ntx + x / kp.t[0];
+          int* lst = tcl.data() + (size_t)tb * kTileClasses;
+          int k = 0;
+          while (k < std::min(tnc[tb], kTileClasses) && lst[k] != (int)ccls[i]) k++;
+          if (k == std::min(tnc[tb], kTileClasses)) {
+            if (tnc[tb] < kTileClasses) lst[k] = ccls[i];
+            tnc[tb]++;
+          }
+          lcl[i] = (unsigned char)std::min(k, 255);
+        }
+        up(d.d_tile_cls, tcl.data(), tcl.size() * 4);
+        up(d.d_tile_ncls, tnc.data(), tnc.size() * 4);
+        up(d.d_cell_lcls, lcl.data(), lcl.size());
       }
       al(d.flow_sync, sizeof(FlowSync));
       al(d.flow_flags, (size_t)kp.ntasks * 4);
