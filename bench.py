@@ -294,6 +294,16 @@ def run_ours(args, rank, world, local):
                 frac=(achieved / peaks["hbm_gbs"]) if achieved else None, peak_source=peaks["source"],
                 traffic=None, launches=kern_n,
                 kernel_share_of_solve=kern_s / dev_time if dev_time > 0 else None)
+    if w["kind"] == "sn" and kern_s > 0:
+        # the transport sweep is bound by FP64 issue on GB300 (FP64 = 1/64 of FP32): per
+        # (cell, group, direction) update one multiply and three FMAs (7 flops); the
+        # mixed-precision workload's correction sweeps are FP32 and only its residual
+        # sweeps count here.  Peak: nominal GB300 FP64, 1.25 TFLOP/s (no measured figure).
+        sw = kern_n / 2.0 if kname == "k_sweep_flow" else float(sweeps * args.steps)
+        if w["precision"] == "fp64":
+            ach = 7.0 * n_psi * sw / kern_s / 1e12
+            roof["fp64"] = dict(flops_per_update=7, achieved_tflops=ach, nominal_peak_tflops=1.25,
+                                frac_of_nominal=ach / 1.25)
     traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic_path):
         with open(traffic_path) as fh:

@@ -102,10 +102,12 @@ struct SNData {
   DevBuf mom;  // per-pattern scalar-flux moments of the dataflow sweep [npat][n*G]
   DevBuf d_tile_cls, d_tile_ncls, d_cell_lcls;  // per-tile class lists (FlowGeom)
   cudaGraphExec_t sweep_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][iso]
+  double* hpin = nullptr;  // pinned host mirror of hbuf (GMRES scalars)
   ~SNData() {
     for (auto& row : sweep_graph)
       for (auto& g : row)
         if (g) cudaGraphExecDestroy(g);
+    if (hpin) cudaFreeHost(hpin);
   }
   bool use_tab = false;
   bool have32 = false;
@@ -451,6 +453,11 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
   T* tsrc = tin + (kFx + kFy + kFz) * S;                      // [kCells][Gc]
   int* tcls = reinterpret_cast<int*>(tsrc + kCells * Gc);     // [kCells] class (local or global)
   __shared__ int s_task;
+  // the tile's cell order, diagonal by diagonal (threads of a warp read different entries)
+  __shared__ unsigned char s_cell[kCells];
+  __shared__ int s_dptr[kDiags + 1];
+  for (int k = threadIdx.x; k < kCells; k += blockDim.x) s_cell[k] = (unsigned char)Shape::cell(k);
+  for (int k = threadIdx.x; k <= kDiags; k += blockDim.x) s_dptr[k] = Shape::dptr(k);
   const T* __restrict__ src = static_cast<const T*>(P->src);
   const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
   T* psi = static_cast<T*>(P->psi);
@@ -527,6 +534,14 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
         }
         tin[fs * S + slot] = val;
       }
+    // the source term of every update, rd * src, into the tile buffer (overwritten by psi
+    // in the passes); needs the staged coefficients and source
+    const bool fold = kClass && staged && iso;
+    if (fold) {
+      __syncthreads();
+      if (active)
+        for (int c = cl; c < kCells; c += ncl) tpsi[c * S + slot] = tcoef[(tcls[c] * S + slot) * 4] * tsrc[c * Gc + gl];
+    }
     // 2. wait for the upwind tiles of this pattern and chunk
     if (threadIdx.x < 3) {
       const int a = threadIdx.x;
@@ -554,10 +569,10 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
       muz = fabs(A.dirs[(size_t)m * 3 + 2]);
     }
     for (int dd = 0; dd < kDiags; dd++) {
-      const int cb = Shape::dptr(dd), cn = Shape::dptr(dd + 1) - cb;
+      const int cb = s_dptr[dd], cn = s_dptr[dd + 1] - cb;
       if (active)
         for (int q = cl; q < cn; q += ncl) {
-          const int c = Shape::cell(cb + q);
+          const int c = s_cell[cb + q];
           const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
           const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
           const size_t l = ((size_t)i * G + g) * M + m;
@@ -565,7 +580,6 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
           const T ux = lx > 0 ? tpsi[tl - S] : tin[(ly + TY * lz) * S + slot];
           const T uy = ly > 0 ? tpsi[tl - TX * S] : tin[(kFx + lx + TX * lz) * S + slot];
           const T uz = lz > 0 ? tpsi[tl - TX * TY * S] : tin[(kFx + kFy + lx + TX * ly) * S + slot];
-          const T s = iso ? tsrc[c * Gc + gl] : src[l];
           T v;
           if (kClass) {
             T cf[4];
@@ -575,12 +589,12 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
             } else {
               flow_load4(coef + (((size_t)tcls[c] * G + g) * M + m) * 4, cf);
             }
-            v = cf[0] * s;
+            v = fold ? tpsi[tl] : cf[0] * (iso ? tsrc[c * Gc + gl] : src[l]);
             v += cf[3] * uz;
             v += cf[2] * uy;
             v += cf[1] * ux;
           } else {
-            T num = s;
+            T num = iso ? tsrc[c * Gc + gl] : src[l];
             num += (muz * W.win[(size_t)fz * n + i]) * uz;
             num += (muy * W.win[(size_t)fy * n + i]) * uy;
             num += (mux * W.win[(size_t)fx * n + i]) * ux;
@@ -1388,6 +1402,9 @@ int ensure_krylov(pgpu_problem* p, size_t len, int restart, int es) {
   if ((st = dev_alloc(d.partials, (size_t)(restart + 4) * kMaxBlocks * 8, &p->bytes))) return st;
   if ((st = dev_alloc(d.ticket, (size_t)(restart + 4) * 4, &p->bytes))) return st;
   if ((st = dev_alloc(d.hbuf, (size_t)4 * (restart + 4) * 8, &p->bytes))) return st;
+  if (d.hpin) cudaFreeHost(d.hpin);
+  d.hpin = nullptr;
+  PGPU_CUDA(cudaMallocHost(&d.hpin, (size_t)4 * (restart + 4) * 8));
   // the scattering source is used by FP64 residual sweeps and by correction sweeps in
   // either precision: size it for FP64
   if ((st = dev_alloc(d.scat, (size_t)d.n * d.G * 8, &p->bytes))) return st;
@@ -1416,7 +1433,8 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
   double* hn = h2 + (m + 4);
   double* yv = hn + (m + 4);
   const int gx = grid_for(len);
-  std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hh(m + 2), hh2(m + 2);
+  std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
+  double* hp = d.hpin;  // pinned mirror of hbuf
   int total = 0, st;
   double res = 0.0, tol = 0.0;
   bool first = true;
@@ -1458,11 +1476,12 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
       launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, w, hn, nslot);
       launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)w, (const double*)hn, 1, V + (size_t)(j + 1) * len);
       PGPU_CUDA(cudaGetLastError());
-      PGPU_CUDA(cudaMemcpyAsync(hh.data(), h1, (j + 1) * 8, cudaMemcpyDeviceToHost, s));
-      PGPU_CUDA(cudaMemcpyAsync(hh2.data(), h2, (j + 1) * 8, cudaMemcpyDeviceToHost, s));
-      double hnext;
-      PGPU_CUDA(cudaMemcpyAsync(&hnext, hn, 8, cudaMemcpyDeviceToHost, s));
+      // h1, h2 and ||w|| are adjacent in hbuf: one copy into pinned host memory
+      PGPU_CUDA(cudaMemcpyAsync(hp, h1, (size_t)(2 * (m + 4) + 1) * 8, cudaMemcpyDeviceToHost, s));
       PGPU_CUDA(cudaStreamSynchronize(s));
+      const double* hh = hp;
+      const double* hh2 = hp + (m + 4);
+      const double hnext = hp[2 * (m + 4)];
       total++;
       double* col = &H[(size_t)j * (m + 1)];
       for (int k = 0; k <= j; k++) col[k] = hh[k] + hh2[k];
