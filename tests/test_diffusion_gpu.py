@@ -92,3 +92,17 @@ def test_iteration_cap_reports_not_converged(case_input):
             dp.solve(max_outer=1)
         # the context stays usable after the error
         assert dp.solve().keff > 0.9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_seven_group_3d(precision, tmp_path):
+    """7-group 3D diffusion with down- and upscatter (the shape of the large mixed-precision
+    workload, 16x16x8 cells here)."""
+    from pampa_gb300 import workloads as wl
+    path = wl.diffusion_3d_7g(str(tmp_path), nx=16, ny=16, nz=8, block=4)
+    ref = po.run_input(path)
+    with pg.Pampa(path, "-silent", "-pgpu_precision", precision) as p:
+        p.solve()
+        k_tol, f_tol = (K_TOL, FLUX_TOL) if precision == "fp64" else (1e-5, 1e-4)
+        assert abs(p.keff - ref["keff"]) <= k_tol, (p.keff, ref["keff"])
+        assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= f_tol
