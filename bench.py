@@ -49,6 +49,10 @@ WORKLOADS = {
     "diffusion_2d_34x34_g2": dict(kind="diffusion2d", args=dict(), precision="fp64", dtype="f64",
                                   desc="2-group diffusion k-eigenvalue, 2D Cartesian 34x34 (5 cm)"),
 }
+WORKLOADS["serve_diffusion"] = dict(
+    kind="serve", args=dict(), precision="mixed", dtype="f32+f64",
+    desc="stream of k-eigenvalue diffusion requests (3D Cartesian 16x16x4..128x128x64 log-uniform, G in {2,4,7}, "
+         "+-5% lognormal XS perturbations), Poisson arrivals at 2x the one-at-a-time FP64 rate, continuous batching")
 DEFAULT = "sn_s8_64x64x32_g2"
 SOLVE_STATS = os.path.join(ROOT, "profiles", "solve_stats.json")
 
@@ -344,6 +348,141 @@ def run_ours(args, rank, world, local):
     return 0
 
 
+def run_serve(args, rank, world, local):
+    """Serving workload: a Poisson stream of diffusion requests of uneven size through the
+    pgpu_serve_* continuous-batching server (FP32 inner solves + FP64 refinement), next to
+    the plain FP64 path solving the first requests one at a time.  Every rank serves its
+    own stream (replicas); value is the total over ranks."""
+    import ctypes as C
+    import math
+    import queue
+    import threading
+
+    import numpy as np
+    import torch
+
+    import pampa_gb300 as pg
+    from pampa_gb300 import workloads as wl
+
+    dev = local
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    rng = np.random.default_rng(4 + rank)
+    nreq = args.requests
+
+    def loguni(lo, hi):
+        return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+
+    specs = [(loguni(16, 128), loguni(16, 128), loguni(4, 64), int(rng.choice([2, 4, 7]))) for _ in range(nreq)]
+    seeds = rng.integers(0, 2**31 - 1, size=nreq)
+
+    def make(k):
+        nx, ny, nz, G = specs[k]
+        return wl.diffusion_request(np.random.default_rng(int(seeds[k])), nx, ny, nz, G)[0]
+
+    fp64 = pg.default_options(precision=pg.PGPU_FP64)
+    mixed = pg.default_options(precision=pg.PGPU_MIXED)
+    # 1. plain FP64, one request at a time, on the first requests of the stream
+    sample = min(nreq, args.serve_sample)
+    ops = [make(k) for k in range(sample)]
+    k64 = []
+    with pg.Server(dev, slots=1) as srv:
+        srv.wait(srv.submit_diffusion(ops[0], fp64))  # warm-up
+        t0 = time.perf_counter()
+        for op in ops:
+            out = srv.wait(srv.submit_diffusion(op, fp64))
+            if out["status"] != pg.PGPU_OK:
+                raise RuntimeError(f"FP64 solve failed: {pg.last_error()}")
+            k64.append(out["keff"])
+        t64 = time.perf_counter() - t0
+    rate64 = sample / t64
+    del ops
+
+    # 2. the served stream: arrivals at twice that rate, mixed precision
+    arrivals = np.cumsum(rng.exponential(1.0 / (2.0 * rate64), size=nreq))
+    made = queue.Queue(maxsize=64)
+
+    def producer():
+        for k in range(nreq):
+            made.put(make(k))
+
+    results = [None] * nreq
+    ids = queue.Queue()
+    late = []
+    with pg.Server(dev, slots=args.slots) as srv:
+        srv.wait(srv.submit_diffusion(make(0), mixed))  # warm-up
+        prod = threading.Thread(target=producer, daemon=True)
+        prod.start()
+
+        def waiter():
+            while True:
+                item = ids.get()
+                if item is None:
+                    return
+                k, rid = item
+                results[k] = srv.wait(rid)
+                results[k]["t_done"] = time.perf_counter()
+
+        wt = [threading.Thread(target=waiter, daemon=True) for _ in range(4)]
+        for t in wt:
+            t.start()
+        with ClockSampler(dev) as clk:
+            t_start = time.perf_counter()
+            for k in range(nreq):
+                op = made.get()
+                delay = t_start + arrivals[k] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                else:
+                    late.append(-delay)
+                ids.put((k, srv.submit_diffusion(op, mixed)))
+            for _ in wt:
+                ids.put(None)
+            for t in wt:
+                t.join()
+            t_end = max(r["t_done"] for r in results)
+    bad = [r for r in results if r["status"] != pg.PGPU_OK]
+    if bad:
+        raise RuntimeError(f"{len(bad)} served solves failed")
+    lat = np.array([r["latency_s"] for r in results])
+    wall = t_end - t_start
+    value = nreq / wall
+    dk = max(abs(results[k]["keff"] - k64[k]) for k in range(sample))
+    launches = sum(r["stats"]["launches"] for r in results)
+    cells = np.array([a * b * c for a, b, c, _ in specs], dtype=float)
+    unknowns = np.array([a * b * c * G for a, b, c, G in specs], dtype=float)
+    if dist is not None:
+        tt = torch.tensor([value], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(tt)
+        value = float(tt.item())
+    line = dict(metric="k-eigen solves/s (served, continuous batching)", value=value, unit="solves/s",
+                n_gpus=world, steps=nreq, warmup=1, ms_per_step=1e3 * wall / nreq, higher_is_better=True,
+                scaling="weak", vs_baseline=None, dtype="f32+f64", data="synthetic (seeded request generator)",
+                config=dict(workload="serve_diffusion", description=WORKLOADS["serve_diffusion"]["desc"],
+                            requests=nreq, slots=args.slots, mean_cells=float(cells.mean()),
+                            mean_unknowns=float(unknowns.mean()), arrival_rate=2.0 * rate64,
+                            arrivals_late_s_max=float(max(late)) if late else 0.0,
+                            l2="requests are independent problems; no flush", parallelism="1 GPU"),
+                latency=dict(p50_ms=1e3 * float(np.percentile(lat, 50)), p99_ms=1e3 * float(np.percentile(lat, 99)),
+                             mean_ms=1e3 * float(lat.mean())),
+                fp64_one_at_a_time=dict(value=rate64, unit="solves/s", sample=sample,
+                                        note="plain FP64 path, one request at a time, first requests of the stream"),
+                dk_max_vs_fp64=dk,
+                e2e=dict(value=value, unit="solves/s",
+                         h2d_bytes_per_step=int(float(np.mean(unknowns * 56 + cells * 36))),
+                         d2h_bytes_per_step=8,
+                         note="the served rate is end to end: host operator arrays in, keff out"),
+                gpu_launches=int(launches), roofline=None, clocks=clk.summary())
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -353,6 +492,10 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--record", action="store_true", help="write profiles/solve_stats.json")
+    ap.add_argument("--requests", type=int, default=1024, help="serve_diffusion: requests in the stream")
+    ap.add_argument("--slots", type=int, default=8, help="serve_diffusion: solves in flight at most")
+    ap.add_argument("--serve-sample", type=int, default=32,
+                    help="serve_diffusion: requests solved one at a time in FP64 for the reference rate")
     ap.add_argument("--profile-outer", type=int, default=0,
                     help="profiling runs under ncu only: cap every solve at this many outer iterations, "
                          "skip the e2e and CPU legs; the printed line is not a benchmark result")
@@ -364,6 +507,8 @@ def main():
         return run_reference(args, rank, world)
     import pampa_gb300.build as b
     b.build()
+    if WORKLOADS[args.workload]["kind"] == "serve":
+        return run_serve(args, rank, world, local)
     return run_ours(args, rank, world, local)
 
 

@@ -247,6 +247,34 @@ int pgpu_normalize_power_noalloc(int num_cells, int num_groups, const int* mater
                                  double power, double keff, double* phi_out, double* q, double* P,
                                  double* total_power, int* negatives, void* stream);
 
+/* ------------------------------------------------------------------------------
+ * 4. Serving: continuous batching of independent k-eigenvalue solves on one GPU
+ *    (new entry points beside the single-solve Solver path; the reference has no
+ *    equivalent).  Requests are copied at submission and admitted first-in first-out
+ *    as soon as one of `slots` workers is free and the request's device footprint fits
+ *    in hbm_fraction of the device memory that was free at creation; each admitted
+ *    request is uploaded, solved on its own stream and freed, so solves of different
+ *    sizes overlap on the device.  A request larger than the whole budget is rejected
+ *    with PGPU_ERR_NO_MEMORY.  Results do not depend on the other requests in flight.
+ *    Submission, polling and waiting may come from any host thread.
+ * ---------------------------------------------------------------------------- */
+typedef struct pgpu_server pgpu_server;
+
+int pgpu_serve_create(int device, int slots, double hbm_fraction, pgpu_server** out);
+long long pgpu_serve_budget_bytes(pgpu_server* s);
+int pgpu_serve_submit_diffusion(pgpu_server* s, const pgpu_diffusion_operator* op, const pgpu_options* opt,
+                                int want_flux, long long* id);
+int pgpu_serve_submit_sn(pgpu_server* s, const pgpu_sn_operator* op, const pgpu_options* opt, int want_flux,
+                         long long* id);
+/* *done = 1 once the request's solve has finished (successfully or not). */
+int pgpu_serve_poll(pgpu_server* s, long long id, int* done);
+/* Blocks until the request is done and releases it; returns its solve status.  Outputs
+ * may be NULL: stats, keff, phi (num_cells*G, only when submitted with want_flux) and
+ * times[3] = {queueing, upload + solve + read-back, total latency} in seconds. */
+int pgpu_serve_wait(pgpu_server* s, long long id, pgpu_stats* stats, double* keff, double* phi, double* times);
+/* Finishes every submitted request, then stops the workers and frees the server. */
+int pgpu_serve_destroy(pgpu_server* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -102,6 +102,15 @@ SYMBOLS = {
     "pgpu_problem_destroy": (None, [C.c_void_p]),
     "pgpu_normalize_power_noalloc": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 5 + [C.c_double, C.c_double]
                                      + [C.c_void_p] * 6),
+    "pgpu_serve_create": (C.c_int, [C.c_int, C.c_int, C.c_double, _P(C.c_void_p)]),
+    "pgpu_serve_budget_bytes": (C.c_longlong, [C.c_void_p]),
+    "pgpu_serve_submit_diffusion": (C.c_int, [C.c_void_p, _P(pgpu_diffusion_operator), _P(pgpu_options), C.c_int,
+                                              _P(C.c_longlong)]),
+    "pgpu_serve_submit_sn": (C.c_int, [C.c_void_p, _P(pgpu_sn_operator), _P(pgpu_options), C.c_int,
+                                       _P(C.c_longlong)]),
+    "pgpu_serve_poll": (C.c_int, [C.c_void_p, C.c_longlong, _pi]),
+    "pgpu_serve_wait": (C.c_int, [C.c_void_p, C.c_longlong, _P(pgpu_stats), _pd, _pd, _pd]),
+    "pgpu_serve_destroy": (C.c_int, [C.c_void_p]),
 }
 
 
@@ -380,3 +389,73 @@ class SNProblem(_Problem):
         out = np.zeros(self.num_cells * self.num_groups * self.num_dirs)
         self._check(lib().pgpu_problem_get_angular_flux(self._h, _dp(out)), "get_angular_flux")
         return out
+
+
+def diffusion_operator_struct(*, neighbors, offdiag, diag, materials, volumes, sigma_s, chi, nu_sigma_f,
+                              kappa_sigma_f):
+    """(pgpu_diffusion_operator, arrays to keep alive) from numpy arrays."""
+    nbr = _i32(neighbors)
+    F, n = nbr.shape
+    G = np.asarray(diag).size // n
+    nm = np.asarray(chi).size // G
+    arrs = dict(neighbors=nbr, offdiag=_f64(offdiag), diag=_f64(diag), materials=_i32(materials),
+                volumes=_f64(volumes), sigma_s=_f64(sigma_s), chi=_f64(chi),
+                nu_sigma_f=_f64(nu_sigma_f), kappa_sigma_f=_f64(kappa_sigma_f))
+    op = pgpu_diffusion_operator(n, G, F, nm)
+    for k, a in arrs.items():
+        setattr(op, k, _ip(a) if a.dtype == np.int32 else _dp(a))
+    return op, list(arrs.values())
+
+
+class Server:
+    """Continuous-batching solve server (pgpu_serve_*): submit operators, wait for results."""
+
+    def __init__(self, device: int = 0, slots: int = 8, hbm_fraction: float = 0.8):
+        self._h = C.c_void_p(None)
+        st = lib().pgpu_serve_create(device, slots, hbm_fraction, C.byref(self._h))
+        if st != PGPU_OK:
+            raise PampaError(f"pgpu_serve_create failed ({st}): {last_error()}")
+        self._sizes = {}
+
+    @property
+    def budget_bytes(self) -> int:
+        return int(lib().pgpu_serve_budget_bytes(self._h))
+
+    def submit_diffusion(self, op: dict, options: pgpu_options | None = None, want_flux: bool = False) -> int:
+        o, _keep = diffusion_operator_struct(**op)
+        rid = C.c_longlong(0)
+        st = lib().pgpu_serve_submit_diffusion(self._h, C.byref(o), C.byref(options) if options else None,
+                                               int(want_flux), C.byref(rid))
+        if st != PGPU_OK:
+            raise PampaError(f"pgpu_serve_submit_diffusion failed ({st})")
+        self._sizes[rid.value] = o.num_cells * o.num_groups if want_flux else 0
+        return rid.value
+
+    def done(self, rid: int) -> bool:
+        d = C.c_int(0)
+        if lib().pgpu_serve_poll(self._h, rid, C.byref(d)) != PGPU_OK:
+            raise PampaError(f"unknown request {rid}")
+        return bool(d.value)
+
+    def wait(self, rid: int) -> dict:
+        """Result of a request: status, keff, stats, phi (when asked for) and times."""
+        stats = pgpu_stats()
+        k = C.c_double(0.0)
+        times = np.zeros(3)
+        nphi = self._sizes.pop(rid, 0)
+        phi = np.zeros(nphi) if nphi else None
+        st = lib().pgpu_serve_wait(self._h, rid, C.byref(stats), C.byref(k), _dp(phi) if phi is not None else None,
+                                   _dp(times))
+        return dict(status=st, keff=k.value, phi=phi, queue_s=times[0], run_s=times[1], latency_s=times[2],
+                    stats={f: getattr(stats, f) for f, _ in pgpu_stats._fields_})
+
+    def close(self):
+        if self._h:
+            lib().pgpu_serve_destroy(self._h)
+            self._h = C.c_void_p(None)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -108,14 +108,16 @@ __device__ __forceinline__ void precond_cell(const DiffOp<T>& A, int i, const T*
 }
 
 // ---------------------------------------------------------------------------------
-// BiCGStab kernels (right preconditioned), T = double or float.
+// BiCGStab kernels (right preconditioned), T = double or float.  Element arithmetic and
+// each thread's partial sums are in T (FP32 accumulation for the mixed-precision inner
+// solve, as GB300's FP64 rate is 1/64 of FP32); block and grid sums are FP64.
 // ---------------------------------------------------------------------------------
 
 // rhat = r = rin; x = p = v = 0; rho = rr = bb = (r, r).
 template <typename T>
 __global__ void k_bicg_init(int N, const T* __restrict__ rin, T* r, T* rhat, T* x, T* p, T* v,
                             BiScal* sc, ReduceSlots<1> slots, double rtol, int max_iters) {
-  double acc[1] = {0.0};
+  T part = T(0);
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
     T val = rin[l];
     r[l] = val;
@@ -123,8 +125,9 @@ __global__ void k_bicg_init(int N, const T* __restrict__ rin, T* r, T* rhat, T* 
     x[l] = T(0);
     p[l] = T(0);
     v[l] = T(0);
-    acc[0] += (double)val * (double)val;
+    part += val * val;
   }
+  double acc[1] = {(double)part};
   double tot[1];
   if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
     sc->rho = tot[0];
@@ -169,13 +172,14 @@ __global__ void k_bicg_v(DiffOp<T> A, const T* __restrict__ phat, T* v, const T*
                          BiScal* sc, ReduceSlots<1> slots) {
   if (sc->converged) return;
   const int N = A.n * A.G;
-  double acc[1] = {0.0};
+  T part = T(0);
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
     const int i = l / A.G, g = l - i * A.G;
     T val = apply_row(A, phat, i, g);
     v[l] = val;
-    acc[0] += (double)rhat[l] * (double)val;
+    part += rhat[l] * val;
   }
+  double acc[1] = {(double)part};
   double tot[1];
   if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
     if (tot[0] == 0.0 || !(tot[0] == tot[0])) {
@@ -213,14 +217,15 @@ __global__ void k_bicg_t(DiffOp<T> A, const T* __restrict__ shat, T* t, const T*
                          BiScal* sc, ReduceSlots<2> slots) {
   if (sc->converged) return;
   const int N = A.n * A.G;
-  double acc[2] = {0.0, 0.0};
+  T p0 = T(0), p1 = T(0);
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
     const int i = l / A.G, g = l - i * A.G;
     T val = apply_row(A, shat, i, g);
     t[l] = val;
-    acc[0] += (double)val * (double)s[l];
-    acc[1] += (double)val * (double)val;
+    p0 += val * s[l];
+    p1 += val * val;
   }
+  double acc[2] = {(double)p0, (double)p1};
   double tot[2];
   if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
     if (tot[1] == 0.0 || !(tot[1] == tot[1])) {
@@ -239,14 +244,15 @@ __global__ void k_bicg_x(int N, T* x, T* r, const T* __restrict__ phat, const T*
                          BiScal* sc, ReduceSlots<2> slots) {
   if (sc->converged) return;
   const T ta = (T)sc->alpha, tw = (T)sc->omega;
-  double acc[2] = {0.0, 0.0};
+  T p0 = T(0), p1 = T(0);
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
     x[l] += ta * phat[l] + tw * shat[l];
     T rv = s[l] - tw * t[l];
     r[l] = rv;
-    acc[0] += (double)rhat[l] * (double)rv;
-    acc[1] += (double)rv * (double)rv;
+    p0 += rhat[l] * rv;
+    p1 += rv * rv;
   }
+  double acc[2] = {(double)p0, (double)p1};
   double tot[2];
   if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
     sc->rho_old = sc->rho;

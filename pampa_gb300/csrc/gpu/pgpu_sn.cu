@@ -779,14 +779,15 @@ __global__ void k_apply_R(SNOp<T> A, const T* __restrict__ psi, const T* __restr
 template <typename T>
 __global__ void k_sub_many(long long N, const T* __restrict__ V, long long ld, int nv, const double* __restrict__ h, T* x) {
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
-    double s = (double)x[l];
-    for (int k = 0; k < nv; k++) s -= h[k] * (double)V[(size_t)k * ld + l];
-    x[l] = (T)s;
+    T s = x[l];
+    for (int k = 0; k < nv; k++) s -= (T)h[k] * V[(size_t)k * ld + l];
+    x[l] = s;
   }
 }
 
 // Gram-Schmidt passes of the GMRES Arnoldi step over nv <= kGsMax basis vectors V_k
-// (stride ld).  Products: each block row (blockIdx.y) takes kGsChunk vectors, so w is
+// (stride ld).  Element arithmetic is in the vectors' precision (FP32 for the mixed-
+// precision correction solve: GB300's FP64 rate is 1/64 of FP32), reductions in FP64.  Products: each block row (blockIdx.y) takes kGsChunk vectors, so w is
 // read once per chunk instead of once per vector, with few registers per thread.
 constexpr int kGsMax = 32;
 constexpr int kGsChunk = 8;
@@ -797,15 +798,19 @@ __global__ void k_gs_dot(long long N, const T* __restrict__ V, long long ld, int
                          double* out, double* partials, unsigned int* tickets) {
   const int k0 = blockIdx.y * kGsChunk;
   const int nk = min(kGsChunk, nv - k0);
-  double acc[kGsChunk];
+  // per-thread sums in precision T (a few elements each), block and grid sums in FP64
+  T part[kGsChunk];
 #pragma unroll
-  for (int k = 0; k < kGsChunk; k++) acc[k] = 0.0;
+  for (int k = 0; k < kGsChunk; k++) part[k] = T(0);
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
-    const double x = (double)w[l];
+    const T x = w[l];
 #pragma unroll
     for (int k = 0; k < kGsChunk; k++)
-      if (k < nk) acc[k] += (double)V[(size_t)(k0 + k) * ld + l] * x;
+      if (k < nk) part[k] += V[(size_t)(k0 + k) * ld + l] * x;
   }
+  double acc[kGsChunk];
+#pragma unroll
+  for (int k = 0; k < kGsChunk; k++) acc[k] = (double)part[k];
   ReduceSlots<kGsChunk> slots{partials + (size_t)blockIdx.y * kGsChunk * kMaxBlocks, tickets + blockIdx.y};
   double tot[kGsChunk];
   if (block_reduce_last<kGsChunk>(acc, slots, tot) && threadIdx.x == 0)
@@ -817,14 +822,14 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) k_gs_sub_norm(long long N, const T* __restrict__ V, long long ld, int nv,
                                                          const double* __restrict__ h, T* w, double* out,
                                                          ReduceSlots<1> slots) {
-  double acc[1] = {0.0};
+  T part = T(0);
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
-    double s = (double)w[l];
-    for (int k = 0; k < nv; k++) s -= h[k] * (double)V[(size_t)k * ld + l];
-    const T sw = (T)s;
-    w[l] = sw;
-    acc[0] += (double)sw * (double)sw;
+    T s = w[l];
+    for (int k = 0; k < nv; k++) s -= (T)h[k] * V[(size_t)k * ld + l];
+    w[l] = s;
+    part += s * s;
   }
+  double acc[1] = {(double)part};
   double tot[1];
   if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) *out = sqrt(tot[0]);
 }
@@ -833,17 +838,17 @@ __global__ void __launch_bounds__(kThreads) k_gs_sub_norm(long long N, const T* 
 template <typename T>
 __global__ void k_add_many(long long N, const T* __restrict__ V, long long ld, int nv, const double* __restrict__ y, T* x) {
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
-    double s = (double)x[l];
-    for (int k = 0; k < nv; k++) s += y[k] * (double)V[(size_t)k * ld + l];
-    x[l] = (T)s;
+    T s = x[l];
+    for (int k = 0; k < nv; k++) s += (T)y[k] * V[(size_t)k * ld + l];
+    x[l] = s;
   }
 }
 
 template <typename T>
 __global__ void k_scale_to(long long N, const T* __restrict__ a, const double* __restrict__ s, int inv, T* b) {
-  const double f = inv ? 1.0 / *s : *s;
+  const T f = (T)(inv ? 1.0 / *s : *s);
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
-    b[l] = (T)((double)a[l] * f);
+    b[l] = a[l] * f;
 }
 
 // c = a - b

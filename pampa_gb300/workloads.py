@@ -265,3 +265,103 @@ def sn_hex(out_dir: str, nq: int = 200, nr: int = 200, nz: int = 40, pitch: floa
     with open(path, "w") as fh:
         fh.write("\n".join(lines) + "\n")
     return path
+
+
+# --------------------------------------------------------------------------------------
+# Operators built in memory (no .pmp round trip): for request streams whose sizes make
+# file parsing the bottleneck.  Same formulas as the reference's DiffusionSolver::
+# buildMatrices (DiffusionSolver.cxx:88-320) on a uniform Cartesian mesh, with the
+# material values rounded as the .pmp writers above round them, so that the arrays equal
+# the ones the drop-in host assembles from the same problem written to files.
+# --------------------------------------------------------------------------------------
+
+KAPPA_OVER_NU = 3.2e-11 / 2.4355  # default kappa-sigma-fission / nu-sigma-fission
+
+
+def _rt(v: float) -> float:
+    return float(f"{v:.10g}")
+
+
+def material_arrays(mats: list[dict]) -> dict:
+    """Per-material tables as the solver reads them from the written material files."""
+    G = mats[0]["G"]
+    D = np.array([[_rt(v) for v in m["D"]] for m in mats])
+    ss = np.array([[[_rt(v) for v in row] for row in np.asarray(m["ss"], dtype=float)] for m in mats])
+    st = np.array([[_rt(m["sa"][g] + np.asarray(m["ss"], dtype=float)[g].sum()) for g in range(G)] for m in mats])
+    fiss = np.array([any(v > 0 for v in m["nsf"]) for m in mats])
+    nsf = np.array([[_rt(v) for v in m["nsf"]] if f else [0.0] * G for m, f in zip(mats, fiss)])
+    chi = np.array([[_rt(v) for v in m["chi"]] if f else [0.0] * G for m, f in zip(mats, fiss)])
+    return dict(G=G, D=D, sigma_s=ss, sigma_t=st, nu_sigma_f=nsf, chi=chi, kappa_sigma_f=nsf * KAPPA_OVER_NU)
+
+
+def cartesian_diffusion_operator(nx: int, ny: int, nz: int, h: float, layout: np.ndarray, mats: list[dict],
+                                 reflective=("-x", "-y", "-z")) -> dict:
+    """pgpu_diffusion_operator arrays of a uniform 3D Cartesian mesh (cells of side h,
+    layout (nz, ny, nx) of 1-based material indices, faces -y +x +y -x -z +z, vacuum on
+    every side not listed in `reflective`)."""
+    t = material_arrays(mats)
+    G = t["G"]
+    n = nx * ny * nz
+    mat = np.ascontiguousarray(layout, dtype=np.int64).reshape(-1) - 1
+    V, A = h * h * h, h * h
+    x = np.arange(n) % nx
+    y = (np.arange(n) // nx) % ny
+    z = np.arange(n) // (nx * ny)
+    Dc = t["D"][mat]  # (n, G)
+    self_ss = t["sigma_s"][:, np.arange(G), np.arange(G)]  # (materials, G)
+    diag = t["sigma_t"][mat] * V - self_ss[mat] * V
+    faces = [("-y", y > 0, -nx), ("+x", x < nx - 1, 1), ("+y", y < ny - 1, nx), ("-x", x > 0, -1),
+             ("-z", z > 0, -nx * ny), ("+z", z < nz - 1, nx * ny)]
+    nbr = np.full((6, n), -1, dtype=np.int32)
+    off = np.zeros((6, n, G))
+    for f, (side, inside, step) in enumerate(faces):
+        cells = np.nonzero(inside)[0]
+        nb = cells + step
+        nbr[f, cells] = nb
+        same = mat[nb] == mat[cells]
+        Di, Dn = Dc[cells], Dc[nb]
+        r = np.where(same[:, None], -(1.0 / h) * Di * A, 0.0)
+        w1 = (2.0 / h) * (Di * A)
+        w2 = (2.0 / h) * (Dn * A)
+        r = np.where(same[:, None], r, -(w1 * w2) / (w1 + w2))
+        off[f, cells] = r
+        diag[cells] -= r
+        bnd = np.nonzero(~inside)[0]
+        if side not in reflective:
+            diag[bnd] += (2.0 / h) * Dc[bnd] * A
+    return dict(neighbors=nbr, offdiag=off.reshape(6, n * G), diag=diag.reshape(-1),
+                materials=mat.astype(np.int32), volumes=np.full(n, V), sigma_s=t["sigma_s"], chi=t["chi"],
+                nu_sigma_f=t["nu_sigma_f"], kappa_sigma_f=t["kappa_sigma_f"])
+
+
+def diffusion_request(rng, nx: int, ny: int, nz: int, G: int, h: float = 2.0, perturb: float = math.log(1.05),
+                      block: int = 4, nmat: int = 4) -> tuple[dict, list[dict], np.ndarray]:
+    """One serving request: random block layout of `nmat` materials (2-group ranges for
+    G = 2, the multigroup family otherwise) with an independent lognormal perturbation
+    (sigma_ln = perturb) of every cross section.  Returns (operator, materials, layout)."""
+    mats = materials_2g(rng, nmat) if G == 2 else materials_multigroup(rng, nmat, G)
+    for m in mats:
+        for key in ("D", "sa", "nsf"):
+            m[key] = [float(v * math.exp(rng.normal(0.0, perturb))) for v in m[key]]
+        ss = np.asarray(m["ss"], dtype=float)
+        m["ss"] = ss * np.exp(rng.normal(0.0, perturb, size=ss.shape))
+    layout = _block_layout(rng, (nz, ny, nx), (block, block, block), nmat)
+    return cartesian_diffusion_operator(nx, ny, nz, h, layout, mats), mats, layout
+
+
+def write_diffusion_input(out_dir: str, nx: int, ny: int, nz: int, h: float, layout: np.ndarray,
+                          mats: list[dict]) -> str:
+    """The .pmp input of a problem built by cartesian_diffusion_operator (same boundaries)."""
+    os.makedirs(out_dir, exist_ok=True)
+    write_cartesian_mesh(os.path.join(out_dir, "mesh.pmp"), h, nx, ny, nz, layout,
+                         {"-x": "reflective", "+x": "vacuum", "-y": "reflective", "+y": "vacuum",
+                          "-z": "reflective", "+z": "vacuum"})
+    for k, m in enumerate(mats):
+        write_material(os.path.join(out_dir, f"mat{k + 1}.pmp"), m)
+    lines = ["mesh cartesian mesh.pmp", ""]
+    lines += [f"material mat{k + 1} mat{k + 1}.pmp" for k in range(len(mats))]
+    lines += ["", "solver diffusion {", f"   energy-groups {mats[0]['G']}", "}"]
+    path = os.path.join(out_dir, "input.pmp")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return path
