@@ -62,7 +62,22 @@ struct SNOp {
   const T* __restrict__ ss;          // [nm][G][G]
   const T* __restrict__ chi;         // [nm][G]
   const T* __restrict__ nsf;         // [nm][G]
+  // incoming directions of the reflective slots: a slot's list (one per distinct normal
+  // among reflective faces) holds the directions with mu <= 0; the reflective inflow
+  // bnd[s][g][k] is stored for those only (k < Mh, zero padded)
+  const int* __restrict__ rkind;     // [nrefl] list of slot s
+  const int* __restrict__ kmap;      // [nlists][M] position of direction m in a list, -1 if outgoing
+  const int* __restrict__ klist;     // [nlists][Mh] directions of a list, -1 padding
+  int Mh;
 };
+
+// Reflective inflow of slot s, group g, direction m (zero for a direction the slot's list
+// does not hold: mu > 0 there, so it is never inflow).
+template <typename T>
+__device__ __forceinline__ T bnd_val(const SNOp<T>& A, const T* __restrict__ bnd, int s, int g, int m) {
+  const int k = A.kmap[A.rkind[s] * A.M + m];
+  return k >= 0 ? bnd[((size_t)s * A.G + g) * A.Mh + k] : T(0);
+}
 
 struct Schedule {
   int npat = 0, nlev = 0;
@@ -83,6 +98,8 @@ struct SNData {
   int use_ls = 0;
   bool upwind = true;       // delta == 1 (no downwind or inflow-side diagonal terms)
   int nrefl = 0;            // reflective face slots
+  int Mh = 0;               // incoming directions stored per reflective slot (SNOp)
+  DevBuf d_rkind, d_kmap, d_klist;
   Schedule sched;
   // operator (FP64 and FP32 copies of the real-valued arrays)
   DevBuf nf, kind, nbr, raxis, rslot, mat, refl;
@@ -163,7 +180,7 @@ __device__ __forceinline__ T mu_of(const SNOp<T>& A, int f, int i, int m) {
 // One level of the sweep for every pattern (blockIdx.y).  Solves each (cell, g, m) row of
 // the upwind part of R: psi = (src - upwind face terms - reflective inflow) / diagonal.
 // src is isotropic ([n*G]) when iso != 0, else angular ([n*G*M]).  bnd holds incoming
-// angular flux at reflective faces ([nrefl][G][M]) or is null (treated as zero).
+// angular flux at reflective faces ([nrefl][G][Mh], see SNOp) or is null (treated as zero).
 // Per-face sweep weights, precomputed at setup so a face costs one or two FP64 operations
 // (GB300's FP64 rate is 1/64 of FP32, and the sweep is FP64-bound):
 //   outflow (mu > 0):  den += mu * wout   (interior: Gauss weight c0 * A; vacuum: A, minus the
@@ -265,7 +282,7 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
         if (kd == PGPU_FACE_INTERIOR) {
           num -= (mu * W.win[o]) * psi[((size_t)A.nbr[o] * G + g) * M + m];
         } else if (kd == PGPU_FACE_REFLECTIVE && bnd) {
-          num -= (mu * W.win[o]) * bnd[((size_t)A.rslot[o] * G + g) * M + m];
+          num -= (mu * W.win[o]) * bnd_val(A, bnd, A.rslot[o], g, m);
         }
       }
       psi[l] = num * W.rden[l];
@@ -283,7 +300,7 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
         if (kd == PGPU_FACE_INTERIOR) {
           num -= (mu * W.win[o]) * psi[((size_t)A.nbr[o] * G + g) * M + m];
         } else if (kd == PGPU_FACE_REFLECTIVE && bnd) {
-          num -= (mu * W.win[o]) * bnd[((size_t)A.rslot[o] * G + g) * M + m];
+          num -= (mu * W.win[o]) * bnd_val(A, bnd, A.rslot[o], g, m);
         }
       }
     }
@@ -530,7 +547,7 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
         if (bnd) {
           const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
           const size_t o = (size_t)f * n + (tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz));
-          if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd[((size_t)A.rslot[o] * G + g) * M + m];
+          if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd_val(A, bnd, A.rslot[o], g, m);
         }
         tin[fs * S + slot] = val;
       }
@@ -701,23 +718,24 @@ __global__ void k_broadcast(int rows, int M, const T* __restrict__ qi, T* qa) {
 }
 
 // Incoming angular flux at reflective faces from the current psi: for slot s (cell i,
-// face f, axis a) and direction m with mu < 0, bnd[s,g,m] = psi[i,g,refl(m,a)].
+// face f, axis a) and its k-th incoming direction m, bnd[s,g,k] = psi[i,g,refl(m,a)].
 template <typename T>
 __global__ void k_reflect_extract(SNOp<T> A, int nrefl, const int* __restrict__ slot_cell,
                                   const int* __restrict__ slot_face, const T* __restrict__ psi, T* bnd) {
-  const int G = A.G, M = A.M;
-  const long long total = (long long)nrefl * G * M;
+  const int G = A.G, M = A.M, Mh = A.Mh;
+  const long long total = (long long)nrefl * G * Mh;
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < total;
        l += (long long)gridDim.x * blockDim.x) {
-    const int m = (int)(l % M);
-    const long long rest = l / M;
+    const int k = (int)(l % Mh);
+    const long long rest = l / Mh;
     const int g = (int)(rest % G);
     const int s = (int)(rest / G);
-    const int i = slot_cell[s], f = slot_face[s];
-    const size_t o = (size_t)f * A.n + i;
-    const T mu = mu_of(A, f, i, m);
+    const int m = A.klist[A.rkind[s] * Mh + k];
     T v = T(0);
-    if (!(mu > T(0))) v = psi[((size_t)i * G + g) * M + A.refl[m * 3 + A.raxis[o]]];
+    if (m >= 0) {
+      const int i = slot_cell[s], f = slot_face[s];
+      v = psi[((size_t)i * G + g) * M + A.refl[m * 3 + A.raxis[(size_t)f * A.n + i]]];
+    }
     bnd[l] = v;
   }
 }
@@ -1142,7 +1160,8 @@ SNOp<double> make_op<double>(const SNData& d) {
                       d.area.as<double>(), d.nrm.as<double>(), d.gauss.as<double>(), d.raxis.as<int>(),
                       d.rslot.as<int>(), d.lsw.as<double>(), d.lsdiag.as<double>(), d.mat.as<int>(),
                       d.vol.as<double>(), d.dirs.as<double>(), d.w.as<double>(), d.refl.as<int>(),
-                      d.st.as<double>(), d.ss.as<double>(), d.chi.as<double>(), d.nsf.as<double>()};
+                      d.st.as<double>(), d.ss.as<double>(), d.chi.as<double>(), d.nsf.as<double>(),
+                      d.d_rkind.as<int>(), d.d_kmap.as<int>(), d.d_klist.as<int>(), d.Mh};
 }
 
 template <>
@@ -1151,7 +1170,8 @@ SNOp<float> make_op<float>(const SNData& d) {
                      d.area32.as<float>(), d.nrm32.as<float>(), d.gauss32.as<float>(), d.raxis.as<int>(),
                      d.rslot.as<int>(), d.lsw32.as<float>(), d.lsdiag32.as<float>(), d.mat.as<int>(),
                      d.vol32.as<float>(), d.dirs32.as<float>(), d.w32.as<float>(), d.refl.as<int>(),
-                     d.st32.as<float>(), d.ss32.as<float>(), d.chi32.as<float>(), d.nsf32.as<float>()};
+                     d.st32.as<float>(), d.ss32.as<float>(), d.chi32.as<float>(), d.nsf32.as<float>(),
+                     d.d_rkind.as<int>(), d.d_kmap.as<int>(), d.d_klist.as<int>(), d.Mh};
 }
 
 template <int NV>
@@ -1375,7 +1395,7 @@ int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y,
     launch(p, k_moment<T>, grid_for((long long)nG * 32), kThreads, p->stream, nG, d.M, A.w, psi, y);
   }
   if (d.nrefl) {
-    const long long nb = (long long)d.nrefl * d.G * d.M;
+    const long long nb = (long long)d.nrefl * d.G * d.Mh;
     launch(p, k_reflect_extract<T>, grid_for(nb), kThreads, p->stream, A, d.nrefl, d.d_slot_cell.as<int>(),
                                                                    d.d_slot_face.as<int>(), psi, y + nG);
   }
@@ -1571,7 +1591,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   const int n = d.n, G = d.G, M = d.M, nG = n * G;
   const long long N = (long long)nG * M;
   const bool phi_space = d.upwind && !d.use_ls;
-  const long long len = phi_space ? (long long)nG + (long long)d.nrefl * G * M : N;
+  const long long len = phi_space ? (long long)nG + (long long)d.nrefl * G * d.Mh : N;
   const int restart = 30;
   int st;
   if ((st = ensure_krylov(p, (size_t)len, restart, (int)sizeof(T)))) return st;
@@ -2138,6 +2158,38 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
   if (d.nrefl) {
     up(d.d_slot_cell, slot_cell.data(), slot_cell.size() * 4);
     up(d.d_slot_face, slot_face.data(), slot_face.size() * 4);
+  }
+  {
+    // incoming-direction lists of the reflective slots, one per distinct face normal
+    // (all directions when mu comes from the normals rather than the table)
+    std::map<int, int> list_of;
+    std::vector<int> rkind(std::max<size_t>(1, slot_cell.size()), 0);
+    std::vector<std::vector<int>> lists;
+    for (size_t s = 0; s < slot_cell.size(); s++) {
+      const int c = use_tab ? cls[(size_t)slot_face[s] * n + slot_cell[s]] : -1;
+      auto it = list_of.find(c);
+      if (it == list_of.end()) {
+        std::vector<int> lst;
+        for (int m = 0; m < M; m++)
+          if (c < 0 || !(mutab[(size_t)c * M + m] > 0.0)) lst.push_back(m);
+        it = list_of.emplace(c, (int)lists.size()).first;
+        lists.push_back(lst);
+      }
+      rkind[s] = it->second;
+    }
+    if (lists.empty()) lists.push_back({});
+    int Mh = 1;
+    for (auto& l : lists) Mh = std::max<int>(Mh, (int)l.size());
+    std::vector<int> kmap(lists.size() * M, -1), klist(lists.size() * Mh, -1);
+    for (size_t r = 0; r < lists.size(); r++)
+      for (size_t k = 0; k < lists[r].size(); k++) {
+        kmap[r * M + lists[r][k]] = (int)k;
+        klist[r * Mh + k] = lists[r][k];
+      }
+    d.Mh = Mh;
+    up(d.d_rkind, rkind.data(), rkind.size() * 4);
+    up(d.d_kmap, kmap.data(), kmap.size() * 4);
+    up(d.d_klist, klist.data(), klist.size() * 4);
   }
   const size_t nG = (size_t)n * G;
   al(d.psi, nG * M * 8);
