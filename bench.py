@@ -465,6 +465,8 @@ def run_serve(args, rank, world, local):
                             requests=nreq, slots=args.slots, mean_cells=float(cells.mean()),
                             mean_unknowns=float(unknowns.mean()), arrival_rate=2.0 * rate64,
                             arrivals_late_s_max=float(max(late)) if late else 0.0,
+                            mean_outer_iterations=float(np.mean([r["stats"]["outer_iterations"] for r in results])),
+                            mean_inner_iterations=float(np.mean([r["stats"]["inner_iterations"] for r in results])),
                             l2="requests are independent problems; no flush", parallelism="1 GPU"),
                 latency=dict(p50_ms=1e3 * float(np.percentile(lat, 50)), p99_ms=1e3 * float(np.percentile(lat, 99)),
                              mean_ms=1e3 * float(lat.mean())),

@@ -34,7 +34,7 @@ struct DiffOp {
   const T* __restrict__ ss;     // [nm][G][G]
   const T* __restrict__ chi;    // [nm][G]
   const T* __restrict__ nsf;    // [nm][G]
-  T lam_s;                      // Wielandt shift: the operator is R - lam_s F
+  const double* __restrict__ lam_s;  // device scalar, Wielandt shift: the operator is R - lam_s F
 };
 
 // Device-resident BiCGStab state; every scalar of the iteration stays on the GPU.
@@ -59,7 +59,15 @@ struct DiffusionData {
   DevBuf w64[9];  // BiCGStab vectors for FP64
   DevBuf w32[9];  // BiCGStab vectors for FP32
   DevBuf partials, ticket, bscal, oscal;
+  DevBuf lam;  // [2]: the Wielandt shift of the running solve, and a constant 0
   bool have32 = false;
+  // BiCGStab iterations captured in CUDA graphs, [fp32][chunk 4, 8, 16]
+  cudaGraphExec_t bicg_graph[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  ~DiffusionData() {
+    for (auto& row : bicg_graph)
+      for (auto& g : row)
+        if (g) cudaGraphExecDestroy(g);
+  }
 };
 
 // ---------------------------------------------------------------------------------
@@ -77,11 +85,12 @@ __device__ __forceinline__ T apply_row(const DiffOp<T>& A, const T* __restrict__
   T sc = T(0);
   for (int g2 = 0; g2 < G; g2++)
     if (g2 != g) sc += ssm[g2 * G + g] * x[(size_t)i * G + g2];
-  if (A.lam_s != T(0)) {
+  const T ls = (T)*A.lam_s;
+  if (ls != T(0)) {
     const T* ns = A.nsf + (size_t)m * G;
     T f = T(0);
     for (int g2 = 0; g2 < G; g2++) f += ns[g2] * x[(size_t)i * G + g2];
-    sc += A.lam_s * A.chi[(size_t)m * G + g] * f;
+    sc += ls * A.chi[(size_t)m * G + g] * f;
   }
   acc -= A.vol[i] * sc;
   const size_t nG = (size_t)A.n * G;
@@ -424,17 +433,20 @@ __global__ void k_convert(long long N, const S* __restrict__ a, D* b) {
 
 namespace {
 
-DiffOp<double> op64(const DiffusionData& d, double lam_s = 0.0) {
+// Operators of the solve (shifted: R - lam_s F with lam_s read from d.lam[0]) or plain R.
+DiffOp<double> op64(const DiffusionData& d, bool shifted = false) {
   return DiffOp<double>{d.n, d.G, d.F, d.nbr.as<int>(), d.off64.as<double>(), d.diag64.as<double>(),
                         d.mat.as<int>(), d.vol64.as<double>(), d.ss64.as<double>(), d.chi.as<double>(),
-                        d.nsf.as<double>(), lam_s};
+                        d.nsf.as<double>(), d.lam.as<double>() + (shifted ? 0 : 1)};
 }
 
-DiffOp<float> op32(const DiffusionData& d, double lam_s = 0.0) {
+DiffOp<float> op32(const DiffusionData& d, bool shifted = false) {
   return DiffOp<float>{d.n, d.G, d.F, d.nbr.as<int>(), d.off32.as<float>(), d.diag32.as<float>(),
                        d.mat.as<int>(), d.vol32.as<float>(), d.ss32.as<float>(), d.chi32.as<float>(),
-                       d.nsf32.as<float>(), (float)lam_s};
+                       d.nsf32.as<float>(), d.lam.as<double>() + (shifted ? 0 : 1)};
 }
+
+__global__ void k_set_scalar(double* p, double v) { *p = v; }
 
 template <int NV>
 ReduceSlots<NV> slots_of(DiffusionData& d) {
@@ -491,19 +503,42 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   // neighbour indices, the material id and the volume.
   const double sv = (double)sizeof(T);
   const double spmv_bytes = (double)N * (d.F + 4) * sv + (double)d.n * (4.0 * d.F + 4.0 + sv);
+  // one BiCGStab iteration: five kernels (every scalar stays on the device; after
+  // convergence the kernels return at once)
+  auto iteration = [&](bool timed) {
+    cudaEvent_t e0;
+    k_bicg_p<T><<<gC, kThreads, 0, st>>>(A, r, pp, v, phat, sc);
+    if (timed) prof_begin(p, &e0);
+    k_bicg_v<T><<<gN, kThreads, 0, st>>>(A, phat, v, rhat, sc, slots_of<1>(d));
+    if (timed) prof_end(p, e0, 1, 0.0);
+    k_bicg_s<T><<<gC, kThreads, 0, st>>>(A, r, v, s, shat, sc);
+    if (timed) prof_begin(p, &e0);
+    k_bicg_t<T><<<gN, kThreads, 0, st>>>(A, shat, t, s, sc, slots_of<2>(d));
+    if (timed) prof_end(p, e0, 1, 0.0);
+    k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phat, shat, s, t, rhat, sc, slots_of<2>(d));
+  };
   for (int launched = 0; launched < max_iters; launched += chunk) {
-    for (int c = 0; c < chunk; c++) {
-      cudaEvent_t e0;
-      launch(p, k_bicg_p<T>, gC, kThreads, st, A, r, pp, v, phat, sc);
-      prof_begin(p, &e0);
-      launch(p, k_bicg_v<T>, gN, kThreads, st, A, phat, v, rhat, sc, slots_of<1>(d));
-      prof_end(p, e0, 1, 0.0);
-      launch(p, k_bicg_s<T>, gC, kThreads, st, A, r, v, s, shat, sc);
-      prof_begin(p, &e0);
-      launch(p, k_bicg_t<T>, gN, kThreads, st, A, shat, t, s, sc, slots_of<2>(d));
-      prof_end(p, e0, 1, 0.0);
-      launch(p, k_bicg_x<T>, gN, kThreads, st, N, x, r, phat, shat, s, t, rhat, sc, slots_of<2>(d));
+    if (p->profile) {
+      for (int c = 0; c < chunk; c++) iteration(true);
+    } else {
+      // chunks of 4, 8 and 16 iterations are captured once per precision and replayed
+      const int gi = chunk == 4 ? 0 : (chunk == 8 ? 1 : 2);
+      cudaGraphExec_t& gx = d.bicg_graph[sizeof(T) == 8 ? 0 : 1][gi];
+      if (!gx) {
+        cudaGraph_t graph;
+        PGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int c = 0; c < chunk; c++) iteration(false);
+        PGPU_CUDA(cudaStreamEndCapture(st, &graph));
+        cudaError_t e = cudaGraphInstantiate(&gx, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+          gx = nullptr;
+          return fail(PGPU_ERR_CUDA, std::string("BiCGStab graph instantiation: ") + cudaGetErrorString(e));
+        }
+      }
+      PGPU_CUDA(cudaGraphLaunch(gx, st));
     }
+    p->launches += 5LL * chunk;
     PGPU_CUDA(cudaGetLastError());
     PGPU_CUDA(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, st));
     PGPU_CUDA(cudaStreamSynchronize(st));
@@ -534,7 +569,8 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   if (mixed && (st = make_fp32(p))) return st;
   cudaStream_t s = p->stream;
   const int gN = grid_for(N), gC = grid_for(n);
-  DiffOp<double> A = op64(d);
+  PGPU_CUDA(cudaMemsetAsync(d.lam.ptr, 0, 2 * sizeof(double), s));
+  DiffOp<double> A = op64(d, true);
   OuterScal* dos = d.oscal.as<OuterScal>();
   cudaEvent_t e0, e1;
   PGPU_CUDA(cudaEventCreate(&e0));
@@ -569,7 +605,6 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   // R - lam_s F, whose solve maps the normalised fission source to x / (1/k - lam_s).
   double lam_s = 0.0;
   for (outer = 1; outer <= opt->max_outer; outer++) {
-    A = op64(d, lam_s);
     launch(p, k_scale_copy, gN, kThreads, s, N, (const double*)d.x.as<double>(), 1.0 / (1.0 / k_prev - lam_s),
            d.y.as<double>());
     // inner solve (R - lam_s F) y = b by refinement: r = b - A y, correction solve, y += d
@@ -584,7 +619,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       int it = 0;
       if (mixed) {
         // FP32 correction solve on the FP32 copy of the FP64 residual
-        DiffOp<float> A32 = op32(d, lam_s);
+        DiffOp<float> A32 = op32(d, true);
         const double rt = fmax(tol_in / rel, 2e-5);
         if ((st = bicgstab<float>(p, A32, d.w32, d.r32.as<float>(), fmin(rt, 0.5), opt->max_inner, &it))) return st;
         launch(p, k_axpy_update<float>, gN, kThreads, s, N, d.y.as<double>(), d.w32[0].as<float>());
@@ -614,7 +649,10 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       converged = true;
       break;
     }
-    if (outer >= kShiftAfter && dk < kShiftWhenDk) lam_s = 1.0 / (os.k + kShiftDk);
+    if (outer >= kShiftAfter && dk < kShiftWhenDk) {
+      lam_s = 1.0 / (os.k + kShiftDk);
+      launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), lam_s);
+    }
   }
   if (!converged) status = PGPU_ERR_NOT_CONVERGED;
 
@@ -726,6 +764,9 @@ int pgpu_diffusion_create(int device, const pgpu_diffusion_operator* op, pgpu_pr
   al(d.ticket, 64);
   al(d.bscal, sizeof(BiScal));
   al(d.oscal, sizeof(OuterScal));
+  al(d.lam, 2 * sizeof(double));
+  if (st == PGPU_OK && cudaMemsetAsync(d.lam.ptr, 0, 2 * sizeof(double), p->stream) != cudaSuccess)
+    st = fail(PGPU_ERR_CUDA, "clearing the shift");
   if (st == PGPU_OK && cudaMemset(d.ticket.ptr, 0, 64) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "memset");
   if (st != PGPU_OK) {
     std::string msg = pgpu_last_error();
