@@ -49,6 +49,14 @@ WORKLOADS = {
     "diffusion_2d_34x34_g2": dict(kind="diffusion2d", args=dict(), precision="fp64", dtype="f64",
                                   desc="2-group diffusion k-eigenvalue, 2D Cartesian 34x34 (5 cm)"),
 }
+WORKLOADS["diffusion_7g_256x256x128_mixed"] = dict(
+    kind="diffusion7g", args=dict(), precision="mixed", dtype="f32+f64",
+    desc="7-group diffusion k-eigenvalue, 3D Cartesian 256x256x128 (2 cm), 6 materials in 8^3 blocks, "
+         "58.7M unknowns, FP32 BiCGStab with FP64 refinement")
+WORKLOADS["sn_hex_s8_g4_mixed"] = dict(
+    kind="snhex", args=dict(), precision="mixed", dtype="f32+f64",
+    desc="4-group S8 SN k-eigenvalue on 200x200 hexagonal prisms x 40 layers (1.6M cells, 512M angular "
+         "unknowns), vacuum, FP32 level-set sweeps with FP64 refinement")
 WORKLOADS["serve_diffusion"] = dict(
     kind="serve", args=dict(), precision="mixed", dtype="f32+f64",
     desc="stream of k-eigenvalue diffusion requests (3D Cartesian 16x16x4..128x128x64 log-uniform, G in {2,4,7}, "
@@ -69,6 +77,10 @@ def make_input(name: str, out_dir: str) -> str:
     w = WORKLOADS[name]
     if w["kind"] == "sn":
         return wl.sn_3d(out_dir, **w["args"])
+    if w["kind"] == "diffusion7g":
+        return wl.diffusion_3d_7g(out_dir, **w["args"])
+    if w["kind"] == "snhex":
+        return wl.sn_hex(out_dir, **w["args"])
     return wl.diffusion_2d(out_dir, **w["args"])
 
 

@@ -35,7 +35,7 @@ extern "C" {
 
 /* Replaces pampa_initialize (pampa.hxx:8, pampa.cxx:11-36).  argv[1] is the .pmp
  * input; other arguments are options (-verbose, -silent, -pgpu_precision fp64|mixed,
- * -pgpu_tol_k X, -pgpu_tol_flux X, -pgpu_max_outer N, -pgpu_device N).  *dt receives a
+ * -pgpu_tol_k X, -pgpu_tol_flux X, -pgpu_max_outer N, -pgpu_shift X, -pgpu_device N).  *dt receives a
  * new[]-allocated copy of the input's time steps, freed by pampa_finalize. */
 void pampa_initialize(int argc, char* argv[], double** dt, int* ndt, int* error);
 
@@ -107,6 +107,9 @@ typedef struct {
   double power;         /* normalisation target, NeutronicSolver.hxx:17 (default 1.0)  */
   int verbose;          /* print one line per outer iteration when > 0                 */
   int profile;          /* time the dominant kernel with CUDA events (default 0)       */
+  double shift;         /* Wielandt shift once k has settled: the inner solves use     */
+                        /* R - F / (k (1 + shift)); 0 = plain power iteration          */
+                        /* (default 0.02)                                              */
 } pgpu_options;
 
 typedef struct {

@@ -38,7 +38,7 @@ class PampaError(RuntimeError):
 class pgpu_options(C.Structure):
     _fields_ = [("precision", C.c_int), ("tol_k", C.c_double), ("tol_flux", C.c_double),
                 ("max_outer", C.c_int), ("max_inner", C.c_int), ("power", C.c_double),
-                ("verbose", C.c_int), ("profile", C.c_int)]
+                ("verbose", C.c_int), ("profile", C.c_int), ("shift", C.c_double)]
 
 
 class pgpu_stats(C.Structure):

@@ -352,7 +352,6 @@ __global__ void k_normalize_source(int n, int G, const int* __restrict__ mat, co
 }
 
 // Wielandt shift schedule (see diffusion_solve).
-constexpr double kShiftDk = 0.05;
 constexpr int kShiftAfter = 3;
 constexpr double kShiftWhenDk = 1e-3;
 
@@ -601,7 +600,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   double change = 1.0, dk = 1.0, k_prev = 1.0;
   bool converged = false;
   int status = PGPU_OK;
-  // Wielandt shift lam_s = 1/(k + kShiftDk) once k has settled; the inner operator is
+  // Wielandt shift lam_s = 1/(k (1 + shift)) once k has settled; the inner operator is
   // R - lam_s F, whose solve maps the normalised fission source to x / (1/k - lam_s).
   double lam_s = 0.0;
   for (outer = 1; outer <= opt->max_outer; outer++) {
@@ -650,7 +649,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       break;
     }
     if (outer >= kShiftAfter && dk < kShiftWhenDk) {
-      lam_s = 1.0 / (os.k + kShiftDk);
+      lam_s = opt->shift > 0.0 ? 1.0 / (os.k * (1.0 + opt->shift)) : 0.0;
       launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), lam_s);
     }
   }

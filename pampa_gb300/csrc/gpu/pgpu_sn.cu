@@ -142,6 +142,7 @@ struct SNData {
   int restart = 0;
   int krylov_prec = -1;  // element size of the Krylov storage (4 or 8)
   int sweeps = 0;        // sweeps of the running solve
+  int reorth = 0;        // Arnoldi steps that needed a second Gram-Schmidt pass
 };
 
 struct SNOuter {
@@ -809,6 +810,7 @@ __global__ void k_sub_many(long long N, const T* __restrict__ V, long long ld, i
 // read once per chunk instead of once per vector, with few registers per thread.
 constexpr int kGsMax = 32;
 constexpr int kGsChunk = 8;
+constexpr double kReorth = 0.5;  // second Gram-Schmidt pass when ||w|| drops below this share
 
 // out[k] = <V_k, w> for k < nv; reduction slots of chunk y at partials + y*kGsChunk*kMaxBlocks
 template <typename T>
@@ -1464,7 +1466,7 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
   double res = 0.0, tol = 0.0;
   bool first = true;
   ReduceSlots<1> nslot{d.partials.as<double>() + (size_t)(m + 2) * kMaxBlocks, d.ticket.as<unsigned int>() + (m + 2)};
-  if (m + 1 > kGsMax) return fail(PGPU_ERR_INVALID, "GMRES restart length above the Gram-Schmidt kernels' limit");
+  if (m + 2 > kGsMax) return fail(PGPU_ERR_INVALID, "GMRES restart length above the Gram-Schmidt kernels' limit");
   PGPU_CUDA(cudaMemsetAsync(dvec, 0, len * sizeof(T), s));
   while (true) {
     if (first) {
@@ -1490,26 +1492,38 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
     int j = 0;
     for (; j < m && total < max_it; j++) {
       T* vj = V + (size_t)j * len;
-      if ((st = applyA(vj, w))) return st;
-      // CGS2: h1 = V^T w; w -= V h1; h2 = V^T w; w -= V h2 and ||w||
+      T* wj = V + (size_t)(j + 1) * len;  // the new vector is built in place
+      if ((st = applyA(vj, wj))) return st;
+      // classical Gram-Schmidt with re-orthogonalisation when needed ("twice is enough"):
+      // h1 = V^T w (and <w, w>), w -= V h1 with its norm; a second pass only when the
+      // norm fell below kReorth of the original (cancellation).
+      const dim3 gd1(std::min(gx, kMaxBlocks / 2), (j + 2 + kGsChunk - 1) / kGsChunk);
       const dim3 gd(std::min(gx, kMaxBlocks / 2), (j + 1 + kGsChunk - 1) / kGsChunk);
       double* part = d.partials.as<double>();
       unsigned int* tick = d.ticket.as<unsigned int>();
-      launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)w, h1, part, tick);
-      launch(p, k_sub_many<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, w);
-      launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)w, h2, part, tick);
-      launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, w, hn, nslot);
-      launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)w, (const double*)hn, 1, V + (size_t)(j + 1) * len);
+      launch(p, k_gs_dot<T>, gd1, kThreads, s, len, (const T*)V, len, j + 2, (const T*)wj, h1, part, tick);
+      launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, wj, hn, nslot);
       PGPU_CUDA(cudaGetLastError());
-      // h1, h2 and ||w|| are adjacent in hbuf: one copy into pinned host memory
+      // h1 and ||w|| (adjacent in hbuf with h2): one copy into pinned host memory
       PGPU_CUDA(cudaMemcpyAsync(hp, h1, (size_t)(2 * (m + 4) + 1) * 8, cudaMemcpyDeviceToHost, s));
       PGPU_CUDA(cudaStreamSynchronize(s));
       const double* hh = hp;
-      const double* hh2 = hp + (m + 4);
-      const double hnext = hp[2 * (m + 4)];
-      total++;
+      double hnext = hp[2 * (m + 4)];
+      const double w0 = std::sqrt(std::fmax(hh[j + 1], 0.0));
       double* col = &H[(size_t)j * (m + 1)];
-      for (int k = 0; k <= j; k++) col[k] = hh[k] + hh2[k];
+      for (int k = 0; k <= j; k++) col[k] = hh[k];
+      if (!(hnext >= kReorth * w0)) {
+        launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)wj, h2, part, tick);
+        launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, wj, hn, nslot);
+        PGPU_CUDA(cudaGetLastError());
+        PGPU_CUDA(cudaMemcpyAsync(hp + (m + 4), h2, (size_t)((m + 4) + 1) * 8, cudaMemcpyDeviceToHost, s));
+        PGPU_CUDA(cudaStreamSynchronize(s));
+        for (int k = 0; k <= j; k++) col[k] += hp[(m + 4) + k];
+        hnext = hp[2 * (m + 4)];
+        d.reorth++;
+      }
+      launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)wj, (const double*)hn, 1, wj);
+      total++;
       col[j + 1] = hnext;
       for (int k = 0; k < j; k++) {
         double a = cs[k] * col[k] + sn[k] * col[k + 1];
@@ -1576,11 +1590,10 @@ int read_outer(pgpu_problem* p, SNOuter& os) {
 // FP32 for mixed precision: iterative refinement), updates x, and renormalises the
 // fission source.  The correction solve reduces the FP64 residual by kEta.
 constexpr double kEta = 0.02;
-// Wielandt shift: lambda_s = 1 / (k + kShiftDk) once at least kShiftAfter outer iterations
-// have run and |dk| < kShiftWhenDk.  The inner operator I - T (S + lambda_s F) stays
-// nonsingular while k + kShiftDk is above the fundamental k; the shifted iteration's
-// dominance ratio is (1/k1 - lambda_s) / (1/k2 - lambda_s).
-constexpr double kShiftDk = 0.05;
+// Wielandt shift: lambda_s = 1 / (k (1 + shift)) (options.shift) once at least kShiftAfter
+// outer iterations have run and |dk| < kShiftWhenDk.  The inner operator I - T (S +
+// lambda_s F) stays nonsingular while k (1 + shift) is above the fundamental k; the
+// shifted iteration's dominance ratio is (1/k1 - lambda_s) / (1/k2 - lambda_s).
 constexpr int kShiftAfter = 3;
 constexpr double kShiftWhenDk = 1e-3;
 
@@ -1644,7 +1657,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   launch(p, k_scale_to<double>, gl, kThreads, s, len, (const double*)x64, (const double*)&dos->S, 1, x64);
   PGPU_CUDA(cudaGetLastError());
 
-  // Wielandt shift lam_s = 1/(k + kShiftDk), switched on once k has settled (scalar-flux
+  // Wielandt shift lam_s = 1/(k (1 + shift)), switched on once k has settled (scalar-flux
   // space only); 0 means plain power iteration.
   double lam_s = 0.0;
 
@@ -1726,7 +1739,8 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
       converged = true;
       break;
     }
-    if (phi_space && outer >= kShiftAfter && dk < kShiftWhenDk) lam_s = 1.0 / (os.k + kShiftDk);
+    if (phi_space && outer >= kShiftAfter && dk < kShiftWhenDk && opt->shift > 0.0)
+      lam_s = 1.0 / (os.k * (1.0 + opt->shift));
   }
 
   // psi in FP64 from the converged state (one more sweep in scalar-flux space)

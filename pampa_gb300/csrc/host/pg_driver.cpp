@@ -158,6 +158,7 @@ int Driver::initialize(int argc, char* argv[], std::vector<double>& dt) {
     else if (s == "-pgpu_tol_flux") PG_TRY(to_double(val(), 0.0, 1.0, opt_.gpu.tol_flux), "wrong -pgpu_tol_flux");
     else if (s == "-pgpu_max_outer") PG_TRY(to_int(val(), 1, 100000000, opt_.gpu.max_outer), "wrong -pgpu_max_outer");
     else if (s == "-pgpu_max_inner") PG_TRY(to_int(val(), 1, 100000000, opt_.gpu.max_inner), "wrong -pgpu_max_inner");
+    else if (s == "-pgpu_shift") PG_TRY(to_double(val(), 0.0, 10.0, opt_.gpu.shift), "wrong -pgpu_shift");
     else if (s == "-pgpu_device") PG_TRY(to_int(val(), 0, 1024, opt_.device), "wrong -pgpu_device");
     else if (s == "-pgpu_verbose") opt_.gpu.verbose = 1;
     // other options (PETSc/SLEPc, -vtk, ...) are accepted and ignored
