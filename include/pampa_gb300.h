@@ -108,8 +108,8 @@ typedef struct {
   int verbose;          /* print one line per outer iteration when > 0                 */
   int profile;          /* time the dominant kernel with CUDA events (default 0)       */
   double shift;         /* Wielandt shift once k has settled: the inner solves use     */
-                        /* R - F / (k (1 + shift)); 0 = plain power iteration          */
-                        /* (default 0.02)                                              */
+                        /* R - F / (k (1 + shift)); 0 = plain power iteration, < 0 =   */
+                        /* the solver's default (0.02 diffusion, 0.05 SN; default -1)  */
 } pgpu_options;
 
 typedef struct {

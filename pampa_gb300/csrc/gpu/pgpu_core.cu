@@ -52,7 +52,7 @@ void pgpu_default_options(pgpu_options* opt) {
   opt->max_inner = 2000;
   opt->power = 1.0;
   opt->verbose = 0;
-  opt->shift = 0.02;
+  opt->shift = -1.0;
 }
 
 const char* pgpu_last_error(void) { return pgpu::g_last_error.c_str(); }

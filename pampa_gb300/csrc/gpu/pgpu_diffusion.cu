@@ -353,6 +353,7 @@ __global__ void k_normalize_source(int n, int G, const int* __restrict__ mat, co
 
 // Wielandt shift schedule (see diffusion_solve).
 constexpr int kShiftAfter = 3;
+constexpr double kShiftDefault = 0.02;  // relative shift of k (measured best on the diffusion workloads)
 constexpr double kShiftWhenDk = 1e-3;
 
 // y = f x
@@ -649,7 +650,9 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       break;
     }
     if (outer >= kShiftAfter && dk < kShiftWhenDk) {
-      lam_s = opt->shift > 0.0 ? 1.0 / (os.k * (1.0 + opt->shift)) : 0.0;
+      const double sh = opt->shift < 0.0 ? kShiftDefault : opt->shift;
+      // the shifted k stays well above the fundamental one: at least 10 |dk| above k
+      lam_s = sh > 0.0 ? 1.0 / std::fmax(os.k * (1.0 + sh), os.k + 10.0 * dk) : 0.0;
       launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), lam_s);
     }
   }
