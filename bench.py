@@ -499,9 +499,10 @@ def run_serve(args, rank, world, local):
             for t in wt:
                 t.join()
             t_end = max(r["t_done"] for r in results)
-    bad = [r for r in results if r["status"] != pg.PGPU_OK]
+    bad = [(k, r) for k, r in enumerate(results) if r["status"] != pg.PGPU_OK]
     if bad:
-        raise RuntimeError(f"{len(bad)} served solves failed")
+        raise RuntimeError(f"{len(bad)} served solves failed: " + "; ".join(
+            f"#{k} {specs[k]} status {r['status']} {r.get('error', '')}" for k, r in bad[:8]))
     lat = np.array([r["latency_s"] for r in results])
     wall = t_end - t_start
     value = nreq / wall

@@ -447,6 +447,7 @@ class Server:
         st = lib().pgpu_serve_wait(self._h, rid, C.byref(stats), C.byref(k), _dp(phi) if phi is not None else None,
                                    _dp(times))
         return dict(status=st, keff=k.value, phi=phi, queue_s=times[0], run_s=times[1], latency_s=times[2],
+                    error=last_error() if st != PGPU_OK else "",
                     stats={f: getattr(stats, f) for f, _ in pgpu_stats._fields_})
 
     def close(self):

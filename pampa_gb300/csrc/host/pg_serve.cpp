@@ -23,6 +23,10 @@
 
 #include "pampa_gb300.h"
 
+namespace pgpu {
+void set_error(const std::string& msg);  // the calling thread's pgpu_last_error()
+}
+
 namespace {
 
 double now_s() {
@@ -317,6 +321,7 @@ int pgpu_serve_wait(pgpu_server* s, long long id, pgpu_stats* stats, double* kef
     r = std::move(it->second);
     s->requests.erase(it);
   }
+  if (r->status != PGPU_OK) pgpu::set_error("request " + std::to_string(id) + ": " + r->error);
   if (stats) *stats = r->stats;
   if (keff) *keff = r->keff;
   if (phi && !r->phi.empty()) std::memcpy(phi, r->phi.data(), r->phi.size() * sizeof(double));
