@@ -60,7 +60,8 @@ WORKLOADS["sn_hex_s8_g4_mixed"] = dict(
 WORKLOADS["serve_diffusion"] = dict(
     kind="serve", args=dict(), precision="mixed", dtype="f32+f64",
     desc="stream of k-eigenvalue diffusion requests (3D Cartesian 16x16x4..128x128x64 log-uniform, G in {2,4,7}, "
-         "+-5% lognormal XS perturbations), Poisson arrivals at 2x the one-at-a-time FP64 rate, continuous batching")
+         "+-5% lognormal XS perturbations), Poisson arrivals at 2x the one-at-a-time FP64 rate, continuous batching, "
+         "k to 1e-8")
 DEFAULT = "sn_s8_64x64x32_g2"
 SOLVE_STATS = os.path.join(ROOT, "profiles", "solve_stats.json")
 
@@ -72,13 +73,17 @@ def dist_env():
     return rank, world, local
 
 
-def make_input(name: str, out_dir: str) -> str:
+def make_input(name: str, out_dir: str, size: str | None = None) -> str:
+    """The workload's input; `size` ("NXxNYxNZ", profiling captures only) shrinks the box."""
     from pampa_gb300 import workloads as wl
     w = WORKLOADS[name]
+    args = dict(w["args"])
+    if size and w["kind"] in ("sn", "diffusion7g"):
+        args.update(zip(("nx", "ny", "nz"), (int(v) for v in size.lower().split("x"))))
     if w["kind"] == "sn":
-        return wl.sn_3d(out_dir, **w["args"])
+        return wl.sn_3d(out_dir, **args)
     if w["kind"] == "diffusion7g":
-        return wl.diffusion_3d_7g(out_dir, **w["args"])
+        return wl.diffusion_3d_7g(out_dir, **args)
     if w["kind"] == "snhex":
         return wl.sn_hex(out_dir, **w["args"])
     return wl.diffusion_2d(out_dir, **w["args"])
@@ -261,7 +266,7 @@ def run_ours(args, rank, world, local):
 
     w = WORKLOADS[args.workload]
     tmp = tempfile.mkdtemp(prefix=f"bench_r{rank}_")
-    path = make_input(args.workload, tmp)
+    path = make_input(args.workload, tmp, args.size)
     prec = ["-pgpu_precision", w["precision"]]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
 
@@ -369,7 +374,8 @@ def run_ours(args, rank, world, local):
                             sweeps_per_solve=sweeps, outer_iterations=results[-1]["outer_iterations"],
                             gmres_iterations=results[-1]["inner_iterations"], l2="flushed (256 MB write) between steps",
                             parallelism=f"replicas x{world}" if world > 1 else "1 GPU",
-                            wall_ms_per_step=1e3 * wall / args.steps),
+                            wall_ms_per_step=1e3 * wall / args.steps,
+                            **(dict(size_override=args.size) if args.size else {})),
                 e2e=dict(value=world / e2e_t, unit="solves/s", h2d_bytes_per_step=upload,
                          d2h_bytes_per_step=8 * (n_phi + n_psi + n_cells),
                          note="drop-in pampa_* API: parse + host assembly + upload + solve + field reads; "
@@ -438,8 +444,10 @@ def run_serve(args, rank, world, local):
         nx, ny, nz, G = specs[k]
         return wl.diffusion_request(np.random.default_rng(int(seeds[k])), nx, ny, nz, G)[0]
 
-    fp64 = pg.default_options(precision=pg.PGPU_FP64)
-    mixed = pg.default_options(precision=pg.PGPU_MIXED)
+    # power iteration to 1e-8 on k and 1e-7 on the fission source, as the small plain
+    # workload is specified (served answers are compared at 1 pcm)
+    fp64 = pg.default_options(precision=pg.PGPU_FP64, tol_k=1e-8, tol_flux=1e-7)
+    mixed = pg.default_options(precision=pg.PGPU_MIXED, tol_k=1e-8, tol_flux=1e-7)
     # 1. plain FP64, one request at a time, on the first requests of the stream
     sample = min(nreq, args.serve_sample)
     ops = [make(k) for k in range(sample)]
@@ -550,6 +558,9 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--record", action="store_true", help="write profiles/solve_stats.json")
+    ap.add_argument("--size", default=None,
+                    help="profiling captures only: NXxNYxNZ box instead of the workload's (the line is then "
+                         "not the workload's result)")
     ap.add_argument("--requests", type=int, default=1024, help="serve_diffusion: requests in the stream")
     ap.add_argument("--slots", type=int, default=8, help="serve_diffusion: solves in flight at most")
     ap.add_argument("--serve-sample", type=int, default=32,

@@ -354,6 +354,7 @@ __global__ void k_normalize_source(int n, int G, const int* __restrict__ mat, co
 // Wielandt shift schedule (see diffusion_solve).
 constexpr int kShiftAfter = 3;
 constexpr double kShiftDefault = 0.02;  // relative shift of k (measured best on the diffusion workloads)
+constexpr double kShiftMargin = 50.0;   // the shifted k is at least k + kShiftMargin |dk|
 constexpr double kShiftWhenDk = 1e-3;
 
 // y = f x
@@ -621,8 +622,19 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
         // FP32 correction solve on the FP32 copy of the FP64 residual
         DiffOp<float> A32 = op32(d, true);
         const double rt = fmax(tol_in / rel, 2e-5);
-        if ((st = bicgstab<float>(p, A32, d.w32, d.r32.as<float>(), fmin(rt, 0.5), opt->max_inner, &it))) return st;
-        launch(p, k_axpy_update<float>, gN, kThreads, s, N, d.y.as<double>(), d.w32[0].as<float>());
+        st = bicgstab<float>(p, A32, d.w32, d.r32.as<float>(), fmin(rt, 0.5), opt->max_inner, &it);
+        if (st == PGPU_ERR_NAN) {
+          // FP32 breakdown (overflow or a nearly singular shifted system): this correction
+          // step runs in FP64 instead
+          const double rt64 = fmax(0.5 * tol_in / rel, 1e-15);
+          if ((st = bicgstab<double>(p, A, d.w64, d.r64.as<double>(), fmin(rt64, 0.5), opt->max_inner, &it)))
+            return st;
+          launch(p, k_axpy_update<double>, gN, kThreads, s, N, d.y.as<double>(), d.w64[0].as<double>());
+        } else if (st) {
+          return st;
+        } else {
+          launch(p, k_axpy_update<float>, gN, kThreads, s, N, d.y.as<double>(), d.w32[0].as<float>());
+        }
       } else {
         const double rt = fmax(0.5 * tol_in / rel, 1e-15);
         if ((st = bicgstab<double>(p, A, d.w64, d.r64.as<double>(), fmin(rt, 0.5), opt->max_inner, &it))) return st;
@@ -651,8 +663,9 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
     }
     if (outer >= kShiftAfter && dk < kShiftWhenDk) {
       const double sh = opt->shift < 0.0 ? kShiftDefault : opt->shift;
-      // the shifted k stays well above the fundamental one: at least 10 |dk| above k
-      lam_s = sh > 0.0 ? 1.0 / std::fmax(os.k * (1.0 + sh), os.k + 10.0 * dk) : 0.0;
+      // the shifted k must stay above the fundamental one; with dominance ratio rho the
+      // estimate is still about dk rho / (1 - rho) below it, so keep 50 |dk| of margin
+      lam_s = sh > 0.0 ? 1.0 / std::fmax(os.k * (1.0 + sh), os.k + kShiftMargin * dk) : 0.0;
       launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), lam_s);
     }
   }

@@ -1596,6 +1596,8 @@ constexpr double kEta = 0.02;
 // shifted iteration's dominance ratio is (1/k1 - lambda_s) / (1/k2 - lambda_s).
 constexpr int kShiftAfter = 3;
 constexpr double kShiftDefault = 0.05;  // relative shift of k (measured best on the S8 workload)
+constexpr double kShiftMargin = 50.0;   // the shifted k is at least k + kShiftMargin |dk| (the estimate
+                                        // lags the fundamental k by about dk rho / (1 - rho))
 constexpr double kShiftWhenDk = 1e-3;
 
 template <typename T>
@@ -1742,7 +1744,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
     }
     const double sh = opt->shift < 0.0 ? kShiftDefault : opt->shift;
     if (phi_space && outer >= kShiftAfter && dk < kShiftWhenDk && sh > 0.0)
-      lam_s = 1.0 / std::fmax(os.k * (1.0 + sh), os.k + 10.0 * dk);  // well above the fundamental k
+      lam_s = 1.0 / std::fmax(os.k * (1.0 + sh), os.k + kShiftMargin * dk);  // above the fundamental k
   }
 
   // psi in FP64 from the converged state (one more sweep in scalar-flux space)
