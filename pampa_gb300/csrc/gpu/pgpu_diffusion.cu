@@ -18,6 +18,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <array>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "pgpu_internal.cuh"
 
@@ -60,6 +64,8 @@ struct DiffusionData {
   DevBuf w32[9];  // BiCGStab vectors for FP32
   DevBuf partials, ticket, bscal, oscal;
   DevBuf lam;  // [2]: the Wielandt shift of the running solve, and a constant 0
+  DevBuf bscal_tune;  // BiCGStab scalars of the launch-shape tuner's timing runs
+  int shape[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};  // [fp32]: row threads, row blocks, cell threads, cell blocks
   bool have32 = false;
   // BiCGStab iterations captured in CUDA graphs, [fp32][chunk 4, 8, 16]
   cudaGraphExec_t bicg_graph[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
@@ -275,6 +281,108 @@ __global__ void k_bicg_x(int N, T* x, T* r, const T* __restrict__ phat, const T*
 }
 
 // ---------------------------------------------------------------------------------
+// Cell-per-thread forms of the SpMV kernels for G = 2, 4, 7 (the group counts of the
+// workloads): one thread computes the G rows of a cell, so the cell's group vector,
+// material tables and neighbour indices are loaded once instead of once per row.  Same
+// operations in the same order as apply_row, so the results are the same.
+// ---------------------------------------------------------------------------------
+template <typename T, int G>
+__device__ __forceinline__ void apply_cell(const DiffOp<T>& A, const T* __restrict__ x, int i, T (&y)[G]) {
+  const size_t base = (size_t)i * G;
+  T xc[G];
+#pragma unroll
+  for (int g = 0; g < G; g++) xc[g] = x[base + g];
+  const int m = A.mat[i];
+  const T* ssm = A.ss + (size_t)m * G * G;
+  const T vol = A.vol[i];
+  const T ls = (T)*A.lam_s;
+  T f = T(0);
+  if (ls != T(0)) {
+    const T* ns = A.nsf + (size_t)m * G;
+#pragma unroll
+    for (int g2 = 0; g2 < G; g2++) f += ns[g2] * xc[g2];
+  }
+#pragma unroll
+  for (int g = 0; g < G; g++) {
+    T acc = A.diag[base + g] * xc[g];
+    T sc = T(0);
+#pragma unroll
+    for (int g2 = 0; g2 < G; g2++)
+      if (g2 != g) sc += ssm[g2 * G + g] * xc[g2];
+    if (ls != T(0)) sc += ls * A.chi[(size_t)m * G + g] * f;
+    acc -= vol * sc;
+    y[g] = acc;
+  }
+  const size_t nG = (size_t)A.n * G;
+  for (int fa = 0; fa < A.F; fa++) {
+    const int j = A.nbr[(size_t)fa * A.n + i];
+    if (j >= 0) {
+      const T* o = A.off + fa * nG + base;
+      const T* xj = x + (size_t)j * G;
+#pragma unroll
+      for (int g = 0; g < G; g++) y[g] += o[g] * xj[g];
+    }
+  }
+}
+
+// v = A phat; alpha = rho / (rhat, v)  (cell form of k_bicg_v)
+template <typename T, int G>
+__global__ void k_bicg_v_cell(DiffOp<T> A, const T* __restrict__ phat, T* v, const T* __restrict__ rhat,
+                              BiScal* sc, ReduceSlots<1> slots) {
+  if (sc->converged) return;
+  T part = T(0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    T y[G];
+    apply_cell<T, G>(A, phat, i, y);
+    const size_t base = (size_t)i * G;
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+      v[base + g] = y[g];
+      part += rhat[base + g] * y[g];
+    }
+  }
+  double acc[1] = {(double)part};
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
+    if (tot[0] == 0.0 || !(tot[0] == tot[0])) {
+      sc->breakdown = 1;
+      sc->converged = 1;
+    } else {
+      sc->alpha = sc->rho / tot[0];
+    }
+  }
+}
+
+// t = A shat; omega = (t, s) / (t, t)  (cell form of k_bicg_t)
+template <typename T, int G>
+__global__ void k_bicg_t_cell(DiffOp<T> A, const T* __restrict__ shat, T* t, const T* __restrict__ s,
+                              BiScal* sc, ReduceSlots<2> slots) {
+  if (sc->converged) return;
+  T p0 = T(0), p1 = T(0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    T y[G];
+    apply_cell<T, G>(A, shat, i, y);
+    const size_t base = (size_t)i * G;
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+      t[base + g] = y[g];
+      p0 += y[g] * s[base + g];
+      p1 += y[g] * y[g];
+    }
+  }
+  double acc[2] = {(double)p0, (double)p1};
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
+    if (tot[1] == 0.0 || !(tot[1] == tot[1])) {
+      sc->omega = 0.0;
+      sc->breakdown = 1;
+    } else {
+      sc->omega = tot[0] / tot[1];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
 // Outer-iteration kernels (always FP64)
 // ---------------------------------------------------------------------------------
 
@@ -482,6 +590,114 @@ int make_fp32(pgpu_problem* p) {
 }
 
 // BiCGStab on A d = rin in precision T.  Kernels are launched in chunks; each kernel
+// SpMV kernels of BiCGStab: the cell form for G = 2, 4, 7, the row form otherwise.
+inline bool cell_form(int G) { return G == 2 || G == 4 || G == 7; }
+
+template <typename T>
+void launch_bicg_v(int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* phat, T* v,
+                   const T* rhat, BiScal* sc, ReduceSlots<1> sl) {
+  switch (A.G) {
+    case 2: k_bicg_v_cell<T, 2><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl); break;
+    case 4: k_bicg_v_cell<T, 4><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl); break;
+    case 7: k_bicg_v_cell<T, 7><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl); break;
+    default: k_bicg_v<T><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl);
+  }
+}
+
+template <typename T>
+void launch_bicg_t(int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* shat, T* t,
+                   const T* s, BiScal* sc, ReduceSlots<2> sl) {
+  switch (A.G) {
+    case 2: k_bicg_t_cell<T, 2><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl); break;
+    case 4: k_bicg_t_cell<T, 4><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl); break;
+    case 7: k_bicg_t_cell<T, 7><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl); break;
+    default: k_bicg_t<T><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Launch-shape autotuner of the BiCGStab kernels.  The row kernels (SpMV fused with
+// products) and the cell kernels (vector update + group-block preconditioner) are timed
+// with CUDA events for threads per block in {128, 256, 512} and at most {2, 4, 8} blocks
+// per SM, on the problem's own operator and vectors, before its first inner solve; the
+// fastest shape per kernel kind is kept for every problem of the same size class
+// (rows rounded to a power of two, groups, precision) in a process-wide table.
+// ---------------------------------------------------------------------------------
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, std::array<int, 4>> g_tune;
+}  // namespace
+
+template <typename T>
+int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
+  DiffusionData& d = *p->diff;
+  int* shape = d.shape[sizeof(T) == 8 ? 0 : 1];
+  if (shape[0]) return PGPU_OK;
+  const int N = d.n * d.G;
+  int lg = 0;
+  while ((1LL << lg) < N) lg++;
+  const auto key = std::make_tuple(lg, d.G, (int)sizeof(T));
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      for (int k = 0; k < 4; k++) shape[k] = it->second[k];
+      return PGPU_OK;
+    }
+  }
+  int dev = 0, sms = 0;
+  PGPU_CUDA(cudaGetDevice(&dev));
+  PGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  if (!d.bscal_tune.ptr) {
+    int st = dev_alloc(d.bscal_tune, sizeof(BiScal), &p->bytes);
+    if (st) return st;
+  }
+  BiScal init{};
+  init.rho = init.rho_old = init.alpha = init.omega = 1.0;
+  BiScal* sc = d.bscal_tune.as<BiScal>();
+  PGPU_CUDA(cudaMemcpyAsync(sc, &init, sizeof(init), cudaMemcpyHostToDevice, p->stream));
+  // inputs: zeroed BiCGStab vectors (overwritten by the solve's own initialisation)
+  for (int k = 0; k < 9; k++) PGPU_CUDA(cudaMemsetAsync(w[k].ptr, 0, (size_t)N * sizeof(T), p->stream));
+  T *r = w[1].as<T>(), *rhat = w[2].as<T>(), *pp = w[3].as<T>(), *v = w[4].as<T>(), *phat = w[7].as<T>();
+  cudaEvent_t e0, e1;
+  PGPU_CUDA(cudaEventCreate(&e0));
+  PGPU_CUDA(cudaEventCreate(&e1));
+  float best[2] = {1e30f, 1e30f};
+  const long long spmv_work = cell_form(d.G) ? d.n : N;
+  int out[4] = {kThreads, grid_for(spmv_work), kThreads, grid_for(d.n)};
+  for (int kind = 0; kind < 2; kind++) {
+    const long long work = kind == 0 ? spmv_work : d.n;
+    for (int threads : {128, 256, 512})
+      for (int per_sm : {2, 4, 8}) {
+        const int blocks = (int)std::max(1LL, std::min<long long>((work + threads - 1) / threads,
+                                                                  std::min(kMaxBlocks, per_sm * sms)));
+        auto run = [&]() {
+          if (kind == 0) launch_bicg_v<T>(blocks, threads, p->stream, A, phat, v, rhat, sc, slots_of<1>(d));
+          else k_bicg_p<T><<<blocks, threads, 0, p->stream>>>(A, r, pp, v, phat, sc);
+        };
+        for (int k = 0; k < 2; k++) run();
+        PGPU_CUDA(cudaEventRecord(e0, p->stream));
+        for (int k = 0; k < 5; k++) run();
+        PGPU_CUDA(cudaEventRecord(e1, p->stream));
+        PGPU_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        p->launches += 7;
+        if (ms < best[kind]) {
+          best[kind] = ms;
+          out[2 * kind] = threads;
+          out[2 * kind + 1] = blocks;
+        }
+      }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (int k = 0; k < 4; k++) shape[k] = out[k];
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = {out[0], out[1], out[2], out[3]};
+  return PGPU_OK;
+}
+
 // returns at once when the device-side `converged` flag is set, so the host only reads
 // the state once per chunk.  The solution is left in w[0].
 template <typename T>
@@ -489,7 +705,11 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
              int* iters_out) {
   DiffusionData& d = *p->diff;
   const int N = d.n * d.G;
-  const int gN = grid_for(N), gC = grid_for(d.n);
+  int tst = tune_bicg<T>(p, A, w);
+  if (tst) return tst;
+  const int* shp = d.shape[sizeof(T) == 8 ? 0 : 1];
+  const int rT = shp[0], gS = shp[1], cT = shp[2], gC = shp[3];  // SpMV and cell-kernel shapes
+  const int gN = grid_for(N);                                     // element-wise kernels
   T *x = w[0].as<T>(), *r = w[1].as<T>(), *rhat = w[2].as<T>(), *pp = w[3].as<T>(), *v = w[4].as<T>(),
     *s = w[5].as<T>(), *t = w[6].as<T>(), *phat = w[7].as<T>(), *shat = w[8].as<T>();
   BiScal* sc = d.bscal.as<BiScal>();
@@ -509,13 +729,13 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   // convergence the kernels return at once)
   auto iteration = [&](bool timed) {
     cudaEvent_t e0;
-    k_bicg_p<T><<<gC, kThreads, 0, st>>>(A, r, pp, v, phat, sc);
+    k_bicg_p<T><<<gC, cT, 0, st>>>(A, r, pp, v, phat, sc);
     if (timed) prof_begin(p, &e0);
-    k_bicg_v<T><<<gN, kThreads, 0, st>>>(A, phat, v, rhat, sc, slots_of<1>(d));
+    launch_bicg_v<T>(gS, rT, st, A, phat, v, rhat, sc, slots_of<1>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
-    k_bicg_s<T><<<gC, kThreads, 0, st>>>(A, r, v, s, shat, sc);
+    k_bicg_s<T><<<gC, cT, 0, st>>>(A, r, v, s, shat, sc);
     if (timed) prof_begin(p, &e0);
-    k_bicg_t<T><<<gN, kThreads, 0, st>>>(A, shat, t, s, sc, slots_of<2>(d));
+    launch_bicg_t<T>(gS, rT, st, A, shat, t, s, sc, slots_of<2>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
     k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phat, shat, s, t, rhat, sc, slots_of<2>(d));
   };
