@@ -39,6 +39,9 @@ struct DiffOp {
   const T* __restrict__ chi;    // [nm][G]
   const T* __restrict__ nsf;    // [nm][G]
   const double* __restrict__ lam_s;  // device scalar, Wielandt shift: the operator is R - lam_s F
+  // [nm][G][G] in-cell coupling g2 -> g of the shifted operator, sigma_s(g2->g) (g2 != g)
+  // + lam_s chi_g nu_sigma_f(g2), rebuilt when lam_s changes; null for the plain operator
+  const T* __restrict__ fold;
 };
 
 // Device-resident BiCGStab state; every scalar of the iteration stays on the GPU.
@@ -59,13 +62,15 @@ struct DiffusionData {
   int n = 0, G = 0, F = 0, nm = 0;
   DevBuf nbr, mat, off64, diag64, vol64, ss64, chi, nsf, ksf;
   DevBuf off32, diag32, vol32, ss32, chi32, nsf32;
+  DevBuf fold64, fold32;  // DiffOp::fold in each precision
   DevBuf x, y, b, r64, r32, fs, fs_old, phi, q, P;
   DevBuf w64[9];  // BiCGStab vectors for FP64
   DevBuf w32[9];  // BiCGStab vectors for FP32
   DevBuf partials, ticket, bscal, oscal;
   DevBuf lam;  // [2]: the Wielandt shift of the running solve, and a constant 0
   DevBuf bscal_tune;  // BiCGStab scalars of the launch-shape tuner's timing runs
-  int shape[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};  // [fp32]: row threads, row blocks, cell threads, cell blocks
+  int shape[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};  // [fp32]: SpMV threads, blocks, cell-kernel threads,
+                                                          // blocks, SpMV form (0 row, 1 cell, 2 folded row)
   bool have32 = false;
   // BiCGStab iterations captured in CUDA graphs, [fp32][chunk 4, 8, 16]
   cudaGraphExec_t bicg_graph[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
@@ -281,10 +286,11 @@ __global__ void k_bicg_x(int N, T* x, T* r, const T* __restrict__ phat, const T*
 }
 
 // ---------------------------------------------------------------------------------
-// Cell-per-thread forms of the SpMV kernels for G = 2, 4, 7 (the group counts of the
-// workloads): one thread computes the G rows of a cell, so the cell's group vector,
-// material tables and neighbour indices are loaded once instead of once per row.  Same
-// operations in the same order as apply_row, so the results are the same.
+// SpMV forms for G = 2, 4, 7 (the group counts of the workloads), G known at compile time
+// and the in-cell coupling of the shifted operator read from one folded G x G table per
+// material: the cell form (one thread computes a cell's G rows: group vector, tables and
+// neighbour indices loaded once) and the folded row form (coalesced row per thread).  The
+// autotuner picks between them per size class.
 // ---------------------------------------------------------------------------------
 template <typename T, int G>
 __device__ __forceinline__ void apply_cell(const DiffOp<T>& A, const T* __restrict__ x, int i, T (&y)[G]) {
@@ -292,26 +298,14 @@ __device__ __forceinline__ void apply_cell(const DiffOp<T>& A, const T* __restri
   T xc[G];
 #pragma unroll
   for (int g = 0; g < G; g++) xc[g] = x[base + g];
-  const int m = A.mat[i];
-  const T* ssm = A.ss + (size_t)m * G * G;
+  const T* fm = A.fold + (size_t)A.mat[i] * G * G;
   const T vol = A.vol[i];
-  const T ls = (T)*A.lam_s;
-  T f = T(0);
-  if (ls != T(0)) {
-    const T* ns = A.nsf + (size_t)m * G;
-#pragma unroll
-    for (int g2 = 0; g2 < G; g2++) f += ns[g2] * xc[g2];
-  }
 #pragma unroll
   for (int g = 0; g < G; g++) {
-    T acc = A.diag[base + g] * xc[g];
     T sc = T(0);
 #pragma unroll
-    for (int g2 = 0; g2 < G; g2++)
-      if (g2 != g) sc += ssm[g2 * G + g] * xc[g2];
-    if (ls != T(0)) sc += ls * A.chi[(size_t)m * G + g] * f;
-    acc -= vol * sc;
-    y[g] = acc;
+    for (int g2 = 0; g2 < G; g2++) sc += fm[g2 * G + g] * xc[g2];
+    y[g] = A.diag[base + g] * xc[g] - vol * sc;
   }
   const size_t nG = (size_t)A.n * G;
   for (int fa = 0; fa < A.F; fa++) {
@@ -321,6 +315,72 @@ __device__ __forceinline__ void apply_cell(const DiffOp<T>& A, const T* __restri
       const T* xj = x + (size_t)j * G;
 #pragma unroll
       for (int g = 0; g < G; g++) y[g] += o[g] * xj[g];
+    }
+  }
+}
+
+// One row of the shifted operator with the folded in-cell table, G known at compile time
+// (row form: consecutive threads take consecutive rows, so every load is coalesced).
+template <typename T, int G>
+__device__ __forceinline__ T apply_row_fold(const DiffOp<T>& A, const T* __restrict__ x, int l) {
+  const int i = l / G, g = l - i * G;
+  const size_t base = (size_t)i * G;
+  const T* fm = A.fold + (size_t)A.mat[i] * G * G + g;
+  T sc = T(0);
+#pragma unroll
+  for (int g2 = 0; g2 < G; g2++) sc += fm[g2 * G] * x[base + g2];
+  T acc = A.diag[l] * x[l] - A.vol[i] * sc;
+  const size_t nG = (size_t)A.n * G;
+  for (int f = 0; f < A.F; f++) {
+    const int j = A.nbr[(size_t)f * A.n + i];
+    if (j >= 0) acc += A.off[f * nG + l] * x[(size_t)j * G + g];
+  }
+  return acc;
+}
+
+template <typename T, int G>
+__global__ void k_bicg_v_row(DiffOp<T> A, const T* __restrict__ phat, T* v, const T* __restrict__ rhat,
+                             BiScal* sc, ReduceSlots<1> slots) {
+  if (sc->converged) return;
+  const int N = A.n * G;
+  T part = T(0);
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
+    const T val = apply_row_fold<T, G>(A, phat, l);
+    v[l] = val;
+    part += rhat[l] * val;
+  }
+  double acc[1] = {(double)part};
+  double tot[1];
+  if (block_reduce_last<1>(acc, slots, tot) && threadIdx.x == 0) {
+    if (tot[0] == 0.0 || !(tot[0] == tot[0])) {
+      sc->breakdown = 1;
+      sc->converged = 1;
+    } else {
+      sc->alpha = sc->rho / tot[0];
+    }
+  }
+}
+
+template <typename T, int G>
+__global__ void k_bicg_t_row(DiffOp<T> A, const T* __restrict__ shat, T* t, const T* __restrict__ s,
+                             BiScal* sc, ReduceSlots<2> slots) {
+  if (sc->converged) return;
+  const int N = A.n * G;
+  T p0 = T(0), p1 = T(0);
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) {
+    const T val = apply_row_fold<T, G>(A, shat, l);
+    t[l] = val;
+    p0 += val * s[l];
+    p1 += val * val;
+  }
+  double acc[2] = {(double)p0, (double)p1};
+  double tot[2];
+  if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
+    if (tot[1] == 0.0 || !(tot[1] == tot[1])) {
+      sc->omega = 0.0;
+      sc->breakdown = 1;
+    } else {
+      sc->omega = tot[0] / tot[1];
     }
   }
 }
@@ -472,7 +532,8 @@ __global__ void k_scale_copy(int N, const double* __restrict__ x, double f, doub
 }
 
 // Initial flat flux: x = y = 1, fission source and b for k = 1.
-__global__ void k_fill(int N, double* a, double v) {
+template <typename T>
+__global__ void k_fill(int N, T* a, T v) {
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < N; l += gridDim.x * blockDim.x) a[l] = v;
 }
 
@@ -547,13 +608,40 @@ namespace {
 DiffOp<double> op64(const DiffusionData& d, bool shifted = false) {
   return DiffOp<double>{d.n, d.G, d.F, d.nbr.as<int>(), d.off64.as<double>(), d.diag64.as<double>(),
                         d.mat.as<int>(), d.vol64.as<double>(), d.ss64.as<double>(), d.chi.as<double>(),
-                        d.nsf.as<double>(), d.lam.as<double>() + (shifted ? 0 : 1)};
+                        d.nsf.as<double>(), d.lam.as<double>() + (shifted ? 0 : 1),
+                        shifted ? d.fold64.as<double>() : nullptr};
 }
 
 DiffOp<float> op32(const DiffusionData& d, bool shifted = false) {
   return DiffOp<float>{d.n, d.G, d.F, d.nbr.as<int>(), d.off32.as<float>(), d.diag32.as<float>(),
                        d.mat.as<int>(), d.vol32.as<float>(), d.ss32.as<float>(), d.chi32.as<float>(),
-                       d.nsf32.as<float>(), d.lam.as<double>() + (shifted ? 0 : 1)};
+                       d.nsf32.as<float>(), d.lam.as<double>() + (shifted ? 0 : 1),
+                       shifted ? d.fold32.as<float>() : nullptr};
+}
+
+// DiffOp::fold for the current shift (lam[0]), in precision T.
+template <typename T>
+__global__ void k_fold(int nm, int G, const double* __restrict__ ss, const double* __restrict__ chi,
+                       const double* __restrict__ nsf, const double* __restrict__ lam, T* fold) {
+  const int total = nm * G * G;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < total; r += gridDim.x * blockDim.x) {
+    const int g = r % G, g2 = (r / G) % G, m = r / (G * G);
+    const double v = (g2 != g ? ss[(size_t)m * G * G + g2 * G + g] : 0.0) +
+                     *lam * chi[(size_t)m * G + g] * nsf[(size_t)m * G + g2];
+    fold[r] = (T)v;
+  }
+}
+
+void refold(pgpu_problem* p) {
+  DiffusionData& d = *p->diff;
+  const int total = d.nm * d.G * d.G;
+  launch(p, k_fold<double>, grid_for(total), kThreads, p->stream, d.nm, d.G, (const double*)d.ss64.as<double>(),
+         (const double*)d.chi.as<double>(), (const double*)d.nsf.as<double>(), (const double*)d.lam.as<double>(),
+         d.fold64.as<double>());
+  if (d.have32)
+    launch(p, k_fold<float>, grid_for(total), kThreads, p->stream, d.nm, d.G, (const double*)d.ss64.as<double>(),
+           (const double*)d.chi.as<double>(), (const double*)d.nsf.as<double>(), (const double*)d.lam.as<double>(),
+           d.fold32.as<float>());
 }
 
 __global__ void k_set_scalar(double* p, double v) { *p = v; }
@@ -578,6 +666,7 @@ int make_fp32(pgpu_problem* p) {
   launch(p, k_convert<double, float>, grid_for(d.n), kThreads, s, d.n, d.vol64.as<double>(), d.vol32.as<float>());
   launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G * d.G, d.ss64.as<double>(), d.ss32.as<float>());
   if ((st = dev_alloc(d.chi32, (size_t)d.nm * d.G * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.fold32, (size_t)d.nm * d.G * d.G * 4, &p->bytes))) return st;
   if ((st = dev_alloc(d.nsf32, (size_t)d.nm * d.G * 4, &p->bytes))) return st;
   launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G, d.chi.as<double>(), d.chi32.as<float>());
   launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G, d.nsf.as<double>(), d.nsf32.as<float>());
@@ -593,26 +682,45 @@ int make_fp32(pgpu_problem* p) {
 // SpMV kernels of BiCGStab: the cell form for G = 2, 4, 7, the row form otherwise.
 inline bool cell_form(int G) { return G == 2 || G == 4 || G == 7; }
 
-template <typename T>
-void launch_bicg_v(int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* phat, T* v,
-                   const T* rhat, BiScal* sc, ReduceSlots<1> sl) {
-  switch (A.G) {
-    case 2: k_bicg_v_cell<T, 2><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl); break;
-    case 4: k_bicg_v_cell<T, 4><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl); break;
-    case 7: k_bicg_v_cell<T, 7><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl); break;
-    default: k_bicg_v<T><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl);
-  }
+// form: 0 row (any G), 1 cell, 2 folded row (G = 2, 4, 7 with the fold table)
+template <typename T, int G>
+void launch_v_g(int form, int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* phat, T* v,
+                const T* rhat, BiScal* sc, ReduceSlots<1> sl) {
+  if (form == 1) k_bicg_v_cell<T, G><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl);
+  else k_bicg_v_row<T, G><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl);
+}
+
+template <typename T, int G>
+void launch_t_g(int form, int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* shat, T* t,
+                const T* s, BiScal* sc, ReduceSlots<2> sl) {
+  if (form == 1) k_bicg_t_cell<T, G><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl);
+  else k_bicg_t_row<T, G><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl);
 }
 
 template <typename T>
-void launch_bicg_t(int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* shat, T* t,
-                   const T* s, BiScal* sc, ReduceSlots<2> sl) {
-  switch (A.G) {
-    case 2: k_bicg_t_cell<T, 2><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl); break;
-    case 4: k_bicg_t_cell<T, 4><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl); break;
-    case 7: k_bicg_t_cell<T, 7><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl); break;
-    default: k_bicg_t<T><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl);
+void launch_bicg_v(int form, int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* phat, T* v,
+                   const T* rhat, BiScal* sc, ReduceSlots<1> sl) {
+  if (form != 0 && A.fold) {
+    switch (A.G) {
+      case 2: return launch_v_g<T, 2>(form, blocks, threads, st, A, phat, v, rhat, sc, sl);
+      case 4: return launch_v_g<T, 4>(form, blocks, threads, st, A, phat, v, rhat, sc, sl);
+      case 7: return launch_v_g<T, 7>(form, blocks, threads, st, A, phat, v, rhat, sc, sl);
+    }
   }
+  k_bicg_v<T><<<blocks, threads, 0, st>>>(A, phat, v, rhat, sc, sl);
+}
+
+template <typename T>
+void launch_bicg_t(int form, int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* shat, T* t,
+                   const T* s, BiScal* sc, ReduceSlots<2> sl) {
+  if (form != 0 && A.fold) {
+    switch (A.G) {
+      case 2: return launch_t_g<T, 2>(form, blocks, threads, st, A, shat, t, s, sc, sl);
+      case 4: return launch_t_g<T, 4>(form, blocks, threads, st, A, shat, t, s, sc, sl);
+      case 7: return launch_t_g<T, 7>(form, blocks, threads, st, A, shat, t, s, sc, sl);
+    }
+  }
+  k_bicg_t<T><<<blocks, threads, 0, st>>>(A, shat, t, s, sc, sl);
 }
 
 // ---------------------------------------------------------------------------------
@@ -625,7 +733,7 @@ void launch_bicg_t(int blocks, int threads, cudaStream_t st, const DiffOp<T>& A,
 // ---------------------------------------------------------------------------------
 namespace {
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int>, std::array<int, 4>> g_tune;
+std::map<std::tuple<int, int, int>, std::array<int, 5>> g_tune;
 }  // namespace
 
 template <typename T>
@@ -641,7 +749,7 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
     if (it != g_tune.end()) {
-      for (int k = 0; k < 4; k++) shape[k] = it->second[k];
+      for (int k = 0; k < 5; k++) shape[k] = it->second[k];
       return PGPU_OK;
     }
   }
@@ -656,23 +764,29 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
   init.rho = init.rho_old = init.alpha = init.omega = 1.0;
   BiScal* sc = d.bscal_tune.as<BiScal>();
   PGPU_CUDA(cudaMemcpyAsync(sc, &init, sizeof(init), cudaMemcpyHostToDevice, p->stream));
-  // inputs: zeroed BiCGStab vectors (overwritten by the solve's own initialisation)
-  for (int k = 0; k < 9; k++) PGPU_CUDA(cudaMemsetAsync(w[k].ptr, 0, (size_t)N * sizeof(T), p->stream));
+  // inputs: BiCGStab vectors of ones (overwritten by the solve's own initialisation); not
+  // zeros, whose zero dot product would flag a breakdown and turn the timed launches into
+  // early returns
+  for (int k = 0; k < 9; k++) k_fill<T><<<grid_for(N), kThreads, 0, p->stream>>>(N, w[k].as<T>(), T(1));
+  PGPU_CUDA(cudaGetLastError());
   T *r = w[1].as<T>(), *rhat = w[2].as<T>(), *pp = w[3].as<T>(), *v = w[4].as<T>(), *phat = w[7].as<T>();
   cudaEvent_t e0, e1;
   PGPU_CUDA(cudaEventCreate(&e0));
   PGPU_CUDA(cudaEventCreate(&e1));
   float best[2] = {1e30f, 1e30f};
-  const long long spmv_work = cell_form(d.G) ? d.n : N;
-  int out[4] = {kThreads, grid_for(spmv_work), kThreads, grid_for(d.n)};
-  for (int kind = 0; kind < 2; kind++) {
-    const long long work = kind == 0 ? spmv_work : d.n;
+  int out[5] = {kThreads, grid_for(N), kThreads, grid_for(d.n), 0};
+  const bool fixed_g = cell_form(d.G) && A.fold;
+  for (int kind = 0; kind < 2; kind++)
+   for (int form : {0, 1, 2}) {
+    if (kind == 1 && form != 0) continue;              // cell kernels have one form
+    if (kind == 0 && fixed_g == (form == 0)) continue;  // fixed G: cell or folded row; else row
+    const long long work = kind == 0 && form == 1 ? d.n : (kind == 0 ? N : d.n);
     for (int threads : {128, 256, 512})
       for (int per_sm : {2, 4, 8}) {
         const int blocks = (int)std::max(1LL, std::min<long long>((work + threads - 1) / threads,
                                                                   std::min(kMaxBlocks, per_sm * sms)));
         auto run = [&]() {
-          if (kind == 0) launch_bicg_v<T>(blocks, threads, p->stream, A, phat, v, rhat, sc, slots_of<1>(d));
+          if (kind == 0) launch_bicg_v<T>(form, blocks, threads, p->stream, A, phat, v, rhat, sc, slots_of<1>(d));
           else k_bicg_p<T><<<blocks, threads, 0, p->stream>>>(A, r, pp, v, phat, sc);
         };
         for (int k = 0; k < 2; k++) run();
@@ -687,14 +801,15 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
           best[kind] = ms;
           out[2 * kind] = threads;
           out[2 * kind + 1] = blocks;
+          if (kind == 0) out[4] = form;
         }
       }
-  }
+   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  for (int k = 0; k < 4; k++) shape[k] = out[k];
+  for (int k = 0; k < 5; k++) shape[k] = out[k];
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = {out[0], out[1], out[2], out[3]};
+  g_tune[key] = {out[0], out[1], out[2], out[3], out[4]};
   return PGPU_OK;
 }
 
@@ -708,7 +823,7 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   int tst = tune_bicg<T>(p, A, w);
   if (tst) return tst;
   const int* shp = d.shape[sizeof(T) == 8 ? 0 : 1];
-  const int rT = shp[0], gS = shp[1], cT = shp[2], gC = shp[3];  // SpMV and cell-kernel shapes
+  const int rT = shp[0], gS = shp[1], cT = shp[2], gC = shp[3], form = shp[4];  // SpMV and cell shapes
   const int gN = grid_for(N);                                     // element-wise kernels
   T *x = w[0].as<T>(), *r = w[1].as<T>(), *rhat = w[2].as<T>(), *pp = w[3].as<T>(), *v = w[4].as<T>(),
     *s = w[5].as<T>(), *t = w[6].as<T>(), *phat = w[7].as<T>(), *shat = w[8].as<T>();
@@ -731,11 +846,11 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
     cudaEvent_t e0;
     k_bicg_p<T><<<gC, cT, 0, st>>>(A, r, pp, v, phat, sc);
     if (timed) prof_begin(p, &e0);
-    launch_bicg_v<T>(gS, rT, st, A, phat, v, rhat, sc, slots_of<1>(d));
+    launch_bicg_v<T>(form, gS, rT, st, A, phat, v, rhat, sc, slots_of<1>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
     k_bicg_s<T><<<gC, cT, 0, st>>>(A, r, v, s, shat, sc);
     if (timed) prof_begin(p, &e0);
-    launch_bicg_t<T>(gS, rT, st, A, shat, t, s, sc, slots_of<2>(d));
+    launch_bicg_t<T>(form, gS, rT, st, A, shat, t, s, sc, slots_of<2>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
     k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phat, shat, s, t, rhat, sc, slots_of<2>(d));
   };
@@ -792,6 +907,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   cudaStream_t s = p->stream;
   const int gN = grid_for(N), gC = grid_for(n);
   PGPU_CUDA(cudaMemsetAsync(d.lam.ptr, 0, 2 * sizeof(double), s));
+  refold(p);
   DiffOp<double> A = op64(d, true);
   OuterScal* dos = d.oscal.as<OuterScal>();
   cudaEvent_t e0, e1;
@@ -804,8 +920,8 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   std::memset(&init, 0, sizeof(init));
   init.k = 1.0;
   PGPU_CUDA(cudaMemcpyAsync(dos, &init, sizeof(init), cudaMemcpyHostToDevice, s));
-  launch(p, k_fill, gN, kThreads, s, N, d.y.as<double>(), 1.0);
-  launch(p, k_fill, gC, kThreads, s, n, d.fs_old.as<double>(), 0.0);
+  launch(p, k_fill<double>, gN, kThreads, s, N, d.y.as<double>(), 1.0);
+  launch(p, k_fill<double>, gC, kThreads, s, n, d.fs_old.as<double>(), 0.0);
   launch(p, k_fission_total, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
                                           d.y.as<double>(), d.fs.as<double>(), dos, slots_of<1>(d), 0.0);
   // the first total only normalises the start vector: keep k = 1
@@ -890,6 +1006,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       // estimate is still about dk rho / (1 - rho) below it, so keep 50 |dk| of margin
       lam_s = sh > 0.0 ? 1.0 / std::fmax(os.k * (1.0 + sh), os.k + kShiftMargin * dk) : 0.0;
       launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), lam_s);
+      refold(p);
     }
   }
   if (!converged) status = PGPU_ERR_NOT_CONVERGED;
@@ -1003,6 +1120,7 @@ int pgpu_diffusion_create(int device, const pgpu_diffusion_operator* op, pgpu_pr
   al(d.bscal, sizeof(BiScal));
   al(d.oscal, sizeof(OuterScal));
   al(d.lam, 2 * sizeof(double));
+  al(d.fold64, (size_t)nm * G * G * 8);
   if (st == PGPU_OK && cudaMemsetAsync(d.lam.ptr, 0, 2 * sizeof(double), p->stream) != cudaSuccess)
     st = fail(PGPU_ERR_CUDA, "clearing the shift");
   if (st == PGPU_OK && cudaMemset(d.ticket.ptr, 0, 64) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "memset");
