@@ -53,6 +53,9 @@ WORKLOADS["diffusion_7g_256x256x128_mixed"] = dict(
     kind="diffusion7g", args=dict(), precision="mixed", dtype="f32+f64",
     desc="7-group diffusion k-eigenvalue, 3D Cartesian 256x256x128 (2 cm), 6 materials in 8^3 blocks, "
          "58.7M unknowns, FP32 BiCGStab with FP64 refinement")
+WORKLOADS["diffusion_7g_256x256x128"] = dict(
+    kind="diffusion7g", args=dict(), precision="fp64", dtype="f64",
+    desc="same 7-group 3D diffusion problem, FP64 BiCGStab")
 WORKLOADS["sn_hex_s8_g4_mixed"] = dict(
     kind="snhex", args=dict(), precision="mixed", dtype="f32+f64",
     desc="4-group S8 SN k-eigenvalue on 200x200 hexagonal prisms x 40 layers (1.6M cells, 512M angular "
@@ -60,8 +63,8 @@ WORKLOADS["sn_hex_s8_g4_mixed"] = dict(
 WORKLOADS["serve_diffusion"] = dict(
     kind="serve", args=dict(), precision="mixed", dtype="f32+f64",
     desc="stream of k-eigenvalue diffusion requests (3D Cartesian 16x16x4..128x128x64 log-uniform, G in {2,4,7}, "
-         "+-5% lognormal XS perturbations), Poisson arrivals at 2x the one-at-a-time FP64 rate, continuous batching, "
-         "k to 1e-8")
+         "+-5% lognormal XS perturbations), continuous batching, k to 1e-8; capacity with the whole stream queued, "
+         "p50/p99 latency with Poisson arrivals at 80% of capacity")
 DEFAULT = "sn_s8_64x64x32_g2"
 SOLVE_STATS = os.path.join(ROOT, "profiles", "solve_stats.json")
 
@@ -318,7 +321,7 @@ def run_ours(args, rank, world, local):
     sweeps = results[-1]["sweeps"]
     upload = int(pg.lib().pgpu_problem_upload_bytes(h))
     n_phi = p.field_size("scalar-flux")
-    n_psi = p.field_size("angular-flux")
+    n_psi = p.field_size("angular-flux") if w["kind"] in ("sn", "snhex") else 0
     n_cells = p.field_size("power")
     p.finalize()
 
@@ -410,12 +413,17 @@ def run_ours(args, rank, world, local):
 
 
 def run_serve(args, rank, world, local):
-    """Serving workload: a Poisson stream of diffusion requests of uneven size through the
+    """Serving workload: a stream of diffusion requests of uneven size through the
     pgpu_serve_* continuous-batching server (FP32 inner solves + FP64 refinement), next to
-    the plain FP64 path solving the first requests one at a time.  Every rank serves its
-    own stream (replicas); value is the total over ranks."""
-    import ctypes as C
+    the plain FP64 path solving the first requests one at a time.
+
+    Two passes over the same requests: (1) capacity: every request is submitted at once,
+    value = requests / time to the last answer; (2) latency: Poisson arrivals at 80 % of
+    that capacity, p50/p99 of submit-to-answer.  Requests are built before the timed
+    passes (in a process pool), so the host generator is not what is measured.  Every rank
+    serves its own stream (replicas); value is the total over ranks."""
     import math
+    import multiprocessing as mp
     import queue
     import threading
 
@@ -426,11 +434,6 @@ def run_serve(args, rank, world, local):
     from pampa_gb300 import workloads as wl
 
     dev = local
-    torch.cuda.set_device(dev)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
     rng = np.random.default_rng(4 + rank)
     nreq = args.requests
 
@@ -439,82 +442,84 @@ def run_serve(args, rank, world, local):
 
     specs = [(loguni(16, 128), loguni(16, 128), loguni(4, 64), int(rng.choice([2, 4, 7]))) for _ in range(nreq)]
     seeds = rng.integers(0, 2**31 - 1, size=nreq)
+    procs = max(1, min(16, (os.cpu_count() or 2) // max(1, world)))
+    with mp.get_context("spawn").Pool(procs) as pool:
+        ops = pool.map(wl.diffusion_request_op, [(*specs[k], int(seeds[k])) for k in range(nreq)], chunksize=4)
 
-    def make(k):
-        nx, ny, nz, G = specs[k]
-        return wl.diffusion_request(np.random.default_rng(int(seeds[k])), nx, ny, nz, G)[0]
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
 
     # power iteration to 1e-8 on k and 1e-7 on the fission source, as the small plain
     # workload is specified (served answers are compared at 1 pcm)
     fp64 = pg.default_options(precision=pg.PGPU_FP64, tol_k=1e-8, tol_flux=1e-7)
     mixed = pg.default_options(precision=pg.PGPU_MIXED, tol_k=1e-8, tol_flux=1e-7)
-    # 1. plain FP64, one request at a time, on the first requests of the stream
+    # 0. plain FP64, one request at a time, on the first requests of the stream
     sample = min(nreq, args.serve_sample)
-    ops = [make(k) for k in range(sample)]
     k64 = []
     with pg.Server(dev, slots=1) as srv:
         srv.wait(srv.submit_diffusion(ops[0], fp64))  # warm-up
         t0 = time.perf_counter()
-        for op in ops:
+        for op in ops[:sample]:
             out = srv.wait(srv.submit_diffusion(op, fp64))
             if out["status"] != pg.PGPU_OK:
                 raise RuntimeError(f"FP64 solve failed: {pg.last_error()}")
             k64.append(out["keff"])
         t64 = time.perf_counter() - t0
     rate64 = sample / t64
-    del ops
 
-    # 2. the served stream: arrivals at twice that rate, mixed precision
-    arrivals = np.cumsum(rng.exponential(1.0 / (2.0 * rate64), size=nreq))
-    made = queue.Queue(maxsize=64)
+    def serve(arrivals):
+        """Submits request k at arrivals[k] seconds after the start; returns the results
+        (with completion times) and the wall time from the start to the last answer."""
+        results = [None] * nreq
+        ids = queue.Queue()
+        with pg.Server(dev, slots=args.slots) as srv:
+            srv.wait(srv.submit_diffusion(ops[0], mixed))  # warm-up
 
-    def producer():
-        for k in range(nreq):
-            made.put(make(k))
+            def waiter():
+                while True:
+                    item = ids.get()
+                    if item is None:
+                        return
+                    k, rid = item
+                    results[k] = srv.wait(rid)
+                    results[k]["t_done"] = time.perf_counter()
 
-    results = [None] * nreq
-    ids = queue.Queue()
-    late = []
-    with pg.Server(dev, slots=args.slots) as srv:
-        srv.wait(srv.submit_diffusion(make(0), mixed))  # warm-up
-        prod = threading.Thread(target=producer, daemon=True)
-        prod.start()
-
-        def waiter():
-            while True:
-                item = ids.get()
-                if item is None:
-                    return
-                k, rid = item
-                results[k] = srv.wait(rid)
-                results[k]["t_done"] = time.perf_counter()
-
-        wt = [threading.Thread(target=waiter, daemon=True) for _ in range(4)]
-        for t in wt:
-            t.start()
-        with ClockSampler(dev) as clk:
+            wt = [threading.Thread(target=waiter, daemon=True) for _ in range(4)]
+            for t in wt:
+                t.start()
             t_start = time.perf_counter()
             for k in range(nreq):
-                op = made.get()
                 delay = t_start + arrivals[k] - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                else:
-                    late.append(-delay)
-                ids.put((k, srv.submit_diffusion(op, mixed)))
+                ids.put((k, srv.submit_diffusion(ops[k], mixed)))
             for _ in wt:
                 ids.put(None)
             for t in wt:
                 t.join()
-            t_end = max(r["t_done"] for r in results)
-    bad = [(k, r) for k, r in enumerate(results) if r["status"] != pg.PGPU_OK]
-    if bad:
-        raise RuntimeError(f"{len(bad)} served solves failed: " + "; ".join(
-            f"#{k} {specs[k]} status {r['status']} {r.get('error', '')}" for k, r in bad[:8]))
-    lat = np.array([r["latency_s"] for r in results])
-    wall = t_end - t_start
+        bad = [(k, r) for k, r in enumerate(results) if r["status"] != pg.PGPU_OK]
+        if bad:
+            raise RuntimeError(f"{len(bad)} served solves failed: " + "; ".join(
+                f"#{k} {specs[k]} status {r['status']} {r.get('error', '')}" for k, r in bad[:8]))
+        return results, max(r["t_done"] for r in results) - t_start
+
+    # 1. capacity: the whole stream at once
+    with ClockSampler(dev) as clk:
+        results, wall = serve(np.zeros(nreq))
     value = nreq / wall
+    lat_sat = np.array([r["latency_s"] for r in results])
+    # 2. latency at 80 % of capacity, Poisson arrivals
+    load = 0.8 * value
+    arrivals = np.cumsum(rng.exponential(1.0 / load, size=nreq))
+    results_p, wall_p = serve(arrivals)
+    lat = np.array([r["latency_s"] for r in results_p])
+    run_s = np.array([r["run_s"] for r in results_p])
+
     dk = max(abs(results[k]["keff"] - k64[k]) for k in range(sample))
+    dk_mix = max(abs(a["keff"] - b["keff"]) for a, b in zip(results, results_p))
     launches = sum(r["stats"]["launches"] for r in results)
     cells = np.array([a * b * c for a, b, c, _ in specs], dtype=float)
     unknowns = np.array([a * b * c * G for a, b, c, G in specs], dtype=float)
@@ -522,21 +527,26 @@ def run_serve(args, rank, world, local):
         tt = torch.tensor([value], device=f"cuda:{dev}", dtype=torch.float64)
         dist.all_reduce(tt)
         value = float(tt.item())
+    pct = lambda a, q: 1e3 * float(np.percentile(a, q))  # noqa: E731
     line = dict(metric="k-eigen solves/s (served, continuous batching)", value=value, unit="solves/s",
                 n_gpus=world, steps=nreq, warmup=1, ms_per_step=1e3 * wall / nreq, higher_is_better=True,
                 scaling="weak", vs_baseline=None, dtype="f32+f64", data="synthetic (seeded request generator)",
                 config=dict(workload="serve_diffusion", description=WORKLOADS["serve_diffusion"]["desc"],
                             requests=nreq, slots=args.slots, mean_cells=float(cells.mean()),
-                            mean_unknowns=float(unknowns.mean()), arrival_rate=2.0 * rate64,
-                            arrivals_late_s_max=float(max(late)) if late else 0.0,
+                            mean_unknowns=float(unknowns.mean()),
+                            capacity_pass="all requests submitted at once; value = requests / time to last answer",
                             mean_outer_iterations=float(np.mean([r["stats"]["outer_iterations"] for r in results])),
                             mean_inner_iterations=float(np.mean([r["stats"]["inner_iterations"] for r in results])),
                             l2="requests are independent problems; no flush", parallelism="1 GPU"),
-                latency=dict(p50_ms=1e3 * float(np.percentile(lat, 50)), p99_ms=1e3 * float(np.percentile(lat, 99)),
-                             mean_ms=1e3 * float(lat.mean())),
+                latency=dict(arrivals="Poisson at 80% of the measured capacity", rate=load,
+                             achieved_rate=nreq / wall_p, p50_ms=pct(lat, 50), p99_ms=pct(lat, 99),
+                             mean_ms=1e3 * float(lat.mean()), run_p50_ms=pct(run_s, 50), run_p99_ms=pct(run_s, 99)),
+                latency_saturated=dict(p50_ms=pct(lat_sat, 50), p99_ms=pct(lat_sat, 99),
+                                       note="capacity pass: every request queued at t = 0"),
                 fp64_one_at_a_time=dict(value=rate64, unit="solves/s", sample=sample,
                                         note="plain FP64 path, one request at a time, first requests of the stream"),
-                dk_max_vs_fp64=dk,
+                speedup_vs_fp64_one_at_a_time=value / rate64,
+                dk_max_vs_fp64=dk, dk_max_between_passes=dk_mix,
                 e2e=dict(value=value, unit="solves/s",
                          h2d_bytes_per_step=int(float(np.mean(unknowns * 56 + cells * 36))),
                          d2h_bytes_per_step=8,
@@ -561,7 +571,8 @@ def main():
     ap.add_argument("--size", default=None,
                     help="profiling captures only: NXxNYxNZ box instead of the workload's (the line is then "
                          "not the workload's result)")
-    ap.add_argument("--requests", type=int, default=1024, help="serve_diffusion: requests in the stream")
+    ap.add_argument("--requests", type=int, default=256,
+                    help="serve_diffusion: requests in the stream (built up front: about 19 MB of host memory each)")
     ap.add_argument("--slots", type=int, default=8, help="serve_diffusion: solves in flight at most")
     ap.add_argument("--serve-sample", type=int, default=32,
                     help="serve_diffusion: requests solved one at a time in FP64 for the reference rate")

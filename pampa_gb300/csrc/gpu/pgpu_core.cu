@@ -2,6 +2,8 @@
 // accessors and destruction.
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <set>
 
 #include "pgpu_internal.cuh"
 
@@ -18,22 +20,50 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
-int dev_alloc(DevBuf& b, size_t bytes, long long* counter) {
+// The device's default pool keeps up to this many freed bytes for reuse instead of
+// returning them to the driver at the next synchronisation (a served stream allocates and
+// frees every request's operator).
+constexpr unsigned long long kPoolKeepBytes = 4ull << 30;
+
+static void keep_pool_memory() {
+  static std::mutex mu;
+  static std::set<int> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!done.insert(dev).second) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) return;
+  unsigned long long keep = kPoolKeepBytes;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+}
+
+int dev_alloc(DevBuf& b, size_t bytes, long long* counter, cudaStream_t stream) {
   b.release();
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(&b.ptr, bytes);
+  cudaError_t e;
+  if (stream) {
+    keep_pool_memory();
+    e = cudaMallocAsync(&b.ptr, bytes, stream);
+    // callers may touch the buffer from the host API (synchronous copies and memsets)
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  } else {
+    e = cudaMalloc(&b.ptr, bytes);
+  }
   if (e != cudaSuccess) {
+    if (b.ptr && stream) cudaFreeAsync(b.ptr, stream);
     b.ptr = nullptr;
     return fail(e == cudaErrorMemoryAllocation ? PGPU_ERR_NO_MEMORY : PGPU_ERR_CUDA,
-                std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+                std::string("device allocation(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
   }
   b.bytes = bytes;
+  b.stream = stream;
   if (counter) *counter += (long long)bytes;
   return PGPU_OK;
 }
 
-int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter) {
-  int st = dev_alloc(b, bytes, counter);
+int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter, cudaStream_t stream) {
+  int st = dev_alloc(b, bytes, counter, stream);
   if (st != PGPU_OK) return st;
   if (host && bytes) PGPU_CUDA(cudaMemcpy(b.ptr, host, bytes, cudaMemcpyHostToDevice));
   return PGPU_OK;

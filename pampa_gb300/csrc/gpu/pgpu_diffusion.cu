@@ -656,23 +656,23 @@ int make_fp32(pgpu_problem* p) {
   if (d.have32) return PGPU_OK;
   const size_t nG = (size_t)d.n * d.G;
   int st;
-  if ((st = dev_alloc(d.off32, (size_t)d.F * nG * 4, &p->bytes))) return st;
-  if ((st = dev_alloc(d.diag32, nG * 4, &p->bytes))) return st;
-  if ((st = dev_alloc(d.vol32, (size_t)d.n * 4, &p->bytes))) return st;
-  if ((st = dev_alloc(d.ss32, (size_t)d.nm * d.G * d.G * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.off32, (size_t)d.F * nG * 4, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.diag32, nG * 4, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.vol32, (size_t)d.n * 4, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.ss32, (size_t)d.nm * d.G * d.G * 4, &p->bytes, p->stream))) return st;
   cudaStream_t s = p->stream;
   launch(p, k_convert<double, float>, grid_for((long long)d.F * nG), kThreads, s, (long long)d.F * nG, d.off64.as<double>(), d.off32.as<float>());
   launch(p, k_convert<double, float>, grid_for(nG), kThreads, s, nG, d.diag64.as<double>(), d.diag32.as<float>());
   launch(p, k_convert<double, float>, grid_for(d.n), kThreads, s, d.n, d.vol64.as<double>(), d.vol32.as<float>());
   launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G * d.G, d.ss64.as<double>(), d.ss32.as<float>());
-  if ((st = dev_alloc(d.chi32, (size_t)d.nm * d.G * 4, &p->bytes))) return st;
-  if ((st = dev_alloc(d.fold32, (size_t)d.nm * d.G * d.G * 4, &p->bytes))) return st;
-  if ((st = dev_alloc(d.nsf32, (size_t)d.nm * d.G * 4, &p->bytes))) return st;
+  if ((st = dev_alloc(d.chi32, (size_t)d.nm * d.G * 4, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.fold32, (size_t)d.nm * d.G * d.G * 4, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.nsf32, (size_t)d.nm * d.G * 4, &p->bytes, p->stream))) return st;
   launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G, d.chi.as<double>(), d.chi32.as<float>());
   launch(p, k_convert<double, float>, 1, kThreads, s, (long long)d.nm * d.G, d.nsf.as<double>(), d.nsf32.as<float>());
   for (int k = 0; k < 9; k++)
-    if ((st = dev_alloc(d.w32[k], nG * 4, &p->bytes))) return st;
-  if ((st = dev_alloc(d.r32, nG * 4, &p->bytes))) return st;
+    if ((st = dev_alloc(d.w32[k], nG * 4, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.r32, nG * 4, &p->bytes, p->stream))) return st;
   PGPU_CUDA(cudaGetLastError());
   d.have32 = true;
   return PGPU_OK;
@@ -757,7 +757,7 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
   PGPU_CUDA(cudaGetDevice(&dev));
   PGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   if (!d.bscal_tune.ptr) {
-    int st = dev_alloc(d.bscal_tune, sizeof(BiScal), &p->bytes);
+    int st = dev_alloc(d.bscal_tune, sizeof(BiScal), &p->bytes, p->stream);
     if (st) return st;
   }
   BiScal init{};
@@ -1089,11 +1089,11 @@ int pgpu_diffusion_create(int device, const pgpu_diffusion_operator* op, pgpu_pr
   const size_t nG = (size_t)n * G;
   int st = PGPU_OK;
   auto up = [&](DevBuf& b, const void* h, size_t bytes) {
-    if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes);
+    if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes, p->stream);
     p->uploaded += (long long)bytes;
   };
   auto al = [&](DevBuf& b, size_t bytes) {
-    if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes);
+    if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes, p->stream);
   };
   if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "stream");
   up(d.nbr, op->neighbors, (size_t)F * n * 4);

@@ -32,26 +32,34 @@ int fail(int code, const std::string& msg);
   } while (0)
 
 // ---------------------------------------------------------------------------------
-// Device buffer (RAII).  Allocations are counted per problem.
+// Device buffer (RAII).  Allocations are counted per problem.  A buffer that belongs to a
+// problem comes from the device's stream-ordered pool on the problem's stream and goes
+// back to it in that stream's order: cudaFree would wait for the whole device, which
+// stalls every other solve in flight whenever a served request finishes.
 // ---------------------------------------------------------------------------------
 struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;  // owning problem's stream; null: plain cudaMalloc
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      if (stream) cudaFreeAsync(ptr, stream);
+      else cudaFree(ptr);
+    }
     ptr = nullptr;
     bytes = 0;
+    stream = nullptr;
   }
   template <typename T>
   T* as() const { return static_cast<T*>(ptr); }
 };
 
-int dev_alloc(DevBuf& b, size_t bytes, long long* counter);
-int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter);
+int dev_alloc(DevBuf& b, size_t bytes, long long* counter, cudaStream_t stream = nullptr);
+int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter, cudaStream_t stream = nullptr);
 
 // ---------------------------------------------------------------------------------
 // Launch geometry.  152 SMs on GB300; grids are capped at a multiple of the SM count

@@ -1188,7 +1188,7 @@ int make_fp32(pgpu_problem* p) {
   auto conv = [&](DevBuf& src, DevBuf& dst) -> int {
     if (!src.ptr) return PGPU_OK;
     const long long cnt = (long long)(src.bytes / 8);
-    int st = dev_alloc(dst, (size_t)cnt * 4, &p->bytes);
+    int st = dev_alloc(dst, (size_t)cnt * 4, &p->bytes, p->stream);
     if (st) return st;
     launch(p, k_cast<double, float>, grid_for(cnt), kThreads, s, cnt, src.as<double>(), dst.as<float>());
     return PGPU_OK;
@@ -1231,7 +1231,7 @@ int ensure_rden(pgpu_problem* p, const SNOp<T>& A) {
   if (buf.ptr) return PGPU_OK;
   const long long N = (long long)d.n * d.G * d.M;
   SweepFaces<T> W = make_faces<T>(d);  // rden still null here
-  int st = dev_alloc(buf, (size_t)N * sizeof(T), &p->bytes);
+  int st = dev_alloc(buf, (size_t)N * sizeof(T), &p->bytes, p->stream);
   if (st) return st;
   launch(p, k_sweep_rden<T>, grid_for(N), kThreads, p->stream, A, W, buf.as<T>());
   PGPU_CUDA(cudaGetLastError());
@@ -1254,7 +1254,7 @@ int ensure_coef(pgpu_problem* p, const SNOp<T>& A) {
   if (buf.ptr) return PGPU_OK;
   const long long N = (long long)d.ncls * d.G * d.M;
   SweepFaces<T> W = make_faces<T>(d);
-  int st = dev_alloc(buf, (size_t)N * 4 * sizeof(T), &p->bytes);
+  int st = dev_alloc(buf, (size_t)N * 4 * sizeof(T), &p->bytes, p->stream);
   if (st) return st;
   launch(p, k_sweep_coef<T>, grid_for(N), kThreads, p->stream, A, W, d.ncls, (const int*)d.d_crep.as<int>(),
          buf.as<T>());
@@ -1311,7 +1311,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   int rst = cls ? ensure_coef<T>(p, A) : ensure_rden<T>(p, A);
   if (rst) return rst;
   const SweepFaces<T> W = make_faces<T>(d);
-  if (!d.sweep_ptrs.ptr && (rst = dev_alloc(d.sweep_ptrs, sizeof(SweepPtrs), &p->bytes))) return rst;
+  if (!d.sweep_ptrs.ptr && (rst = dev_alloc(d.sweep_ptrs, sizeof(SweepPtrs), &p->bytes, p->stream))) return rst;
   SweepPtrs* P = d.sweep_ptrs.as<SweepPtrs>();
   // the sweep's launches are captured once per (precision, source kind) and replayed; the
   // buffers of this sweep go through the device-side pointer block
@@ -1388,7 +1388,7 @@ int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y,
   int st;
   if (d.kba) {
     // the dataflow sweep writes per-pattern moments; they are summed in pattern order
-    if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)d.sched.npat * nG * sizeof(double), &p->bytes))) return st;
+    if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)d.sched.npat * nG * sizeof(double), &p->bytes, p->stream))) return st;
     T* mom = d.mom.as<T>();
     if ((st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi, mom))) return st;
     launch(p, k_mom_reduce<T>, grid_for(nG), kThreads, p->stream, (long long)nG, d.sched.npat, (const T*)mom, y);
@@ -1421,21 +1421,21 @@ int ensure_krylov(pgpu_problem* p, size_t len, int restart, int es) {
   SNData& d = *p->sn;
   if (d.basis_len == len && d.restart == restart && d.krylov_prec == es) return PGPU_OK;
   int st;
-  if ((st = dev_alloc(d.basis, (size_t)(restart + 1) * len * es, &p->bytes))) return st;
-  if ((st = dev_alloc(d.wvec, len * es, &p->bytes))) return st;
-  if ((st = dev_alloc(d.xvec, len * es, &p->bytes))) return st;
-  if ((st = dev_alloc(d.rhs, len * es, &p->bytes))) return st;
-  if ((st = dev_alloc(d.tmp, len * es, &p->bytes))) return st;
-  if ((st = dev_alloc(d.partials, (size_t)(restart + 4) * kMaxBlocks * 8, &p->bytes))) return st;
-  if ((st = dev_alloc(d.ticket, (size_t)(restart + 4) * 4, &p->bytes))) return st;
-  if ((st = dev_alloc(d.hbuf, (size_t)4 * (restart + 4) * 8, &p->bytes))) return st;
+  if ((st = dev_alloc(d.basis, (size_t)(restart + 1) * len * es, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.wvec, len * es, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.xvec, len * es, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.rhs, len * es, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.tmp, len * es, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.partials, (size_t)(restart + 4) * kMaxBlocks * 8, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.ticket, (size_t)(restart + 4) * 4, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.hbuf, (size_t)4 * (restart + 4) * 8, &p->bytes, p->stream))) return st;
   if (d.hpin) cudaFreeHost(d.hpin);
   d.hpin = nullptr;
   PGPU_CUDA(cudaMallocHost(&d.hpin, (size_t)4 * (restart + 4) * 8));
   // the scattering source is used by FP64 residual sweeps and by correction sweeps in
   // either precision: size it for FP64
-  if ((st = dev_alloc(d.scat, (size_t)d.n * d.G * 8, &p->bytes))) return st;
-  if ((st = dev_alloc(d.phtmp, (size_t)d.n * d.G * es, &p->bytes))) return st;
+  if ((st = dev_alloc(d.scat, (size_t)d.n * d.G * 8, &p->bytes, p->stream))) return st;
+  if ((st = dev_alloc(d.phtmp, (size_t)d.n * d.G * es, &p->bytes, p->stream))) return st;
   PGPU_CUDA(cudaMemsetAsync(d.ticket.ptr, 0, (size_t)(restart + 4) * 4, p->stream));
   d.basis_len = len;
   d.restart = restart;
@@ -1614,8 +1614,8 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   int st;
   if ((st = ensure_krylov(p, (size_t)len, restart, (int)sizeof(T)))) return st;
   if (d.x64.bytes < (size_t)len * 8) {
-    if ((st = dev_alloc(d.x64, (size_t)len * 8, &p->bytes)) || (st = dev_alloc(d.r64, (size_t)len * 8, &p->bytes)) ||
-        (st = dev_alloc(d.rhs64, (size_t)len * 8, &p->bytes)))
+    if ((st = dev_alloc(d.x64, (size_t)len * 8, &p->bytes, p->stream)) || (st = dev_alloc(d.r64, (size_t)len * 8, &p->bytes, p->stream)) ||
+        (st = dev_alloc(d.rhs64, (size_t)len * 8, &p->bytes, p->stream)))
       return st;
   }
   SNOp<T> A = make_op<T>(d);
@@ -1795,7 +1795,7 @@ int sn_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
     int st = make_fp32(p);
     if (st) return st;
     if (!p->sn->psi32.ptr) {
-      st = dev_alloc(p->sn->psi32, (size_t)p->sn->n * p->sn->G * p->sn->M * 4, &p->bytes);
+      st = dev_alloc(p->sn->psi32, (size_t)p->sn->n * p->sn->G * p->sn->M * 4, &p->bytes, p->stream);
       if (st) return st;
     }
     return solve_T<float>(p, opt, stats);
@@ -2086,11 +2086,11 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
   d.sched = sched;
   st = PGPU_OK;
   auto up = [&](DevBuf& b, const void* h, size_t bytes) {
-    if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes);
+    if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes, p->stream);
     p->uploaded += (long long)bytes;
   };
   auto al = [&](DevBuf& b, size_t bytes) {
-    if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes);
+    if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes, p->stream);
   };
   if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "stream");
   const size_t Fn = (size_t)F * n;

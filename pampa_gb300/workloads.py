@@ -349,6 +349,14 @@ def diffusion_request(rng, nx: int, ny: int, nz: int, G: int, h: float = 2.0, pe
     return cartesian_diffusion_operator(nx, ny, nz, h, layout, mats), mats, layout
 
 
+def diffusion_request_op(spec: tuple) -> dict:
+    """Operator of the serving request spec = (nx, ny, nz, G, seed): diffusion_request with
+    a generator seeded by `seed` (a top-level function, so a process pool can build a
+    stream of requests in parallel)."""
+    nx, ny, nz, G, seed = spec
+    return diffusion_request(np.random.default_rng(int(seed)), int(nx), int(ny), int(nz), int(G))[0]
+
+
 def write_diffusion_input(out_dir: str, nx: int, ny: int, nz: int, h: float, layout: np.ndarray,
                           mats: list[dict]) -> str:
     """The .pmp input of a problem built by cartesian_diffusion_operator (same boundaries)."""
