@@ -475,7 +475,7 @@ def run_serve(args, rank, world, local):
         (with completion times) and the wall time from the start to the last answer."""
         results = [None] * nreq
         ids = queue.Queue()
-        with pg.Server(dev, slots=args.slots) as srv:
+        with pg.Server(dev, slots=args.slots, sm_share=args.sm_share) as srv:
             srv.wait(srv.submit_diffusion(ops[0], mixed))  # warm-up
 
             def waiter():
@@ -532,7 +532,8 @@ def run_serve(args, rank, world, local):
                 n_gpus=world, steps=nreq, warmup=1, ms_per_step=1e3 * wall / nreq, higher_is_better=True,
                 scaling="weak", vs_baseline=None, dtype="f32+f64", data="synthetic (seeded request generator)",
                 config=dict(workload="serve_diffusion", description=WORKLOADS["serve_diffusion"]["desc"],
-                            requests=nreq, slots=args.slots, mean_cells=float(cells.mean()),
+                            requests=nreq, slots=args.slots, sm_share=args.sm_share or "server default",
+                            mean_cells=float(cells.mean()),
                             mean_unknowns=float(unknowns.mean()),
                             capacity_pass="all requests submitted at once; value = requests / time to last answer",
                             mean_outer_iterations=float(np.mean([r["stats"]["outer_iterations"] for r in results])),
@@ -574,6 +575,8 @@ def main():
     ap.add_argument("--requests", type=int, default=256,
                     help="serve_diffusion: requests in the stream (built up front: about 19 MB of host memory each)")
     ap.add_argument("--slots", type=int, default=8, help="serve_diffusion: solves in flight at most")
+    ap.add_argument("--sm-share", type=int, default=None,
+                    help="serve_diffusion: SMs each served solve sizes its grids for (default: the server's)")
     ap.add_argument("--serve-sample", type=int, default=32,
                     help="serve_diffusion: requests solved one at a time in FP64 for the reference rate")
     ap.add_argument("--profile-outer", type=int, default=0,

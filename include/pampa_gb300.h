@@ -225,6 +225,13 @@ int pgpu_problem_get_power(pgpu_problem* p, double* q, double* P, double* total_
 /* Device memory held by the problem, in bytes. */
 long long pgpu_problem_device_bytes(pgpu_problem* p);
 
+/* Size the problem's grids for `sms` streaming multiprocessors (0: the whole device), for
+ * callers that run several solves on one device at once: each solve's small kernels then
+ * leave room for the others' instead of the streams taking turns on a full device.  Results
+ * depend on the share (reduction order), not on what else runs.  Diffusion solves only;
+ * SN solves ignore it.  PGPU_ERR_INVALID for a null problem or sms < 0. */
+int pgpu_problem_set_sm_share(pgpu_problem* p, int sms);
+
 /* Bytes copied host-to-device when the problem was created (the operator). */
 long long pgpu_problem_upload_bytes(pgpu_problem* p);
 
@@ -265,6 +272,9 @@ typedef struct pgpu_server pgpu_server;
 
 int pgpu_serve_create(int device, int slots, double hbm_fraction, pgpu_server** out);
 long long pgpu_serve_budget_bytes(pgpu_server* s);
+/* SMs each solve started from now on sizes its grids for (pgpu_problem_set_sm_share);
+ * the server's default is 2 / slots of the device (0, the whole device, for one slot). */
+int pgpu_serve_set_sm_share(pgpu_server* s, int sms);
 int pgpu_serve_submit_diffusion(pgpu_server* s, const pgpu_diffusion_operator* op, const pgpu_options* opt,
                                 int want_flux, long long* id);
 int pgpu_serve_submit_sn(pgpu_server* s, const pgpu_sn_operator* op, const pgpu_options* opt, int want_flux,

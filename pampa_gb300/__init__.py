@@ -98,12 +98,14 @@ SYMBOLS = {
     "pgpu_problem_get_angular_flux": (C.c_int, [C.c_void_p, _pd]),
     "pgpu_problem_get_power": (C.c_int, [C.c_void_p, _pd, _pd, _pd]),
     "pgpu_problem_device_bytes": (C.c_longlong, [C.c_void_p]),
+    "pgpu_problem_set_sm_share": (C.c_int, [C.c_void_p, C.c_int]),
     "pgpu_problem_upload_bytes": (C.c_longlong, [C.c_void_p]),
     "pgpu_problem_destroy": (None, [C.c_void_p]),
     "pgpu_normalize_power_noalloc": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 5 + [C.c_double, C.c_double]
                                      + [C.c_void_p] * 6),
     "pgpu_serve_create": (C.c_int, [C.c_int, C.c_int, C.c_double, _P(C.c_void_p)]),
     "pgpu_serve_budget_bytes": (C.c_longlong, [C.c_void_p]),
+    "pgpu_serve_set_sm_share": (C.c_int, [C.c_void_p, C.c_int]),
     "pgpu_serve_submit_diffusion": (C.c_int, [C.c_void_p, _P(pgpu_diffusion_operator), _P(pgpu_options), C.c_int,
                                               _P(C.c_longlong)]),
     "pgpu_serve_submit_sn": (C.c_int, [C.c_void_p, _P(pgpu_sn_operator), _P(pgpu_options), C.c_int,
@@ -410,12 +412,14 @@ def diffusion_operator_struct(*, neighbors, offdiag, diag, materials, volumes, s
 class Server:
     """Continuous-batching solve server (pgpu_serve_*): submit operators, wait for results."""
 
-    def __init__(self, device: int = 0, slots: int = 8, hbm_fraction: float = 0.8):
+    def __init__(self, device: int = 0, slots: int = 8, hbm_fraction: float = 0.8, sm_share: int | None = None):
         self._h = C.c_void_p(None)
         st = lib().pgpu_serve_create(device, slots, hbm_fraction, C.byref(self._h))
         if st != PGPU_OK:
             raise PampaError(f"pgpu_serve_create failed ({st}): {last_error()}")
         self._sizes = {}
+        if sm_share is not None and lib().pgpu_serve_set_sm_share(self._h, sm_share) != PGPU_OK:
+            raise PampaError("pgpu_serve_set_sm_share failed")
 
     @property
     def budget_bytes(self) -> int:

@@ -147,6 +147,12 @@ int pgpu_problem_get_power(pgpu_problem* p, double* q, double* P, double* total)
 
 long long pgpu_problem_device_bytes(pgpu_problem* p) { return p ? p->bytes : 0; }
 
+int pgpu_problem_set_sm_share(pgpu_problem* p, int sms) {
+  if (!p || sms < 0) return pgpu::fail(PGPU_ERR_INVALID, "invalid SM share");
+  p->sm_share = sms;
+  return PGPU_OK;
+}
+
 long long pgpu_problem_upload_bytes(pgpu_problem* p) { return p ? p->uploaded : 0; }
 
 void pgpu_problem_destroy(pgpu_problem* p) {

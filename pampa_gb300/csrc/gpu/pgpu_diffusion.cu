@@ -727,13 +727,14 @@ void launch_bicg_t(int form, int blocks, int threads, cudaStream_t st, const Dif
 // Launch-shape autotuner of the BiCGStab kernels.  The row kernels (SpMV fused with
 // products) and the cell kernels (vector update + group-block preconditioner) are timed
 // with CUDA events for threads per block in {128, 256, 512} and at most {2, 4, 8} blocks
-// per SM, on the problem's own operator and vectors, before its first inner solve; the
-// fastest shape per kernel kind is kept for every problem of the same size class
-// (rows rounded to a power of two, groups, precision) in a process-wide table.
+// per SM (within the problem's SM share), on the problem's own operator and vectors,
+// before its first inner solve; the fastest shape per kernel kind is kept for every
+// problem of the same size class (rows rounded to a power of two, groups, precision, SM
+// share) in a process-wide table.
 // ---------------------------------------------------------------------------------
 namespace {
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int>, std::array<int, 5>> g_tune;
+std::map<std::tuple<int, int, int, int>, std::array<int, 5>> g_tune;
 }  // namespace
 
 template <typename T>
@@ -744,7 +745,7 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
   const int N = d.n * d.G;
   int lg = 0;
   while ((1LL << lg) < N) lg++;
-  const auto key = std::make_tuple(lg, d.G, (int)sizeof(T));
+  const auto key = std::make_tuple(lg, d.G, (int)sizeof(T), p->sm_share);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -774,7 +775,7 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
   PGPU_CUDA(cudaEventCreate(&e0));
   PGPU_CUDA(cudaEventCreate(&e1));
   float best[2] = {1e30f, 1e30f};
-  int out[5] = {kThreads, grid_for(N), kThreads, grid_for(d.n), 0};
+  int out[5] = {kThreads, grid_for(N, p->sm_share, kThreads), kThreads, grid_for(d.n, p->sm_share, kThreads), 0};
   const bool fixed_g = cell_form(d.G) && A.fold;
   for (int kind = 0; kind < 2; kind++)
    for (int form : {0, 1, 2}) {
@@ -784,7 +785,8 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
     for (int threads : {128, 256, 512})
       for (int per_sm : {2, 4, 8}) {
         const int blocks = (int)std::max(1LL, std::min<long long>((work + threads - 1) / threads,
-                                                                  std::min(kMaxBlocks, per_sm * sms)));
+                                                                  std::min(grid_cap(p->sm_share, threads),
+                                                                           per_sm * sms)));
         auto run = [&]() {
           if (kind == 0) launch_bicg_v<T>(form, blocks, threads, p->stream, A, phat, v, rhat, sc, slots_of<1>(d));
           else k_bicg_p<T><<<blocks, threads, 0, p->stream>>>(A, r, pp, v, phat, sc);
@@ -824,7 +826,7 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   if (tst) return tst;
   const int* shp = d.shape[sizeof(T) == 8 ? 0 : 1];
   const int rT = shp[0], gS = shp[1], cT = shp[2], gC = shp[3], form = shp[4];  // SpMV and cell shapes
-  const int gN = grid_for(N);                                     // element-wise kernels
+  const int gN = grid_for(N, p->sm_share, kThreads);              // element-wise kernels
   T *x = w[0].as<T>(), *r = w[1].as<T>(), *rhat = w[2].as<T>(), *pp = w[3].as<T>(), *v = w[4].as<T>(),
     *s = w[5].as<T>(), *t = w[6].as<T>(), *phat = w[7].as<T>(), *shat = w[8].as<T>();
   BiScal* sc = d.bscal.as<BiScal>();
@@ -905,7 +907,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   int st;
   if (mixed && (st = make_fp32(p))) return st;
   cudaStream_t s = p->stream;
-  const int gN = grid_for(N), gC = grid_for(n);
+  const int gN = grid_for(N, p->sm_share, kThreads), gC = grid_for(n, p->sm_share, kThreads);
   PGPU_CUDA(cudaMemsetAsync(d.lam.ptr, 0, 2 * sizeof(double), s));
   refold(p);
   DiffOp<double> A = op64(d, true);

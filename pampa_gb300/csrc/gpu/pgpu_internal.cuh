@@ -76,6 +76,19 @@ inline int grid_for(long long work, int threads = kThreads) {
   return (int)b;
 }
 
+// Block cap of a problem's grids of `threads`-thread blocks: its SM share times the
+// blocks of that size one SM holds at 2048 threads (no cap without a share).
+inline int grid_cap(int sm_share, int threads = kThreads) {
+  if (sm_share <= 0) return kMaxBlocks;
+  const int b = sm_share * (2048 / threads);
+  return b < 1 ? 1 : (b > kMaxBlocks ? kMaxBlocks : b);
+}
+
+inline int grid_for(long long work, int sm_share, int threads) {
+  const int b = grid_for(work, threads), c = grid_cap(sm_share, threads);
+  return b < c ? b : c;
+}
+
 // ---------------------------------------------------------------------------------
 // Deterministic multi-value block reduction.  Each block writes NV partial sums; the
 // last block to finish (ticket counter) adds the partials in block order and calls
@@ -169,6 +182,10 @@ struct pgpu_problem {
   long long bytes = 0;     // device memory held
   long long uploaded = 0;  // host-to-device bytes copied at creation
   cudaStream_t stream = nullptr;
+  // SMs this problem sizes its grids for (0: the whole device).  Solves that share the
+  // device (a server's slots) take a share each, so that their kernels run side by side
+  // instead of each small kernel filling the device and the streams taking turns.
+  int sm_share = 0;
   bool solved = false;
   double keff = 0.0;
   pgpu::DiffusionData* diff = nullptr;

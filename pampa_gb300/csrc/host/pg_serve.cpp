@@ -8,6 +8,7 @@
 // runs, and the kernels of concurrent solves overlap on the device.  Every solve uses the
 // same deterministic kernels and its own device state, so a result does not depend on
 // what else runs beside it.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -141,8 +142,11 @@ struct Request {
 
 }  // namespace
 
+constexpr int kShareOverlap = 2;  // device shares of all slots add up to this many devices
+
 struct pgpu_server {
   int device = 0;
+  int sm_share = 0;   // SMs each solve sizes its grids for (0: whole device)
   size_t budget = 0;  // bytes of HBM the in-flight solves may hold
   size_t held = 0;
   int running = 0;
@@ -157,9 +161,10 @@ struct pgpu_server {
 
 namespace {
 
-void run_request(pgpu_server* s, Request* r) {
+void run_request(pgpu_server* s, Request* r, int sm_share) {
   pgpu_problem* p = nullptr;
   int st = r->diff ? pgpu_diffusion_create(s->device, &r->diff->op, &p) : pgpu_sn_create(s->device, &r->sn->op, &p);
+  if (st == PGPU_OK) st = pgpu_problem_set_sm_share(p, sm_share);
   if (st == PGPU_OK) st = pgpu_problem_solve(p, &r->opt, &r->stats);
   if (st == PGPU_OK) st = pgpu_problem_get_keff(p, &r->keff);
   if (st == PGPU_OK && r->want_flux) {
@@ -180,6 +185,7 @@ void worker_loop(pgpu_server* s) {
   cudaSetDevice(s->device);
   for (;;) {
     Request* r = nullptr;
+    int share = 0;
     {
       std::unique_lock<std::mutex> lk(s->mu);
       // first in, first admitted: the head waits until its footprint fits beside the
@@ -195,8 +201,9 @@ void worker_loop(pgpu_server* s) {
       s->held += r->bytes;
       s->running++;
       r->t_start = now_s();
+      share = s->sm_share;
     }
-    run_request(s, r);
+    run_request(s, r, share);
     {
       std::lock_guard<std::mutex> lk(s->mu);
       s->held -= r->bytes;
@@ -266,15 +273,27 @@ int pgpu_serve_create(int device, int slots, double hbm_fraction, pgpu_server** 
   if (cudaSetDevice(device) != cudaSuccess) return PGPU_ERR_CUDA;
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return PGPU_ERR_CUDA;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return PGPU_ERR_CUDA;
   pgpu_server* s = new pgpu_server();
   s->device = device;
   s->budget = (size_t)(hbm_fraction * (double)free_b);
+  // each solve gets kShareOverlap / slots of the device: the slots' small kernels run side
+  // by side, and a large solve still reaches full bandwidth while the others are small
+  s->sm_share = slots == 1 ? 0 : std::min(sms, (kShareOverlap * sms + slots - 1) / slots);
   for (int k = 0; k < slots; k++) s->workers.emplace_back(worker_loop, s);
   *out = s;
   return PGPU_OK;
 }
 
 long long pgpu_serve_budget_bytes(pgpu_server* s) { return s ? (long long)s->budget : 0; }
+
+int pgpu_serve_set_sm_share(pgpu_server* s, int sms) {
+  if (!s || sms < 0) return PGPU_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->sm_share = sms;
+  return PGPU_OK;
+}
 
 int pgpu_serve_submit_diffusion(pgpu_server* s, const pgpu_diffusion_operator* op, const pgpu_options* opt,
                                 int want_flux, long long* id) {
