@@ -726,8 +726,8 @@ void launch_bicg_t(int form, int blocks, int threads, cudaStream_t st, const Dif
 // ---------------------------------------------------------------------------------
 // Launch-shape autotuner of the BiCGStab kernels.  The row kernels (SpMV fused with
 // products) and the cell kernels (vector update + group-block preconditioner) are timed
-// with CUDA events for threads per block in {128, 256, 512} and at most {2, 4, 8} blocks
-// per SM (within the problem's SM share), on the problem's own operator and vectors,
+// with CUDA events for threads per block in {128, 256, 512} and at most {2, 4, 8, 16}
+// blocks per SM (within the problem's SM share), on the problem's own operator and vectors,
 // before its first inner solve; the fastest shape per kernel kind is kept for every
 // problem of the same size class (rows rounded to a power of two, groups, precision, SM
 // share) in a process-wide table.
@@ -783,7 +783,7 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
     if (kind == 0 && fixed_g == (form == 0)) continue;  // fixed G: cell or folded row; else row
     const long long work = kind == 0 && form == 1 ? d.n : (kind == 0 ? N : d.n);
     for (int threads : {128, 256, 512})
-      for (int per_sm : {2, 4, 8}) {
+      for (int per_sm : {2, 4, 8, 16}) {
         const int blocks = (int)std::max(1LL, std::min<long long>((work + threads - 1) / threads,
                                                                   std::min(grid_cap(p->sm_share, threads),
                                                                            per_sm * sms)));

@@ -66,13 +66,14 @@ int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter, cu
 // and loop grid-stride, so partial-sum arrays have a fixed, small size.
 // ---------------------------------------------------------------------------------
 constexpr int kThreads = 256;
-constexpr int kMaxBlocks = 152 * 8;
+constexpr int kMaxGrid = 152 * 8;     // default grid cap of grid-stride kernels
+constexpr int kMaxBlocks = 152 * 16;  // largest grid of a reducing kernel (partial-sum slots)
 constexpr int kMaxGroups = 16;  // groups per cell handled in registers
 
 inline int grid_for(long long work, int threads = kThreads) {
   long long b = (work + threads - 1) / threads;
   if (b < 1) b = 1;
-  if (b > kMaxBlocks) b = kMaxBlocks;
+  if (b > kMaxGrid) b = kMaxGrid;
   return (int)b;
 }
 

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -112,10 +113,12 @@ struct SNData {
   // dataflow tiled sweep of a full Cartesian box (k_sweep_flow), when the operator qualifies
   bool kba = false;
   int kba_nx = 0, kba_ny = 0, kba_ntx = 0, kba_nty = 0, kba_ntz = 0, kba_nd = 0, kba_ntasks = 0, kba_nchunk = 1, kba_gchunk = 1;
+  int kba_npat = 0;  // sweep patterns of the dataflow sweep (octants, split into direction chunks)
   int kba_t[3] = {4, 4, 4};                // tile shape (4x4x4 or 8x8x4)
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
+  DevBuf d_fpat_dirs_ptr, d_fpat_dirs;  // directions of the dataflow sweep's patterns
   DevBuf mom;  // per-pattern scalar-flux moments of the dataflow sweep [npat][n*G]
   DevBuf d_tile_cls, d_tile_ncls, d_cell_lcls;  // per-tile class lists (FlowGeom)
   cudaGraphExec_t sweep_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][iso]
@@ -1326,8 +1329,8 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
     cudaGraph_t graph;
     PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     if (d.kba) {
-      const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, S.npat, d.kba_nd, d.kba_ntasks, d.kba_gchunk, d.kba_nchunk,
-                       d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(),
+      const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, d.kba_npat, d.kba_nd, d.kba_ntasks, d.kba_gchunk, d.kba_nchunk,
+                       d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_fpat_dirs_ptr.as<int>(), d.d_fpat_dirs.as<int>(),
                        cls ? d.d_ccls.as<unsigned short>() : nullptr,
                        cls ? (sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr) : nullptr, d.d_tile_cls.as<int>(),
                        d.d_tile_ncls.as<int>(), d.d_cell_lcls.as<unsigned char>(), d.flow_sync.as<FlowSync>(),
@@ -1388,10 +1391,10 @@ int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y,
   int st;
   if (d.kba) {
     // the dataflow sweep writes per-pattern moments; they are summed in pattern order
-    if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)d.sched.npat * nG * sizeof(double), &p->bytes, p->stream))) return st;
+    if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)d.kba_npat * nG * sizeof(double), &p->bytes, p->stream))) return st;
     T* mom = d.mom.as<T>();
     if ((st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi, mom))) return st;
-    launch(p, k_mom_reduce<T>, grid_for(nG), kThreads, p->stream, (long long)nG, d.sched.npat, (const T*)mom, y);
+    launch(p, k_mom_reduce<T>, grid_for(nG), kThreads, p->stream, (long long)nG, d.kba_npat, (const T*)mom, y);
   } else {
     if ((st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi))) return st;
     launch(p, k_moment<T>, grid_for((long long)nG * 32), kThreads, p->stream, nG, d.M, A.w, psi, y);
@@ -1497,8 +1500,8 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
       // classical Gram-Schmidt with re-orthogonalisation when needed ("twice is enough"):
       // h1 = V^T w (and <w, w>), w -= V h1 with its norm; a second pass only when the
       // norm fell below kReorth of the original (cancellation).
-      const dim3 gd1(std::min(gx, kMaxBlocks / 2), (j + 2 + kGsChunk - 1) / kGsChunk);
-      const dim3 gd(std::min(gx, kMaxBlocks / 2), (j + 1 + kGsChunk - 1) / kGsChunk);
+      const dim3 gd1(std::min(gx, kMaxGrid / 2), (j + 2 + kGsChunk - 1) / kGsChunk);
+      const dim3 gd(std::min(gx, kMaxGrid / 2), (j + 1 + kGsChunk - 1) / kGsChunk);
       double* part = d.partials.as<double>();
       unsigned int* tick = d.ticket.as<unsigned int>();
       launch(p, k_gs_dot<T>, gd1, kThreads, s, len, (const T*)V, len, j + 2, (const T*)wj, h1, part, tick);
@@ -1838,9 +1841,17 @@ void sn_destroy(pgpu_problem* p) {
 // axis for every sweep pattern; returns false (level sweeps are used) otherwise.
 struct KbaPlan {
   int t[3];  // tile shape
-  int ntx, nty, ntz, nd, gchunk, nchunk, ntasks;
-  std::vector<int> tiles, pat_sign;
+  int ntx, nty, ntz, nd, gchunk, nchunk, ntasks, npat;
+  std::vector<int> tiles, pat_sign, pat_dirs_ptr, pat_dirs;
 };
+
+// Directions per dataflow-sweep task at most (0: a whole octant).  Fewer directions per
+// task make each task shorter, and the sweep's critical path is one task per tile
+// diagonal; PGPU_FLOW_DIRS overrides it.
+static int flow_dirs_max() {
+  const char* e = std::getenv("PGPU_FLOW_DIRS");
+  return e ? std::max(0, std::atoi(e)) : 0;
+}
 
 static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) {
   const int nx = op->cart_nx, ny = op->cart_ny, nz = op->cart_nz, n = op->num_cells;
@@ -1862,7 +1873,12 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
           if (inside && op->neighbors[o] != x2 + nx * (y2 + ny * z2)) return false;
         }
       }
+  // the sweep's patterns: every octant's directions, in chunks of at most dmax
+  const int dmax = flow_dirs_max();
   K.nd = 0;
+  K.npat = 0;
+  K.pat_dirs_ptr.assign(1, 0);
+  K.pat_dirs.clear();
   for (int p = 0; p < S.npat; p++) {
     int sg[3] = {0, 0, 0};
     for (int k = S.pat_dirs_ptr[p]; k < S.pat_dirs_ptr[p + 1]; k++) {
@@ -1873,8 +1889,16 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
         sg[a] = s;
       }
     }
-    for (int a = 0; a < 3; a++) K.pat_sign.push_back(sg[a]);
-    K.nd = std::max(K.nd, S.pat_dirs_ptr[p + 1] - S.pat_dirs_ptr[p]);
+    const int d0 = S.pat_dirs_ptr[p], ndp = S.pat_dirs_ptr[p + 1] - d0;
+    const int parts = dmax > 0 ? (ndp + dmax - 1) / dmax : 1;
+    for (int q = 0; q < parts; q++) {
+      const int lo = d0 + (int)((long long)ndp * q / parts), hi = d0 + (int)((long long)ndp * (q + 1) / parts);
+      for (int a = 0; a < 3; a++) K.pat_sign.push_back(sg[a]);
+      for (int k = lo; k < hi; k++) K.pat_dirs.push_back(S.pat_dirs[k]);
+      K.pat_dirs_ptr.push_back((int)K.pat_dirs.size());
+      K.nd = std::max(K.nd, hi - lo);
+      K.npat++;
+    }
   }
   // groups per task: as many as fit in kFlowSlots (group, direction) slots
   K.gchunk = std::max(1, std::min(op->num_groups, kFlowSlots / std::max(1, K.nd)));
@@ -1899,7 +1923,7 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
         K.tiles.push_back(ty);
         K.tiles.push_back(tz);
       }
-  const long long ntasks = (long long)K.ntx * K.nty * K.ntz * S.npat * K.nchunk;
+  const long long ntasks = (long long)K.ntx * K.nty * K.ntz * K.npat * K.nchunk;
   if (ntasks >= (1LL << 31)) return false;
   K.ntasks = (int)ntasks;
   return true;
@@ -2139,9 +2163,12 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       d.kba_ntasks = kp.ntasks;
       d.kba_nchunk = kp.nchunk;
       d.kba_gchunk = kp.gchunk;
+      d.kba_npat = kp.npat;
       for (int a = 0; a < 3; a++) d.kba_t[a] = kp.t[a];
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
       up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
+      up(d.d_fpat_dirs_ptr, kp.pat_dirs_ptr.data(), kp.pat_dirs_ptr.size() * 4);
+      up(d.d_fpat_dirs, kp.pat_dirs.data(), kp.pat_dirs.size() * 4);
       std::vector<unsigned short> ccls;
       std::vector<int> crep;
       if (kba_classes(op, cls, wout, windiag, winw, ccls, crep)) {
