@@ -518,6 +518,10 @@ def run_serve(args, rank, world, local):
     lat = np.array([r["latency_s"] for r in results_p])
     run_s = np.array([r["run_s"] for r in results_p])
 
+    # work of the stream: unknowns x inner iterations summed over requests (a BiCGStab
+    # iteration streams each unknown's vectors and matrix row a fixed number of times)
+    inner = np.array([r["stats"]["inner_iterations"] for r in results], dtype=float)
+    unk_it = float(np.sum(np.array([a * b * c * G for a, b, c, G in specs], dtype=float) * inner))
     dk = max(abs(results[k]["keff"] - k64[k]) for k in range(sample))
     dk_mix = max(abs(a["keff"] - b["keff"]) for a, b in zip(results, results_p))
     launches = sum(r["stats"]["launches"] for r in results)
@@ -538,6 +542,7 @@ def run_serve(args, rank, world, local):
                             capacity_pass="all requests submitted at once; value = requests / time to last answer",
                             mean_outer_iterations=float(np.mean([r["stats"]["outer_iterations"] for r in results])),
                             mean_inner_iterations=float(np.mean([r["stats"]["inner_iterations"] for r in results])),
+                            unknown_iterations=unk_it, unknown_iterations_per_s=unk_it / wall,
                             l2="requests are independent problems; no flush", parallelism="1 GPU"),
                 latency=dict(arrivals="Poisson at 80% of the measured capacity", rate=load,
                              achieved_rate=nreq / wall_p, p50_ms=pct(lat, 50), p99_ms=pct(lat, 99),

@@ -285,6 +285,82 @@ __global__ void k_bicg_x(int N, T* x, T* r, const T* __restrict__ phat, const T*
   }
 }
 
+// Forms of the two cell kernels with G known at compile time (G = 2, 4, 7): the cell's
+// group vectors stay in registers and its loads are issued together.  Same arithmetic
+// in the same order as k_bicg_p / k_bicg_s.
+template <typename T, int G>
+__device__ __forceinline__ void precond_cell_g(const DiffOp<T>& A, int i, const T (&rin)[G], T (&z)[G]) {
+  const T* ssm = A.ss + (size_t)A.mat[i] * G * G;
+  const T V = A.vol[i];
+  const size_t base = (size_t)i * G;
+#pragma unroll
+  for (int g = 0; g < G; g++) {
+    T s = rin[g];
+#pragma unroll
+    for (int g2 = 0; g2 < g; g2++) s += V * ssm[g2 * G + g] * z[g2];
+    z[g] = s / A.diag[base + g];
+  }
+}
+
+template <typename T, int G>
+__global__ void k_bicg_p_cell(DiffOp<T> A, const T* __restrict__ r, T* p, const T* __restrict__ v,
+                              T* phat, const BiScal* sc) {
+  if (sc->converged) return;
+  const double beta = (sc->rho / sc->rho_old) * (sc->alpha / sc->omega);
+  const T tb = (T)beta, tw = (T)sc->omega;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    const size_t base = (size_t)i * G;
+    T pc[G], zc[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) pc[g] = r[base + g] + tb * (p[base + g] - tw * v[base + g]);
+#pragma unroll
+    for (int g = 0; g < G; g++) p[base + g] = pc[g];
+    precond_cell_g<T, G>(A, i, pc, zc);
+#pragma unroll
+    for (int g = 0; g < G; g++) phat[base + g] = zc[g];
+  }
+}
+
+template <typename T, int G>
+__global__ void k_bicg_s_cell(DiffOp<T> A, const T* __restrict__ r, const T* __restrict__ v, T* s, T* shat,
+                              const BiScal* sc) {
+  if (sc->converged) return;
+  const T ta = (T)sc->alpha;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    const size_t base = (size_t)i * G;
+    T sv[G], zc[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) sv[g] = r[base + g] - ta * v[base + g];
+#pragma unroll
+    for (int g = 0; g < G; g++) s[base + g] = sv[g];
+    precond_cell_g<T, G>(A, i, sv, zc);
+#pragma unroll
+    for (int g = 0; g < G; g++) shat[base + g] = zc[g];
+  }
+}
+
+template <typename T>
+void launch_bicg_p(int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* r, T* p, const T* v,
+                   T* phat, const BiScal* sc) {
+  switch (A.G) {
+    case 2: k_bicg_p_cell<T, 2><<<blocks, threads, 0, st>>>(A, r, p, v, phat, sc); return;
+    case 4: k_bicg_p_cell<T, 4><<<blocks, threads, 0, st>>>(A, r, p, v, phat, sc); return;
+    case 7: k_bicg_p_cell<T, 7><<<blocks, threads, 0, st>>>(A, r, p, v, phat, sc); return;
+  }
+  k_bicg_p<T><<<blocks, threads, 0, st>>>(A, r, p, v, phat, sc);
+}
+
+template <typename T>
+void launch_bicg_s(int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* r, const T* v, T* s,
+                   T* shat, const BiScal* sc) {
+  switch (A.G) {
+    case 2: k_bicg_s_cell<T, 2><<<blocks, threads, 0, st>>>(A, r, v, s, shat, sc); return;
+    case 4: k_bicg_s_cell<T, 4><<<blocks, threads, 0, st>>>(A, r, v, s, shat, sc); return;
+    case 7: k_bicg_s_cell<T, 7><<<blocks, threads, 0, st>>>(A, r, v, s, shat, sc); return;
+  }
+  k_bicg_s<T><<<blocks, threads, 0, st>>>(A, r, v, s, shat, sc);
+}
+
 // ---------------------------------------------------------------------------------
 // SpMV forms for G = 2, 4, 7 (the group counts of the workloads), G known at compile time
 // and the in-cell coupling of the shifted operator read from one folded G x G table per
@@ -789,7 +865,7 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
                                                                            per_sm * sms)));
         auto run = [&]() {
           if (kind == 0) launch_bicg_v<T>(form, blocks, threads, p->stream, A, phat, v, rhat, sc, slots_of<1>(d));
-          else k_bicg_p<T><<<blocks, threads, 0, p->stream>>>(A, r, pp, v, phat, sc);
+          else launch_bicg_p<T>(blocks, threads, p->stream, A, r, pp, v, phat, sc);
         };
         for (int k = 0; k < 2; k++) run();
         PGPU_CUDA(cudaEventRecord(e0, p->stream));
@@ -846,11 +922,11 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   // convergence the kernels return at once)
   auto iteration = [&](bool timed) {
     cudaEvent_t e0;
-    k_bicg_p<T><<<gC, cT, 0, st>>>(A, r, pp, v, phat, sc);
+    launch_bicg_p<T>(gC, cT, st, A, r, pp, v, phat, sc);
     if (timed) prof_begin(p, &e0);
     launch_bicg_v<T>(form, gS, rT, st, A, phat, v, rhat, sc, slots_of<1>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
-    k_bicg_s<T><<<gC, cT, 0, st>>>(A, r, v, s, shat, sc);
+    launch_bicg_s<T>(gC, cT, st, A, r, v, s, shat, sc);
     if (timed) prof_begin(p, &e0);
     launch_bicg_t<T>(form, gS, rT, st, A, shat, t, s, sc, slots_of<2>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
