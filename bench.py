@@ -457,18 +457,25 @@ def run_serve(args, rank, world, local):
     fp64 = pg.default_options(precision=pg.PGPU_FP64, tol_k=1e-8, tol_flux=1e-7)
     mixed = pg.default_options(precision=pg.PGPU_MIXED, tol_k=1e-8, tol_flux=1e-7)
     # 0. plain FP64, one request at a time, on the first requests of the stream
-    sample = min(nreq, args.serve_sample)
-    k64 = []
-    with pg.Server(dev, slots=1) as srv:
-        srv.wait(srv.submit_diffusion(ops[0], fp64))  # warm-up
-        t0 = time.perf_counter()
-        for op in ops[:sample]:
-            out = srv.wait(srv.submit_diffusion(op, fp64))
-            if out["status"] != pg.PGPU_OK:
-                raise RuntimeError(f"FP64 solve failed: {pg.last_error()}")
-            k64.append(out["keff"])
-        t64 = time.perf_counter() - t0
+    sample = min(nreq, args.serve_sample) if args.serve_sample > 0 else nreq
+    def one_at_a_time(opts):
+        """keff and run seconds of the sample's requests solved one after the other."""
+        ks, runs = [], []
+        with pg.Server(dev, slots=1) as srv:
+            srv.wait(srv.submit_diffusion(ops[0], opts))  # warm-up
+            t0 = time.perf_counter()
+            for op in ops[:sample]:
+                out = srv.wait(srv.submit_diffusion(op, opts))
+                if out["status"] != pg.PGPU_OK:
+                    raise RuntimeError(f"one-at-a-time solve failed: {out.get('error')}")
+                ks.append(out["keff"])
+                runs.append(out["run_s"])
+            return ks, runs, time.perf_counter() - t0
+
+    k64, run64, t64 = one_at_a_time(fp64)
     rate64 = sample / t64
+    _, run32, t32 = one_at_a_time(mixed)
+    rate32 = sample / t32
 
     def serve(arrivals):
         """Submits request k at arrivals[k] seconds after the start; returns the results
@@ -523,6 +530,22 @@ def run_serve(args, rank, world, local):
     inner = np.array([r["stats"]["inner_iterations"] for r in results], dtype=float)
     unk_it = float(np.sum(np.array([a * b * c * G for a, b, c, G in specs], dtype=float) * inner))
     dk = max(abs(results[k]["keff"] - k64[k]) for k in range(sample))
+    # where the time goes, by request size (quartiles of unknowns over the FP64 sample)
+    unk = np.array([a * b * c * G for a, b, c, G in specs], dtype=float)
+    edges = np.quantile(unk[:sample], [0.25, 0.5, 0.75])
+    by_size = []
+    for q in range(4):
+        lo = edges[q - 1] if q > 0 else -1.0
+        hi = edges[q] if q < 3 else np.inf
+        ks = [k for k in range(sample) if lo < unk[k] <= hi]
+        if not ks:
+            continue
+        by_size.append(dict(requests=len(ks), mean_unknowns=float(np.mean(unk[ks])),
+                            mean_inner_iterations=float(np.mean(inner[ks])),
+                            fp64_alone_mean_ms=1e3 * float(np.mean([run64[k] for k in ks])),
+                            fp64_alone_share=float(np.sum([run64[k] for k in ks]) / np.sum(run64)),
+                            mixed_alone_mean_ms=1e3 * float(np.mean([run32[k] for k in ks])),
+                            served_run_mean_ms=1e3 * float(np.mean([results[k]["run_s"] for k in ks]))))
     dk_mix = max(abs(a["keff"] - b["keff"]) for a, b in zip(results, results_p))
     launches = sum(r["stats"]["launches"] for r in results)
     cells = np.array([a * b * c for a, b, c, _ in specs], dtype=float)
@@ -550,8 +573,12 @@ def run_serve(args, rank, world, local):
                 latency_saturated=dict(p50_ms=pct(lat_sat, 50), p99_ms=pct(lat_sat, 99),
                                        note="capacity pass: every request queued at t = 0"),
                 fp64_one_at_a_time=dict(value=rate64, unit="solves/s", sample=sample,
-                                        note="plain FP64 path, one request at a time, first requests of the stream"),
-                speedup_vs_fp64_one_at_a_time=value / rate64,
+                                        note="plain FP64 path, one request at a time, on the first `sample` "
+                                             "requests of the same stream"),
+                mixed_one_at_a_time=dict(value=rate32, unit="solves/s", sample=sample,
+                                         note="the served precision, one request at a time (no batching)"),
+                speedup_vs_fp64_one_at_a_time=value / rate64, by_size=by_size,
+                capacity_pass_mean_in_flight=float(sum(r["run_s"] for r in results) / wall),
                 dk_max_vs_fp64=dk, dk_max_between_passes=dk_mix,
                 e2e=dict(value=value, unit="solves/s",
                          h2d_bytes_per_step=int(float(np.mean(unknowns * 56 + cells * 36))),
@@ -582,8 +609,9 @@ def main():
     ap.add_argument("--slots", type=int, default=8, help="serve_diffusion: solves in flight at most")
     ap.add_argument("--sm-share", type=int, default=None,
                     help="serve_diffusion: SMs each served solve sizes its grids for (default: the server's)")
-    ap.add_argument("--serve-sample", type=int, default=32,
-                    help="serve_diffusion: requests solved one at a time in FP64 for the reference rate")
+    ap.add_argument("--serve-sample", type=int, default=0,
+                    help="serve_diffusion: requests (first of the stream) solved one at a time in FP64 for "
+                         "the reference rate; 0: all of them")
     ap.add_argument("--profile-outer", type=int, default=0,
                     help="profiling runs under ncu only: cap every solve at this many outer iterations, "
                          "skip the e2e and CPU legs; the printed line is not a benchmark result")

@@ -312,62 +312,6 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
   }
 }
 
-// The same level update for meshes of at most NF faces per cell, with the reciprocal
-// diagonal precomputed: the face loop is unrolled, so a row's face data (normal class,
-// kind, weight, neighbour), then its mu values, then its upwind angular fluxes are each
-// fetched in one round of independent loads instead of one dependent chain per face.
-// Same operations in the same order as k_sweep_level.
-template <typename T, int NF>
-__global__ void k_sweep_level_f(SNOp<T> A, SweepFaces<T> W, int level, const int* __restrict__ pat_dirs_ptr,
-                                const int* __restrict__ pat_dirs, const int* __restrict__ pat_lev_ptr,
-                                const int* __restrict__ pat_nlev, const int* __restrict__ lev_ptr,
-                                const int* __restrict__ order, const SweepPtrs* __restrict__ P, int iso) {
-  const int p = blockIdx.y;
-  if (level >= pat_nlev[p]) return;
-  const T* __restrict__ src = static_cast<const T*>(P->src);
-  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
-  T* psi = static_cast<T*>(P->psi);
-  const int d0 = pat_dirs_ptr[p], nd = pat_dirs_ptr[p + 1] - d0;
-  const int* lp = lev_ptr + pat_lev_ptr[p];
-  const int c0 = lp[level], nc = lp[level + 1] - c0;
-  const int* ord = order + (size_t)p * A.n;
-  const int G = A.G, M = A.M, n = A.n;
-  const int items = nc * G * nd;  // < 2^31 (checked at setup)
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < items; it += gridDim.x * blockDim.x) {
-    const int rest = it / nd;
-    const int di = it - rest * nd;
-    const int ci = rest / G;
-    const int g = rest - ci * G;
-    const int i = ord[c0 + ci];
-    const int m = pat_dirs[d0 + di];
-    const size_t l = ((size_t)i * G + g) * M + m;
-    T num = iso ? src[(size_t)i * G + g] : src[l];
-    const T rd = W.rden[l];
-    const int nfi = A.nf[i];
-    T mu[NF], w[NF];
-    int kd[NF], nb[NF];
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-      const size_t o = (size_t)f * n + i;
-      const bool on = f < nfi;
-      kd[f] = on ? A.kind[o] : -1;
-      w[f] = on ? W.win[o] : T(0);
-      nb[f] = on ? A.nbr[o] : 0;
-      mu[f] = on ? sweep_mu(A, W, f, i, m) : T(1);
-    }
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-      if (mu[f] > T(0)) continue;
-      if (kd[f] == PGPU_FACE_INTERIOR) {
-        num -= (mu[f] * w[f]) * psi[((size_t)nb[f] * G + g) * M + m];
-      } else if (kd[f] == PGPU_FACE_REFLECTIVE && bnd) {
-        num -= (mu[f] * w[f]) * bnd_val(A, bnd, A.rslot[(size_t)f * n + i], g, m);
-      }
-    }
-    psi[l] = num * rd;
-  }
-}
-
 // ---------------------------------------------------------------------------------
 // Dataflow tiled sweep for a full Cartesian box (one persistent launch per sweep).
 //
@@ -1397,12 +1341,9 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
       else
         flow_launch<T, false>(d, p->stream, A, W, K, P, iso);
     } else {
-      // unrolled face loop for meshes of up to 8 faces per cell (rden is always built here)
-      auto kern = !W.rden ? k_sweep_level<T>
-                          : (d.F <= 6 ? k_sweep_level_f<T, 6> : (d.F <= 8 ? k_sweep_level_f<T, 8> : k_sweep_level<T>));
       for (int L = 0; L < S.nlev; L++) {
         dim3 g(S.grid_x[L], S.npat);
-        kern<<<g, kThreads, 0, p->stream>>>(
+        k_sweep_level<T><<<g, kThreads, 0, p->stream>>>(
             A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
             d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
       }
