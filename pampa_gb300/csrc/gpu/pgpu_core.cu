@@ -1,5 +1,6 @@
 // pgpu_* entry points shared by both solver kinds: error state, options, problem
 // accessors and destruction.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -59,6 +60,41 @@ int dev_alloc(DevBuf& b, size_t bytes, long long* counter, cudaStream_t stream) 
   b.bytes = bytes;
   b.stream = stream;
   if (counter) *counter += (long long)bytes;
+  return PGPU_OK;
+}
+
+namespace {
+struct PinnedScratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  ~PinnedScratch() {
+    if (ptr) cudaFreeHost(ptr);
+  }
+};
+thread_local PinnedScratch t_pinned;
+}  // namespace
+
+void* pinned_scratch(size_t bytes) {
+  if (t_pinned.bytes < bytes) {
+    if (t_pinned.ptr) cudaFreeHost(t_pinned.ptr);
+    t_pinned.ptr = nullptr;
+    t_pinned.bytes = 0;
+    const size_t n = std::max<size_t>(bytes, 4096);
+    if (cudaMallocHost(&t_pinned.ptr, n) != cudaSuccess) {
+      t_pinned.ptr = nullptr;
+      return nullptr;
+    }
+    t_pinned.bytes = n;
+  }
+  return t_pinned.ptr;
+}
+
+int read_small(void* host, const void* dev, size_t n, cudaStream_t s) {
+  void* h = pinned_scratch(n);
+  if (!h) return fail(PGPU_ERR_CUDA, "page-locked host scratch");
+  PGPU_CUDA(cudaMemcpyAsync(h, dev, n, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(cudaStreamSynchronize(s));
+  std::memcpy(host, h, n);
   return PGPU_OK;
 }
 

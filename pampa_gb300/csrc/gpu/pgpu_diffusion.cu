@@ -840,7 +840,7 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
   BiScal init{};
   init.rho = init.rho_old = init.alpha = init.omega = 1.0;
   BiScal* sc = d.bscal_tune.as<BiScal>();
-  PGPU_CUDA(cudaMemcpyAsync(sc, &init, sizeof(init), cudaMemcpyHostToDevice, p->stream));
+  k_put<BiScal><<<1, 1, 0, p->stream>>>(sc, init);
   // inputs: BiCGStab vectors of ones (overwritten by the solve's own initialisation); not
   // zeros, whose zero dot product would flag a breakdown and turn the timed launches into
   // early returns
@@ -955,24 +955,18 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
     }
     p->launches += 5LL * chunk;
     PGPU_CUDA(cudaGetLastError());
-    PGPU_CUDA(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, st));
-    PGPU_CUDA(cudaStreamSynchronize(st));
+    if (int rst = read_small(&hs, sc, sizeof(hs), st)) return rst;
     if (hs.converged) break;
     if (chunk < 16 && !p->profile) chunk *= 2;
   }
-  PGPU_CUDA(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, st));
-  PGPU_CUDA(cudaStreamSynchronize(st));
+  if (int rst = read_small(&hs, sc, sizeof(hs), st)) return rst;
   p->prof_bytes += p->profile ? 2.0 * hs.iters * spmv_bytes : 0.0;
   *iters_out = hs.iters;
   if (!(hs.rr == hs.rr)) return fail(PGPU_ERR_NAN, "NaN in the inner Krylov solve");
   return PGPU_OK;
 }
 
-int read_outer(pgpu_problem* p, OuterScal& os) {
-  PGPU_CUDA(cudaMemcpyAsync(&os, p->diff->oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
-  PGPU_CUDA(cudaStreamSynchronize(p->stream));
-  return PGPU_OK;
-}
+int read_outer(pgpu_problem* p, OuterScal& os) { return read_small(&os, p->diff->oscal.ptr, sizeof(os), p->stream); }
 
 }  // namespace
 
@@ -997,7 +991,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   OuterScal init;
   std::memset(&init, 0, sizeof(init));
   init.k = 1.0;
-  PGPU_CUDA(cudaMemcpyAsync(dos, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+  launch(p, k_put<OuterScal>, 1, 1, s, dos, init);
   launch(p, k_fill<double>, gN, kThreads, s, N, d.y.as<double>(), 1.0);
   launch(p, k_fill<double>, gC, kThreads, s, n, d.fs_old.as<double>(), 0.0);
   launch(p, k_fission_total, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.nsf.as<double>(),
@@ -1007,7 +1001,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   if ((st = read_outer(p, os))) return st;
   if (os.nonfinite || os.S <= 0.0) return fail(PGPU_ERR_INVALID, "no fission source in the initial flux");
   os.k = 1.0;
-  PGPU_CUDA(cudaMemcpyAsync(dos, &os, sizeof(os), cudaMemcpyHostToDevice, s));
+  launch(p, k_put<OuterScal>, 1, 1, s, dos, os);
   launch(p, k_normalize_source, gC, kThreads, s, n, G, d.mat.as<int>(), d.chi.as<double>(), d.y.as<double>(),
                                              d.x.as<double>(), d.fs.as<double>(), d.fs_old.as<double>(),
                                              d.b.as<double>(), dos, slots_of<2>(d));
@@ -1125,8 +1119,7 @@ int diffusion_get_power(pgpu_problem* p, double* q, double* P, double* total) {
   if (q) PGPU_CUDA(cudaMemcpyAsync(q, d.q.ptr, (size_t)d.n * 8, cudaMemcpyDeviceToHost, p->stream));
   if (P) PGPU_CUDA(cudaMemcpyAsync(P, d.P.ptr, (size_t)d.n * 8, cudaMemcpyDeviceToHost, p->stream));
   OuterScal os;
-  PGPU_CUDA(cudaMemcpyAsync(&os, d.oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
-  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  if (int rst = read_small(&os, d.oscal.ptr, sizeof(os), p->stream)) return rst;
   if (total) *total = os.total_power;
   return PGPU_OK;
 }

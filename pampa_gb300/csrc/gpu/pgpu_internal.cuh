@@ -59,6 +59,23 @@ struct DevBuf {
 };
 
 int dev_alloc(DevBuf& b, size_t bytes, long long* counter, cudaStream_t stream = nullptr);
+
+// Page-locked host scratch of the calling thread (grows on demand, freed when the thread
+// exits), for the small device-to-host reads of a solve's control scalars.  A read into
+// pageable memory goes through the driver's staging path, which solves running on other
+// host threads then wait for; from page-locked memory it is a plain DMA on the stream.
+void* pinned_scratch(size_t bytes);
+
+// Reads n bytes of device memory (ordered on stream s) into host memory through the
+// thread's page-locked scratch; the stream is synchronised.
+int read_small(void* host, const void* dev, size_t n, cudaStream_t s);
+
+// Writes a small value to device memory in stream order, as a kernel argument (no host
+// buffer has to outlive the call).
+template <typename V>
+__global__ void k_put(V* dst, V v) {
+  *dst = v;
+}
 int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter, cudaStream_t stream = nullptr);
 
 // ---------------------------------------------------------------------------------

@@ -1480,8 +1480,7 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
     }
     launch(p, k_norm2<T>, gx, kThreads, s, len, (const T*)V, hn, nslot);
     double beta;
-    PGPU_CUDA(cudaMemcpyAsync(&beta, hn, 8, cudaMemcpyDeviceToHost, s));
-    PGPU_CUDA(cudaStreamSynchronize(s));
+    if ((st = read_small(&beta, hn, 8, s))) return st;
     if (!(beta == beta)) return fail(PGPU_ERR_NAN, "NaN in the transport correction solve");
     if (first) {
       tol = std::fmax(rtol * beta, atol);
@@ -1580,9 +1579,9 @@ int norm_of(pgpu_problem* p, long long len, const T* x, double* out) {
 int read_outer(pgpu_problem* p, SNOuter& os) {
   SNData& d = *p->sn;
   FlowSync fs{0u, 0u, 0u, 0u};
-  PGPU_CUDA(cudaMemcpyAsync(&os, d.oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
-  if (d.kba) PGPU_CUDA(cudaMemcpyAsync(&fs, d.flow_sync.ptr, sizeof(fs), cudaMemcpyDeviceToHost, p->stream));
-  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  int st = read_small(&os, d.oscal.ptr, sizeof(os), p->stream);
+  if (st == PGPU_OK && d.kba) st = read_small(&fs, d.flow_sync.ptr, sizeof(fs), p->stream);
+  if (st) return st;
   if (fs.error) return fail(PGPU_ERR_TIMEOUT, "sweep: a wait for an upwind tile ran out (kernel returned early)");
   return PGPU_OK;
 }
@@ -1647,7 +1646,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   SNOuter init;
   std::memset(&init, 0, sizeof(init));
   init.k = 1.0;
-  PGPU_CUDA(cudaMemcpyAsync(dos, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+  launch(p, k_put<SNOuter>, 1, 1, s, dos, init);
   if (d.kba) PGPU_CUDA(cudaMemsetAsync(&d.flow_sync.as<FlowSync>()->error, 0, sizeof(unsigned int), s));
   launch(p, k_fill<double>, gG, kThreads, s, (long long)nG, phi0, 1.0);
   PGPU_CUDA(cudaMemsetAsync(x64, 0, len * 8, s));
@@ -1658,7 +1657,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   if ((st = read_outer(p, os))) return st;
   if (os.nonfinite || os.S <= 0.0) return fail(PGPU_ERR_INVALID, "no fission source in the initial flux");
   os.k = 1.0;
-  PGPU_CUDA(cudaMemcpyAsync(dos, &os, sizeof(os), cudaMemcpyHostToDevice, s));
+  launch(p, k_put<SNOuter>, 1, 1, s, dos, os);
   PGPU_CUDA(cudaMemsetAsync(d.fs_old.ptr, 0, (size_t)n * 8, s));
   launch(p, k_sn_source, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.chi.as<double>(),
          d.fs.as<double>(), d.fs_old.as<double>(), bsrc, dos, s2);
@@ -1825,8 +1824,7 @@ int sn_get_power(pgpu_problem* p, double* q, double* P, double* total) {
   if (q) PGPU_CUDA(cudaMemcpyAsync(q, d.q.ptr, (size_t)d.n * 8, cudaMemcpyDeviceToHost, p->stream));
   if (P) PGPU_CUDA(cudaMemcpyAsync(P, d.P.ptr, (size_t)d.n * 8, cudaMemcpyDeviceToHost, p->stream));
   SNOuter os;
-  PGPU_CUDA(cudaMemcpyAsync(&os, d.oscal.ptr, sizeof(os), cudaMemcpyDeviceToHost, p->stream));
-  PGPU_CUDA(cudaStreamSynchronize(p->stream));
+  if (int rst = read_small(&os, d.oscal.ptr, sizeof(os), p->stream)) return rst;
   if (total) *total = os.total_power;
   return PGPU_OK;
 }
