@@ -106,3 +106,27 @@ def test_seven_group_3d(precision, tmp_path):
         k_tol, f_tol = (K_TOL, FLUX_TOL) if precision == "fp64" else (1e-5, 1e-4)
         assert abs(p.keff - ref["keff"]) <= k_tol, (p.keff, ref["keff"])
         assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= f_tol
+
+
+@pytest.mark.parametrize("G,precision", [(2, "fp64"), (4, "mixed"), (7, "fp64"), (7, "mixed")])
+def test_inner_solve_paths_agree(G, precision, tmp_path):
+    """The one-launch cluster inner solve (problems up to 2^19 rows, G = 2, 4, 7) and the
+    multi-kernel inner solve (larger problems; forced here by profile mode, which times
+    its kernels) converge to the same eigenpair, and both match the oracle."""
+    from pampa_gb300 import workloads as wl
+    rng = np.random.default_rng(7 + G)
+    nx, ny, nz = 12, 10, 6
+    op, mats, layout = wl.diffusion_request(rng, nx, ny, nz, G, block=2)
+    prec = pg.PGPU_FP64 if precision == "fp64" else pg.PGPU_MIXED
+    with pg.DiffusionProblem(**op) as dp:
+        a = dp.solve(precision=prec)
+        phi_a = dp.scalar_flux()
+        b = dp.solve(precision=prec, profile=1)
+        phi_b = dp.scalar_flux()
+    k_tol, f_tol = (K_TOL, FLUX_TOL) if precision == "fp64" else (1e-5, 1e-4)
+    assert abs(a.keff - b.keff) <= k_tol
+    assert rel_l2(phi_a, phi_b) <= f_tol
+    ref = po.run_input(wl.write_diffusion_input(str(tmp_path), nx, ny, nz, 2.0, layout, mats))
+    for res, phi in ((a, phi_a), (b, phi_b)):
+        assert abs(res.keff - ref["keff"]) <= k_tol, (res.keff, ref["keff"])
+        assert rel_l2(phi, ref["phi"]) <= f_tol
