@@ -23,8 +23,6 @@
 #include <mutex>
 #include <tuple>
 
-#include <cooperative_groups.h>
-
 #include "pgpu_internal.cuh"
 
 namespace pgpu {
@@ -760,267 +758,6 @@ int make_fp32(pgpu_problem* p) {
 // SpMV kernels of BiCGStab: the cell form for G = 2, 4, 7, the row form otherwise.
 inline bool cell_form(int G) { return G == 2 || G == 4 || G == 7; }
 
-// ---------------------------------------------------------------------------------
-// Whole inner solve in one launch for small problems: one thread-block cluster of
-// kClusterCTAs CTAs runs every BiCGStab iteration, with the cluster's hardware barrier
-// between the phases and the dot products summed across the cluster through distributed
-// shared memory.  A small problem's iteration is five launches of a few microseconds
-// each on the multi-kernel path (plus a host read per chunk); here it is a handful of
-// barriers, and a server's small requests each hold kClusterCTAs SMs instead of
-// queueing their launches on the whole device.
-//
-// Every CTA reads all the CTAs' partial sums in rank order, so all of them compute the
-// same scalars, take the same branches and leave the loop at the same iteration (the
-// barrier needs every CTA each time).  Vectors written inside the launch are read with
-// ld.global.cg (L2, the point where the CTAs' writes meet); the operator is read-only.
-// Same iteration, scalars and stopping tests as the multi-kernel path (k_bicg_*).
-// ---------------------------------------------------------------------------------
-constexpr int kClusterCTAs = 8;
-constexpr int kClusterThreads = 1024;
-constexpr long long kClusterMaxRows = 1 << 19;  // rows above this use the multi-kernel path
-
-template <int NV>
-__device__ __forceinline__ void cluster_sum(double (&v)[NV], double (*red)[NV], int& buf, double (&tot)[NV]) {
-  namespace cg = cooperative_groups;
-  cg::cluster_group cluster = cg::this_cluster();
-  __shared__ double sh[NV][32];
-  warp_sum<NV>(v);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < NV; k++) sh[k][warp] = v[k];
-  __syncthreads();
-  if (warp == 0) {
-    double w[NV];
-#pragma unroll
-    for (int k = 0; k < NV; k++) w[k] = lane < nw ? sh[k][lane] : 0.0;
-    warp_sum<NV>(w);
-    if (lane == 0)
-#pragma unroll
-      for (int k = 0; k < NV; k++) red[buf][k] = w[k];
-  }
-  cluster.sync();  // every CTA's partial is in its shared memory
-#pragma unroll
-  for (int k = 0; k < NV; k++) tot[k] = 0.0;
-  for (int r = 0; r < kClusterCTAs; r++) {
-    const double* rp = cluster.map_shared_rank(&red[buf][0], r);
-#pragma unroll
-    for (int k = 0; k < NV; k++) tot[k] += rp[k];
-  }
-  // the other buffer next time: this one is overwritten only after the next reduction's
-  // barrier, which every CTA reaches after reading it
-  buf ^= 1;
-}
-
-template <typename T, int G>
-__device__ __forceinline__ void precond_cell_cg(const DiffOp<T>& A, int i, const T (&rin)[G], T (&z)[G]) {
-  const T* ssm = A.ss + (size_t)A.mat[i] * G * G;
-  const T V = A.vol[i];
-  const size_t base = (size_t)i * G;
-#pragma unroll
-  for (int g = 0; g < G; g++) {
-    T acc = rin[g];
-#pragma unroll
-    for (int g2 = 0; g2 < g; g2++) acc += V * ssm[g2 * G + g] * z[g2];
-    z[g] = acc / A.diag[base + g];
-  }
-}
-
-// y = A x for the G rows of cell i (folded in-cell table), x read through L2
-template <typename T, int G>
-__device__ __forceinline__ void apply_cell_cg(const DiffOp<T>& A, const T* x, int i, T (&y)[G]) {
-  const size_t base = (size_t)i * G;
-  T xc[G];
-#pragma unroll
-  for (int g = 0; g < G; g++) xc[g] = __ldcg(x + base + g);
-  const T* fm = A.fold + (size_t)A.mat[i] * G * G;
-  const T vol = A.vol[i];
-#pragma unroll
-  for (int g = 0; g < G; g++) {
-    T sc = T(0);
-#pragma unroll
-    for (int g2 = 0; g2 < G; g2++) sc += fm[g2 * G + g] * xc[g2];
-    y[g] = A.diag[base + g] * xc[g] - vol * sc;
-  }
-  const size_t nG = (size_t)A.n * G;
-  for (int fa = 0; fa < A.F; fa++) {
-    const int j = A.nbr[(size_t)fa * A.n + i];
-    if (j >= 0) {
-      const T* o = A.off + fa * nG + base;
-      const T* xj = x + (size_t)j * G;
-#pragma unroll
-      for (int g = 0; g < G; g++) y[g] += o[g] * __ldcg(xj + g);
-    }
-  }
-}
-
-template <typename T, int G>
-__global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kClusterThreads, 1)
-    k_bicg_cluster(DiffOp<T> A, const T* rin, T* x, T* r, T* rhat, T* p, T* v, T* s, T* t, T* phat, T* shat,
-                   BiScal* out, double rtol, int max_iters) {
-  namespace cg = cooperative_groups;
-  cg::cluster_group cluster = cg::this_cluster();
-  __shared__ double red2[2][2];
-  __shared__ double red1[2][1];
-  int b1 = 0, b2 = 0;
-  const int rank = (int)cluster.block_rank();
-  const int n = A.n;
-  const int c0 = (int)((long long)n * rank / kClusterCTAs), c1 = (int)((long long)n * (rank + 1) / kClusterCTAs);
-  const int tid = threadIdx.x, nt = blockDim.x;
-  // rhat = r = rin; x = p = v = 0; rho = rr = bb = (r, r)
-  T part = T(0);
-  for (int i = c0 + tid; i < c1; i += nt)
-#pragma unroll
-    for (int g = 0; g < G; g++) {
-      const size_t l = (size_t)i * G + g;
-      const T val = rin[l];
-      r[l] = val;
-      rhat[l] = val;
-      x[l] = T(0);
-      p[l] = T(0);
-      v[l] = T(0);
-      part += val * val;
-    }
-  double a1[1] = {(double)part}, t1[1];
-  cluster_sum<1>(a1, red1, b1, t1);
-  double rho = t1[0], rho_old = 1.0, alpha = 1.0, omega = 1.0, rr = t1[0];
-  const double bb = t1[0], tol2 = rtol * rtol * t1[0];
-  int iters = 0, breakdown = 0;
-  int converged = (t1[0] <= tol2) || !(t1[0] == t1[0]) || t1[0] == 0.0;
-  while (!converged) {
-    // p = r + beta (p - omega v); phat = M^-1 p
-    const double beta = (rho / rho_old) * (alpha / omega);
-    const T tb = (T)beta, tw = (T)omega;
-    for (int i = c0 + tid; i < c1; i += nt) {
-      const size_t base = (size_t)i * G;
-      T pc[G], zc[G];
-#pragma unroll
-      for (int g = 0; g < G; g++) pc[g] = __ldcg(r + base + g) + tb * (__ldcg(p + base + g) - tw * __ldcg(v + base + g));
-#pragma unroll
-      for (int g = 0; g < G; g++) p[base + g] = pc[g];
-      precond_cell_cg<T, G>(A, i, pc, zc);
-#pragma unroll
-      for (int g = 0; g < G; g++) phat[base + g] = zc[g];
-    }
-    cluster.sync();  // phat complete (the SpMV reads neighbours of other CTAs)
-    // v = A phat; alpha = rho / (rhat, v)
-    part = T(0);
-    for (int i = c0 + tid; i < c1; i += nt) {
-      T y[G];
-      apply_cell_cg<T, G>(A, phat, i, y);
-      const size_t base = (size_t)i * G;
-#pragma unroll
-      for (int g = 0; g < G; g++) {
-        v[base + g] = y[g];
-        part += __ldcg(rhat + base + g) * y[g];
-      }
-    }
-    a1[0] = (double)part;
-    cluster_sum<1>(a1, red1, b1, t1);
-    if (t1[0] == 0.0 || !(t1[0] == t1[0])) {
-      breakdown = 1;
-      converged = 1;
-      break;
-    }
-    alpha = rho / t1[0];
-    // s = r - alpha v; shat = M^-1 s
-    const T ta = (T)alpha;
-    for (int i = c0 + tid; i < c1; i += nt) {
-      const size_t base = (size_t)i * G;
-      T sv[G], zc[G];
-#pragma unroll
-      for (int g = 0; g < G; g++) sv[g] = __ldcg(r + base + g) - ta * __ldcg(v + base + g);
-#pragma unroll
-      for (int g = 0; g < G; g++) s[base + g] = sv[g];
-      precond_cell_cg<T, G>(A, i, sv, zc);
-#pragma unroll
-      for (int g = 0; g < G; g++) shat[base + g] = zc[g];
-    }
-    cluster.sync();  // shat complete
-    // t = A shat; omega = (t, s) / (t, t)
-    T q0 = T(0), q1 = T(0);
-    for (int i = c0 + tid; i < c1; i += nt) {
-      T y[G];
-      apply_cell_cg<T, G>(A, shat, i, y);
-      const size_t base = (size_t)i * G;
-#pragma unroll
-      for (int g = 0; g < G; g++) {
-        t[base + g] = y[g];
-        q0 += y[g] * __ldcg(s + base + g);
-        q1 += y[g] * y[g];
-      }
-    }
-    double a2[2] = {(double)q0, (double)q1}, t2[2];
-    cluster_sum<2>(a2, red2, b2, t2);
-    if (t2[1] == 0.0 || !(t2[1] == t2[1])) {
-      omega = 0.0;
-      breakdown = 1;
-    } else {
-      omega = t2[0] / t2[1];
-    }
-    // x += alpha phat + omega shat; r = s - omega t; rho = (rhat, r); rr = (r, r)
-    const T tw2 = (T)omega;
-    q0 = T(0);
-    q1 = T(0);
-    for (int i = c0 + tid; i < c1; i += nt) {
-      const size_t base = (size_t)i * G;
-#pragma unroll
-      for (int g = 0; g < G; g++) {
-        const size_t l = base + g;
-        x[l] = __ldcg(x + l) + ta * __ldcg(phat + l) + tw2 * __ldcg(shat + l);
-        const T rv = __ldcg(s + l) - tw2 * __ldcg(t + l);
-        r[l] = rv;
-        q0 += __ldcg(rhat + l) * rv;
-        q1 += rv * rv;
-      }
-    }
-    a2[0] = (double)q0;
-    a2[1] = (double)q1;
-    cluster_sum<2>(a2, red2, b2, t2);
-    rho_old = rho;
-    rho = t2[0];
-    rr = t2[1];
-    iters += 1;
-    const bool bad = !(t2[1] == t2[1]);
-    if (t2[1] <= tol2 || iters >= max_iters || breakdown || bad) converged = 1;
-    if (t2[0] == 0.0) converged = 1;
-  }
-  if (rank == 0 && tid == 0) {
-    BiScal o;
-    o.rho = rho;
-    o.rho_old = rho_old;
-    o.alpha = alpha;
-    o.omega = omega;
-    o.rr = rr;
-    o.bb = bb;
-    o.tol2 = tol2;
-    o.converged = converged;
-    o.breakdown = breakdown;
-    o.iters = iters;
-    o.max_iters = max_iters;
-    *out = o;
-  }
-  cluster.sync();  // no CTA leaves while another may still read its shared memory
-}
-
-template <typename T>
-bool launch_bicg_cluster(cudaStream_t st, const DiffOp<T>& A, const T* rin, T* const* w, BiScal* out, double rtol,
-                         int max_iters) {
-  // w: x, r, rhat, p, v, s, t, phat, shat
-  switch (A.G) {
-    case 2:
-      k_bicg_cluster<T, 2><<<kClusterCTAs, kClusterThreads, 0, st>>>(A, rin, w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7], w[8], out, rtol, max_iters);
-      return true;
-    case 4:
-      k_bicg_cluster<T, 4><<<kClusterCTAs, kClusterThreads, 0, st>>>(A, rin, w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7], w[8], out, rtol, max_iters);
-      return true;
-    case 7:
-      k_bicg_cluster<T, 7><<<kClusterCTAs, kClusterThreads, 0, st>>>(A, rin, w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7], w[8], out, rtol, max_iters);
-      return true;
-  }
-  return false;
-}
-
 // form: 0 row (any G), 1 cell, 2 folded row (G = 2, 4, 7 with the fold table)
 template <typename T, int G>
 void launch_v_g(int form, int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* phat, T* v,
@@ -1166,18 +903,6 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   BiScal hs;
   T *x = w[0].as<T>(), *r = w[1].as<T>(), *rhat = w[2].as<T>(), *pp = w[3].as<T>(), *v = w[4].as<T>(),
     *s = w[5].as<T>(), *t = w[6].as<T>(), *phat = w[7].as<T>(), *shat = w[8].as<T>();
-  if (A.fold && N <= kClusterMaxRows && !p->profile) {
-    // small problem: the whole inner solve in one cluster launch
-    T* const wv[9] = {x, r, rhat, pp, v, s, t, phat, shat};
-    if (launch_bicg_cluster<T>(st, A, rin, wv, sc, rtol, max_iters)) {
-      p->launches += 1;
-      PGPU_CUDA(cudaGetLastError());
-      if (int rst = read_small(&hs, sc, sizeof(hs), st)) return rst;
-      *iters_out = hs.iters;
-      if (!(hs.rr == hs.rr)) return fail(PGPU_ERR_NAN, "NaN in the inner Krylov solve");
-      return PGPU_OK;
-    }
-  }
   int tst = tune_bicg<T>(p, A, w);
   if (tst) return tst;
   const int* shp = d.shape[sizeof(T) == 8 ? 0 : 1];

@@ -110,9 +110,10 @@ def test_seven_group_3d(precision, tmp_path):
 
 @pytest.mark.parametrize("G,precision", [(2, "fp64"), (4, "mixed"), (7, "fp64"), (7, "mixed")])
 def test_inner_solve_paths_agree(G, precision, tmp_path):
-    """The one-launch cluster inner solve (problems up to 2^19 rows, G = 2, 4, 7) and the
-    multi-kernel inner solve (larger problems; forced here by profile mode, which times
-    its kernels) converge to the same eigenpair, and both match the oracle."""
+    """The inner solve replayed from captured CUDA graphs in chunks of 4-16 iterations and
+    the same iteration launched one iteration at a time with its kernels timed (profile
+    mode) converge to the same eigenpair, and both match the oracle (G = 2, 4, 7: the
+    compile-time-G kernel forms with the folded in-cell table)."""
     from pampa_gb300 import workloads as wl
     rng = np.random.default_rng(7 + G)
     nx, ny, nz = 12, 10, 6
