@@ -25,6 +25,7 @@
 // schedule, so a Cartesian mesh has 8 (one per octant).  All schedules advance together,
 // one kernel launch per level.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1038,10 +1039,36 @@ struct SlotMaps {
   std::vector<int> cell, face;
 };
 
-// Upwind level sets.  Directions are grouped by the sign of mu against every distinct
-// face normal of the mesh (or against every face when the mesh has too many distinct
-// normals); each group's dependency graph is ordered by Kahn's algorithm.
-int build_schedule(const pgpu_sn_operator* op, Schedule& S) {
+// Ids of distinct face normals (rounded to `scale`).  Face slot f of neighbouring cells
+// usually has the same normal, so the last normal seen in each slot is checked before
+// the map.
+class NormalIds {
+ public:
+  NormalIds(int F, double scale) : scale_(scale), last_(F), last_id_(F, -1) {}
+  int id(int f, const double* nr) {
+    const std::array<long long, 3> key{std::llround(nr[0] * scale_), std::llround(nr[1] * scale_),
+                                       std::llround(nr[2] * scale_)};
+    if (last_id_[f] >= 0 && last_[f] == key) return last_id_[f];
+    auto it = ids_.find(key);
+    const int id = it == ids_.end() ? ids_.emplace(key, (int)ids_.size()).first->second : it->second;
+    last_[f] = key;
+    last_id_[f] = id;
+    return id;
+  }
+  size_t size() const { return ids_.size(); }
+
+ private:
+  double scale_;
+  std::map<std::array<long long, 3>, int> ids_;
+  std::vector<std::array<long long, 3>> last_;
+  std::vector<int> last_id_;
+};
+
+// Sweep patterns and upwind level sets.  Directions are grouped by the sign of mu against
+// every distinct face normal of the mesh (or against every face when the mesh has too
+// many distinct normals); with `levels`, each group's dependency graph is ordered by
+// Kahn's algorithm (the level-set sweep; the tiled dataflow sweep needs the patterns only).
+int build_schedule(const pgpu_sn_operator* op, Schedule& S, bool levels) {
   const int n = op->num_cells, F = op->num_faces, M = op->num_dirs, G = op->num_groups;
   auto mu = [&](int f, int i, int m) {
     const double* nr = op->normals + ((size_t)f * n + i) * 3;
@@ -1049,17 +1076,13 @@ int build_schedule(const pgpu_sn_operator* op, Schedule& S) {
     return d[0] * nr[0] + d[1] * nr[1] + d[2] * nr[2];
   };
   // distinct normals of interior faces
-  std::map<std::vector<long long>, int> normal_id;
+  NormalIds normal_id(F, 1e9);
   std::vector<int> face_nid((size_t)F * n, -1);
   for (int i = 0; i < n; i++)
     for (int f = 0; f < op->num_cell_faces[i]; f++) {
       const size_t o = (size_t)f * n + i;
       if (op->face_kind[o] != PGPU_FACE_INTERIOR) continue;
-      const double* nr = op->normals + o * 3;
-      std::vector<long long> key{std::llround(nr[0] * 1e9), std::llround(nr[1] * 1e9), std::llround(nr[2] * 1e9)};
-      auto it = normal_id.find(key);
-      int id = it == normal_id.end() ? (normal_id[key] = (int)normal_id.size()) : it->second;
-      face_nid[o] = id;
+      face_nid[o] = normal_id.id(f, op->normals + o * 3);
     }
   const bool by_normal = normal_id.size() <= 4096;
   std::vector<std::vector<double>> nvec(normal_id.size());
@@ -1099,6 +1122,7 @@ int build_schedule(const pgpu_sn_operator* op, Schedule& S) {
     for (int m : v) S.pat_dirs.push_back(m);
     S.pat_dirs_ptr.push_back((int)S.pat_dirs.size());
   }
+  if (!levels) return PGPU_OK;
   S.order.resize((size_t)S.npat * n);
   std::vector<int> indeg(n), head(n + 1), adj;
   for (int p = 0; p < S.npat; p++) {
@@ -2044,7 +2068,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
   // sweep face weights and the table of mu over distinct face normals (SweepFaces)
   std::vector<double> wout((size_t)F * n, 0.0), windiag((size_t)F * n, 0.0), winw((size_t)F * n, 0.0);
   std::vector<unsigned char> cls((size_t)F * n, 0);
-  std::map<std::vector<long long>, int> cls_of;
+  NormalIds cls_of(F, 1e12);
   std::vector<const double*> cls_nrm;
   bool use_tab = true;
   for (int i = 0; i < n; i++)
@@ -2063,16 +2087,8 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
         winw[o] = A;
       }
       const double* nr = op->normals + o * 3;
-      std::vector<long long> key{std::llround(nr[0] * 1e12), std::llround(nr[1] * 1e12), std::llround(nr[2] * 1e12)};
-      auto it = cls_of.find(key);
-      int id;
-      if (it == cls_of.end()) {
-        id = (int)cls_nrm.size();
-        cls_of[key] = id;
-        cls_nrm.push_back(nr);
-      } else {
-        id = it->second;
-      }
+      const int id = cls_of.id(f, nr);
+      if (id == (int)cls_nrm.size()) cls_nrm.push_back(nr);
       if (id > 255) use_tab = false;
       cls[o] = (unsigned char)(id & 255);
     }
@@ -2086,8 +2102,11 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       }
   }
   Schedule sched;
-  int st = build_schedule(op, sched);
+  int st = build_schedule(op, sched, false);
   if (st) return st;
+  KbaPlan kp;
+  const bool tiled = kba_plan(op, sched, kp);
+  if (!tiled && (st = build_schedule(op, sched, true))) return st;
   PGPU_CUDA(cudaSetDevice(device));
   pgpu_problem* p = new pgpu_problem();
   p->kind = 2;
@@ -2148,8 +2167,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
   up(d.wout, wout.data(), Fn * 8);
   up(d.windiag, windiag.data(), Fn * 8);
   up(d.win, winw.data(), Fn * 8);
-  KbaPlan kp;
-  if (st == PGPU_OK && kba_plan(op, sched, kp)) {
+  if (st == PGPU_OK && tiled) {
     if ((st = kba_tables()) == PGPU_OK) {
       d.kba = true;
       d.kba_nx = op->cart_nx;
