@@ -1044,13 +1044,20 @@ struct SlotMaps {
 // the map.
 class NormalIds {
  public:
-  NormalIds(int F, double scale) : scale_(scale), last_(F), last_id_(F, -1) {}
+  NormalIds(int F, double scale) : scale_(scale), last_nr_(F), last_(F), last_id_(F, -1) {}
   int id(int f, const double* nr) {
+    if (last_id_[f] >= 0 && nr[0] == last_nr_[f][0] && nr[1] == last_nr_[f][1] && nr[2] == last_nr_[f][2])
+      return last_id_[f];
     const std::array<long long, 3> key{std::llround(nr[0] * scale_), std::llround(nr[1] * scale_),
                                        std::llround(nr[2] * scale_)};
-    if (last_id_[f] >= 0 && last_[f] == key) return last_id_[f];
-    auto it = ids_.find(key);
-    const int id = it == ids_.end() ? ids_.emplace(key, (int)ids_.size()).first->second : it->second;
+    int id;
+    if (last_id_[f] >= 0 && last_[f] == key) {
+      id = last_id_[f];
+    } else {
+      auto it = ids_.find(key);
+      id = it == ids_.end() ? ids_.emplace(key, (int)ids_.size()).first->second : it->second;
+    }
+    last_nr_[f] = {nr[0], nr[1], nr[2]};
     last_[f] = key;
     last_id_[f] = id;
     return id;
@@ -1060,6 +1067,7 @@ class NormalIds {
  private:
   double scale_;
   std::map<std::array<long long, 3>, int> ids_;
+  std::vector<std::array<double, 3>> last_nr_;
   std::vector<std::array<long long, 3>> last_;
   std::vector<int> last_id_;
 };
