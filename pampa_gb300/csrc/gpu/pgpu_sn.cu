@@ -1883,6 +1883,12 @@ static int flow_dirs_max() {
   return e ? std::max(0, std::atoi(e)) : 0;
 }
 
+// (group, direction) slots of one task at most: kFlowSlots, or PGPU_FLOW_SLOTS (1-64).
+static int flow_slots() {
+  const char* e = std::getenv("PGPU_FLOW_SLOTS");
+  return e ? std::min(64, std::max(1, std::atoi(e))) : kFlowSlots;
+}
+
 static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) {
   const int nx = op->cart_nx, ny = op->cart_ny, nz = op->cart_nz, n = op->num_cells;
   if (nx <= 0 || ny <= 0 || nz <= 0 || (long long)nx * ny * nz != n || op->num_faces != 6) return false;
@@ -1930,8 +1936,8 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
       K.npat++;
     }
   }
-  // groups per task: as many as fit in kFlowSlots (group, direction) slots
-  K.gchunk = std::max(1, std::min(op->num_groups, kFlowSlots / std::max(1, K.nd)));
+  // groups per task: as many as fit in the task's (group, direction) slots
+  K.gchunk = std::max(1, std::min(op->num_groups, flow_slots() / std::max(1, K.nd)));
   K.nchunk = (op->num_groups + K.gchunk - 1) / K.gchunk;
   // 8x8x4 tiles when the box divides into them, 4x4x4 otherwise
   const bool big = nx % 8 == 0 && ny % 8 == 0;
