@@ -816,10 +816,23 @@ constexpr int kGsMax = 32;
 constexpr int kGsChunk = 8;
 constexpr double kReorth = 0.5;  // second Gram-Schmidt pass when ||w|| drops below this share
 
-// out[k] = <V_k, w> for k < nv; reduction slots of chunk y at partials + y*kGsChunk*kMaxBlocks
+// Decides on the device whether the Arnoldi step needs the second Gram-Schmidt pass:
+// ||w|| after the first pass (*hn) below kReorth of its norm before (sqrt(*ww)).  *gate
+// = 1 runs the gated second-pass kernels; otherwise h2 is zeroed, so the host adds
+// nothing, and the step needs no host round trip between the passes.
+__global__ void k_gs_gate(const double* ww, const double* hn, double* gate, double* h2, int nh) {
+  const bool need = !(*hn >= kReorth * sqrt(fmax(*ww, 0.0)));
+  *gate = need ? 1.0 : 0.0;
+  if (!need)
+    for (int k = 0; k < nh; k++) h2[k] = 0.0;
+}
+
+// out[k] = <V_k, w> for k < nv; reduction slots of chunk y at partials + y*kGsChunk*kMaxBlocks.
+// With a gate, the whole grid returns at once when *gate == 0.
 template <typename T>
 __global__ void k_gs_dot(long long N, const T* __restrict__ V, long long ld, int nv, const T* __restrict__ w,
-                         double* out, double* partials, unsigned int* tickets) {
+                         double* out, double* partials, unsigned int* tickets, const double* gate) {
+  if (gate && *gate == 0.0) return;
   const int k0 = blockIdx.y * kGsChunk;
   const int nk = min(kGsChunk, nv - k0);
   // per-thread sums in precision T (a few elements each), block and grid sums in FP64
@@ -841,11 +854,12 @@ __global__ void k_gs_dot(long long N, const T* __restrict__ V, long long ld, int
     for (int k = 0; k < nk; k++) out[k0 + k] = tot[k];
 }
 
-// w -= sum_k h[k] V_k, then *out = ||w||
+// w -= sum_k h[k] V_k, then *out = ||w|| (skipped when a gate holds 0)
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_gs_sub_norm(long long N, const T* __restrict__ V, long long ld, int nv,
                                                          const double* __restrict__ h, T* w, double* out,
-                                                         ReduceSlots<1> slots) {
+                                                         ReduceSlots<1> slots, const double* gate) {
+  if (gate && *gate == 0.0) return;
   T part = T(0);
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
     T s = w[l];
@@ -1535,28 +1549,29 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
       const dim3 gd(std::min(gx, kMaxGrid / 2), (j + 1 + kGsChunk - 1) / kGsChunk);
       double* part = d.partials.as<double>();
       unsigned int* tick = d.ticket.as<unsigned int>();
-      launch(p, k_gs_dot<T>, gd1, kThreads, s, len, (const T*)V, len, j + 2, (const T*)wj, h1, part, tick);
-      launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, wj, hn, nslot);
+      double* gate = hn + 1;
+      launch(p, k_gs_dot<T>, gd1, kThreads, s, len, (const T*)V, len, j + 2, (const T*)wj, h1, part, tick,
+             (const double*)nullptr);
+      launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, wj, hn, nslot,
+             (const double*)nullptr);
+      // the second pass, decided and (if needed) run on the device
+      launch(p, k_gs_gate, 1, 1, s, (const double*)(h1 + j + 1), (const double*)hn, gate, h2, j + 1);
+      launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)wj, h2, part, tick,
+             (const double*)gate);
+      launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, wj, hn, nslot,
+             (const double*)gate);
+      launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)wj, (const double*)hn, 1, wj);
       PGPU_CUDA(cudaGetLastError());
-      // h1 and ||w|| (adjacent in hbuf with h2): one copy into pinned host memory
-      PGPU_CUDA(cudaMemcpyAsync(hp, h1, (size_t)(2 * (m + 4) + 1) * 8, cudaMemcpyDeviceToHost, s));
+      // h1, h2, ||w|| and the gate (adjacent in hbuf): one copy into pinned host memory
+      PGPU_CUDA(cudaMemcpyAsync(hp, h1, (size_t)(2 * (m + 4) + 2) * 8, cudaMemcpyDeviceToHost, s));
       PGPU_CUDA(cudaStreamSynchronize(s));
-      const double* hh = hp;
       double hnext = hp[2 * (m + 4)];
-      const double w0 = std::sqrt(std::fmax(hh[j + 1], 0.0));
       double* col = &H[(size_t)j * (m + 1)];
-      for (int k = 0; k <= j; k++) col[k] = hh[k];
-      if (!(hnext >= kReorth * w0)) {
-        launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)wj, h2, part, tick);
-        launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, wj, hn, nslot);
-        PGPU_CUDA(cudaGetLastError());
-        PGPU_CUDA(cudaMemcpyAsync(hp + (m + 4), h2, (size_t)((m + 4) + 1) * 8, cudaMemcpyDeviceToHost, s));
-        PGPU_CUDA(cudaStreamSynchronize(s));
+      for (int k = 0; k <= j; k++) col[k] = hp[k];
+      if (hp[2 * (m + 4) + 1] != 0.0) {
         for (int k = 0; k <= j; k++) col[k] += hp[(m + 4) + k];
-        hnext = hp[2 * (m + 4)];
         d.reorth++;
       }
-      launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)wj, (const double*)hn, 1, wj);
       total++;
       col[j + 1] = hnext;
       for (int k = 0; k < j; k++) {
