@@ -272,6 +272,8 @@ def run_ours(args, rank, world, local):
     w = WORKLOADS[args.workload]
     tmp = tempfile.mkdtemp(prefix=f"bench_r{rank}_")
     path = make_input(args.workload, tmp, args.size)
+    if args.shift is not None:
+        w = dict(w, shift=args.shift)
     prec = ["-pgpu_precision", w["precision"]]
     if w.get("shift"):
         prec += ["-pgpu_shift", str(w["shift"])]
@@ -463,6 +465,8 @@ def run_serve(args, rank, world, local):
     # workload is specified (served answers are compared at 1 pcm)
     fp64 = pg.default_options(precision=pg.PGPU_FP64, tol_k=1e-8, tol_flux=1e-7)
     mixed = pg.default_options(precision=pg.PGPU_MIXED, tol_k=1e-8, tol_flux=1e-7)
+    if args.shift is not None:
+        fp64.shift = mixed.shift = args.shift
     # 0. plain FP64, one request at a time, on the first requests of the stream
     sample = min(nreq, args.serve_sample) if args.serve_sample > 0 else nreq
     def one_at_a_time(opts):
@@ -614,6 +618,8 @@ def main():
     ap.add_argument("--requests", type=int, default=256,
                     help="serve_diffusion: requests in the stream (built up front: about 19 MB of host memory each)")
     ap.add_argument("--slots", type=int, default=16, help="serve_diffusion: solves in flight at most")
+    ap.add_argument("--shift", type=float, default=None,
+                    help="relative Wielandt shift of every solve (default: the workload's, else the solver's)")
     ap.add_argument("--sm-share", type=int, default=None,
                     help="serve_diffusion: SMs each served solve sizes its grids for (default: the server's)")
     ap.add_argument("--serve-sample", type=int, default=0,
