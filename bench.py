@@ -71,6 +71,17 @@ DEFAULT = "sn_s8_64x64x32_g2"
 SOLVE_STATS = os.path.join(ROOT, "profiles", "solve_stats.json")
 
 
+def reduce_over_ranks(value: float, dist, device: str, op: str = "max") -> float:
+    """`value` reduced over the job's ranks: the maximum for times, the sum for
+    throughputs.  Without a process group (one rank) the value itself."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -316,11 +327,7 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     barrier()
-    dev_time = sum(r["seconds"] for r in results)
-    if dist is not None:
-        tt = torch.tensor([dev_time], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_time = float(tt.item())
+    dev_time = reduce_over_ranks(sum(r["seconds"] for r in results), dist, f"cuda:{dev}", "max")
     keff = results[-1]["keff"]
     kern_s = sum(r["kernel_seconds"] for r in results)
     kern_b = sum(r["kernel_bytes"] for r in results)
@@ -347,11 +354,7 @@ def run_ours(args, rank, world, local):
         q.finalize()
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t1)
-    e2e_t = statistics.mean(e2e_times) if e2e_times else float("inf")
-    if dist is not None:
-        tt = torch.tensor([e2e_t], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+    e2e_t = reduce_over_ranks(statistics.mean(e2e_times) if e2e_times else float("inf"), dist, f"cuda:{dev}", "max")
 
     peaks = measured_peaks()
     achieved = kern_b / kern_s / 1e9 if kern_s > 0 else None
@@ -561,10 +564,7 @@ def run_serve(args, rank, world, local):
     launches = sum(r["stats"]["launches"] for r in results)
     cells = np.array([a * b * c for a, b, c, _ in specs], dtype=float)
     unknowns = np.array([a * b * c * G for a, b, c, G in specs], dtype=float)
-    if dist is not None:
-        tt = torch.tensor([value], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(tt)
-        value = float(tt.item())
+    value = reduce_over_ranks(value, dist, f"cuda:{dev}", "sum")
     pct = lambda a, q: 1e3 * float(np.percentile(a, q))  # noqa: E731
     line = dict(metric="k-eigen solves/s (served, continuous batching)", value=value, unit="solves/s",
                 n_gpus=world, steps=nreq, warmup=1, ms_per_step=1e3 * wall / nreq, higher_is_better=True,
