@@ -101,7 +101,13 @@ int read_small(void* host, const void* dev, size_t n, cudaStream_t s) {
 int dev_upload(DevBuf& b, const void* host, size_t bytes, long long* counter, cudaStream_t stream) {
   int st = dev_alloc(b, bytes, counter, stream);
   if (st != PGPU_OK) return st;
-  if (host && bytes) PGPU_CUDA(cudaMemcpy(b.ptr, host, bytes, cudaMemcpyHostToDevice));
+  // on the problem's stream (the legacy default stream would queue the uploads of
+  // problems created on different threads behind each other); creators synchronise the
+  // stream before handing the problem back, so the host arrays may be freed then
+  if (host && bytes) {
+    if (stream) PGPU_CUDA(cudaMemcpyAsync(b.ptr, host, bytes, cudaMemcpyHostToDevice, stream));
+    else PGPU_CUDA(cudaMemcpy(b.ptr, host, bytes, cudaMemcpyHostToDevice));
+  }
   return PGPU_OK;
 }
 

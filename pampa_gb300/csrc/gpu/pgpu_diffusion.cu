@@ -1194,7 +1194,8 @@ int pgpu_diffusion_create(int device, const pgpu_diffusion_operator* op, pgpu_pr
   al(d.fold64, (size_t)nm * G * G * 8);
   if (st == PGPU_OK && cudaMemsetAsync(d.lam.ptr, 0, 2 * sizeof(double), p->stream) != cudaSuccess)
     st = fail(PGPU_ERR_CUDA, "clearing the shift");
-  if (st == PGPU_OK && cudaMemset(d.ticket.ptr, 0, 64) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "memset");
+  if (st == PGPU_OK && cudaMemsetAsync(d.ticket.ptr, 0, 64, p->stream) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "memset");
+  if (st == PGPU_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "upload");
   if (st != PGPU_OK) {
     std::string msg = pgpu_last_error();
     pgpu_problem_destroy(p);

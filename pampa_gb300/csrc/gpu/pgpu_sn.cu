@@ -2293,6 +2293,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
   al(d.q, std::max(nG, (size_t)n) * 8);
   al(d.P, (size_t)n * 8);
   al(d.oscal, sizeof(SNOuter));
+  if (st == PGPU_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "upload");
   if (st != PGPU_OK) {
     std::string msg = pgpu_last_error();
     pgpu_problem_destroy(p);
