@@ -676,6 +676,79 @@ __global__ void k_sweep_coef(SNOp<T> A, SweepFaces<T> W, int ncls, const int* __
   }
 }
 
+// Per-class coefficients of the level-set sweep (any mesh with a table of face normals):
+// for class c, group g, direction m the row [rd, a_0 .. a_{F-1}] with rd = 1 / diagonal
+// and a_f = -(mu_f w_in,f) rd on inflow faces that carry a flux in (interior, reflective),
+// 0 on outflow, vacuum and absent faces; psi = rd src + sum_f a_f psi_in,f.
+template <typename T>
+__global__ void k_sweep_coef_faces(SNOp<T> A, SweepFaces<T> W, int ncls, const int* __restrict__ rep, T* coef) {
+  const int G = A.G, M = A.M, F = A.F;
+  const long long N = (long long)ncls * G * M;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < N; r += (long long)gridDim.x * blockDim.x) {
+    const int m = (int)(r % M);
+    const int cg = (int)(r / M);
+    const int c = cg / G, g = cg - c * G;
+    const int i = rep[c];
+    const T rd = T(1) / sweep_den(A, W, i, g, m);
+    T* row = coef + r * (1 + F);
+    row[0] = rd;
+    for (int f = 0; f < F; f++) {
+      T a = T(0);
+      if (f < A.nf[i]) {
+        const size_t o = (size_t)f * A.n + i;
+        const T mu = sweep_mu(A, W, f, i, m);
+        const int kd = A.kind[o];
+        if (!(mu > T(0)) && (kd == PGPU_FACE_INTERIOR || kd == PGPU_FACE_REFLECTIVE)) a = -(mu * W.win[o]) * rd;
+      }
+      row[1 + f] = a;
+    }
+  }
+}
+
+// One level of the sweep for every pattern, coefficients from the per-class table: a row
+// reads its cell's class, then per face one coefficient and, on an inflow face, the
+// upwind angular flux (or the reflective inflow).  Same sums as k_sweep_level with the
+// reciprocal diagonal distributed over the terms.
+template <typename T>
+__global__ void k_sweep_level_cls(SNOp<T> A, const unsigned short* __restrict__ ccls, const T* __restrict__ coef,
+                                  int level, const int* __restrict__ pat_dirs_ptr, const int* __restrict__ pat_dirs,
+                                  const int* __restrict__ pat_lev_ptr, const int* __restrict__ pat_nlev,
+                                  const int* __restrict__ lev_ptr, const int* __restrict__ order,
+                                  const SweepPtrs* __restrict__ P, int iso) {
+  const int p = blockIdx.y;
+  if (level >= pat_nlev[p]) return;
+  const T* __restrict__ src = static_cast<const T*>(P->src);
+  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
+  T* psi = static_cast<T*>(P->psi);
+  const int d0 = pat_dirs_ptr[p], nd = pat_dirs_ptr[p + 1] - d0;
+  const int* lp = lev_ptr + pat_lev_ptr[p];
+  const int c0 = lp[level], nc = lp[level + 1] - c0;
+  const int* ord = order + (size_t)p * A.n;
+  const int G = A.G, M = A.M, n = A.n, F = A.F;
+  const int items = nc * G * nd;  // < 2^31 (checked at setup)
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < items; it += gridDim.x * blockDim.x) {
+    const int rest = it / nd;
+    const int di = it - rest * nd;
+    const int ci = rest / G;
+    const int g = rest - ci * G;
+    const int i = ord[c0 + ci];
+    const int m = pat_dirs[d0 + di];
+    const size_t l = ((size_t)i * G + g) * M + m;
+    const T* cf = coef + (((size_t)ccls[i] * G + g) * M + m) * (1 + F);
+    T v = cf[0] * (iso ? src[(size_t)i * G + g] : src[l]);
+    const int nfi = A.nf[i];
+    for (int f = 0; f < nfi; f++) {
+      const T a = cf[1 + f];
+      if (a == T(0)) continue;
+      const size_t o = (size_t)f * n + i;
+      const int nb = A.nbr[o];
+      if (nb >= 0) v += a * psi[((size_t)nb * G + g) * M + m];
+      else if (bnd) v += a * bnd_val(A, bnd, A.rslot[o], g, m);
+    }
+    psi[l] = v;
+  }
+}
+
 // phi0[i,g] = sum_m w_m psi[i,g,m] (one warp per (i,g) row, fixed order within the warp).
 template <typename T>
 __global__ void k_moment(int rows, int M, const T* __restrict__ w, const T* __restrict__ psi, T* phi0) {
@@ -1311,6 +1384,22 @@ int ensure_coef(pgpu_problem* p, const SNOp<T>& A) {
   return PGPU_OK;
 }
 
+// Per-class level-sweep coefficients in precision T, computed on first use.
+template <typename T>
+int ensure_level_coef(pgpu_problem* p, const SNOp<T>& A) {
+  SNData& d = *p->sn;
+  DevBuf& buf = sizeof(T) == 8 ? d.coef : d.coef32;
+  if (buf.ptr) return PGPU_OK;
+  const long long N = (long long)d.ncls * d.G * d.M;
+  SweepFaces<T> W = make_faces<T>(d);
+  int st = dev_alloc(buf, (size_t)N * (1 + d.F) * sizeof(T), &p->bytes, p->stream);
+  if (st) return st;
+  launch(p, k_sweep_coef_faces<T>, grid_for(N), kThreads, p->stream, A, W, d.ncls, (const int*)d.d_crep.as<int>(),
+         buf.as<T>());
+  PGPU_CUDA(cudaGetLastError());
+  return PGPU_OK;
+}
+
 // The dataflow sweep for the problem's tile shape runs on a persistent grid: every CTA
 // that fits on the device at once, at most one per task.  flow_prepare sizes it (before
 // the launch is captured in the sweep graph), flow_launch enqueues it.
@@ -1357,7 +1446,8 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   SNData& d = *p->sn;
   const Schedule& S = d.sched;
   const bool cls = d.kba && d.ncls > 0;
-  int rst = cls ? ensure_coef<T>(p, A) : ensure_rden<T>(p, A);
+  const bool level_cls = !d.kba && d.ncls > 0;  // level sets with per-class coefficients
+  int rst = cls ? ensure_coef<T>(p, A) : (level_cls ? ensure_level_coef<T>(p, A) : ensure_rden<T>(p, A));
   if (rst) return rst;
   const SweepFaces<T> W = make_faces<T>(d);
   if (!d.sweep_ptrs.ptr && (rst = dev_alloc(d.sweep_ptrs, sizeof(SweepPtrs), &p->bytes, p->stream))) return rst;
@@ -1389,9 +1479,15 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
     } else {
       for (int L = 0; L < S.nlev; L++) {
         dim3 g(S.grid_x[L], S.npat);
-        k_sweep_level<T><<<g, kThreads, 0, p->stream>>>(
-            A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
-            d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
+        if (level_cls)
+          k_sweep_level_cls<T><<<g, kThreads, 0, p->stream>>>(
+              A, d.d_ccls.as<unsigned short>(), (const T*)(sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr), L,
+              d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(), d.d_pat_nlev.as<int>(),
+              d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
+        else
+          k_sweep_level<T><<<g, kThreads, 0, p->stream>>>(
+              A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
+              d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
       }
     }
     PGPU_CUDA(cudaStreamEndCapture(p->stream, &graph));
@@ -1988,9 +2084,10 @@ constexpr size_t kMaxClassTable = 8u << 20;
 
 static bool kba_classes(const pgpu_sn_operator* op, const std::vector<unsigned char>& ncls,
                         const std::vector<double>& wout, const std::vector<double>& windiag,
-                        const std::vector<double>& win, std::vector<unsigned short>& ccls, std::vector<int>& rep) {
+                        const std::vector<double>& win, std::vector<unsigned short>& ccls, std::vector<int>& rep,
+                        int values_per_row = 4) {
   const int n = op->num_cells, F = op->num_faces, G = op->num_groups, M = op->num_dirs;
-  const size_t per_class = (size_t)G * M * 4 * sizeof(double);
+  const size_t per_class = (size_t)G * M * values_per_row * sizeof(double);
   std::map<std::vector<unsigned long long>, int> ids;
   std::vector<unsigned long long> key((size_t)2 + (size_t)F * 5);
   auto bits = [](double v) {
@@ -2245,6 +2342,17 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       if (st == PGPU_OK && (cudaMemsetAsync(d.flow_sync.ptr, 0, sizeof(FlowSync), p->stream) != cudaSuccess ||
                             cudaMemsetAsync(d.flow_flags.ptr, 0, (size_t)kp.ntasks * 4, p->stream) != cudaSuccess))
         st = fail(PGPU_ERR_CUDA, "clearing the sweep flags");
+    }
+  }
+  if (st == PGPU_OK && !tiled && use_tab) {
+    // level sets: per-class coefficient rows [rd, a_f] instead of a reciprocal diagonal per
+    // (cell, group, direction), when the classes' table stays small
+    std::vector<unsigned short> ccls;
+    std::vector<int> crep;
+    if (kba_classes(op, cls, wout, windiag, winw, ccls, crep, 1 + F)) {
+      d.ncls = (int)crep.size();
+      up(d.d_ccls, ccls.data(), ccls.size() * 2);
+      up(d.d_crep, crep.data(), crep.size() * 4);
     }
   }
   if (d.nrefl) {
