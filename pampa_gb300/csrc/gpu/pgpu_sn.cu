@@ -2076,9 +2076,9 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
   return true;
 }
 
-// Cell classes of the dataflow sweep's coefficient table: cells with the same material,
-// volume and, per face, kind, normal class and sweep weights have the same (rd, a_x, a_y,
-// a_z) for every group and direction.  Returns false when the table would hold more than
+// Cell classes of the sweeps' coefficient tables: cells with the same material, volume
+// and, per face, kind, normal class and sweep weights (equal to 2^-36 relative) have the
+// same coefficient rows for every group and direction.  Returns false when the table would hold more than
 // kMaxClassTable bytes in FP64 (the per-row reciprocal diagonal is used instead).
 constexpr size_t kMaxClassTable = 8u << 20;
 
@@ -2090,10 +2090,13 @@ static bool kba_classes(const pgpu_sn_operator* op, const std::vector<unsigned c
   const size_t per_class = (size_t)G * M * values_per_row * sizeof(double);
   std::map<std::vector<unsigned long long>, int> ids;
   std::vector<unsigned long long> key((size_t)2 + (size_t)F * 5);
+  // values that differ only in their last 16 mantissa bits (relative 2^-36, e.g. cell
+  // volumes of a lattice computed from rounded coordinates) share a class; the class
+  // uses its first cell's exact values
   auto bits = [](double v) {
     unsigned long long u;
     std::memcpy(&u, &v, sizeof(u));
-    return u;
+    return u & ~0xFFFFull;
   };
   ccls.assign(n, 0);
   rep.clear();
