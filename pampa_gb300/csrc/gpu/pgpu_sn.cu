@@ -2081,11 +2081,14 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
 // same coefficient rows for every group and direction.  Returns false when the table would hold more than
 // kMaxClassTable bytes in FP64 (the per-row reciprocal diagonal is used instead).
 constexpr size_t kMaxClassTable = 8u << 20;
+// the level sweep's rows hold 1 + F values (the boundary layers of an unstructured lattice
+// give a few hundred classes); its table may take 64 MiB in FP64, half of L2 in FP32
+constexpr size_t kMaxLevelClassTable = 64u << 20;
 
 static bool kba_classes(const pgpu_sn_operator* op, const std::vector<unsigned char>& ncls,
                         const std::vector<double>& wout, const std::vector<double>& windiag,
                         const std::vector<double>& win, std::vector<unsigned short>& ccls, std::vector<int>& rep,
-                        int values_per_row = 4) {
+                        int values_per_row = 4, size_t max_bytes = kMaxClassTable) {
   const int n = op->num_cells, F = op->num_faces, G = op->num_groups, M = op->num_dirs;
   const size_t per_class = (size_t)G * M * values_per_row * sizeof(double);
   std::map<std::vector<unsigned long long>, int> ids;
@@ -2116,7 +2119,7 @@ static bool kba_classes(const pgpu_sn_operator* op, const std::vector<unsigned c
     int id;
     if (it == ids.end()) {
       id = (int)rep.size();
-      if (id > 65535 || (size_t)(id + 1) * per_class > kMaxClassTable) return false;
+      if (id > 65535 || (size_t)(id + 1) * per_class > max_bytes) return false;
       ids.emplace(key, id);
       rep.push_back(i);
     } else {
@@ -2352,7 +2355,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
     // (cell, group, direction), when the classes' table stays small
     std::vector<unsigned short> ccls;
     std::vector<int> crep;
-    if (kba_classes(op, cls, wout, windiag, winw, ccls, crep, 1 + F)) {
+    if (kba_classes(op, cls, wout, windiag, winw, ccls, crep, 1 + F, kMaxLevelClassTable)) {
       d.ncls = (int)crep.size();
       up(d.d_ccls, ccls.data(), ccls.size() * 2);
       up(d.d_crep, crep.data(), crep.size() * 4);
