@@ -101,7 +101,9 @@ def make_input(name: str, out_dir: str, size: str | None = None) -> str:
     if w["kind"] == "diffusion7g":
         return wl.diffusion_3d_7g(out_dir, **args)
     if w["kind"] == "snhex":
-        return wl.sn_hex(out_dir, **w["args"])
+        if size:
+            args.update(zip(("nq", "nr", "nz"), (int(v) for v in size.lower().split("x"))))
+        return wl.sn_hex(out_dir, **args)
     return wl.diffusion_2d(out_dir, **w["args"])
 
 
@@ -613,8 +615,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--record", action="store_true", help="write profiles/solve_stats.json")
     ap.add_argument("--size", default=None,
-                    help="profiling captures only: NXxNYxNZ box instead of the workload's (the line is then "
-                         "not the workload's result)")
+                    help="profiling captures only: NXxNYxNZ box (hexagonal workload: NQxNRxNZ lattice) instead "
+                         "of the workload's (the line is then not the workload's result)")
     ap.add_argument("--requests", type=int, default=256,
                     help="serve_diffusion: requests in the stream (built up front: about 19 MB of host memory each)")
     ap.add_argument("--slots", type=int, default=16, help="serve_diffusion: solves in flight at most")
