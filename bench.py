@@ -314,6 +314,12 @@ def run_ours(args, rank, world, local):
             raise RuntimeError(f"solve failed: {pg.last_error()}")
         return {k: getattr(stats, k) for k, _ in pg.pgpu_stats._fields_}
 
+    # Diffusion: with per-launch events an inner solve runs one BiCGStab iteration per host
+    # round trip (no graph chunks), which would slow the timed solves of small problems, so
+    # the timed region runs the normal path and the SpMV timing comes from one more solve
+    # with events right after it.  SN: the events bracket the sweep graph launches and
+    # change nothing, so they run inside the timed region.
+    timed_profile = 0 if w["kind"] in ("diffusion2d", "diffusion7g") else 1
     for _ in range(args.warmup):
         solve(0)
     results = []
@@ -325,15 +331,17 @@ def run_ours(args, rank, world, local):
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
-            results.append(solve(1))
+            results.append(solve(timed_profile))
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     barrier()
     dev_time = reduce_over_ranks(sum(r["seconds"] for r in results), dist, f"cuda:{dev}", "max")
     keff = results[-1]["keff"]
-    kern_s = sum(r["kernel_seconds"] for r in results)
-    kern_b = sum(r["kernel_bytes"] for r in results)
-    kern_n = sum(r["kernel_launches"] for r in results)
+    kres = results if timed_profile else [solve(1)]
+    kres_time = dev_time if timed_profile else sum(r["seconds"] for r in kres)
+    kern_s = sum(r["kernel_seconds"] for r in kres)
+    kern_b = sum(r["kernel_bytes"] for r in kres)
+    kern_n = sum(r["kernel_launches"] for r in kres)
     launches = sum(r["launches"] for r in results)
     sweeps = results[-1]["sweeps"]
     upload = int(pg.lib().pgpu_problem_upload_bytes(h))
@@ -360,13 +368,15 @@ def run_ours(args, rank, world, local):
 
     peaks = measured_peaks()
     achieved = kern_b / kern_s / 1e9 if kern_s > 0 else None
-    kname = results[-1]["kernel_name"]
+    kname = kres[-1]["kernel_name"]
     kname = kname.decode() if isinstance(kname, bytes) else str(kname)
     roof = dict(bound="hbm", kernel=kname,
                 achieved=achieved, peak=peaks["hbm_gbs"], unit="GB/s",
                 frac=(achieved / peaks["hbm_gbs"]) if achieved else None, peak_source=peaks["source"],
                 traffic=None, launches=kern_n,
-                kernel_share_of_solve=kern_s / dev_time if dev_time > 0 else None)
+                kernel_share_of_solve=kern_s / kres_time if kres_time > 0 else None,
+                timing="CUDA events around every launch of the kernel in the timed solves" if timed_profile
+                else "CUDA events around every launch of the kernel in one solve right after the timed ones")
     if w["kind"] == "sn" and kern_s > 0:
         # the transport sweep is bound by FP64 issue on GB300 (FP64 = 1/64 of FP32): per
         # (cell, group, direction) update one multiply and three FMAs (7 flops); the
