@@ -65,3 +65,29 @@ def test_set_field_roundtrip(case_input):
         assert np.array_equal(p.field("temperature"), T)
         with pytest.raises(pg.PampaError):
             p.field("no-such-field")
+
+
+@pytest.mark.parametrize("opts,msg", [(["-pgpu_precision", "fp16"], "wrong -pgpu_precision"),
+                                      (["-pgpu_shift", "-1"], "wrong -pgpu_shift"),
+                                      (["-pgpu_max_outer", "0"], "wrong -pgpu_max_outer"),
+                                      (["-pgpu_device", "x"], "wrong -pgpu_device")])
+def test_gpu_options_are_checked(opts, msg, case_input, capfd):
+    """Bad GPU options fail pampa_initialize with the reference's error convention (a
+    file:line: error: message line and *error > 0)."""
+    with pytest.raises(pg.PampaError):
+        pg.Pampa(case_input("slabs/reflected-diffusion"), "-silent", *opts)
+    assert msg in capfd.readouterr().out
+
+
+@pytest.mark.parametrize("block,msg", [("solver diffusion {\n   energy-groups 0\n}\n", "error"),
+                                       ("solver sn {\n   energy-groups 2\n   order 10\n}\n", "error"),
+                                       ("solver nothing {\n}\n", "error")])
+def test_solver_block_errors(block, msg, case_input, capfd):
+    path = case_input("slabs/reflected-diffusion")
+    text = open(path).read()
+    head = text[:text.index("solver diffusion")]
+    with open(path, "w") as fh:
+        fh.write(head + block)
+    with pytest.raises(pg.PampaError):
+        pg.Pampa(path, "-silent")
+    assert msg in capfd.readouterr().out
