@@ -246,12 +246,18 @@ void pgpu_problem_destroy(pgpu_problem* p);
  *   out: phi_out[n*G] = phi * power / p0 with p0 = sum phi kappa_sigma_f V,
  *        q[n] (cell power), P[n] (production rate, divided by keff),
  *        total_power[1] and negatives[1] (may be NULL)
- * Work goes into `stream` (a cudaStream_t; NULL = legacy default stream).  The scratch
- * is a fixed __device__ array inside the library holding at most 1,048,576 cells;
- * larger num_cells is rejected with PGPU_ERR_INVALID.  The first call on a device looks
- * up that array's device address (cudaGetSymbolAddress) and must happen before any
- * stream capture.  All calls share the one array and it keeps the previous call's
- * contents: calls that overlap on the GPU (different streams, no ordering) race. */
+ * Work goes into `stream` (a cudaStream_t; NULL = legacy default stream of the current
+ * device) and runs on the device that owns it; every buffer must live on that device.
+ * Any group count is accepted.  The scratch is a fixed __device__ array inside the
+ * library holding at most 1,048,576 cells; larger num_cells is rejected with
+ * PGPU_ERR_INVALID before anything is queued.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress) and must happen before any stream
+ * capture.  All calls share the one array and it keeps the previous call's contents:
+ * calls that overlap on the GPU (different streams, no ordering) race, so order them
+ * on one stream or with events.  A flux whose power p0 is not positive and finite (an
+ * all-zero flux, no fissile material, NaN) cannot be normalised: phi_out, q and P are
+ * then set to zero, *total_power to 0 and *negatives to -1, which is the marker to check
+ * after the stream has run (the return value only reports argument and launch errors). */
 int pgpu_normalize_power_noalloc(int num_cells, int num_groups, const int* materials, const double* volumes,
                                  const double* kappa_sigma_f, const double* nu_sigma_f, const double* phi,
                                  double power, double keff, double* phi_out, double* q, double* P,

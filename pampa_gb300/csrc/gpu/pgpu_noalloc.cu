@@ -25,7 +25,6 @@ namespace {
 
 constexpr int kNoAllocMaxCells = 1 << 20;   // 1,048,576 cells
 constexpr int kNoAllocBlocks = 512;         // grid cap: partial sums per reduction
-constexpr int kNoAllocGroups = 16;
 
 // Layout of the scratch array (in doubles):
 //   [0, kNoAllocMaxCells)                raw cell power  sum_g phi kappa_sigma_f V
@@ -72,24 +71,29 @@ __global__ void k_na_power(int n, int G, const int* __restrict__ mat, const doub
 }
 
 // Pass 2: phi_out = phi * power / p0, q = q_raw * power / p0, P = sum_g phi_out nu_sigma_f V / k,
-// total power and the count of negative entries.
+// total power and the count of negative entries.  A flux without a positive, finite power
+// (p0 <= 0, NaN or Inf: no fissile material, an all-zero or broken flux) cannot be
+// normalised: every output is set to zero and the negatives count to -1, the marker the
+// caller checks (the call itself returns before the kernels run).
 __global__ void k_na_fields(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
                             const double* __restrict__ nsf, const double* __restrict__ phi, double power,
                             double keff, double* phi_out, double* q, double* P, NoAllocScratch S,
                             double* total_out, int* negatives_out) {
-  const double f = power / S.scal[0];
+  const double p0 = S.scal[0];
+  const bool bad = !(p0 > 0.0) || !isfinite(p0);
+  const double f = bad ? 0.0 : power / p0;
   double acc[2] = {0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double* ns = nsf + (size_t)mat[i] * G;
     const double V = vol[i];
     double Pi = 0.0;
     for (int g = 0; g < G; g++) {
-      const double v = phi[(size_t)i * G + g] * f;
+      const double v = bad ? 0.0 : phi[(size_t)i * G + g] * f;
       phi_out[(size_t)i * G + g] = v;
       if (v < 0.0) acc[1] += 1.0;
       Pi += v * ns[g] * V / keff;
     }
-    const double qi = S.cellp[i] * f;
+    const double qi = bad ? 0.0 : S.cellp[i] * f;
     q[i] = qi;
     P[i] = Pi;
     acc[0] += qi;
@@ -98,9 +102,9 @@ __global__ void k_na_fields(int n, int G, const int* __restrict__ mat, const dou
   double tot[2];
   if (block_reduce_last<2>(acc, slots, tot) && threadIdx.x == 0) {
     S.scal[1] = tot[0];
-    S.scal[2] = tot[1];
+    S.scal[2] = bad ? -1.0 : tot[1];
     if (total_out) *total_out = tot[0];
-    if (negatives_out) *negatives_out = (int)tot[1];
+    if (negatives_out) *negatives_out = bad ? -1 : (int)tot[1];
   }
 }
 
@@ -132,29 +136,39 @@ int pgpu_normalize_power_noalloc(int num_cells, int num_groups, const int* mater
                                  double power, double keff, double* phi_out, double* q, double* P,
                                  double* total_power, int* negatives, void* stream) {
   using namespace pgpu;
-  if (num_cells < 1 || num_groups < 1 || num_groups > kNoAllocGroups)
-    return fail(PGPU_ERR_INVALID, "pgpu_normalize_power_noalloc: bad sizes");
+  if (num_cells < 1 || num_groups < 1) return fail(PGPU_ERR_INVALID, "pgpu_normalize_power_noalloc: bad sizes");
   if (num_cells > kNoAllocMaxCells)
     return fail(PGPU_ERR_INVALID, "pgpu_normalize_power_noalloc: " + std::to_string(num_cells) +
                                       " cells exceed the fixed scratch capacity of " + std::to_string(kNoAllocMaxCells) +
                                       " cells; use the allocating path");
   if (!materials || !volumes || !kappa_sigma_f || !nu_sigma_f || !phi || !phi_out || !q || !P || !(keff > 0.0))
     return fail(PGPU_ERR_INVALID, "pgpu_normalize_power_noalloc: null buffer or non-positive keff");
-  int device = 0;
-  PGPU_CUDA(cudaGetDevice(&device));
+  // The work runs on the device that owns `stream` (the current device for the legacy
+  // default stream); the scratch address is that device's, looked up with it current.
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int current = 0, device = 0;
+  PGPU_CUDA(cudaGetDevice(&current));
+  device = current;
+  if (s) PGPU_CUDA(cudaStreamGetDevice(s, &device));
+  if (device != current) PGPU_CUDA(cudaSetDevice(device));
   double* base = nullptr;
   int st = scratch_address(device, &base);
-  if (st) return st;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  NoAllocScratch S = view_of(base);
-  // the ticket counter must start at zero; the previous call's values are otherwise kept
-  PGPU_CUDA(cudaMemsetAsync(S.ticket, 0, sizeof(unsigned int), s));
-  const int blocks = std::min(kNoAllocBlocks, (num_cells + kThreads - 1) / kThreads);
-  k_na_power<<<blocks, kThreads, 0, s>>>(num_cells, num_groups, materials, volumes, kappa_sigma_f, phi, S);
-  k_na_fields<<<blocks, kThreads, 0, s>>>(num_cells, num_groups, materials, volumes, nu_sigma_f, phi, power,
-                                          keff, phi_out, q, P, S, total_power, negatives);
-  PGPU_CUDA(cudaGetLastError());
-  return PGPU_OK;
+  if (st == PGPU_OK) {
+    NoAllocScratch S = view_of(base);
+    // the ticket counter must start at zero; the previous call's values are otherwise kept
+    cudaError_t e = cudaMemsetAsync(S.ticket, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) {
+      const int blocks = std::min(kNoAllocBlocks, (num_cells + kThreads - 1) / kThreads);
+      k_na_power<<<blocks, kThreads, 0, s>>>(num_cells, num_groups, materials, volumes, kappa_sigma_f, phi, S);
+      k_na_fields<<<blocks, kThreads, 0, s>>>(num_cells, num_groups, materials, volumes, nu_sigma_f, phi, power,
+                                              keff, phi_out, q, P, S, total_power, negatives);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess)
+      st = fail(PGPU_ERR_CUDA, std::string("pgpu_normalize_power_noalloc: ") + cudaGetErrorString(e));
+  }
+  if (device != current) cudaSetDevice(current);
+  return st;
 }
 
 }  // extern "C"

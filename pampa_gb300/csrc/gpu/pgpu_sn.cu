@@ -341,6 +341,7 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 constexpr int kFlowSlots = 10;  // (group, direction) slots of one task at most
 constexpr int kTileClasses = 16;  // cell classes of a tile whose coefficients are staged
 constexpr unsigned int kFlowSpinLimit = 1u << 23;  // ~0.3-0.5 s of polling
+constexpr unsigned int kFlowStallLimit = 1u << 12;  // polls of the failure-injection wait (~1 ms)
 
 // Tile shapes: 4x4x4 cells (128 threads) for small boxes, 8x8x4 (256 threads) for large
 // ones, where fewer tile hops per sweep pay for the longer in-tile diagonals.  Local
@@ -370,7 +371,12 @@ struct FlowSync {
   unsigned int next;   // task counter of the running sweep
   unsigned int epoch;  // sweep number; a task's flag holds it once the task is done
   unsigned int error;  // set when a wait ran out
-  unsigned int pad;
+  // Failure injection for the tests of the bounded wait (0: off).  When it holds t + 1,
+  // task t also waits, with the short bound kFlowStallLimit, for this word to become 0,
+  // which nothing does during a sweep: that wait runs out, sets the error word, and the
+  // solve must report PGPU_ERR_TIMEOUT with the context still usable.  Set per solve from
+  // PGPU_DEBUG_SWEEP_STALL.
+  unsigned int stall;
 };
 
 struct FlowGeom {
@@ -407,11 +413,12 @@ __device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) 
 
 // Waits until *flag == epoch (relaxed polling, then one acquire load of the flag);
 // returns without waiting once any wait of the sweep ran out.
-__device__ __forceinline__ void flow_wait(const unsigned int* flag, unsigned int epoch, unsigned int* error) {
+__device__ __forceinline__ void flow_wait(const unsigned int* flag, unsigned int epoch, unsigned int* error,
+                                          unsigned int limit = kFlowSpinLimit) {
   for (unsigned int it = 0;; it++) {
     if (ld_relaxed_gpu(flag) == epoch) break;
     if (*(volatile unsigned int*)error) return;
-    if (it >= kFlowSpinLimit) {
+    if (it >= limit) {
       atomicExch(error, 1u);
       return;
     }
@@ -569,6 +576,8 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
       const int a = threadIdx.x;
       const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
       if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
+      if (a == 0 && *(volatile unsigned int*)&K.sync->stall == (unsigned int)t + 1u)
+        flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure: runs out
     }
     __syncthreads();
     // 3. inflow from the upwind tiles (through L2)
@@ -1623,7 +1632,16 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
     launch(p, k_norm2<T>, gx, kThreads, s, len, (const T*)V, hn, nslot);
     double beta;
     if ((st = read_small(&beta, hn, 8, s))) return st;
-    if (!(beta == beta)) return fail(PGPU_ERR_NAN, "NaN in the transport correction solve");
+    if (!(beta == beta)) {
+      // a sweep that returned early after a bounded wait ran out leaves unfinished tiles;
+      // report that cause rather than the NaN it may lead to
+      if (d.kba) {
+        unsigned int err = 0;
+        if ((st = read_small(&err, &d.flow_sync.as<FlowSync>()->error, sizeof(err), s))) return st;
+        if (err) return fail(PGPU_ERR_TIMEOUT, "sweep: a wait for an upwind tile ran out (kernel returned early)");
+      }
+      return fail(PGPU_ERR_NAN, "NaN in the transport correction solve");
+    }
     if (first) {
       tol = std::fmax(rtol * beta, atol);
       first = false;
@@ -1719,6 +1737,14 @@ int norm_of(pgpu_problem* p, long long len, const T* x, double* out) {
   return PGPU_OK;
 }
 
+// Failure injection of the dataflow sweep's bounded wait (FlowSync::stall): the value of
+// PGPU_DEBUG_SWEEP_STALL (a task index + 1), read at the start of every solve; unset or 0
+// in normal use.
+unsigned int debug_sweep_stall() {
+  const char* e = std::getenv("PGPU_DEBUG_SWEEP_STALL");
+  return e ? (unsigned int)std::strtoul(e, nullptr, 10) : 0u;
+}
+
 int read_outer(pgpu_problem* p, SNOuter& os) {
   SNData& d = *p->sn;
   FlowSync fs{0u, 0u, 0u, 0u};
@@ -1790,7 +1816,10 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   std::memset(&init, 0, sizeof(init));
   init.k = 1.0;
   launch(p, k_put<SNOuter>, 1, 1, s, dos, init);
-  if (d.kba) PGPU_CUDA(cudaMemsetAsync(&d.flow_sync.as<FlowSync>()->error, 0, sizeof(unsigned int), s));
+  if (d.kba) {
+    PGPU_CUDA(cudaMemsetAsync(&d.flow_sync.as<FlowSync>()->error, 0, sizeof(unsigned int), s));
+    launch(p, k_put<unsigned int>, 1, 1, s, &d.flow_sync.as<FlowSync>()->stall, debug_sweep_stall());
+  }
   launch(p, k_fill<double>, gG, kThreads, s, (long long)nG, phi0, 1.0);
   PGPU_CUDA(cudaMemsetAsync(x64, 0, len * 8, s));
   launch(p, k_fill<double>, grid_for(phi_space ? nG : N), kThreads, s, phi_space ? (long long)nG : N, x64, 1.0);

@@ -68,6 +68,52 @@ def test_noalloc_normalisation_matches_solver_output(tmp_path):
         assert _rel(P.cpu().numpy(), P_ref) <= REL_TOL
         assert total.item() == pytest.approx(1.0, rel=REL_TOL)
         assert neg.item() == 0
+        # and against the oracle's restatement of the reference's normalisation
+        # (NeutronicSolver::normalizeScalarFlux, calculatePowerAndProductionRate)
+        phi_o = po.normalize_scalar_flux(prob, phi_ref * scale)
+        q_o, P_o, tot_o = po.power_and_production(prob, phi_o, k)
+        assert _rel(phi_out.cpu().numpy(), phi_o) <= REL_TOL
+        assert _rel(q.cpu().numpy(), q_o) <= REL_TOL
+        assert _rel(P.cpu().numpy(), P_o) <= REL_TOL
+        assert total.item() == pytest.approx(tot_o, rel=REL_TOL)
+
+
+def test_noalloc_flux_without_power_is_marked(tmp_path):
+    """An all-zero flux has no power to normalise by: the outputs are zeroed and the
+    negatives count carries the -1 marker, and the next call on a good flux is clean."""
+    import torch
+    from pampa_gb300 import workloads as wl
+    from oracle import pampa_oracle as po
+
+    prob = po.read_problem(wl.diffusion_2d(str(tmp_path), n=6))
+    st, nsf, ksf, chi, ss, D = po._material_tables(prob)
+    n, G = prob.mesh.n, prob.G
+    dev = torch.device("cuda", 0)
+    mat = torch.tensor(prob.mesh.materials.astype(np.int32), device=dev)
+    vol = torch.tensor(prob.mesh.volumes, dtype=torch.float64, device=dev)
+    ksf_d = torch.tensor(ksf.reshape(-1), dtype=torch.float64, device=dev)
+    nsf_d = torch.tensor(nsf.reshape(-1), dtype=torch.float64, device=dev)
+    phi_out = torch.full((n * G,), 7.0, dtype=torch.float64, device=dev)
+    q = torch.full((n,), 7.0, dtype=torch.float64, device=dev)
+    P = torch.full((n,), 7.0, dtype=torch.float64, device=dev)
+    total = torch.full((1,), 7.0, dtype=torch.float64, device=dev)
+    neg = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    fn = _fn()
+    args = lambda phi: (n, G, mat.data_ptr(), vol.data_ptr(), ksf_d.data_ptr(), nsf_d.data_ptr(),  # noqa: E731
+                        phi.data_ptr(), 1.0, 1.0, phi_out.data_ptr(), q.data_ptr(), P.data_ptr(),
+                        total.data_ptr(), neg.data_ptr(), stream)
+    zero = torch.zeros(n * G, dtype=torch.float64, device=dev)
+    assert fn(*args(zero)) == pg.PGPU_OK, pg.last_error()
+    torch.cuda.synchronize()
+    assert neg.item() == -1
+    assert total.item() == 0.0
+    assert not phi_out.any() and not q.any() and not P.any()
+    ones = torch.ones(n * G, dtype=torch.float64, device=dev)
+    assert fn(*args(ones)) == pg.PGPU_OK, pg.last_error()
+    torch.cuda.synchronize()
+    assert neg.item() == 0
+    assert total.item() == pytest.approx(1.0, rel=REL_TOL)
 
 
 def test_noalloc_rejects_problems_beyond_its_scratch():
