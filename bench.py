@@ -18,10 +18,15 @@ unknowns), pure upwind, reflective -x/-y/-z, vacuum +x/+y/+z.
 * roofline: the transport-sweep kernel, algorithmic bytes (psi written and read once per
   cell-group-direction update, source, moment and material id per cell-group) over its
   CUDA-event time inside the timed solves; peak = measured HBM copy bandwidth.
-* cpu_baseline: oracle/cpu_sweep.c (C + OpenMP restatement of the same upwind sweep) on
-  the host cores for a bounded sample of sweeps, scaled by the sweeps one solve takes.
-* --impl reference: the CPU restatement alone (the reference's own LU + Krylov-Schur on
-  this operator would need ~82 GB of AIJ storage and is not buildable here).
+* cpu_baseline / parity: one complete k-eigenvalue solve of the same input on the host
+  cores by oracle/sn_cpu.py (the same power iteration with GMRES over transport sweeps,
+  FP64, C + OpenMP sweeps on all host threads), after the timed region; its k and fluxes
+  are compared with the GPU's ("parity").
+* mixed: the same workload in mixed precision (FP32 sweeps and GMRES, FP64 residual
+  refinement), device-timed on the same problem; served: the serving stream's summary.
+* --impl reference: complete CPU solves of the same input by oracle/sn_cpu.py, one per
+  step (the reference's own LU + Krylov-Schur on this operator would need ~82 GB of AIJ
+  storage and is not buildable here).
 
 Multi-GPU: the path does not shard (one solve is one GPU); --gpus N under torchrun runs N
 independent replicas and value is the total over ranks.
@@ -68,7 +73,12 @@ WORKLOADS["serve_diffusion"] = dict(
          "+-5% lognormal XS perturbations), continuous batching, k to 1e-8; capacity with the whole stream queued, "
          "p50/p99 latency with Poisson arrivals at 80% of capacity")
 DEFAULT = "sn_s8_64x64x32_g2"
-SOLVE_STATS = os.path.join(ROOT, "profiles", "solve_stats.json")
+# DRAM bytes (read + write) of one launch of each workload's dominant kernel, from ncu
+# captures summarised under profiles/: k_sweep_flow on the full S8 workload
+# (k_sweep_flow_sn_s8_64x64x32.md); k_bicg_v_cell<float, 7> captured at 128x128x64
+# (7.34M rows, 320.7 MB) and scaled by the 8x rows of 256x256x128, its traffic being
+# proportional to the rows (k_bicg_v_cell_diffusion_7g_128x128x64.md).
+TRAFFIC = {"sn_s8_64x64x32_g2": 256460032, "diffusion_7g_256x256x128_mixed": 2565486592}
 
 
 def reduce_over_ranks(value: float, dist, device: str, op: str = "max") -> float:
@@ -169,27 +179,12 @@ class ClockSampler:
                     reasons=sorted(reasons), samples=len(sm))
 
 
-def load_solve_stats() -> dict:
-    if os.path.exists(SOLVE_STATS):
-        with open(SOLVE_STATS) as fh:
-            return json.load(fh)
-    return {}
-
-
-def cpu_baseline(input_path: str, sweeps_per_solve: float, budget_s: float = 20.0) -> dict:
-    """Time the oracle's C sweep on the host cores; scale to solves/s."""
+def cpu_solve(input_path: str) -> dict:
+    """One complete CPU k-eigenvalue solve (oracle/sn_cpu.py) of an SN input, with the
+    setup (operator tables, upwind orders) outside the timed part."""
     from oracle import pampa_oracle as po, sn_cpu
-    prob = po.read_problem(input_path)
-    inp = sn_cpu.sweep_inputs(prob)
-    t1, threads = sn_cpu.time_sweeps(inp, 1)
-    nsw = max(1, min(50, int(budget_s / max(t1, 1e-6))))
-    t, threads = sn_cpu.time_sweeps(inp, nsw, threads)
-    per_solve = t * sweeps_per_solve
-    return dict(value=1.0 / per_solve, unit="solves/s", cores=threads, kind="port",
-                sample=(f"{nsw} upwind sweeps + scalar-flux moments of this workload with oracle/cpu_sweep.c "
-                        f"({threads} OpenMP threads, {t * 1e3:.1f} ms/sweep), scaled by the "
-                        f"{sweeps_per_solve:.0f} sweeps one GPU k-eigenvalue solve of the same algorithm takes"),
-                seconds_per_sweep=t)
+    S = sn_cpu.SNCpu(po.read_problem(input_path))
+    return S.solve()
 
 
 def run_reference(args, rank, world):
@@ -204,32 +199,31 @@ def run_reference(args, rank, world):
                           "workload's matrix is too large for it on this host, or (serving) the reference "
                           "has no counterpart"}))
         return 0
-    stats = load_solve_stats().get(args.workload)
-    if not stats:
-        print(json.dumps({"impl": "reference", "unavailable": "no recorded sweeps-per-solve for this workload "
-                          "(run bench.py --impl ours once to record profiles/solve_stats.json)"}))
-        return 0
     with tempfile.TemporaryDirectory() as d:
-        path = make_input(args.workload, d)
+        path = make_input(args.workload, d, args.size)
         from oracle import pampa_oracle as po, sn_cpu
-        prob = po.read_problem(path)
-        inp = sn_cpu.sweep_inputs(prob)
-        per = []
-        threads = None
-        for i in range(args.warmup + args.steps):
-            t, threads = sn_cpu.time_sweeps(inp, 1, threads)
-            if i >= args.warmup:
-                per.append(t)
+        S = sn_cpu.SNCpu(po.read_problem(path))
+        # warm-up steps: solves capped at two outer iterations (page-in, thread start-up)
+        for _ in range(args.warmup):
+            try:
+                S.solve(max_outer=2)
+            except RuntimeError:
+                pass
+        per, res = [], None
+        for _ in range(args.steps):
+            res = S.solve()
+            per.append(res["seconds"])
     t = statistics.mean(per)
-    value = 1.0 / (t * stats["sweeps"])
-    cpu = dict(value=value, unit="solves/s", cores=threads, kind="port",
-               sample=f"one upwind sweep + moment per step ({t * 1e3:.1f} ms) with oracle/cpu_sweep.c, "
-                      f"scaled by {stats['sweeps']} sweeps per solve")
-    line = dict(metric="k-eigen solves/s", value=value, unit="solves/s", n_gpus=world, steps=args.steps,
-                warmup=args.warmup, ms_per_step=1e3 * t * stats["sweeps"], higher_is_better=True, scaling="weak",
+    cpu = dict(value=1.0 / t, unit="solves/s", cores=res["threads"], kind="port",
+               sample=f"complete k-eigenvalue solves of this workload by oracle/sn_cpu.py (power iteration "
+                      f"with GMRES over C + OpenMP transport sweeps, FP64, {res['threads']} threads), one per "
+                      f"step: {res['sweeps']} sweeps, {res['outer_iterations']} outer iterations")
+    line = dict(metric="k-eigen solves/s", value=1.0 / t, unit="solves/s", n_gpus=world, steps=args.steps,
+                warmup=args.warmup, ms_per_step=1e3 * t, higher_is_better=True, scaling="weak",
                 vs_baseline=None, dtype="f64", data="synthetic (seeded generator, reference .pmp format)",
-                config=dict(workload=args.workload, description=w["desc"]), impl="reference", cpu_baseline=cpu,
-                e2e=dict(value=value, unit="solves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+                config=dict(workload=args.workload, description=w["desc"], keff=res["keff"],
+                            **(dict(size_override=args.size) if args.size else {})), impl="reference",
+                cpu_baseline=cpu, e2e=dict(value=1.0 / t, unit="solves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line))
     return 0
 
@@ -348,6 +342,49 @@ def run_ours(args, rank, world, local):
     n_phi = p.field_size("scalar-flux")
     n_psi = p.field_size("angular-flux") if w["kind"] in ("sn", "snhex") else 0
     n_cells = p.field_size("power")
+
+    def fields():
+        """Normalised scalar and angular flux of the problem's last solve (host copies)."""
+        phi = np.zeros(n_phi)
+        if pg.lib().pgpu_problem_get_scalar_flux(h, phi.ctypes.data_as(C.POINTER(C.c_double))) != pg.PGPU_OK:
+            raise RuntimeError(pg.last_error())
+        psi = None
+        if n_psi:
+            psi = np.zeros(n_psi)
+            if pg.lib().pgpu_problem_get_angular_flux(h, psi.ctypes.data_as(C.POINTER(C.c_double))) != pg.PGPU_OK:
+                raise RuntimeError(pg.last_error())
+        return phi, psi
+
+    phi64, psi64 = fields() if not args.profile_outer else (None, None)
+
+    # ---- the same problem in mixed precision (FP32 sweeps and GMRES, FP64 refinement) ----
+    mixed = None
+    if w["kind"] == "sn" and w["precision"] == "fp64" and not args.profile_outer and not args.no_mixed:
+        opts.precision = pg.PGPU_MIXED
+        for _ in range(args.warmup):
+            solve(0)
+        mres = []
+        torch.cuda.synchronize()
+        barrier()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            mres.append(solve(0))
+        torch.cuda.synchronize()
+        barrier()
+        mtime = reduce_over_ranks(sum(r["seconds"] for r in mres), dist, f"cuda:{dev}", "max")
+        phim, psim = fields()
+        rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+        mixed = dict(value=world * args.steps / mtime, unit="solves/s", ms_per_step=1e3 * mtime / args.steps,
+                     dtype="f32+f64", speedup_vs_fp64=(args.steps / mtime) / (args.steps / dev_time),
+                     keff=mres[-1]["keff"], dk_vs_fp64=abs(mres[-1]["keff"] - keff),
+                     flux_l2_vs_fp64=rel(phim, phi64), psi_l2_vs_fp64=rel(psim, psi64),
+                     sweeps_per_solve=mres[-1]["sweeps"], outer_iterations=mres[-1]["outer_iterations"],
+                     gmres_iterations=mres[-1]["inner_iterations"],
+                     gpu_launches=int(sum(r["launches"] for r in mres)),
+                     timing="device time (CUDA events) of the same number of complete solves as the FP64 "
+                            "line, same problem resident in HBM, L2 flushed between solves")
+        opts.precision = pg.PGPU_FP64
     p.finalize()
 
     # ---- end-to-end through the drop-in API -------------------------------------
@@ -387,10 +424,7 @@ def run_ours(args, rank, world, local):
             ach = 7.0 * n_psi * sw / kern_s / 1e12
             roof["fp64"] = dict(flops_per_update=7, achieved_tflops=ach, nominal_peak_tflops=1.25,
                                 frac_of_nominal=ach / 1.25)
-    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(traffic_path):
-        with open(traffic_path) as fh:
-            roof["traffic"] = json.load(fh).get(args.workload)
+    roof["traffic"] = TRAFFIC.get(args.workload)
 
     line = dict(metric="k-eigen solves/s", value=world * args.steps / dev_time, unit="solves/s", n_gpus=world,
                 steps=args.steps, warmup=args.warmup, ms_per_step=1e3 * dev_time / args.steps,
@@ -417,19 +451,39 @@ def run_ours(args, rank, world, local):
                                         sample="one complete solve by oracle/pampa_oracle.py (SuperLU + ARPACK)")
         except Exception as e:
             line["cpu_baseline"] = dict(value=None, unavailable=str(e))
+    if mixed is not None:
+        line["mixed"] = mixed
     if rank == 0 and world == 1 and w["kind"] == "sn" and not args.no_cpu and not args.profile_outer:
+        # one complete CPU solve of the same input: the CPU baseline, and the parity check
+        # of the GPU result at the workload's full size
         try:
-            line["cpu_baseline"] = cpu_baseline(path, sweeps)
+            cpu = cpu_solve(path)
+            rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+            line["cpu_baseline"] = dict(
+                value=1.0 / cpu["seconds"], unit="solves/s", cores=cpu["threads"], kind="port",
+                sample=f"one complete k-eigenvalue solve of this workload by oracle/sn_cpu.py (power iteration with "
+                       f"GMRES over C + OpenMP transport sweeps, FP64, {cpu['threads']} threads; {cpu['sweeps']} "
+                       f"sweeps, {cpu['outer_iterations']} outer iterations)")
+            line["parity"] = dict(
+                vs="oracle/sn_cpu.py complete FP64 CPU solve of the same input (checked against the oracle's direct "
+                   "solve on small meshes by the CPU tests)",
+                dk=abs(keff - cpu["keff"]), flux_l2=rel(phi64, cpu["phi"]),
+                psi_l2=rel(psi64, cpu["psi"]) if psi64 is not None else None,
+                k_tol=1e-6, flux_tol=1e-5)
+            if mixed is not None:
+                line["parity"]["mixed_dk"] = abs(mixed["keff"] - cpu["keff"])
+                line["parity"]["mixed_k_tol"] = 1e-5
         except Exception as e:  # the baseline never decides the GPU result
             line["cpu_baseline"] = dict(value=None, unavailable=str(e))
+    if world == 1 and args.workload == DEFAULT and not args.no_serve and not args.profile_outer and not args.size:
+        served = serve_stream(args, rank, dev, dist)
+        line["served"] = {k: served[k] for k in (
+            "value", "unit", "speedup_vs_fp64_one_at_a_time", "fp64_one_at_a_time", "mixed_one_at_a_time",
+            "latency", "dk_max_vs_fp64", "dk_max_between_passes", "gpu_launches")}
+        line["served"]["config"] = {k: served["config"][k] for k in (
+            "workload", "description", "requests", "slots", "mean_unknowns", "mean_outer_iterations",
+            "mean_inner_iterations")}
     if rank == 0:
-        rec = load_solve_stats()
-        rec[args.workload] = dict(sweeps=sweeps, outer_iterations=results[-1]["outer_iterations"],
-                                  gmres_iterations=results[-1]["inner_iterations"], keff=keff)
-        if args.record and not args.profile_outer:
-            os.makedirs(os.path.dirname(SOLVE_STATS), exist_ok=True)
-            with open(SOLVE_STATS, "w") as fh:
-                json.dump(rec, fh, indent=1, sort_keys=True)
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
@@ -446,6 +500,24 @@ def run_serve(args, rank, world, local):
     that capacity, p50/p99 of submit-to-answer.  Requests are built before the timed
     passes (in a process pool), so the host generator is not what is measured.  Every rank
     serves its own stream (replicas); value is the total over ranks."""
+    import torch
+
+    dev = local
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    line = serve_stream(args, rank, dev, dist)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def serve_stream(args, rank, dev, dist) -> dict:
+    """Builds the seeded request stream and measures it (see run_serve); returns the line."""
     import math
     import multiprocessing as mp
     import queue
@@ -457,9 +529,9 @@ def run_serve(args, rank, world, local):
     import pampa_gb300 as pg
     from pampa_gb300 import workloads as wl
 
-    dev = local
     rng = np.random.default_rng(4 + rank)
     nreq = args.requests
+    world = dist.get_world_size() if dist is not None else 1
 
     def loguni(lo, hi):
         return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
@@ -469,12 +541,6 @@ def run_serve(args, rank, world, local):
     procs = max(1, min(16, (os.cpu_count() or 2) // max(1, world)))
     with mp.get_context("spawn").Pool(procs) as pool:
         ops = pool.map(wl.diffusion_request_op, [(*specs[k], int(seeds[k])) for k in range(nreq)], chunksize=4)
-
-    torch.cuda.set_device(dev)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
 
     # power iteration to 1e-8 on k and 1e-7 on the fission source, as the small plain
     # workload is specified (served answers are compared at 1 pcm)
@@ -608,11 +674,7 @@ def run_serve(args, rank, world, local):
                          d2h_bytes_per_step=8,
                          note="the served rate is end to end: host operator arrays in, keff out"),
                 gpu_launches=int(launches), roofline=None, clocks=clk.summary())
-    if rank == 0:
-        print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
-    return 0
+    return line
 
 
 def main():
@@ -622,8 +684,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
-    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--record", action="store_true", help="write profiles/solve_stats.json")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline and parity leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision object of the default line")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served object of the default line")
     ap.add_argument("--size", default=None,
                     help="profiling captures only: NXxNYxNZ box (hexagonal workload: NQxNRxNZ lattice) instead "
                          "of the workload's (the line is then not the workload's result)")

@@ -61,7 +61,7 @@ def test_reference_arm_two_ranks():
     sn_cpu.build()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), os.path.join(ROOT, "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--size", "16x16x8"]
     env = dict(os.environ, OMP_NUM_THREADS="2")
     res = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
     assert res.returncode == 0, res.stderr[-2000:]
