@@ -43,7 +43,8 @@ void pampa_initialize(int argc, char* argv[], double** dt, int* ndt, int* error)
 void pampa_initialize_steady_state(int argc, char* argv[], int* error);
 
 /* Replaces pampa_solve (pampa.hxx:14, pampa.cxx:60-66).  n = 0 is the steady-state
- * k-eigenvalue solve; n > 0 (transient steps) reports an error in this build. */
+ * k-eigenvalue solve; n > 0 is a transient step of size dt (diffusion solvers; it needs
+ * the steady state solved first and reports an error for SN solvers). */
 void pampa_solve(int n, double dt, double t, int* error);
 
 /* Replaces pampa_solve_steady_state (pampa.hxx:17, pampa.cxx:69-75). */
@@ -213,6 +214,21 @@ int pgpu_sn_apply(pgpu_problem* p, const double* x, double* y);
 /* Solve R x = (1/k) F x on the GPU, starting from a flat flux.  Results stay on the
  * device; read them with pgpu_problem_get_*.  Returns the solve status. */
 int pgpu_problem_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats);
+
+/* Linear solve with a diffusion problem's operator: (R - lam F) x = b, F[(i,g),(i,g2)] =
+ * chi[mat(i)][g] nu_sigma_f[mat(i)][g2] V_i as in pgpu_diffusion_operator.  This is the
+ * transient step of DiffusionSolver (DiffusionSolver.cxx:108-175 assembles R with the
+ * 1/(v dt) terms on its diagonal and -(1 - beta) chi_p nu_sigma_f V / keff in-cell terms;
+ * getSolution n > 0, :337-345, solves it with KSP, petsc.cxx:147-172): the caller
+ * creates the problem with that diagonal and chi = (1 - beta) chi_prompt and passes
+ * lam = 1/keff.  x (host, num_cells*G) is the initial guess on entry and the solution on
+ * return; b is host memory.  Converged when ||b - (R - lam F) x|| <= tol_flux ||b||
+ * (options.tol_flux, at least 1e-14); PGPU_ERR_NOT_CONVERGED after max_inner Krylov
+ * iterations.  options.precision selects FP64 or FP32 corrections with FP64 residuals.
+ * stats: outer_iterations = refinement steps, inner_iterations = Krylov iterations,
+ * residual = final relative residual.  Diffusion problems only (PGPU_ERR_INVALID else). */
+int pgpu_problem_solve_linear(pgpu_problem* p, double lam, const double* b, double* x,
+                              const pgpu_options* opt, pgpu_stats* stats);
 
 /* Results of the last solve, normalised as NeutronicSolver::normalizeScalarFlux and
  * SNSolver::normalizeAngularFlux do (sum phi*kappa_sigma_f*V = power).  Host buffers:

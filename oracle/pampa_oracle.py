@@ -169,6 +169,9 @@ class Material:
     D: np.ndarray | None = None
     chi: np.ndarray | None = None     # effective fission spectrum
     beta_total: float = 0.0
+    chi_p: np.ndarray | None = None   # prompt fission spectrum
+    chi_d: np.ndarray | None = None   # delayed fission spectrum
+    vel: np.ndarray | None = None     # neutron velocities
 
     def read(self, tok: Tokens):
         nd = {}
@@ -267,6 +270,8 @@ class Material:
         self.st = nd.get("sigma-total")
         self.nsf, self.ksf, self.chi, self.D = nsf, ksf, chi, D
         self.ss = nd.get("sigma-scattering")
+        self.chi_p, self.chi_d = chi_p, chi_d
+        self.vel = nd.get("neutron-velocity")
 
     def check_for_solver(self, G: int, diffusion: bool):
         if not self.has_nd:
@@ -1181,3 +1186,67 @@ def solve_problem(prob: Problem, tol: float = 1e-13) -> dict:
 
 def run_input(path: str, tol: float = 1e-13) -> dict:
     return solve_problem(read_problem(path), tol)
+
+
+def diffusion_transient_system(prob: Problem, R0: sp.csr_matrix, dt: float, keff: float, phi0: np.ndarray,
+                               S: np.ndarray):
+    """R and b of DiffusionSolver::buildMatrices for a time step n > 0
+    (DiffusionSolver.cxx:108-175): R = R(n=0) + V/(v_g dt) on the diagonal
+    - (1 - beta) chi_p,g nu_sigma_f,g2 V / keff in the cell's (g, g2) block;
+    b = chi_d,g S_i + V/(v_g dt) phi0.  R0 is the n = 0 operator of assemble_diffusion."""
+    mesh, G = prob.mesh, prob.G
+    n = mesh.n
+    mat = mesh.materials
+    V = mesh.volumes
+    for m in prob.materials:
+        if m.vel is None:
+            raise ValueError("missing neutron velocities")
+    vel = np.array([m.vel for m in prob.materials])
+    chip = np.array([(1.0 - m.beta_total) * m.chi_p for m in prob.materials])
+    chid = np.array([m.chi_d for m in prob.materials])
+    st, nsf, ksf, chi, ss, D = _material_tables(prob)
+    d = (V[:, None] / (vel[mat] * dt)).reshape(-1)
+    cell = np.arange(n)
+    rows, cols, vals = [], [], []
+    for g in range(G):
+        for g2 in range(G):
+            rows.append(cell * G + g)
+            cols.append(cell * G + g2)
+            vals.append(-chip[mat, g] * nsf[mat, g2] * V / keff)
+    N = n * G
+    Rp = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(N, N))
+    R = (R0 + sp.diags(d) + Rp).tocsr()
+    b = (chid[mat] * S[:, None]).reshape(-1) + d * phi0
+    return R, b
+
+
+def run_transient(path: str, delayed_source_scale: float = 1.0, tol: float = 1e-13) -> list[dict]:
+    """The C front end's time loop (c/main.c:16-29) for a diffusion input with time steps:
+    the steady state, then every step of the input's dt list with a direct solve of the
+    step's linear system (the reference solves it with KSP, petsc.cxx:147-172).  The
+    delayed source S = beta P of calculatePowerAndProductionRate (NeutronicSolver.cxx:81-116)
+    is scaled by delayed_source_scale after the steady state, as a coupled caller setting
+    the "delayed-source" field would.  Returns per step keff (steady state), phi, q, P and the
+    total power."""
+    prob = read_problem(path)
+    if prob.solver != "diffusion":
+        raise ValueError("transients are restated for diffusion only")
+    res = solve_problem(prob, tol)
+    keff = res["keff"]
+    ksf, nsf = _kappa_nu_tables(prob)
+    V = prob.mesh.volumes
+    beta = np.array([m.beta_total for m in prob.materials])[prob.mesh.materials]
+    out = [dict(keff=keff, phi=res["phi"], q=res["q"], P=res["P"], power=res["power"])]
+    phi = res["phi"]
+    S = beta * res["P"] * delayed_source_scale
+    t = 0.0
+    for dt in prob.dt:
+        t += dt
+        R, b = diffusion_transient_system(prob, res["R"], dt, keff, phi, S)
+        phi = spla.spsolve(R.tocsc(), b)
+        ph2 = phi.reshape(prob.mesh.n, prob.G)
+        q = np.sum(ph2 * ksf * V[:, None], axis=1)
+        P = np.sum(ph2 * nsf * V[:, None] / keff, axis=1)
+        S = beta * P
+        out.append(dict(dt=dt, t=t, phi=phi, q=q, P=P, power=float(np.sum(q))))
+    return out

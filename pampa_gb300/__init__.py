@@ -93,6 +93,7 @@ SYMBOLS = {
     "pgpu_sn_create": (C.c_int, [C.c_int, _P(pgpu_sn_operator), _P(C.c_void_p)]),
     "pgpu_sn_apply": (C.c_int, [C.c_void_p, _pd, _pd]),
     "pgpu_problem_solve": (C.c_int, [C.c_void_p, _P(pgpu_options), _P(pgpu_stats)]),
+    "pgpu_problem_solve_linear": (C.c_int, [C.c_void_p, C.c_double, _pd, _pd, _P(pgpu_options), _P(pgpu_stats)]),
     "pgpu_problem_get_keff": (C.c_int, [C.c_void_p, _pd]),
     "pgpu_problem_get_scalar_flux": (C.c_int, [C.c_void_p, _pd]),
     "pgpu_problem_get_angular_flux": (C.c_int, [C.c_void_p, _pd]),
@@ -289,6 +290,18 @@ class _Problem:
         if st != PGPU_OK:
             raise PampaError(f"pgpu_problem_solve failed ({st}): {last_error()} stats={stats}")
         return SolveResult(s.keff, stats)
+
+    def solve_linear(self, lam: float, b, x0=None, **opts) -> tuple[np.ndarray, dict]:
+        """x with (R - lam F) x = b (diffusion problems), from the guess x0 (zeros)."""
+        o = default_options(**opts)
+        s = pgpu_stats()
+        bb = _f64(b)
+        x = np.array(x0, dtype=np.float64) if x0 is not None else np.zeros_like(bb)
+        st = lib().pgpu_problem_solve_linear(self._h, lam, _dp(bb), _dp(x), C.byref(o), C.byref(s))
+        stats = {k: getattr(s, k) for k, _ in pgpu_stats._fields_}
+        if st != PGPU_OK:
+            raise PampaError(f"pgpu_problem_solve_linear failed ({st}): {last_error()} stats={stats}")
+        return x, stats
 
     def scalar_flux(self) -> np.ndarray:
         out = np.zeros(self.num_cells * self.num_groups)

@@ -129,6 +129,29 @@ void pgpu_default_options(pgpu_options* opt) {
 
 const char* pgpu_last_error(void) { return pgpu::g_last_error.c_str(); }
 
+int pgpu_problem_solve_linear(pgpu_problem* p, double lam, const double* b, double* x, const pgpu_options* opt,
+                              pgpu_stats* stats) {
+  if (!p) return pgpu::fail(PGPU_ERR_INVALID, "null problem");
+  if (p->kind != 1) return pgpu::fail(PGPU_ERR_INVALID, "linear solves are available for diffusion problems");
+  if (!b || !x) return pgpu::fail(PGPU_ERR_INVALID, "null right-hand side or solution buffer");
+  if (!(lam == lam)) return pgpu::fail(PGPU_ERR_INVALID, "lam is NaN");
+  pgpu_options def;
+  pgpu_default_options(&def);
+  if (!opt) opt = &def;
+  pgpu_stats local;
+  std::memset(&local, 0, sizeof(local));
+  if (!stats) stats = &local;
+  std::memset(stats, 0, sizeof(*stats));
+  PGPU_CUDA(cudaSetDevice(p->device));
+  p->launches = 0;
+  p->profile = false;
+  int st = pgpu::diffusion_solve_linear(p, lam, b, x, opt, stats);
+  cudaStreamSynchronize(p->stream);
+  stats->launches = p->launches;
+  stats->status = st;
+  return st;
+}
+
 int pgpu_problem_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   if (!p) return pgpu::fail(PGPU_ERR_INVALID, "null problem");
   pgpu_options def;

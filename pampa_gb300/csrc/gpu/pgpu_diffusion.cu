@@ -1107,6 +1107,84 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   return PGPU_OK;
 }
 
+// Linear solve (R - lam F) y = b with the problem's operator (the transient step of
+// DiffusionSolver, DiffusionSolver.cxx:108-175 and getSolution n > 0, :337-345): FP64
+// residual refinement around BiCGStab corrections in FP64 or, for mixed precision, FP32.
+// y starts from the caller's guess (the reference sets KSPSetInitialGuessNonzero,
+// petsc.cxx:168) and stops at ||b - A y|| <= tol ||b||.
+int diffusion_solve_linear(pgpu_problem* p, double lam, const double* b, double* x, const pgpu_options* opt,
+                           pgpu_stats* stats) {
+  DiffusionData& d = *p->diff;
+  const int N = d.n * d.G;
+  const bool mixed = opt->precision == PGPU_MIXED;
+  int st;
+  if (mixed && (st = make_fp32(p))) return st;
+  cudaStream_t s = p->stream;
+  const int gN = grid_for(N, p->sm_share, kThreads);
+  cudaEvent_t e0, e1;
+  PGPU_CUDA(cudaEventCreate(&e0));
+  PGPU_CUDA(cudaEventCreate(&e1));
+  PGPU_CUDA(cudaEventRecord(e0, s));
+  PGPU_CUDA(cudaMemcpyAsync(d.b.ptr, b, (size_t)N * 8, cudaMemcpyHostToDevice, s));
+  PGPU_CUDA(cudaMemcpyAsync(d.y.ptr, x, (size_t)N * 8, cudaMemcpyHostToDevice, s));
+  launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), lam);
+  refold(p);
+  DiffOp<double> A = op64(d, true);
+  const double tol = std::fmax(opt->tol_flux, 1e-14);
+  OuterScal os;
+  int inner_total = 0, ref = 0;
+  bool converged = false;
+  for (ref = 0; ref < 100; ref++) {
+    launch(p, k_residual<float>, gN, kThreads, s, A, (const double*)d.b.as<double>(), (const double*)d.y.as<double>(),
+           d.r64.as<double>(), mixed ? d.r32.as<float>() : (float*)nullptr, d.oscal.as<OuterScal>(), slots_of<2>(d));
+    if ((st = read_outer(p, os))) return st;
+    if (!(os.rr == os.rr)) return fail(PGPU_ERR_NAN, "NaN in the residual of the linear solve");
+    const double rel = os.bb > 0 ? sqrt(os.rr / os.bb) : 0.0;
+    if (rel <= tol) {
+      converged = true;
+      break;
+    }
+    if (inner_total >= opt->max_inner) break;
+    int it = 0;
+    if (mixed) {
+      DiffOp<float> A32 = op32(d, true);
+      st = bicgstab<float>(p, A32, d.w32, d.r32.as<float>(), fmin(fmax(tol / rel, 2e-5), 0.5),
+                           opt->max_inner - inner_total, &it);
+      if (st == PGPU_OK) launch(p, k_axpy_update<float>, gN, kThreads, s, N, d.y.as<double>(), d.w32[0].as<float>());
+    }
+    if (!mixed || st == PGPU_ERR_NAN) {
+      if ((st = bicgstab<double>(p, A, d.w64, d.r64.as<double>(), fmin(fmax(0.5 * tol / rel, 1e-15), 0.5),
+                                 opt->max_inner - inner_total, &it)))
+        return st;
+      launch(p, k_axpy_update<double>, gN, kThreads, s, N, d.y.as<double>(), d.w64[0].as<double>());
+    } else if (st) {
+      return st;
+    }
+    inner_total += it;
+    if (it == 0) break;
+  }
+  PGPU_CUDA(cudaMemcpyAsync(x, d.y.ptr, (size_t)N * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(cudaEventRecord(e1, s));
+  PGPU_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  PGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // the eigen solve sets its own shift; leave the operator unshifted
+  launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), 0.0);
+  refold(p);
+  if (stats) {
+    stats->keff = 0.0;
+    stats->outer_iterations = ref;
+    stats->inner_iterations = inner_total;
+    stats->sweeps = 0;
+    stats->residual = os.bb > 0 ? sqrt(os.rr / os.bb) : 0.0;
+    stats->seconds = ms * 1e-3;
+  }
+  if (!converged) return fail(PGPU_ERR_NOT_CONVERGED, "linear solve reached its iteration cap without converging");
+  return PGPU_OK;
+}
+
 int diffusion_get_flux(pgpu_problem* p, double* phi) {
   DiffusionData& d = *p->diff;
   PGPU_CUDA(cudaMemcpyAsync(phi, d.phi.ptr, (size_t)d.n * d.G * 8, cudaMemcpyDeviceToHost, p->stream));

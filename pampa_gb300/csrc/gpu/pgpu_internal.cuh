@@ -263,6 +263,8 @@ inline double prof_collect(pgpu_problem* p) {
 
 // Per-kind entry points implemented in pgpu_diffusion.cu / pgpu_sn.cu.
 int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats);
+int diffusion_solve_linear(pgpu_problem* p, double lam, const double* b, double* x, const pgpu_options* opt,
+                           pgpu_stats* stats);
 int diffusion_get_flux(pgpu_problem* p, double* phi);
 int diffusion_get_power(pgpu_problem* p, double* q, double* P, double* total);
 void diffusion_destroy(pgpu_problem* p);

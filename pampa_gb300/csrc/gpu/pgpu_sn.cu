@@ -119,6 +119,8 @@ struct SNData {
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
+  DevBuf d_task_order;  // hand-out order of the dataflow sweep's tasks (null: canonical)
+  int flow_sleep = 32;  // back-off between flag polls (ns)
   DevBuf d_fpat_dirs_ptr, d_fpat_dirs;  // directions of the dataflow sweep's patterns
   DevBuf mom;  // per-pattern scalar-flux moments of the dataflow sweep [npat][n*G]
   DevBuf d_tile_cls, d_tile_ncls, d_cell_lcls;  // per-tile class lists (FlowGeom)
@@ -393,6 +395,10 @@ struct FlowGeom {
   const unsigned char* __restrict__ cell_lcls;  // [n] a cell's index in its tile's class list
   FlowSync* sync;
   unsigned int* flags;  // [npat][nchunk][ntz][nty][ntx] by oriented tile coordinates
+  // order in which tasks are handed out: entry t holds (tile * npat + pattern) * nchunk +
+  // chunk; every pattern's tasks appear tile diagonal by tile diagonal (null: that order)
+  const int* __restrict__ order;
+  int sleep_ns;  // back-off between polls of an upwind flag
 };
 
 __device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
@@ -414,7 +420,7 @@ __device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) 
 // Waits until *flag == epoch (relaxed polling, then one acquire load of the flag);
 // returns without waiting once any wait of the sweep ran out.
 __device__ __forceinline__ void flow_wait(const unsigned int* flag, unsigned int epoch, unsigned int* error,
-                                          unsigned int limit = kFlowSpinLimit) {
+                                          unsigned int limit = kFlowSpinLimit, int sleep_ns = 32) {
   for (unsigned int it = 0;; it++) {
     if (ld_relaxed_gpu(flag) == epoch) break;
     if (*(volatile unsigned int*)error) return;
@@ -422,7 +428,7 @@ __device__ __forceinline__ void flow_wait(const unsigned int* flag, unsigned int
       atomicExch(error, 1u);
       return;
     }
-    __nanosleep(32);
+    if (sleep_ns > 0) __nanosleep(sleep_ns);
   }
   (void)ld_acquire_gpu(flag);
 }
@@ -502,7 +508,8 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     __syncthreads();
     const int t = s_task;
     if (t >= K.ntasks) return;  // uniform over the CTA
-    const int jp = t / K.nchunk, ch = t - jp * K.nchunk;
+    const int tc = K.order ? K.order[t] : t;
+    const int jp = tc / K.nchunk, ch = tc - jp * K.nchunk;
     const int j = jp / K.npat, p = jp - j * K.npat;
     const int g0 = ch * Gc, gn = min(Gc, G - g0);
     const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
@@ -575,7 +582,8 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     if (threadIdx.x < 3) {
       const int a = threadIdx.x;
       const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
-      if (ux >= 0 && uy >= 0 && uz >= 0) flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error);
+      if (ux >= 0 && uy >= 0 && uz >= 0)
+        flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error, kFlowSpinLimit, K.sleep_ns);
       if (a == 0 && *(volatile unsigned int*)&K.sync->stall == (unsigned int)t + 1u)
         flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure: runs out
     }
@@ -636,11 +644,10 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
         }
       __syncthreads();
     }
-    // 5. publish the tile, then its scalar-flux moment over this pattern's directions
-    if (threadIdx.x == 0) {
-      __threadfence();
-      st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
-    }
+    // 5. publish the tile, then its scalar-flux moment over this pattern's directions: the
+    //    barrier that ended the last diagonal orders every thread's psi stores before thread
+    //    0's release store (release is cumulative), which the consumer pairs with an acquire
+    if (threadIdx.x == 0) st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
     if (mom) {
       for (int r = threadIdx.x; r < kCells * gn; r += blockDim.x) {
         const int c = r / gn, gg = r - c * gn;
@@ -1479,7 +1486,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
                        cls ? d.d_ccls.as<unsigned short>() : nullptr,
                        cls ? (sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr) : nullptr, d.d_tile_cls.as<int>(),
                        d.d_tile_ncls.as<int>(), d.d_cell_lcls.as<unsigned char>(), d.flow_sync.as<FlowSync>(),
-                       d.flow_flags.as<unsigned int>()};
+                       d.flow_flags.as<unsigned int>(), d.d_task_order.as<int>(), d.flow_sleep};
       k_flow_begin<<<1, 1, 0, p->stream>>>(K.sync);
       if (cls)
         flow_launch<T, true>(d, p->stream, A, W, K, P, iso);
@@ -2013,6 +2020,7 @@ struct KbaPlan {
   int t[3];  // tile shape
   int ntx, nty, ntz, nd, gchunk, nchunk, ntasks, npat;
   std::vector<int> tiles, pat_sign, pat_dirs_ptr, pat_dirs;
+  std::vector<int> order;  // hand-out order of the tasks (empty: canonical)
 };
 
 // Directions per dataflow-sweep task at most (0: a whole octant).  Fewer directions per
@@ -2021,6 +2029,28 @@ struct KbaPlan {
 static int flow_dirs_max() {
   const char* e = std::getenv("PGPU_FLOW_DIRS");
   return e ? std::max(0, std::atoi(e)) : 0;
+}
+
+// Hand-out order of the dataflow sweep's tasks: PGPU_FLOW_STAGGER = "W:K" splits the
+// independent pipelines (pattern, group chunk) into W waves and hands out wave w's tasks
+// as if they were K*w tile diagonals later, so that the pipelines' fill and drain phases
+// overlap instead of coinciding (unset: every pipeline starts at once).
+static void flow_stagger(int& waves, int& offset) {
+  waves = 1;
+  offset = 0;
+  const char* e = std::getenv("PGPU_FLOW_STAGGER");
+  if (!e) return;
+  int w = 1, k = 0;
+  if (std::sscanf(e, "%d:%d", &w, &k) == 2 && w >= 1 && w <= 64 && k >= 0 && k <= 1024) {
+    waves = w;
+    offset = k;
+  }
+}
+
+// Back-off between polls of an upwind tile's flag, in ns (PGPU_FLOW_SLEEP, default 32).
+static int flow_sleep_ns() {
+  const char* e = std::getenv("PGPU_FLOW_SLEEP");
+  return e ? std::min(1000, std::max(0, std::atoi(e))) : 32;
 }
 
 // (group, direction) slots of one task at most: kFlowSlots, or PGPU_FLOW_SLOTS (1-64).
@@ -2102,6 +2132,25 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
   const long long ntasks = (long long)K.ntx * K.nty * K.ntz * K.npat * K.nchunk;
   if (ntasks >= (1LL << 31)) return false;
   K.ntasks = (int)ntasks;
+  int waves, offset;
+  flow_stagger(waves, offset);
+  K.order.clear();
+  if (waves > 1 && offset > 0) {
+    // keys: tile diagonal + wave offset; a stable sort keeps each pipeline's tasks in
+    // diagonal order, so every task's upwind tasks are still handed out before it
+    std::vector<std::pair<long long, int>> key(K.ntasks);
+    for (int t = 0; t < K.ntasks; t++) {
+      const int jp = t / K.nchunk, ch = t - jp * K.nchunk;
+      const int j = jp / K.npat, pp = jp - j * K.npat;
+      const int D = K.tiles[3 * j] + K.tiles[3 * j + 1] + K.tiles[3 * j + 2];
+      const int q = pp * K.nchunk + ch;
+      key[t] = {(long long)D + (long long)(q % waves) * offset, t};
+    }
+    std::stable_sort(key.begin(), key.end(),
+                     [](const std::pair<long long, int>& a, const std::pair<long long, int>& b) { return a.first < b.first; });
+    K.order.resize(K.ntasks);
+    for (int t = 0; t < K.ntasks; t++) K.order[t] = key[t].second;
+  }
   return true;
 }
 
@@ -2343,6 +2392,8 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       d.kba_npat = kp.npat;
       for (int a = 0; a < 3; a++) d.kba_t[a] = kp.t[a];
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
+      if (!kp.order.empty()) up(d.d_task_order, kp.order.data(), kp.order.size() * 4);
+      d.flow_sleep = flow_sleep_ns();
       up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
       up(d.d_fpat_dirs_ptr, kp.pat_dirs_ptr.data(), kp.pat_dirs_ptr.size() * 4);
       up(d.d_fpat_dirs, kp.pat_dirs.data(), kp.pat_dirs.size() * 4);

@@ -186,6 +186,9 @@ int Driver::solve(int n, double dt, double t) {
     double s = std::chrono::duration<double>(t2 - t1).count();
     std::cout << std::scientific << std::setprecision(3) << "Solution time: " << s << "." << std::endl;
   }
+  if (n > 0 && !opt_.silent)
+    std::cout << std::scientific << std::setprecision(3) << "Time step size: " << dt << "." << std::endl
+              << "Physical time: " << t << "." << std::endl;
   PG_TRY(solver_->output(n), "unable to output the solution");
   print("\nDone.");
   return 0;

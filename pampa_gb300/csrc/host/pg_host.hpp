@@ -77,7 +77,7 @@ struct Material {
 
   int read(Tokens& tok);
   int read_file(const std::string& path);
-  int check_for_solver(int G, bool diffusion) const;
+  int check_for_solver(int G, bool diffusion, bool transient = false) const;
 
  private:
   int read_nuclear_data(Tokens& tok);
@@ -171,6 +171,10 @@ class NeutronicSolver : public Solver {
   int readCommon(const std::vector<std::string>& line, Tokens& tok, const Mesh& mesh, bool& used);
   virtual int buildProblem() = 0;   // assemble and upload the operator
   virtual int fetchSolution() = 0;  // copy fluxes back after a solve
+  // Transient step n > 0 (NeutronicSolver::solve with n > 0, NeutronicSolver.cxx:13-29);
+  // solvers without one report an error.
+  virtual int solveTransient(int n, double dt, double t);
+  void powerAndProduction();        // q, P, S and the total power from phi_ (host)
   const std::map<int, BoundaryCondition>& boundaryConditions() const;
 
   const Mesh* mesh_ = nullptr;
@@ -185,16 +189,24 @@ class NeutronicSolver : public Solver {
   std::vector<double> T_, S_, phi_, q_, P_;
   pgpu_problem* problem_ = nullptr;
   pgpu_stats stats_{};
+  bool transient_ = false;
+  int n0_ = -1;                      // last time step whose flux was kept (Solver.hxx:56)
+  std::vector<double> phi_prev_;     // scalar flux of the previous time step (phi0)
 };
 
 class DiffusionSolver : public NeutronicSolver {
  public:
   DiffusionSolver() : NeutronicSolver("diffusion") {}
+  ~DiffusionSolver() override;
   int read(Tokens& tok, const Mesh& mesh) override;
+  int finalize() override;
 
  protected:
   int buildProblem() override;
   int fetchSolution() override;
+  int solveTransient(int n, double dt, double t) override;
+  pgpu_problem* transient_problem_ = nullptr;  // R with the 1/(v dt) terms, chi = (1 - beta) chi_p
+  double transient_dt_ = 0.0;
 };
 
 class SNSolver : public NeutronicSolver {

@@ -295,13 +295,18 @@ int Material::finish_nuclear_data() {
 }
 
 // ConstantNuclearData::check(G, diffusion, transient) (ConstantNuclearData.cxx:180-200).
-int Material::check_for_solver(int G, bool diffusion_solver) const {
+int Material::check_for_solver(int G, bool diffusion_solver, bool transient) const {
   PG_CHECK(!has_nd, "missing nuclear data");
   PG_CHECK(num_groups != G, "wrong number of energy groups");
   PG_CHECK(sigma_t.empty(), "missing total cross sections");
   PG_CHECK(sigma_s.empty(), "missing scattering cross sections");
   PG_CHECK(chi.empty(), "missing effective fission spectrum");
   if (diffusion_solver) PG_CHECK(diffusion.empty(), "missing diffusion coefficients");
+  if (transient) {
+    PG_CHECK(chi_prompt.empty(), "missing prompt fission spectrum");
+    PG_CHECK(chi_delayed.empty(), "missing delayed fission spectrum");
+    PG_CHECK(velocity.empty(), "missing neutron velocities");
+  }
   return 0;
 }
 

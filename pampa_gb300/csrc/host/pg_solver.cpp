@@ -89,13 +89,15 @@ const std::map<int, BoundaryCondition>& NeutronicSolver::boundaryConditions() co
 
 int NeutronicSolver::initialize(const Mesh& mesh, const std::vector<Material>& mats,
                                 const RunOptions& opt, bool transient) {
-  (void)transient;
   mesh_ = &mesh;
   mats_ = &mats;
   opt_ = opt;
   opt_.gpu.power = power_;
+  transient_ = transient;
+  n0_ = -1;
   PG_CHECK(G_ < 1, "missing number of energy groups");
-  for (const auto& m : mats) PG_TRY(m.check_for_solver(G_, name_ == "diffusion"), "wrong material data");
+  for (const auto& m : mats)
+    PG_TRY(m.check_for_solver(G_, name_ == "diffusion", transient), "wrong material data");
   const int n = mesh.num_cells;
   T_.assign(n, 0.0);
   S_.assign(n, 0.0);
@@ -111,11 +113,10 @@ int NeutronicSolver::initialize(const Mesh& mesh, const std::vector<Material>& m
   return 0;
 }
 
-// NeutronicSolver::solve (NeutronicSolver.cxx:4-43), steady state only.
+// NeutronicSolver::solve (NeutronicSolver.cxx:4-43): n = 0 is the k-eigenvalue solve,
+// n > 0 a transient step.
 int NeutronicSolver::solve(int n, double dt, double t) {
-  (void)dt;
-  (void)t;
-  PG_CHECK(n != 0, "transient steps (n > 0) are not part of this build's k-eigenvalue path");
+  if (n > 0) return solveTransient(n, dt, t);
   if (!problem_) PG_TRY(buildProblem(), "unable to build the coefficient matrices");
   int st = pgpu_problem_solve(problem_, &opt_.gpu, &stats_);
   PG_CHECK(st != PGPU_OK, std::string("GPU k-eigenvalue solve failed: ") + pgpu_last_error());
@@ -128,6 +129,34 @@ int NeutronicSolver::solve(int n, double dt, double t) {
   for (int i = 0; i < mesh_->num_cells; i++) S_[i] = (*mats_)[mesh_->materials[i]].beta_total * P_[i];
   PG_TRY(fetchSolution(), "unable to get the solution");
   return 0;
+}
+
+int NeutronicSolver::solveTransient(int n, double dt, double t) {
+  (void)n;
+  (void)dt;
+  (void)t;
+  PG_CHECK(true, "transient steps (n > 0) are not available for the " + name_ + " solver in this build");
+}
+
+// NeutronicSolver::calculatePowerAndProductionRate (NeutronicSolver.cxx:81-116) for a
+// flux that is not normalised (transient steps): q_i = sum_g phi kappa_sigma_f V,
+// P_i = sum_g phi nu_sigma_f V / keff, S_i = beta P_i, and the total power.
+void NeutronicSolver::powerAndProduction() {
+  const int n = mesh_->num_cells;
+  total_power_ = 0.0;
+  for (int i = 0; i < n; i++) {
+    const Material& mat = (*mats_)[mesh_->materials[i]];
+    const double V = mesh_->volumes[i];
+    q_[i] = 0.0;
+    P_[i] = 0.0;
+    for (int g = 0; g < G_; g++) {
+      const double ph = phi_[(size_t)i * G_ + g];
+      q_[i] += ph * mat.kappa_sigma_f[g] * V;
+      P_[i] += ph * mat.nu_sigma_f[g] * V / keff_;
+    }
+    S_[i] = mat.beta_total * P_[i];
+    total_power_ += q_[i];
+  }
 }
 
 // NeutronicSolver::printLog (NeutronicSolver.cxx:119-127) through PhysicsSolver::output.
@@ -287,6 +316,81 @@ int DiffusionSolver::buildProblem() {
 }
 
 int DiffusionSolver::fetchSolution() { return 0; }
+
+DiffusionSolver::~DiffusionSolver() {
+  if (transient_problem_) pgpu_problem_destroy(transient_problem_);
+}
+
+int DiffusionSolver::finalize() {
+  if (transient_problem_) pgpu_problem_destroy(transient_problem_);
+  transient_problem_ = nullptr;
+  return NeutronicSolver::finalize();
+}
+
+// Transient step n > 0 of DiffusionSolver (DiffusionSolver.cxx:94-175, getSolution :337-345):
+// keep the previous step's flux as phi0 when the step advances, then solve
+//   (R + V/(v dt) - (1 - beta) chi_p nu_sigma_f V / keff) phi = chi_d S + V/(v dt) phi0
+// on the GPU (pgpu_problem_solve_linear), starting from the current flux as the
+// reference's KSP does (petsc.cxx:168), and compute the power, the production rate and the
+// delayed source S = beta P (NeutronicSolver.cxx:81-116).
+int DiffusionSolver::solveTransient(int n, double dt, double t) {
+  (void)t;
+  PG_CHECK(keff_ <= 0.0, "the steady state must be solved before a transient step");
+  PG_CHECK(!(dt > 0.0), "wrong time-step size");
+  const Mesh& mesh = *mesh_;
+  const int nc = mesh.num_cells;
+  if (n > n0_ + 1) {
+    phi_prev_ = phi_;
+    n0_++;
+  }
+  if (!transient_problem_ || dt != transient_dt_) {
+    if (transient_problem_) pgpu_problem_destroy(transient_problem_);
+    transient_problem_ = nullptr;
+    std::vector<int> nbr;
+    std::vector<double> off, diag, st, ss, chi, nsf, ksf;
+    PG_TRY(assemble_diffusion(mesh, *mats_, G_, boundaryConditions(), nbr, off, diag),
+           "unable to assemble the diffusion operator");
+    material_tables(*mats_, G_, st, ss, chi, nsf, ksf);
+    for (int i = 0; i < nc; i++) {
+      const Material& mat = (*mats_)[mesh.materials[i]];
+      for (int g = 0; g < G_; g++) diag[(size_t)i * G_ + g] += mesh.volumes[i] / (mat.velocity[g] * dt);
+    }
+    for (size_t m = 0; m < mats_->size(); m++) {
+      const Material& mat = (*mats_)[m];
+      if (!mat.has_nd) continue;
+      for (int g = 0; g < G_; g++) chi[m * G_ + g] = (1.0 - mat.beta_total) * mat.chi_prompt[g];
+    }
+    pgpu_diffusion_operator op;
+    op.num_cells = nc;
+    op.num_groups = G_;
+    op.num_faces = mesh.fmax;
+    op.num_materials = (int)mats_->size();
+    op.neighbors = nbr.data();
+    op.offdiag = off.data();
+    op.diag = diag.data();
+    op.materials = mesh.materials.data();
+    op.volumes = mesh.volumes.data();
+    op.sigma_s = ss.data();
+    op.chi = chi.data();
+    op.nu_sigma_f = nsf.data();
+    op.kappa_sigma_f = ksf.data();
+    int code = pgpu_diffusion_create(opt_.device, &op, &transient_problem_);
+    PG_CHECK(code != PGPU_OK, std::string("unable to upload the transient operator: ") + pgpu_last_error());
+    transient_dt_ = dt;
+  }
+  std::vector<double> b((size_t)nc * G_);
+  for (int i = 0; i < nc; i++) {
+    const Material& mat = (*mats_)[mesh.materials[i]];
+    for (int g = 0; g < G_; g++) {
+      const size_t l = (size_t)i * G_ + g;
+      b[l] = mat.chi_delayed[g] * S_[i] + mesh.volumes[i] / (mat.velocity[g] * dt) * phi_prev_[l];
+    }
+  }
+  int st = pgpu_problem_solve_linear(transient_problem_, 1.0 / keff_, b.data(), phi_.data(), &opt_.gpu, &stats_);
+  PG_CHECK(st != PGPU_OK, std::string("GPU transient solve failed: ") + pgpu_last_error());
+  powerAndProduction();
+  return 0;
+}
 
 // ----------------------------------------------------------------------------------
 // SN

@@ -35,3 +35,36 @@ def diffusion_operator_from_oracle(prob, R):
     return dict(neighbors=nbr, offdiag=off, diag=R.diagonal(), materials=mesh.materials,
                 volumes=mesh.volumes, sigma_s=m["sigma_s"], chi=m["chi"], nu_sigma_f=m["nu_sigma_f"],
                 kappa_sigma_f=m["kappa_sigma_f"])
+
+
+def bc_split_input(d: str, solver: str = "diffusion", right: str = "reflective") -> str:
+    """A 2D 10x8 input whose third material is a split boundary-condition material
+    (`bc 1`, `split 1`; Mesh.cxx:24-204): its cells form two disconnected strips (x = 0 and
+    x = 9), which splitting turns into the boundaries edge-0 and edge-1, and which are then
+    removed from the mesh (68 cells remain).  edge-0 is vacuum, edge-1 `right`."""
+    import os
+
+    from pampa_gb300 import workloads as wl
+
+    rng = np.random.default_rng(7)
+    self_scatter = (0.2, 0.5) if solver == "sn" else None
+    mats = wl.materials_2g(rng, 3, self_scatter=self_scatter)
+    nx, ny = 10, 8
+    lay = np.full((1, ny, nx), 2)
+    lay[0, 2:6, 3:7] = 1
+    lay[0, 1:7, 0] = 3
+    lay[0, 1:7, nx - 1] = 3
+    wl.write_cartesian_mesh(os.path.join(d, "mesh.pmp"), 5.0, nx, ny, 0, lay, {})
+    for k, m in enumerate(mats):
+        wl.write_material(os.path.join(d, f"mat{k + 1}.pmp"), m, solver == "diffusion")
+    with open(os.path.join(d, "mat3.pmp"), "a") as fh:
+        fh.write("bc 1\nsplit 1\n")
+    lines = ["mesh cartesian mesh.pmp", "", "material fuel mat1.pmp", "material refl mat2.pmp",
+             "material edge mat3.pmp", "", f"solver {solver} {{", "   energy-groups 2"]
+    if solver == "sn":
+        lines += ["   order 2", "   mixed-face-interpolation 1.0"]
+    lines += ["   bc -x vacuum", "   bc +x vacuum", "   bc -y reflective", "   bc +y vacuum",
+              "   bc edge-0 vacuum", f"   bc edge-1 {right}", "}"]
+    with open(os.path.join(d, "input.pmp"), "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return os.path.join(d, "input.pmp")
