@@ -169,6 +169,8 @@ class Material:
     D: np.ndarray | None = None
     chi: np.ndarray | None = None     # effective fission spectrum
     beta_total: float = 0.0
+    lam: np.ndarray | None = None     # precursor decay constants (precursor-data)
+    beta: np.ndarray | None = None    # delayed-neutron fractions per precursor group
     chi_p: np.ndarray | None = None   # prompt fission spectrum
     chi_d: np.ndarray | None = None   # delayed fission spectrum
     vel: np.ndarray | None = None     # neutron velocities
@@ -195,9 +197,10 @@ class Material:
                     if l2[0] == "precursor-groups":
                         npg = int(l2[1])
                     elif l2[0] == "lambda":
-                        tok.read_values(npg)
+                        self.lam = np.array(tok.read_values(npg), dtype=np.float64)
                     elif l2[0] == "beta":
                         beta = tok.read_values(npg)
+                        self.beta = np.array(beta, dtype=np.float64)
                         bt = 0.0
                         for b in beta:          # PrecursorData.cxx:44-45 (sequential sum)
                             bt += b
@@ -1249,4 +1252,59 @@ def run_transient(path: str, delayed_source_scale: float = 1.0, tol: float = 1e-
         P = np.sum(ph2 * nsf * V[:, None] / keff, axis=1)
         S = beta * P
         out.append(dict(dt=dt, t=t, phi=phi, q=q, P=P, power=float(np.sum(q))))
+    return out
+
+
+
+def precursor_step(prob: Problem, npg: int, P: np.ndarray, C0: np.ndarray | None, dt: float):
+    """PrecursorSolver::solve (PrecursorSolver.cxx:59-127): C = beta/lambda P (steady
+    state, C0 None) or (C0 + dt beta P) / (1 + dt lambda); S = sum_g lambda C."""
+    n = prob.mesh.n
+    C = np.zeros((n, npg))
+    S = np.zeros(n)
+    for i in range(n):
+        m = prob.materials[prob.mesh.materials[i]]
+        if m.lam is None:
+            continue
+        for g in range(npg):
+            if C0 is None:
+                C[i, g] = (m.beta[g] / m.lam[g]) * P[i]
+            else:
+                C[i, g] = (C0[i, g] + dt * m.beta[g] * P[i]) / (1.0 + dt * m.lam[g])
+            S[i] += m.lam[g] * C[i, g]
+    return C, S
+
+
+def run_coupled_transient(prob: Problem, npg: int, tol: float = 1e-12, max_iter: int = 200,
+                          precursor_scale: float = 1.0) -> list[dict]:
+    """Diffusion coupled to the precursor solver by implicit fixed-point iteration
+    (CouplingSolver.cxx:77-145) over the steady state and every time step of prob.dt:
+    diffusion solve, production rate to the precursors, their delayed source back to the
+    diffusion solve, until the power and the delayed source stop changing (relative
+    2-norm below tol).  The precursor populations are scaled by precursor_scale after the
+    steady state, as a caller setting the "precursors" field would.  Returns per step phi,
+    q, P, C, S and the total power."""
+    res = solve_problem(prob)
+    keff = res["keff"]
+    ksf, nsf = _kappa_nu_tables(prob)
+    V = prob.mesh.volumes
+    C, S = precursor_step(prob, npg, res["P"], None, 0.0)
+    out = [dict(keff=keff, phi=res["phi"], q=res["q"], P=res["P"], C=C, S=S, power=res["power"])]
+    phi = res["phi"]
+    C = C * precursor_scale
+    for dt in prob.dt:
+        phi_prev, C0 = phi.copy(), C.copy()
+        q_old = S_old = None
+        for _ in range(max_iter):
+            R, b = diffusion_transient_system(prob, res["R"], dt, keff, phi_prev, S)
+            phi = spla.spsolve(R.tocsc(), b)
+            ph2 = phi.reshape(prob.mesh.n, prob.G)
+            q = np.sum(ph2 * ksf * V[:, None], axis=1)
+            P = np.sum(ph2 * nsf * V[:, None] / keff, axis=1)
+            C, S = precursor_step(prob, npg, P, C0, dt)
+            if q_old is not None and np.linalg.norm(q - q_old) < tol * np.linalg.norm(q) and \
+                    np.linalg.norm(S - S_old) < tol * np.linalg.norm(S):
+                break
+            q_old, S_old = q, S
+        out.append(dict(dt=dt, phi=phi, q=q, P=P, C=C, S=S, power=float(np.sum(q))))
     return out

@@ -1431,6 +1431,11 @@ int flow_prepare(SNData& d) {
   PGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   PGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_flow<T, kClass, TX, TY, TZ>, nt, smem));
   if (per_sm < 1) return fail(PGPU_ERR_CUDA, "the dataflow sweep does not fit on an SM");
+  // CTAs per SM of the persistent grid: all that fit, or PGPU_FLOW_CTAS{64,32} (fewer CTAs
+  // contend less for an SM's FP64 pipe, so each task -- and the wavefront's critical path
+  // of tasks -- runs faster)
+  const char* ce = std::getenv(sizeof(T) == 8 ? "PGPU_FLOW_CTAS64" : "PGPU_FLOW_CTAS32");
+  if (ce && std::atoi(ce) > 0) per_sm = std::min(per_sm, std::atoi(ce));
   d.flow_grid[sizeof(T) == 8 ? 0 : 1] = std::min(d.kba_ntasks, sms * per_sm);
   return PGPU_OK;
 }
@@ -2110,7 +2115,8 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
   K.gchunk = std::max(1, std::min(op->num_groups, flow_slots() / std::max(1, K.nd)));
   K.nchunk = (op->num_groups + K.gchunk - 1) / K.gchunk;
   // 8x8x4 tiles when the box divides into them, 4x4x4 otherwise
-  const bool big = nx % 8 == 0 && ny % 8 == 0;
+  const char* te = std::getenv("PGPU_FLOW_TILE");  // 4: force 4x4x4 tiles (measurement)
+  const bool big = nx % 8 == 0 && ny % 8 == 0 && !(te && std::atoi(te) == 4);
   K.t[0] = big ? 8 : 4;
   K.t[1] = big ? 8 : 4;
   K.t[2] = 4;

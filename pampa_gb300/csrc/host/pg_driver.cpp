@@ -85,17 +85,28 @@ int parse(const std::string& filename, ParseState& st) {
                    "wrong material index in the mesh");
         st.ready = true;
       }
+      // the factory of Parser.cxx:148-165 under the reference's keywords
       std::unique_ptr<Solver> s;
+      size_t arg = 2;
       if (line[1] == "diffusion") s.reset(new DiffusionSolver());
       else if (line[1] == "sn") s.reset(new SNSolver());
-      else PG_CHECK(true, "solver type '" + line[1] + "' is not supported by this build");
-      if (line[2] == "{") {
-        PG_TRY(s->read(tok, *st.mesh), "unable to read the solver from " + filename);
+      else if (line[1] == "precursors") s.reset(new PrecursorSolver());
+      else if (line[1] == "coupled") {
+        PG_CHECK(line.size() < 4, "wrong number of arguments for keyword 'solver'");
+        s.reset(new CouplingSolver(line[2]));
+        arg = 3;
+      } else {
+        PG_CHECK(true, "solver type '" + line[1] + "' is not supported by this build");
+      }
+      std::vector<Solver*> defined;
+      for (auto& d : st.solvers) defined.push_back(d.get());
+      if (line[arg] == "{") {
+        PG_TRY(s->read(tok, *st.mesh, defined), "unable to read the solver from " + filename);
       } else {
         Tokens t2;
-        std::string path = resolve_path(line[2], base);
+        std::string path = resolve_path(line[arg], base);
         PG_TRY(t2.open(path), "unable to open " + path);
-        PG_TRY(s->read(t2, *st.mesh), "unable to read the solver from " + path);
+        PG_TRY(s->read(t2, *st.mesh, defined), "unable to read the solver from " + path);
       }
       st.solvers.push_back(std::move(s));
     } else if (k == "dt") {
@@ -167,9 +178,16 @@ int Driver::initialize(int argc, char* argv[], std::vector<double>& dt) {
   st_ = ParseState();
   PG_TRY(parse(filename, st_), "unable to parse " + filename);
   dt = st_.dt;
+  // Driver::getMainSolver (Driver.cxx:115-129): the only solver, or the one named "main"
   PG_CHECK(st_.solvers.empty(), "no solvers defined");
-  PG_CHECK(st_.solvers.size() != 1, "only a single neutronic solver is supported by this build");
-  solver_ = st_.solvers[0].get();
+  solver_ = nullptr;
+  if (st_.solvers.size() == 1) {
+    solver_ = st_.solvers[0].get();
+  } else {
+    for (auto& s : st_.solvers)
+      if (s->name() == "main") solver_ = s.get();
+    PG_CHECK(!solver_, "unable to find the main solver");
+  }
   PG_TRY(solver_->initialize(*st_.mesh, st_.materials, opt_, !dt.empty()), "unable to initialize the solver");
   print("Done.");
   return 0;
@@ -270,7 +288,7 @@ void pampa_set_field(const double* v, const char name[], int* error) {
 }
 
 void pampa_get_keff(double* keff, int* error) {
-  auto* s = dynamic_cast<pg::NeutronicSolver*>(g_pampa.solver());
+  auto* s = g_pampa.solver() ? g_pampa.solver()->neutronic() : nullptr;
   *error = s ? 0 : 1;
   if (s) *keff = s->keff();
 }
@@ -281,13 +299,13 @@ void pampa_get_field_size(const char name[], int* size, int* error) {
 }
 
 void pampa_get_problem(pgpu_problem** problem, int* error) {
-  auto* s = dynamic_cast<pg::NeutronicSolver*>(g_pampa.solver());
+  auto* s = g_pampa.solver() ? g_pampa.solver()->neutronic() : nullptr;
   *error = s ? s->problem(problem) : 1;
   if (*error > 0) std::printf("Error in pampa_get_problem().\n");
 }
 
 void pampa_get_solve_stats(int* outer, int* inner, double* seconds, int* error) {
-  auto* s = dynamic_cast<pg::NeutronicSolver*>(g_pampa.solver());
+  auto* s = g_pampa.solver() ? g_pampa.solver()->neutronic() : nullptr;
   *error = s ? 0 : 1;
   if (!s) return;
   *outer = s->stats().outer_iterations;

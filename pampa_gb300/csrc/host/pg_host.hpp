@@ -71,6 +71,10 @@ struct Material {
   int num_groups = -1;
   double beta_total = 0.0;
   int num_sub = 0;
+  // precursor data (PrecursorData.hxx): groups, decay constants, delayed fractions
+  bool has_pd = false;
+  int num_precursor_groups = 0;
+  std::vector<double> precursor_lambda, precursor_beta;
   std::vector<double> sigma_t, nu_sigma_f, kappa_sigma_f, sigma_tr, diffusion, chi_prompt,
       chi_delayed, chi, velocity;
   std::vector<double> sigma_s;  // [from][to]
@@ -122,10 +126,33 @@ int remove_bc_materials(const Mesh& in, const std::vector<Material>& materials, 
 // ----------------------------------------------------------------------------------
 // Solvers (Solver.hxx:31-98, PhysicsSolver.hxx, NeutronicSolver.hxx).
 // ----------------------------------------------------------------------------------
+// ConvergenceError (ConvergenceError.hxx): the norm of the change of a field between two
+// coupling iterations, absolute or relative to the field's L2 norm, against a tolerance.
+class ConvergenceError {
+ public:
+  ConvergenceError(std::string name, int norm, bool relative, double tol)
+      : name_(std::move(name)), norm_(norm), relative_(relative), tol_(tol) {}
+  // converged = false on the first call (no previous iterate), then |v - v_prev| < tol.
+  int check(const std::vector<double>& v, bool& converged, bool verbose);
+
+ private:
+  std::string name_;
+  int norm_;  // 1, 2, or 0 for the max norm
+  bool relative_;
+  double tol_;
+  bool have_prev_ = false;
+  std::vector<double> prev_;
+};
+
+// `convergence <field> <1|2|max> <relative 0|1> <tol>` (input.cxx:406-425); name is the
+// field, line[i] its first argument.
+int read_convergence(const std::vector<std::string>& line, size_t i, std::shared_ptr<ConvergenceError>& out);
+
 struct Field {
   std::string name;
   std::vector<double>* vec = nullptr;
   bool input = false, output = false;
+  std::shared_ptr<ConvergenceError> delta;  // convergence of an output field (coupling)
 };
 
 struct RunOptions {
@@ -134,25 +161,83 @@ struct RunOptions {
   bool verbose = false, silent = false;
 };
 
+class NeutronicSolver;
+
 class Solver {
  public:
   explicit Solver(std::string name) : name_(std::move(name)) {}
   virtual ~Solver() = default;
-  virtual int read(Tokens& tok, const Mesh& mesh) = 0;
+  // Solver::read (Solver.hxx:31-98): the solver block, with the solvers defined before it
+  // (a coupled solver names them).
+  virtual int read(Tokens& tok, const Mesh& mesh, std::vector<Solver*>& solvers) = 0;
   virtual int initialize(const Mesh& mesh, const std::vector<Material>& mats,
                          const RunOptions& opt, bool transient) = 0;
   virtual int solve(int n, double dt, double t) = 0;
   virtual int output(int n) const = 0;
   virtual int finalize() = 0;
+  // The neutronic solver of this solver's tree (itself, or the first one a coupled solver
+  // holds), for the C API's keff / statistics / problem accessors; null if none.
+  virtual NeutronicSolver* neutronic() { return nullptr; }
   int getField(double* v, const std::string& name) const;
   int setField(const double* v, const std::string& name);
   int fieldSize(const std::string& name, int& size) const;
   const std::string& name() const { return name_; }
+  std::vector<Field>& fields() { return fields_; }
 
  protected:
   std::string name_;
   std::vector<Field> fields_;
+  int n0_ = -1;  // last time step whose solution was kept (Solver.hxx:56)
 };
+
+// PrecursorSolver (PrecursorSolver.cxx): delayed-neutron precursor populations per cell and
+// precursor group from the production rate, steady state C = beta/lambda P, time step
+// C = (C0 + dt beta P) / (1 + dt lambda), and the delayed source S = sum lambda C.  The
+// update is a few operations per cell, done on the host next to the coupling loop.
+class PrecursorSolver : public Solver {
+ public:
+  PrecursorSolver() : Solver("precursors") {}
+  int read(Tokens& tok, const Mesh& mesh, std::vector<Solver*>& solvers) override;
+  int initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
+                 bool transient) override;
+  int solve(int n, double dt, double t) override;
+  int output(int n) const override;
+  int finalize() override { return 0; }
+
+ private:
+  const Mesh* mesh_ = nullptr;
+  const std::vector<Material>* mats_ = nullptr;
+  RunOptions opt_;
+  int npg_ = -1;
+  // convergence errors of the output fields (PrecursorSolver.hxx:18-22 defaults)
+  std::shared_ptr<ConvergenceError> dC_ = std::make_shared<ConvergenceError>("precursors", 2, true, 1.0);
+  std::shared_ptr<ConvergenceError> dS_ = std::make_shared<ConvergenceError>("delayed-source", 2, true, 1.0);
+  std::vector<double> P_, C_, C0_, S_;
+};
+
+// CouplingSolver (CouplingSolver.cxx): fixed-point (Picard) iteration over coupled solvers,
+// copying every output field into the solvers that take it as input, until the output
+// fields' convergence errors are met (implicit coupling) or once (explicit coupling).
+class CouplingSolver : public Solver {
+ public:
+  explicit CouplingSolver(std::string name) : Solver(std::move(name)) {}
+  int read(Tokens& tok, const Mesh& mesh, std::vector<Solver*>& solvers) override;
+  int initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
+                 bool transient) override;
+  int solve(int n, double dt, double t) override;
+  int output(int n) const override;
+  int finalize() override;
+  NeutronicSolver* neutronic() override;
+
+ private:
+  std::vector<Solver*> coupled_;
+  bool implicit_ = false;
+  RunOptions opt_;
+};
+
+// The reference iterates an implicit coupling until it converges, with no cap; here a
+// coupling that has not converged after this many iterations is an error.
+constexpr int kMaxCouplingIterations = 1000;
 
 class NeutronicSolver : public Solver {
  public:
@@ -163,12 +248,16 @@ class NeutronicSolver : public Solver {
   int solve(int n, double dt, double t) override;
   int output(int n) const override;
   int finalize() override;
+  NeutronicSolver* neutronic() override { return this; }
   double keff() const { return keff_; }
   int problem(pgpu_problem** out);
   const pgpu_stats& stats() const { return stats_; }
 
  protected:
   int readCommon(const std::vector<std::string>& line, Tokens& tok, const Mesh& mesh, bool& used);
+  // convergence errors of the output fields (NeutronicSolver.hxx:39-43 defaults)
+  std::shared_ptr<ConvergenceError> dq_ = std::make_shared<ConvergenceError>("power", 2, true, 1.0);
+  std::shared_ptr<ConvergenceError> dP_ = std::make_shared<ConvergenceError>("production-rate", 2, true, 1.0);
   virtual int buildProblem() = 0;   // assemble and upload the operator
   virtual int fetchSolution() = 0;  // copy fluxes back after a solve
   // Transient step n > 0 (NeutronicSolver::solve with n > 0, NeutronicSolver.cxx:13-29);
@@ -190,7 +279,6 @@ class NeutronicSolver : public Solver {
   pgpu_problem* problem_ = nullptr;
   pgpu_stats stats_{};
   bool transient_ = false;
-  int n0_ = -1;                      // last time step whose flux was kept (Solver.hxx:56)
   std::vector<double> phi_prev_;     // scalar flux of the previous time step (phi0)
 };
 
@@ -198,7 +286,7 @@ class DiffusionSolver : public NeutronicSolver {
  public:
   DiffusionSolver() : NeutronicSolver("diffusion") {}
   ~DiffusionSolver() override;
-  int read(Tokens& tok, const Mesh& mesh) override;
+  int read(Tokens& tok, const Mesh& mesh, std::vector<Solver*>& solvers) override;
   int finalize() override;
 
  protected:
@@ -212,7 +300,7 @@ class DiffusionSolver : public NeutronicSolver {
 class SNSolver : public NeutronicSolver {
  public:
   SNSolver() : NeutronicSolver("sn") {}
-  int read(Tokens& tok, const Mesh& mesh) override;
+  int read(Tokens& tok, const Mesh& mesh, std::vector<Solver*>& solvers) override;
   int initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
                  bool transient) override;
 

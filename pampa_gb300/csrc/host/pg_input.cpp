@@ -191,22 +191,25 @@ int Material::read(Tokens& tok) {
     } else if (k == "precursor-data") {
       PG_CHECK(line.size() != 2 || line[1] != "{", "missing opening '{' for precursor data");
       int npg = 0;
+      has_pd = true;
       while (true) {
         std::vector<std::string> l2 = tok.next();
         if (l2.empty() || l2[0] == "}") break;
         if (l2[0] == "precursor-groups") {
           PG_TRY(to_int(l2.at(1), 1, INT_MAX, npg), "wrong number of precursor groups");
         } else if (l2[0] == "lambda") {
-          std::vector<double> lam;
-          PG_TRY(tok.read_doubles(lam, npg, 0.0, DBL_MAX), "wrong precursor decay constants");
+          PG_TRY(tok.read_doubles(precursor_lambda, npg, 0.0, DBL_MAX), "wrong precursor decay constants");
         } else if (l2[0] == "beta") {
-          std::vector<double> beta;
-          PG_TRY(tok.read_doubles(beta, npg, 0.0, DBL_MAX), "wrong precursor fractions");
-          for (double b : beta) beta_total += b;  // PrecursorData.cxx:44-45
+          PG_TRY(tok.read_doubles(precursor_beta, npg, 0.0, DBL_MAX), "wrong precursor fractions");
+          beta_total = 0.0;
+          for (double b : precursor_beta) beta_total += b;  // PrecursorData.cxx:44-45
         } else {
           PG_CHECK(true, "unrecognized keyword '" + l2[0] + "'");
         }
       }
+      num_precursor_groups = npg;
+      PG_CHECK(precursor_lambda.size() != (size_t)npg || precursor_beta.size() != (size_t)npg,
+               "missing precursor decay constants or fractions");
     } else if (k == "thermal-properties") {
       PG_CHECK(line.size() < 2, "wrong number of arguments for keyword 'thermal-properties'");
     } else if (k == "fuel") {

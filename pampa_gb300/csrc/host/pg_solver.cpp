@@ -74,8 +74,15 @@ int NeutronicSolver::readCommon(const std::vector<std::string>& line, Tokens& to
     PG_CHECK(line.size() != 2, "wrong number of arguments for keyword '" + k + "'");
     PG_TRY(to_double(line[1], 0.0, DBL_MAX, power_), "wrong power level");
   } else if (k == "convergence") {
-    // Convergence errors only drive the coupled (Picard) solver; read and ignored here.
+    // convergence errors of the output fields drive an implicit coupling (CouplingSolver)
     PG_CHECK(line.size() != 5, "wrong number of arguments for keyword '" + k + "'");
+    if (line[1] == "power") {
+      PG_TRY(read_convergence(line, 1, dq_), "wrong convergence error");
+    } else if (line[1] == "production-rate") {
+      PG_TRY(read_convergence(line, 1, dP_), "wrong convergence error");
+    } else {
+      PG_CHECK(true, "wrong field");
+    }
   } else {
     used = false;
   }
@@ -105,11 +112,11 @@ int NeutronicSolver::initialize(const Mesh& mesh, const std::vector<Material>& m
   q_.assign(n, 0.0);
   P_.assign(n, 0.0);
   fields_.clear();
-  fields_.push_back({"temperature", &T_, true, false});
-  fields_.push_back({"delayed-source", &S_, true, false});
-  fields_.push_back({"scalar-flux", &phi_, false, false});
-  fields_.push_back({"power", &q_, false, true});
-  fields_.push_back({"production-rate", &P_, false, true});
+  fields_.push_back({"temperature", &T_, true, false, nullptr});
+  fields_.push_back({"delayed-source", &S_, true, false, nullptr});
+  fields_.push_back({"scalar-flux", &phi_, false, false, nullptr});
+  fields_.push_back({"power", &q_, false, true, dq_});
+  fields_.push_back({"production-rate", &P_, false, true, dP_});
   return 0;
 }
 
@@ -186,7 +193,8 @@ int NeutronicSolver::finalize() {
 // Diffusion
 // ----------------------------------------------------------------------------------
 
-int DiffusionSolver::read(Tokens& tok, const Mesh& mesh) {
+int DiffusionSolver::read(Tokens& tok, const Mesh& mesh, std::vector<Solver*>& solvers) {
+  (void)solvers;
   while (true) {
     std::vector<std::string> line = tok.next();
     if (line.empty() || line[0] == "}") break;
@@ -396,7 +404,8 @@ int DiffusionSolver::solveTransient(int n, double dt, double t) {
 // SN
 // ----------------------------------------------------------------------------------
 
-int SNSolver::read(Tokens& tok, const Mesh& mesh) {
+int SNSolver::read(Tokens& tok, const Mesh& mesh, std::vector<Solver*>& solvers) {
+  (void)solvers;
   while (true) {
     std::vector<std::string> line = tok.next();
     if (line.empty() || line[0] == "}") break;
@@ -659,7 +668,7 @@ int SNSolver::initialize(const Mesh& mesh, const std::vector<Material>& mats,
   PG_CHECK(order_ != 2 && order_ != 4 && order_ != 6 && order_ != 8, "SN order not implemented");
   M_ = order_ * (order_ + 2);
   psi_.assign((size_t)mesh.num_cells * G_ * M_, 0.0);
-  fields_.push_back({"angular-flux", &psi_, false, false});  // SNSolver.cxx:745-747
+  fields_.push_back({"angular-flux", &psi_, false, false, nullptr});  // SNSolver.cxx:745-747
   return 0;
 }
 

@@ -49,3 +49,24 @@ def test_own_front_end_compiles_against_the_header(tmp_path):
     subprocess.run(["gcc", "-O2", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "frontend", "pampa_main.c"), "-L", libdir, "-lpampa_gb300",
                     f"-Wl,-rpath,{libdir}", "-o", str(tmp_path / "pampa")], check=True)
+
+
+def test_precursor_golden_case_without_a_gpu(tmp_path):
+    """pwr-iaea-benchmark/cartesian-precursors-3d runs the precursor solver alone (steady
+    state and four steps; PrecursorSolver.cxx), which needs no GPU: the front end's output
+    must equal the reference's printed lines, including "Precursor population: 0.000e+00
+    (min), 1.424e-06 (max)." at every step."""
+    import pampa_gb300.build as b
+    lib = b.build()
+    libdir = os.path.dirname(lib)
+    exe = str(tmp_path / "pampa")
+    subprocess.run(["gcc", "-O2", "-std=c99", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "frontend", "pampa_main.c"), "-L", libdir, "-lpampa_gb300",
+                    f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
+    case = "pwr-iaea-benchmark/cartesian-precursors-3d"
+    path = materialize_case(case, str(tmp_path))
+    res = subprocess.run([exe, "input.pmp"], cwd=os.path.dirname(path), capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stdout[-2000:]
+    expected = json.load(open(os.path.join(GOLDEN, "check_ref_stdout.json")))[case]
+    strip = lambda ls: ls[:max(i for i, x in enumerate(ls) if x) + 1]  # noqa: E731
+    assert strip(res.stdout.split("\n")) == strip(expected)
