@@ -136,13 +136,18 @@ int PrecursorSolver::solve(int n, double dt, double t) {
 }
 
 // printLog (PrecursorSolver.cxx:183-192).
-int PrecursorSolver::output(int n) const {
-  (void)n;
-  if (opt_.silent) return 0;
-  double cmin = C_.empty() ? 0.0 : *std::min_element(C_.begin(), C_.end());
-  double cmax = C_.empty() ? 0.0 : *std::max_element(C_.begin(), C_.end());
-  std::cout << std::scientific << std::setprecision(3) << "Precursor population: " << cmin << " (min), " << cmax
-            << " (max)." << std::endl;
+int PrecursorSolver::output(int n, bool write_mesh) const {
+  if (!opt_.silent) {
+    double cmin = C_.empty() ? 0.0 : *std::min_element(C_.begin(), C_.end());
+    double cmax = C_.empty() ? 0.0 : *std::max_element(C_.begin(), C_.end());
+    std::cout << std::scientific << std::setprecision(3) << "Precursor population: " << cmin << " (min), " << cmax
+              << " (max)." << std::endl;
+  }
+  // writeVTK and writePETSc (PrecursorSolver.cxx:195-215)
+  if (write_mesh) PG_TRY(write_vtk_mesh("./output", n, opt_, *mesh_), "unable to write the mesh in .vtk format");
+  PG_TRY(write_vtk_field("./output", n, opt_, "precursor", C_, mesh_->num_cells, npg_),
+         "unable to write the precursor population");
+  PG_TRY(write_petsc_vec("precursors", n, opt_, C_), "unable to write the precursor population");
   return 0;
 }
 
@@ -182,6 +187,7 @@ int CouplingSolver::read(Tokens& tok, const Mesh& mesh, std::vector<Solver*>& so
 int CouplingSolver::initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
                                bool transient) {
   opt_ = opt;
+  mesh_ = &mesh;
   PG_CHECK(coupled_.empty(), "no coupled solvers");
   for (Solver* s : coupled_) PG_TRY(s->initialize(mesh, mats, opt, transient), "unable to initialize the solver");
   fields_.clear();
@@ -225,8 +231,11 @@ int CouplingSolver::solve(int n, double dt, double t) {
   return 0;
 }
 
-int CouplingSolver::output(int n) const {
-  for (Solver* s : coupled_) PG_TRY(s->output(n), "unable to output the solution");
+// CouplingSolver::output (CouplingSolver.cxx:148-163): the mesh once, then every coupled
+// solver's summary and fields.
+int CouplingSolver::output(int n, bool write_mesh) const {
+  if (write_mesh) PG_TRY(write_vtk_mesh("./output", n, opt_, *mesh_), "unable to write the mesh in .vtk format");
+  for (Solver* s : coupled_) PG_TRY(s->output(n, false), "unable to output the solution");
   return 0;
 }
 

@@ -7,6 +7,7 @@
 // file that names them.  Driver (Driver.cxx:4-129) and the pampa_* functions
 // (pampa.cxx:5-115) keep the reference's sequence, messages and error convention.
 #include <chrono>
+#include <climits>
 #include <cstring>
 #include <iomanip>
 #include <iostream>
@@ -28,6 +29,9 @@ struct ParseState {
   std::vector<std::unique_ptr<Solver>> solvers;
   std::vector<double> dt;
   bool ready = false;
+  // output switches set by the input (they override the command line)
+  bool vtk = false, vtk_set = false, dump = false, dump_set = false;
+  int vtk_interval = 1;
 };
 
 int parse(const std::string& filename, ParseState& st) {
@@ -119,8 +123,23 @@ int parse(const std::string& filename, ParseState& st) {
         PG_TRY(tok.read_doubles(st.dt, 1, 0.0, 1e308), "wrong dt data");
         st.dt.assign(-nt, st.dt[0]);
       }
-    } else if (k == "vtk" || k == "petsc") {
-      // Output switches and PETSc/SLEPc options have no effect on the GPU path.
+    } else if (k == "vtk") {
+      // `vtk <switch> [interval]` (Parser.cxx:202-215)
+      PG_CHECK(line.size() < 2 || line.size() > 3, "wrong number of arguments for keyword 'vtk'");
+      PG_TRY(to_bool(line[1], st.vtk), "wrong switch for .vtk output");
+      st.vtk_set = true;
+      if (line.size() == 3) PG_TRY(to_int(line[2], 1, INT_MAX, st.vtk_interval), "wrong .vtk output interval");
+    } else if (k == "petsc") {
+      // `petsc <option> <value>` (Parser.cxx:216-236): dump and verbose are switches; other
+      // PETSc/SLEPc solver options have no counterpart on the GPU path
+      PG_CHECK(line.size() != 3, "wrong number of arguments for keyword 'petsc'");
+      if (line[1] == "dump") {
+        PG_TRY(to_bool(line[2], st.dump), "wrong switch to write the solution in PETSc format");
+        st.dump_set = true;
+      } else if (line[1] == "verbose") {
+        bool v = false;
+        PG_TRY(to_bool(line[2], v), "wrong switch for verbose PETSc output");
+      }
     } else if (k == "include") {
       PG_CHECK(line.size() < 2, "wrong number of arguments for keyword 'include'");
       std::string path = resolve_path(line[1], base);
@@ -172,11 +191,26 @@ int Driver::initialize(int argc, char* argv[], std::vector<double>& dt) {
     else if (s == "-pgpu_shift") PG_TRY(to_double(val(), 0.0, 10.0, opt_.gpu.shift), "wrong -pgpu_shift");
     else if (s == "-pgpu_device") PG_TRY(to_int(val(), 0, 1024, opt_.device), "wrong -pgpu_device");
     else if (s == "-pgpu_verbose") opt_.gpu.verbose = 1;
+    else if (s == "-vtk" || s == "-petsc_dump") {
+      // PETSc boolean options: the flag alone means on, or an explicit value follows
+      bool on = true;
+      if (a + 1 < argc) {
+        const std::string v(argv[a + 1]);
+        if (v == "1" || v == "true" || v == "yes") a++;
+        else if (v == "0" || v == "false" || v == "no") on = false, a++;
+      }
+      (s == "-vtk" ? opt_.vtk : opt_.dump) = on;
+    } else if (s == "-vtk_interval") PG_TRY(to_int(val(), 1, INT_MAX, opt_.vtk_interval), "wrong -vtk_interval");
     // other options (PETSc/SLEPc, -vtk, ...) are accepted and ignored
   }
   print("\nInitialize...");
   st_ = ParseState();
   PG_TRY(parse(filename, st_), "unable to parse " + filename);
+  if (st_.vtk_set) {
+    opt_.vtk = st_.vtk;
+    opt_.vtk_interval = st_.vtk_interval;
+  }
+  if (st_.dump_set) opt_.dump = st_.dump;
   dt = st_.dt;
   // Driver::getMainSolver (Driver.cxx:115-129): the only solver, or the one named "main"
   PG_CHECK(st_.solvers.empty(), "no solvers defined");

@@ -109,6 +109,10 @@ struct Mesh {
   std::vector<std::string> boundaries;
   std::map<int, BoundaryCondition> bcs;  // 1-based boundary index
   bool has_bcs = false;
+  // geometry for the .vtk output (Mesh::writeVTK, Mesh.cxx:397-405): point coordinates and
+  // each cell's points in the gmsh order the reference builds them in
+  std::vector<double> points;                 // num_points*3
+  std::vector<int> cell_pts_ptr{0}, cell_pts;  // CSR: cell i owns cell_pts[ptr[i] .. ptr[i+1])
 
   int nbr(int i, int f) const { return neighbors[(size_t)i * fmax + f]; }
   double area(int i, int f) const { return areas[(size_t)i * fmax + f]; }
@@ -159,7 +163,17 @@ struct RunOptions {
   pgpu_options gpu;
   int device = 0;
   bool verbose = false, silent = false;
+  // output switches: -vtk / -vtk_interval (vtk.cxx:15-25) or `vtk on [interval]` in the
+  // input, -petsc_dump (petsc.cxx:32) or `petsc dump on`
+  bool vtk = false, dump = false;
+  int vtk_interval = 1;
 };
+
+// .vtk and PETSc binary output (vtk.cxx, petsc.cxx:491-511).
+int write_vtk_mesh(const std::string& prefix, int n, const RunOptions& opt, const Mesh& mesh);
+int write_vtk_field(const std::string& prefix, int n, const RunOptions& opt, const std::string& name,
+                    const std::vector<double>& v, int num_cells, int num_groups = 1, int num_directions = 1);
+int write_petsc_vec(const std::string& prefix, int n, const RunOptions& opt, const std::vector<double>& v);
 
 class NeutronicSolver;
 
@@ -173,7 +187,9 @@ class Solver {
   virtual int initialize(const Mesh& mesh, const std::vector<Material>& mats,
                          const RunOptions& opt, bool transient) = 0;
   virtual int solve(int n, double dt, double t) = 0;
-  virtual int output(int n) const = 0;
+  // PhysicsSolver::output (PhysicsSolver.cxx:17-35): the summary on stdout, then the mesh
+  // (write_mesh) and the fields in .vtk format and the PETSc dump when switched on
+  virtual int output(int n, bool write_mesh = true) const = 0;
   virtual int finalize() = 0;
   // The neutronic solver of this solver's tree (itself, or the first one a coupled solver
   // holds), for the C API's keff / statistics / problem accessors; null if none.
@@ -201,7 +217,7 @@ class PrecursorSolver : public Solver {
   int initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
                  bool transient) override;
   int solve(int n, double dt, double t) override;
-  int output(int n) const override;
+  int output(int n, bool write_mesh = true) const override;
   int finalize() override { return 0; }
 
  private:
@@ -209,6 +225,7 @@ class PrecursorSolver : public Solver {
   const std::vector<Material>* mats_ = nullptr;
   RunOptions opt_;
   int npg_ = -1;
+  const Mesh* mesh_out_ = nullptr;
   // convergence errors of the output fields (PrecursorSolver.hxx:18-22 defaults)
   std::shared_ptr<ConvergenceError> dC_ = std::make_shared<ConvergenceError>("precursors", 2, true, 1.0);
   std::shared_ptr<ConvergenceError> dS_ = std::make_shared<ConvergenceError>("delayed-source", 2, true, 1.0);
@@ -225,7 +242,7 @@ class CouplingSolver : public Solver {
   int initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
                  bool transient) override;
   int solve(int n, double dt, double t) override;
-  int output(int n) const override;
+  int output(int n, bool write_mesh = true) const override;
   int finalize() override;
   NeutronicSolver* neutronic() override;
 
@@ -233,6 +250,7 @@ class CouplingSolver : public Solver {
   std::vector<Solver*> coupled_;
   bool implicit_ = false;
   RunOptions opt_;
+  const Mesh* mesh_ = nullptr;
 };
 
 // The reference iterates an implicit coupling until it converges, with no cap; here a
@@ -246,7 +264,7 @@ class NeutronicSolver : public Solver {
   int initialize(const Mesh& mesh, const std::vector<Material>& mats, const RunOptions& opt,
                  bool transient) override;
   int solve(int n, double dt, double t) override;
-  int output(int n) const override;
+  int output(int n, bool write_mesh = true) const override;
   int finalize() override;
   NeutronicSolver* neutronic() override { return this; }
   double keff() const { return keff_; }
@@ -263,6 +281,8 @@ class NeutronicSolver : public Solver {
   // Transient step n > 0 (NeutronicSolver::solve with n > 0, NeutronicSolver.cxx:13-29);
   // solvers without one report an error.
   virtual int solveTransient(int n, double dt, double t);
+  // writeVTK / writePETSc of the solver (DiffusionSolver.cxx:410-432, SNSolver.cxx:753-780)
+  virtual int writeFields(int n) const;
   void powerAndProduction();        // q, P, S and the total power from phi_ (host)
   const std::map<int, BoundaryCondition>& boundaryConditions() const;
 
@@ -307,6 +327,7 @@ class SNSolver : public NeutronicSolver {
  protected:
   int buildProblem() override;
   int fetchSolution() override;
+  int writeFields(int n) const override;
   int order_ = -1;
   double delta_ = 0.1;  // SNSolver.hxx:16
   bool ls_ = false;

@@ -131,6 +131,34 @@ int read_cartesian_mesh(const std::string& path, Mesh& mesh) {
   mesh = Mesh();
   mesh.allocate(n, F);
   mesh.num_dims = num_dims;
+  // points and cell points (CartesianMesh.cxx:146-228): the whole grid's points, each
+  // physical cell's 2, 4 or 8 points in gmsh order
+  for (int k = 0; k < nz + 1; k++)
+    for (int j = 0; j < ny + 1; j++)
+      for (int i = 0; i < nx + 1; i++) {
+        mesh.points.push_back(x[i]);
+        mesh.points.push_back(y[j]);
+        mesh.points.push_back(z[k]);
+      }
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < nx; i++) {
+        if (cid[((size_t)k * NY + j) * nx + i] < 0) continue;
+        const int sy = nx + 1, sz = (nx + 1) * (ny + 1);
+        mesh.cell_pts.push_back(i + j * sy + k * sz);
+        mesh.cell_pts.push_back(i + 1 + j * sy + k * sz);
+        if (ny > 0) {
+          mesh.cell_pts.push_back(i + 1 + (j + 1) * sy + k * sz);
+          mesh.cell_pts.push_back(i + (j + 1) * sy + k * sz);
+          if (nz > 0) {
+            mesh.cell_pts.push_back(i + j * sy + (k + 1) * sz);
+            mesh.cell_pts.push_back(i + 1 + j * sy + (k + 1) * sz);
+            mesh.cell_pts.push_back(i + 1 + (j + 1) * sy + (k + 1) * sz);
+            mesh.cell_pts.push_back(i + (j + 1) * sy + (k + 1) * sz);
+          }
+        }
+        mesh.cell_pts_ptr.push_back((int)mesh.cell_pts.size());
+      }
   mesh.boundaries = boundaries;
   mesh.bcs = bcs;
   mesh.has_bcs = has_bcs;
@@ -366,6 +394,21 @@ int read_unstructured_mesh(const std::string& path, Mesh& mesh) {
   mesh = Mesh();
   mesh.allocate(nxy * NZ, F);
   mesh.num_dims = num_dims;
+  // points and cell points (UnstructuredExtrudedMesh.cxx:153-201): the xy points on every
+  // z level; a cell's polygon on its lower level, then on its upper level
+  for (int k = 0; k < nz + 1; k++)
+    for (int p = 0; p < npts; p++) {
+      mesh.points.push_back(pts[(size_t)p * 2]);
+      mesh.points.push_back(pts[(size_t)p * 2 + 1]);
+      mesh.points.push_back(z[k]);
+    }
+  for (int k = 0; k < NZ; k++)
+    for (int i = 0; i < nxy; i++) {
+      for (int p : cells[i]) mesh.cell_pts.push_back(p + k * npts);
+      if (nz > 0)
+        for (int p : cells[i]) mesh.cell_pts.push_back(p + (k + 1) * npts);
+      mesh.cell_pts_ptr.push_back((int)mesh.cell_pts.size());
+    }
   mesh.boundaries = boundaries;
   mesh.bcs = bcs;
   mesh.has_bcs = has_bcs;
@@ -470,6 +513,24 @@ int remove_bc_materials(const Mesh& in, const std::vector<Material>& materials, 
   out.boundaries = in.boundaries;
   out.bcs = in.bcs;
   out.has_bcs = in.has_bcs;
+  // points used by the remaining cells, renumbered in order (Mesh.cxx:91-114)
+  if ((int)in.cell_pts_ptr.size() == n0 + 1) {
+    const int np = (int)in.points.size() / 3;
+    std::vector<int> used(np, 0), ip(np, -1);
+    for (int i = 0; i < n0; i++)
+      if (newid[i] >= 0)
+        for (int k = in.cell_pts_ptr[i]; k < in.cell_pts_ptr[i + 1]; k++) used[in.cell_pts[k]] = 1;
+    for (int p = 0, q = 0; p < np; p++)
+      if (used[p]) {
+        ip[p] = q++;
+        for (int d = 0; d < 3; d++) out.points.push_back(in.points[(size_t)p * 3 + d]);
+      }
+    for (int i = 0; i < n0; i++)
+      if (newid[i] >= 0) {
+        for (int k = in.cell_pts_ptr[i]; k < in.cell_pts_ptr[i + 1]; k++) out.cell_pts.push_back(ip[in.cell_pts[k]]);
+        out.cell_pts_ptr.push_back((int)out.cell_pts.size());
+      }
+  }
   for (int i = 0; i < n0; i++) {
     int ic = newid[i];
     if (ic < 0) continue;

@@ -167,13 +167,25 @@ void NeutronicSolver::powerAndProduction() {
 }
 
 // NeutronicSolver::printLog (NeutronicSolver.cxx:119-127) through PhysicsSolver::output.
-int NeutronicSolver::output(int n) const {
-  if (opt_.silent) return 0;
-  if (n == 0)
-    std::cout << std::fixed << std::setprecision(6) << "Effective multiplication factor: " << keff_
-              << "." << std::endl;
-  std::cout << std::scientific << std::setprecision(3) << "Power: " << total_power_ << "."
-            << std::endl;
+int NeutronicSolver::output(int n, bool write_mesh) const {
+  if (!opt_.silent) {
+    if (n == 0)
+      std::cout << std::fixed << std::setprecision(6) << "Effective multiplication factor: " << keff_
+                << "." << std::endl;
+    std::cout << std::scientific << std::setprecision(3) << "Power: " << total_power_ << "."
+              << std::endl;
+  }
+  if (write_mesh) PG_TRY(write_vtk_mesh("./output", n, opt_, *mesh_), "unable to write the mesh in .vtk format");
+  PG_TRY(writeFields(n), "unable to write the solution");
+  return 0;
+}
+
+// DiffusionSolver::writeVTK and writePETSc (DiffusionSolver.cxx:410-432).
+int NeutronicSolver::writeFields(int n) const {
+  const int nc = mesh_->num_cells;
+  PG_TRY(write_vtk_field("./output", n, opt_, "flux", phi_, nc, G_), "unable to write the scalar flux");
+  PG_TRY(write_vtk_field("./output", n, opt_, "power", q_, nc), "unable to write the thermal power");
+  PG_TRY(write_petsc_vec("scalar_flux", n, opt_, phi_), "unable to write the scalar flux");
   return 0;
 }
 
@@ -674,6 +686,20 @@ int SNSolver::initialize(const Mesh& mesh, const std::vector<Material>& mats,
 
 int SNSolver::fetchSolution() {
   PG_TRY(pgpu_problem_get_angular_flux(problem_, psi_.data()), "unable to get the angular flux");
+  return 0;
+}
+
+}  // namespace pg
+
+namespace pg {
+
+// SNSolver::writeVTK and writePETSc (SNSolver.cxx:753-780).
+int SNSolver::writeFields(int n) const {
+  const int nc = mesh_->num_cells;
+  PG_TRY(write_vtk_field("./output", n, opt_, "flux", phi_, nc, G_), "unable to write the scalar flux");
+  PG_TRY(write_vtk_field("./output", n, opt_, "flux", psi_, nc, G_, M_), "unable to write the angular flux");
+  PG_TRY(write_vtk_field("./output", n, opt_, "power", q_, nc), "unable to write the thermal power");
+  PG_TRY(write_petsc_vec("angular_flux", n, opt_, psi_), "unable to write the angular flux");
   return 0;
 }
 
