@@ -118,6 +118,7 @@ struct SNData {
   int kba_t[3] = {4, 4, 4};                // tile shape (4x4x4 or 8x8x4)
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
+  bool flow_warp[2] = {false, true};       // warp-per-slot sweep kernel per precision [fp32]
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
   DevBuf d_task_order;  // hand-out order of the dataflow sweep's tasks (null: canonical)
   int flow_sleep = 32;  // back-off between flag polls (ns)
@@ -653,6 +654,202 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
         const int c = r / gn, gg = r - c * gn;
         T acc = T(0);
         for (int dj = 0; dj < ndp; dj++) acc += A.w[K.pat_dirs[d0 + dj]] * tpsi[c * S + gg * nd + dj];
+        mom[(size_t)p * n * G + (size_t)cell_index(c) * G + g0 + gg] = acc;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Warp-per-slot form of the dataflow sweep.  Same tasks, flags, hand-out order and
+// arithmetic as k_sweep_flow, but each (group, direction) slot of a task is one warp that
+// walks the tile's cell diagonals on its own: a cell diagonal of an 8x8x4 tile holds at
+// most 28 cells (4x4x4: 12), so a lane takes one cell per diagonal, and the dependencies
+// of a slot (its upwind cells, same group and direction) stay inside the warp.  A diagonal
+// step ends with __syncwarp instead of a block barrier; block barriers remain only where
+// slots meet (task hand-out, the shared source and cell classes, the upwind wait, and the
+// end of the tile before the flag and the scalar-flux moment).  Shared memory per task:
+// the source and cell classes (shared), and per slot the staged coefficient rows, the
+// tile's angular flux and its inflow faces.
+// ---------------------------------------------------------------------------------
+template <typename T>
+__host__ __device__ constexpr size_t flow_wsmem_bytes(int TX, int TY, int TZ, int S, int Gc) {
+  return ((size_t)TX * TY * TZ * Gc +
+          (size_t)S * ((size_t)kTileClasses * 4 + (size_t)TX * TY * TZ + (size_t)(TY * TZ + TX * TZ + TX * TY))) *
+             sizeof(T) +
+         (size_t)TX * TY * TZ * sizeof(int);
+}
+
+template <typename T, bool kClass, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(kFlowSlots * 32)
+    k_sweep_wflow(SNOp<T> A, SweepFaces<T> W, FlowGeom K, const SweepPtrs* __restrict__ P, int iso) {
+  using Shape = TileShape<TX, TY, TZ>;
+  constexpr int kCells = TX * TY * TZ, kDiags = TX + TY + TZ - 2;
+  constexpr int kFx = TY * TZ, kFy = TX * TZ, kFz = TX * TY, kFaces = kFx + kFy + kFz;
+  constexpr int kPerSlot = kTileClasses * 4 + kCells + kFaces;
+  extern __shared__ __align__(16) unsigned char flow_smem[];
+  const int G = A.G, M = A.M, n = A.n, Gc = K.gchunk, nd = K.nd, S = nd * Gc;
+  T* tsrc = reinterpret_cast<T*>(flow_smem);                  // [kCells][Gc]
+  T* slotmem = tsrc + kCells * Gc;                            // [S][kPerSlot]
+  int* tcls = reinterpret_cast<int*>(slotmem + S * kPerSlot);  // [kCells]
+  __shared__ int s_task;
+  __shared__ unsigned char s_cell[kCells];
+  __shared__ int s_dptr[kDiags + 1];
+  for (int k = threadIdx.x; k < kCells; k += blockDim.x) s_cell[k] = (unsigned char)Shape::cell(k);
+  for (int k = threadIdx.x; k <= kDiags; k += blockDim.x) s_dptr[k] = Shape::dptr(k);
+  const T* __restrict__ src = static_cast<const T*>(P->src);
+  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
+  T* psi = static_cast<T*>(P->psi);
+  T* mom = static_cast<T*>(P->mom);
+  const T* __restrict__ coef = static_cast<const T*>(K.coef);
+  const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
+  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
+  const int lane = threadIdx.x & 31, slot = threadIdx.x >> 5;  // one warp per slot
+  const int gl = slot / nd, di = slot - gl * nd;
+  T* tcoef = slotmem + slot * kPerSlot;  // [kTileClasses][4]
+  T* tpsi = tcoef + kTileClasses * 4;    // [kCells]
+  T* tin = tpsi + kCells;                // [kFaces]
+  for (;;) {
+    if (threadIdx.x == 0) s_task = (int)atomicAdd(&K.sync->next, 1u);
+    __syncthreads();
+    const int t = s_task;
+    if (t >= K.ntasks) return;  // uniform over the CTA
+    const int tc = K.order ? K.order[t] : t;
+    const int jp = tc / K.nchunk, ch = tc - jp * K.nchunk;
+    const int j = jp / K.npat, p = jp - j * K.npat;
+    const int g0 = ch * Gc, gn = min(Gc, G - g0);
+    const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
+    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
+    const int atx = sx > 0 ? tx : K.ntx - 1 - tx, aty = sy > 0 ? ty : K.nty - 1 - ty, atz = sz > 0 ? tz : K.ntz - 1 - tz;
+    const FlowTile<TX, TY, TZ> tile{atx * TX, aty * TY, atz * TZ, sx, sy, sz};
+    auto cell_index = [&](int c) {
+      return tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY));
+    };
+    const int d0 = K.pat_dirs_ptr[p], ndp = K.pat_dirs_ptr[p + 1] - d0;
+    const bool active = slot < S && gl < gn && di < ndp;  // uniform over the warp
+    const int g = g0 + gl;
+    const int m = active ? K.pat_dirs[d0 + di] : 0;
+    unsigned int* pflags = K.flags + ((size_t)p * K.nchunk + ch) * ntiles;
+    const int tb = (atz * K.nty + aty) * K.ntx + atx;
+    const int nk = kClass ? K.tile_ncls[tb] : 0;
+    const bool staged = kClass && nk <= kTileClasses;
+    // 1. shared data that does not depend on the upwind tiles: source and cell classes
+    if (iso)
+      for (int r = threadIdx.x; r < kCells * Gc; r += blockDim.x) {
+        const int c = r / Gc, gg = r - c * Gc;
+        if (gg < gn) tsrc[r] = src[(size_t)cell_index(c) * G + g0 + gg];
+      }
+    if (kClass)
+      for (int c = threadIdx.x; c < kCells; c += blockDim.x) {
+        const int i = cell_index(c);
+        tcls[c] = staged ? (int)K.cell_lcls[i] : (int)K.ccls[i];
+      }
+    // 2. per slot: coefficient rows of the tile's classes and the inflow on upwind faces
+    //    that lie on the box boundary
+    auto face_cell = [&](int fs, int& a, int& lx, int& ly, int& lz) {
+      if (fs < kFx) {
+        a = 0, lx = 0, ly = fs % TY, lz = fs / TY;
+      } else if (fs < kFx + kFy) {
+        a = 1, lx = (fs - kFx) % TX, ly = 0, lz = (fs - kFx) / TX;
+      } else {
+        a = 2, lx = (fs - kFx - kFy) % TX, ly = (fs - kFx - kFy) / TX, lz = 0;
+      }
+    };
+    const int inner = (tx > 0) | (ty > 0) << 1 | (tz > 0) << 2;  // upwind faces inside the box
+    if (active) {
+      if (staged)
+        for (int k = lane; k < nk; k += 32)
+          flow_load4(coef + (((size_t)K.tile_cls[(size_t)tb * kTileClasses + k] * G + g) * M + m) * 4,
+                     *reinterpret_cast<T(*)[4]>(tcoef + k * 4));
+      for (int fs = lane; fs < kFaces; fs += 32) {
+        int a, lx, ly, lz;
+        face_cell(fs, a, lx, ly, lz);
+        if ((inner >> a) & 1) continue;
+        T val = T(0);
+        if (bnd) {
+          const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
+          const size_t o = (size_t)f * n + (tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz));
+          if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd_val(A, bnd, A.rslot[o], g, m);
+        }
+        tin[fs] = val;
+      }
+    }
+    // 3. wait for the upwind tiles of this pattern and chunk
+    if (threadIdx.x < 3) {
+      const int a = threadIdx.x;
+      const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
+      if (ux >= 0 && uy >= 0 && uz >= 0)
+        flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error, kFlowSpinLimit, K.sleep_ns);
+      if (a == 0 && *(volatile unsigned int*)&K.sync->stall == (unsigned int)t + 1u)
+        flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure: runs out
+    }
+    __syncthreads();
+    if (active) {
+      // 4. inflow from the upwind tiles (through L2)
+      for (int fs = lane; fs < kFaces; fs += 32) {
+        int a, lx, ly, lz;
+        face_cell(fs, a, lx, ly, lz);
+        if (!((inner >> a) & 1)) continue;
+        const int sg = a == 0 ? sx : (a == 1 ? sy : sz);
+        const int nb = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz) - sg * (a == 0 ? 1 : (a == 1 ? nx : nxy));
+        tin[fs] = __ldcg(psi + ((size_t)nb * G + g) * M + m);
+      }
+      __syncwarp();
+      // 5. the tile's cell diagonals, one cell per lane, within the warp
+      const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
+      T mux = T(0), muy = T(0), muz = T(0);
+      if (!kClass) {
+        mux = fabs(A.dirs[(size_t)m * 3]);
+        muy = fabs(A.dirs[(size_t)m * 3 + 1]);
+        muz = fabs(A.dirs[(size_t)m * 3 + 2]);
+      }
+      for (int dd = 0; dd < kDiags; dd++) {
+        const int cb = s_dptr[dd], cn = s_dptr[dd + 1] - cb;
+        if (lane < cn) {
+          const int c = s_cell[cb + lane];
+          const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
+          const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
+          const size_t l = ((size_t)i * G + g) * M + m;
+          const T ux = lx > 0 ? tpsi[c - 1] : tin[ly + TY * lz];
+          const T uy = ly > 0 ? tpsi[c - TX] : tin[kFx + lx + TX * lz];
+          const T uz = lz > 0 ? tpsi[c - TX * TY] : tin[kFx + kFy + lx + TX * ly];
+          const T q = iso ? tsrc[c * Gc + gl] : src[l];
+          T v;
+          if (kClass) {
+            T cf[4];
+            if (staged) {
+              const T* sc = tcoef + tcls[c] * 4;
+              cf[0] = sc[0], cf[1] = sc[1], cf[2] = sc[2], cf[3] = sc[3];
+            } else {
+              flow_load4(coef + (((size_t)tcls[c] * G + g) * M + m) * 4, cf);
+            }
+            v = cf[0] * q;
+            v += cf[3] * uz;
+            v += cf[2] * uy;
+            v += cf[1] * ux;
+          } else {
+            T num = q;
+            num += (muz * W.win[(size_t)fz * n + i]) * uz;
+            num += (muy * W.win[(size_t)fy * n + i]) * uy;
+            num += (mux * W.win[(size_t)fx * n + i]) * ux;
+            v = num * W.rden[l];
+          }
+          psi[l] = v;
+          tpsi[c] = v;
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    // 6. publish the tile (the barrier orders every warp's psi stores before the release),
+    //    then its scalar-flux moment over this pattern's directions
+    if (threadIdx.x == 0) st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
+    if (mom) {
+      for (int r = threadIdx.x; r < kCells * gn; r += blockDim.x) {
+        const int c = r / gn, gg = r - c * gn;
+        T acc = T(0);
+        for (int dj = 0; dj < ndp; dj++)
+          acc += A.w[K.pat_dirs[d0 + dj]] * slotmem[(gg * nd + dj) * kPerSlot + kTileClasses * 4 + c];
         mom[(size_t)p * n * G + (size_t)cell_index(c) * G + g0 + gg] = acc;
       }
     }
@@ -1418,22 +1615,25 @@ int ensure_level_coef(pgpu_problem* p, const SNOp<T>& A) {
 
 // The dataflow sweep for the problem's tile shape runs on a persistent grid: every CTA
 // that fits on the device at once, at most one per task.  flow_prepare sizes it (before
-// the launch is captured in the sweep graph), flow_launch enqueues it.
+// the launch is captured in the sweep graph), flow_launch enqueues it.  Two kernels do
+// the same work: k_sweep_wflow (a warp per (group, direction) slot, warp-level steps
+// between cell diagonals) and k_sweep_flow (the slots' cells spread over the block, block
+// barriers between diagonals); flow_warp picks one per precision.
 template <typename T, bool kClass, int TX, int TY, int TZ>
 int flow_prepare(SNData& d) {
-  constexpr int nt = TileShape<TX, TY, TZ>::kThreads;
-  const size_t smem = flow_smem_bytes<T>(TX, TY, TZ, d.kba_nd * d.kba_gchunk, d.kba_gchunk);
+  const bool warp = d.flow_warp[sizeof(T) == 8 ? 0 : 1];
+  const int S = d.kba_nd * d.kba_gchunk;
+  const int nt = warp ? S * 32 : TileShape<TX, TY, TZ>::kThreads;
+  const size_t smem = warp ? flow_wsmem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk)
+                           : flow_smem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
+  const void* fn = warp ? (const void*)k_sweep_wflow<T, kClass, TX, TY, TZ> : (const void*)k_sweep_flow<T, kClass, TX, TY, TZ>;
   int dev = 0, sms = 0, per_sm = 0;
-  if (smem > 48u * 1024u)
-    PGPU_CUDA(cudaFuncSetAttribute(k_sweep_flow<T, kClass, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+  if (smem > 48u * 1024u) PGPU_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   PGPU_CUDA(cudaGetDevice(&dev));
   PGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  PGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_flow<T, kClass, TX, TY, TZ>, nt, smem));
+  PGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, smem));
   if (per_sm < 1) return fail(PGPU_ERR_CUDA, "the dataflow sweep does not fit on an SM");
-  // CTAs per SM of the persistent grid: all that fit, or PGPU_FLOW_CTAS{64,32} (fewer CTAs
-  // contend less for an SM's FP64 pipe, so each task -- and the wavefront's critical path
-  // of tasks -- runs faster)
+  // CTAs per SM of the persistent grid: all that fit, or PGPU_FLOW_CTAS{64,32} (measurement)
   const char* ce = std::getenv(sizeof(T) == 8 ? "PGPU_FLOW_CTAS64" : "PGPU_FLOW_CTAS32");
   if (ce && std::atoi(ce) > 0) per_sm = std::min(per_sm, std::atoi(ce));
   d.flow_grid[sizeof(T) == 8 ? 0 : 1] = std::min(d.kba_ntasks, sms * per_sm);
@@ -1443,9 +1643,15 @@ int flow_prepare(SNData& d) {
 template <typename T, bool kClass, int TX, int TY, int TZ>
 void flow_launch(SNData& d, cudaStream_t s, const SNOp<T>& A, const SweepFaces<T>& W, const FlowGeom& K,
                  const SweepPtrs* P, int iso) {
-  constexpr int nt = TileShape<TX, TY, TZ>::kThreads;
-  const size_t smem = flow_smem_bytes<T>(TX, TY, TZ, d.kba_nd * d.kba_gchunk, d.kba_gchunk);
-  k_sweep_flow<T, kClass, TX, TY, TZ><<<d.flow_grid[sizeof(T) == 8 ? 0 : 1], nt, smem, s>>>(A, W, K, P, iso);
+  const int S = d.kba_nd * d.kba_gchunk, grid = d.flow_grid[sizeof(T) == 8 ? 0 : 1];
+  if (d.flow_warp[sizeof(T) == 8 ? 0 : 1]) {
+    const size_t smem = flow_wsmem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
+    k_sweep_wflow<T, kClass, TX, TY, TZ><<<grid, S * 32, smem, s>>>(A, W, K, P, iso);
+  } else {
+    constexpr int nt = TileShape<TX, TY, TZ>::kThreads;
+    const size_t smem = flow_smem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
+    k_sweep_flow<T, kClass, TX, TY, TZ><<<grid, nt, smem, s>>>(A, W, K, P, iso);
+  }
 }
 
 template <typename T, bool kClass>
@@ -2052,6 +2258,15 @@ static void flow_stagger(int& waves, int& offset) {
   }
 }
 
+// Which dataflow-sweep kernel each precision uses (SNData::flow_warp), overridable with
+// PGPU_FLOW_WARP64 / PGPU_FLOW_WARP32 = 0 or 1 (measurement).
+static void flow_kernels(bool* warp) {
+  const char* e64 = std::getenv("PGPU_FLOW_WARP64");
+  const char* e32 = std::getenv("PGPU_FLOW_WARP32");
+  if (e64) warp[0] = std::atoi(e64) != 0;
+  if (e32) warp[1] = std::atoi(e32) != 0;
+}
+
 // Back-off between polls of an upwind tile's flag, in ns (PGPU_FLOW_SLEEP, default 32).
 static int flow_sleep_ns() {
   const char* e = std::getenv("PGPU_FLOW_SLEEP");
@@ -2400,6 +2615,7 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
       if (!kp.order.empty()) up(d.d_task_order, kp.order.data(), kp.order.size() * 4);
       d.flow_sleep = flow_sleep_ns();
+      flow_kernels(d.flow_warp);
       up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
       up(d.d_fpat_dirs_ptr, kp.pat_dirs_ptr.data(), kp.pat_dirs_ptr.size() * 4);
       up(d.d_fpat_dirs, kp.pat_dirs.data(), kp.pat_dirs.size() * 4);

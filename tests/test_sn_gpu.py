@@ -119,3 +119,34 @@ def test_hex_prism_lattice(nq, nr, nz, order, tmp_path):
         assert abs(p.keff - ref["keff"]) <= K_TOL, (p.keff, ref["keff"])
         assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= FLUX_TOL
         assert rel_l2(p.field("angular-flux"), ref["psi"]) <= FLUX_TOL
+
+
+@pytest.mark.parametrize("precision,k_tol,flux_tol", [("fp64", K_TOL, FLUX_TOL), ("mixed", 1e-5, 1e-4)])
+def test_benchmark_box_full_size_against_cpu_solve(precision, k_tol, flux_tol, tmp_path):
+    """The bench's default workload at its full size (S8, 2 groups, 64x64x32 cells, 21M
+    angular unknowns, dataflow sweeps of 8x8x4 tiles) against the CPU sweep solve of
+    oracle/sn_cpu.py, which the CPU tests pin to the oracle's direct solve."""
+    from pampa_gb300 import workloads as wl
+    from oracle import sn_cpu
+    path = wl.sn_3d(str(tmp_path))
+    ref = sn_cpu.solve_input(path)
+    with pg.Pampa(path, "-silent", "-pgpu_precision", precision) as p:
+        p.solve()
+        assert abs(p.keff - ref["keff"]) <= k_tol, (p.keff, ref["keff"])
+        assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= flux_tol
+        assert rel_l2(p.field("angular-flux"), ref["psi"]) <= flux_tol
+
+
+@pytest.mark.parametrize("precision,k_tol,flux_tol", [("fp64", K_TOL, FLUX_TOL), ("mixed", 1e-5, 1e-4)])
+def test_hex_lattice_40x40x8_s8_against_cpu_solve(precision, k_tol, flux_tol, tmp_path):
+    """The hexagonal-prism workload's family at 40x40 hexagons x 8 layers, S8, 4 groups
+    (4.1M angular unknowns, level-set sweeps), against the CPU sweep solve."""
+    from pampa_gb300 import workloads as wl
+    from oracle import sn_cpu
+    path = wl.sn_hex(str(tmp_path), nq=40, nr=40, nz=8, order=8, block=10)
+    ref = sn_cpu.solve_input(path)
+    with pg.Pampa(path, "-silent", "-pgpu_precision", precision, "-pgpu_shift", "0.02") as p:
+        p.solve()
+        assert abs(p.keff - ref["keff"]) <= k_tol, (p.keff, ref["keff"])
+        assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= flux_tol
+        assert rel_l2(p.field("angular-flux"), ref["psi"]) <= flux_tol
