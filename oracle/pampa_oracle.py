@@ -174,6 +174,8 @@ class Material:
     chi_p: np.ndarray | None = None   # prompt fission spectrum
     chi_d: np.ndarray | None = None   # delayed fission spectrum
     vel: np.ndarray | None = None     # neutron velocities
+    tref: list = field(default_factory=list)   # feedback data: reference temperatures
+    sets: list = field(default_factory=list)   # feedback data: one Material per temperature
 
     def read(self, tok: Tokens):
         nd = {}
@@ -188,7 +190,25 @@ class Material:
                 nd = self._read_nd(tok)
                 self.has_nd = True
             elif key == "nuclear-data-set":
-                raise NotImplementedError("feedback nuclear data is outside the k-eigen path")
+                # FeedbackNuclearData::read (FeedbackNuclearData.cxx): reference temperatures
+                # and one constant data set per temperature
+                if line[1] != "{":
+                    raise ValueError("missing '{'")
+                self.tref, sets = [], []
+                while True:
+                    l2 = tok.next_line()
+                    if not l2 or l2[0] == "}":
+                        break
+                    if l2[0] == "temperature":
+                        self.tref = list(tok.read_values(int(l2[1])))
+                    elif l2[0] == "nuclear-data":
+                        sets.append(self._read_nd(tok))
+                    else:
+                        raise ValueError(f"unrecognized keyword {l2[0]}")
+                if not sets or len(sets) != len(self.tref):
+                    raise ValueError("one nuclear-data set per reference temperature")
+                self.has_nd = True
+                nd = sets
             elif key == "precursor-data":
                 while True:
                     l2 = tok.next_line()
@@ -217,7 +237,14 @@ class Material:
                 self.split = bool(int(line[1]))
             else:
                 raise ValueError(f"unrecognized keyword '{key}'")
-        if self.has_nd:
+        if self.has_nd and isinstance(nd, list):
+            self.sets = []
+            for one in nd:          # FeedbackNuclearData::check(beta_total)
+                sub = Material(name=self.name, beta_total=self.beta_total, G=self.G)
+                sub._check(one)
+                self.sets.append(sub)
+            self._copy_from(self.sets[0])
+        elif self.has_nd:
             self._check(nd)
 
     def _read_nd(self, tok: Tokens) -> dict:
@@ -275,6 +302,42 @@ class Material:
         self.ss = nd.get("sigma-scattering")
         self.chi_p, self.chi_d = chi_p, chi_d
         self.vel = nd.get("neutron-velocity")
+
+    _FIELDS = ("st", "nsf", "ksf", "ss", "D", "chi", "chi_p", "chi_d", "vel")
+
+    def _copy_from(self, other: "Material"):
+        for f in self._FIELDS:
+            setattr(self, f, getattr(other, f))
+
+    def at(self, T: float) -> "Material":
+        """The material's data at temperature T (FeedbackNuclearData::interpolate and
+        its getters, FeedbackNuclearData.hxx:60-140): below the first reference
+        temperature the first set, above the last the last, else linear between the two
+        sets around T.  The reference reads the set before the first when T equals the
+        first reference value; the first set is used there."""
+        if not self.sets:
+            return self
+        tref = self.tref
+        if T < tref[0]:
+            i1 = i2 = 0
+            f = 0.0
+        elif T > tref[-1]:
+            i1 = i2 = len(tref) - 1
+            f = 0.0
+        else:
+            i2 = int(np.searchsorted(tref, T, side="left"))
+            if i2 == 0:
+                i1, f = 0, 0.0
+            else:
+                i1 = i2 - 1
+                f = (T - tref[i1]) / (tref[i2] - tref[i1])
+        a, b = self.sets[i1], self.sets[i2]
+        out = Material(name=self.name, G=self.G, has_nd=True, beta_total=self.beta_total, lam=self.lam,
+                       beta=self.beta)
+        for fld in self._FIELDS:
+            x, y = getattr(a, fld), getattr(b, fld)
+            setattr(out, fld, None if x is None else (1.0 - f) * x + f * y)
+        return out
 
     def check_for_solver(self, G: int, diffusion: bool):
         if not self.has_nd:
@@ -675,6 +738,7 @@ class Problem:
     delta: float = 0.1
     ls: bool = False
     dt: list = field(default_factory=list)
+    T: np.ndarray | None = None   # the "temperature" field per cell (zero when not set)
 
     def boundary_conditions(self) -> dict:
         # DiffusionSolver.cxx:91 / SNSolver.cxx:346: solver BCs if any were given, else mesh BCs
@@ -785,8 +849,30 @@ def surface_leakage_factor(p1: np.ndarray, p2: np.ndarray, n: np.ndarray) -> np.
 
 
 def _material_tables(prob: Problem):
+    """Per-material tables (constant data; a feedback material contributes its first set)."""
+    return _tables_of(prob.materials, prob.G)
+
+
+def _cell_materials(prob: Problem):
+    """The data every cell sees: its material at the cell's temperature when the material
+    has feedback data.  Returns (materials, index per cell); without feedback data the
+    problem's materials and the mesh's material indices."""
     mats = prob.materials
-    G = prob.G
+    if not any(m.sets for m in mats):
+        return mats, prob.mesh.materials
+    T = prob.T if prob.T is not None else np.zeros(prob.mesh.n)
+    eff, index, cell = [], {}, np.zeros(prob.mesh.n, dtype=np.int64)
+    for i, m in enumerate(prob.mesh.materials):
+        t = float(T[i]) if mats[m].sets else 0.0
+        key = (int(m), t)
+        if key not in index:
+            index[key] = len(eff)
+            eff.append(mats[m].at(t))
+        cell[i] = index[key]
+    return eff, cell
+
+
+def _tables_of(mats: list, G: int):
     st = np.array([m.st for m in mats])
     nsf = np.array([m.nsf for m in mats])
     ksf = np.array([m.ksf for m in mats])
@@ -806,10 +892,12 @@ def assemble_diffusion(prob: Problem):
     G = prob.G
     for m in prob.materials:
         m.check_for_solver(G, True)
-    st, nsf, ksf, chi, ss, D = _material_tables(prob)
+    eff, mat = _cell_materials(prob)
+    st, nsf, ksf, chi, ss, D = _tables_of(eff, G)
+    orig = mesh.materials
+    Tc = prob.T if prob.T is not None else np.zeros(mesh.n)
     bcs = prob.boundary_conditions()
     n = mesh.n
-    mat = mesh.materials
     V = mesh.volumes
     rows, cols, vals = [], [], []
     frows, fcols, fvals = [], [], []
@@ -854,7 +942,7 @@ def assemble_diffusion(prob: Problem):
             if len(c) == 0:
                 continue
             c2 = nb[c]
-            same = mat[c2] == mat[c]
+            same = orig[c2] == orig[c]
             r = np.empty(len(c))
             cs = c[same]
             w = surface_leakage_factor(mesh.centroids[cs], mesh.centroids[c2[same]], mesh.normals[cs, f])
@@ -864,7 +952,10 @@ def assemble_diffusion(prob: Problem):
             w1 = surface_leakage_factor(mesh.centroids[cd], mesh.fcent[cd, f], mesh.normals[cd, f])
             w1 = w1 * (Dg[cd] * A[cd])
             w2 = surface_leakage_factor(mesh.centroids[cd2], mesh.fcent[cd, f], mesh.normals[cd, f])
-            w2 = w2 * (-D[mat[cd2], g] * A[cd])
+            # the neighbour's coefficient at this cell's temperature (DiffusionSolver.cxx:270-273)
+            Dn = np.array([prob.materials[orig[b]].at(float(Tc[a])).D[g] if prob.materials[orig[b]].sets
+                           else prob.materials[orig[b]].D[g] for a, b in zip(cd, cd2)])
+            w2 = w2 * (-Dn * A[cd])
             r[~same] = -(w1 * w2) / (w1 + w2)
             diag[c, g] -= r
             rows.append(c * G + g)
@@ -1014,12 +1105,13 @@ def assemble_sn(prob: Problem):
     G = prob.G
     for m in prob.materials:
         m.check_for_solver(G, False)
-    st, nsf, ksf, chi, ss, D = _material_tables(prob)
+    eff, mat_c = _cell_materials(prob)
+    st, nsf, ksf, chi, ss, D = _tables_of(eff, G)
     dirs, w, refl = quadrature(prob.order)
     M = len(w)
     bcs = prob.boundary_conditions()
     n = mesh.n
-    mat = mesh.materials
+    mat = mat_c
     V = mesh.volumes
     gc = gauss_coefs(mesh, prob.delta)
     ic_to_ibc = boundary_cells(mesh)
@@ -1136,8 +1228,8 @@ def solve_eigen(R: sp.csr_matrix, Fm: sp.csr_matrix, tol: float = 1e-13):
 
 
 def _kappa_nu_tables(prob: Problem):
-    st, nsf, ksf, chi, ss, D = _material_tables(prob)
-    mat = prob.mesh.materials
+    eff, mat = _cell_materials(prob)
+    st, nsf, ksf, chi, ss, D = _tables_of(eff, prob.G)
     return ksf[mat], nsf[mat]
 
 
@@ -1199,15 +1291,15 @@ def diffusion_transient_system(prob: Problem, R0: sp.csr_matrix, dt: float, keff
     b = chi_d,g S_i + V/(v_g dt) phi0.  R0 is the n = 0 operator of assemble_diffusion."""
     mesh, G = prob.mesh, prob.G
     n = mesh.n
-    mat = mesh.materials
+    eff, mat = _cell_materials(prob)
     V = mesh.volumes
-    for m in prob.materials:
+    for m in eff:
         if m.vel is None:
             raise ValueError("missing neutron velocities")
-    vel = np.array([m.vel for m in prob.materials])
-    chip = np.array([(1.0 - m.beta_total) * m.chi_p for m in prob.materials])
-    chid = np.array([m.chi_d for m in prob.materials])
-    st, nsf, ksf, chi, ss, D = _material_tables(prob)
+    vel = np.array([m.vel for m in eff])
+    chip = np.array([(1.0 - m.beta_total) * m.chi_p for m in eff])
+    chid = np.array([m.chi_d for m in eff])
+    st, nsf, ksf, chi, ss, D = _tables_of(eff, G)
     d = (V[:, None] / (vel[mat] * dt)).reshape(-1)
     cell = np.arange(n)
     rows, cols, vals = [], [], []

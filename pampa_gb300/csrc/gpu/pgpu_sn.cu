@@ -32,6 +32,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "pgpu_internal.cuh"
@@ -118,9 +119,14 @@ struct SNData {
   int kba_t[3] = {4, 4, 4};                // tile shape (4x4x4 or 8x8x4)
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
-  bool flow_warp[2] = {false, true};       // warp-per-slot sweep kernel per precision [fp32]
+  bool flow_warp[2] = {false, false};      // warp-per-slot sweep kernel per precision [fp32]
+  bool flow_lane[2] = {true, true};        // lane-per-cell sweep kernel where it applies [fp32]
+  bool kba_contig = false;                 // every pattern's directions are contiguous
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
   DevBuf d_task_order;  // hand-out order of the dataflow sweep's tasks (null: canonical)
+  DevBuf trace_buf;     // timeline of one traced sweep (PGPU_FLOW_TRACE), [ntasks][5]
+  int trace_sweep = -1; // which sweep of a solve is traced (-1: none)
+  std::string trace_file;
   int flow_sleep = 32;  // back-off between flag polls (ns)
   DevBuf d_fpat_dirs_ptr, d_fpat_dirs;  // directions of the dataflow sweep's patterns
   DevBuf mom;  // per-pattern scalar-flux moments of the dataflow sweep [npat][n*G]
@@ -380,6 +386,7 @@ struct FlowSync {
   // solve must report PGPU_ERR_TIMEOUT with the context still usable.  Set per solve from
   // PGPU_DEBUG_SWEEP_STALL.
   unsigned int stall;
+  unsigned int trace_on;  // record FlowGeom::trace during this sweep
 };
 
 struct FlowGeom {
@@ -400,7 +407,23 @@ struct FlowGeom {
   // chunk; every pattern's tasks appear tile diagonal by tile diagonal (null: that order)
   const int* __restrict__ order;
   int sleep_ns;  // back-off between polls of an upwind flag
+  // timeline of one sweep for measurement (PGPU_FLOW_TRACE), or null: per handed-out task
+  // the global timer when it was taken, when its upwind wait ended, when its diagonals
+  // ended and when it finished, and the SM it ran on
+  unsigned long long* trace;
 };
+
+__device__ __forceinline__ unsigned long long flow_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned int flow_smid() {
+  unsigned int r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
 
 __device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
   unsigned int v;
@@ -509,6 +532,8 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     __syncthreads();
     const int t = s_task;
     if (t >= K.ntasks) return;  // uniform over the CTA
+    const bool tr = K.trace && threadIdx.x == 0 && *(volatile unsigned int*)&K.sync->trace_on;
+    if (tr) K.trace[(size_t)t * 5] = flow_clock();
     const int tc = K.order ? K.order[t] : t;
     const int jp = tc / K.nchunk, ch = tc - jp * K.nchunk;
     const int j = jp / K.npat, p = jp - j * K.npat;
@@ -589,6 +614,7 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
         flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure: runs out
     }
     __syncthreads();
+    if (tr) K.trace[(size_t)t * 5 + 1] = flow_clock();
     // 3. inflow from the upwind tiles (through L2)
     if (active)
       for (int fs = cl; fs < kFx + kFy + kFz; fs += ncl) {
@@ -648,6 +674,7 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     // 5. publish the tile, then its scalar-flux moment over this pattern's directions: the
     //    barrier that ended the last diagonal orders every thread's psi stores before thread
     //    0's release store (release is cumulative), which the consumer pairs with an acquire
+    if (tr) K.trace[(size_t)t * 5 + 2] = flow_clock();
     if (threadIdx.x == 0) st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
     if (mom) {
       for (int r = threadIdx.x; r < kCells * gn; r += blockDim.x) {
@@ -656,6 +683,10 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
         for (int dj = 0; dj < ndp; dj++) acc += A.w[K.pat_dirs[d0 + dj]] * tpsi[c * S + gg * nd + dj];
         mom[(size_t)p * n * G + (size_t)cell_index(c) * G + g0 + gg] = acc;
       }
+    }
+    if (tr) {
+      K.trace[(size_t)t * 5 + 3] = flow_clock();
+      K.trace[(size_t)t * 5 + 4] = flow_smid();
     }
   }
 }
@@ -714,6 +745,8 @@ __global__ void __launch_bounds__(kFlowSlots * 32)
     __syncthreads();
     const int t = s_task;
     if (t >= K.ntasks) return;  // uniform over the CTA
+    const bool tr = K.trace && threadIdx.x == 0 && *(volatile unsigned int*)&K.sync->trace_on;
+    if (tr) K.trace[(size_t)t * 5] = flow_clock();
     const int tc = K.order ? K.order[t] : t;
     const int jp = tc / K.nchunk, ch = tc - jp * K.nchunk;
     const int j = jp / K.npat, p = jp - j * K.npat;
@@ -784,6 +817,7 @@ __global__ void __launch_bounds__(kFlowSlots * 32)
         flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure: runs out
     }
     __syncthreads();
+    if (tr) K.trace[(size_t)t * 5 + 1] = flow_clock();
     if (active) {
       // 4. inflow from the upwind tiles (through L2)
       for (int fs = lane; fs < kFaces; fs += 32) {
@@ -843,6 +877,7 @@ __global__ void __launch_bounds__(kFlowSlots * 32)
     __syncthreads();
     // 6. publish the tile (the barrier orders every warp's psi stores before the release),
     //    then its scalar-flux moment over this pattern's directions
+    if (tr) K.trace[(size_t)t * 5 + 2] = flow_clock();
     if (threadIdx.x == 0) st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
     if (mom) {
       for (int r = threadIdx.x; r < kCells * gn; r += blockDim.x) {
@@ -853,6 +888,242 @@ __global__ void __launch_bounds__(kFlowSlots * 32)
         mom[(size_t)p * n * G + (size_t)cell_index(c) * G + g0 + gg] = acc;
       }
     }
+    if (tr) {
+      K.trace[(size_t)t * 5 + 3] = flow_clock();
+      K.trace[(size_t)t * 5 + 4] = flow_smid();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Lane-per-cell form of the dataflow sweep (one warp per task).  A task's critical path is
+// its 18 (8x8x4) or 10 (4x4x4) cell diagonals; in the forms above every diagonal step
+// costs a chain of dependent shared-memory loads, index arithmetic and a barrier per
+// update.  Here a lane owns one cell of the diagonal (at most 28 cells) and computes all
+// NS directions of the task's octant for it: the NS updates are independent chains that
+// share the cell's index arithmetic, class lookup and upwind addresses, the angular flux
+// of a cell is NS contiguous values (vector loads and stores), and the lane forms the
+// cell's scalar-flux moment directly.  Used when a task is one group and the octant's
+// directions are contiguous, NS of them (the level-symmetric sets order directions
+// octant by octant).
+// ---------------------------------------------------------------------------------
+template <typename T, int NS, int TX, int TY, int TZ>
+__host__ __device__ constexpr size_t flow_lsmem_bytes() {
+  return ((size_t)TX * TY * TZ * NS + (size_t)(TY * TZ + TX * TZ + TX * TY) * NS + (size_t)kTileClasses * NS * 4 +
+          (size_t)TX * TY * TZ) *
+             sizeof(T) +
+         (size_t)TX * TY * TZ * sizeof(int);
+}
+
+// NS values from / to p (T, 2-element vectors when pair-aligned).
+template <typename T, int NS>
+__device__ __forceinline__ void row_load(const T* p, T (&v)[NS], bool pairs, bool cg) {
+  using V2 = typename std::conditional<sizeof(T) == 8, double2, float2>::type;
+  if (pairs && NS % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < NS; k += 2) {
+      const V2 a = cg ? __ldcg(reinterpret_cast<const V2*>(p + k)) : *reinterpret_cast<const V2*>(p + k);
+      v[k] = a.x;
+      v[k + 1] = a.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NS; k++) v[k] = cg ? __ldcg(p + k) : p[k];
+  }
+}
+
+template <typename T, int NS>
+__device__ __forceinline__ void row_store(T* p, const T (&v)[NS], bool pairs) {
+  using V2 = typename std::conditional<sizeof(T) == 8, double2, float2>::type;
+  if (pairs && NS % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < NS; k += 2) {
+      V2 a;
+      a.x = v[k];
+      a.y = v[k + 1];
+      *reinterpret_cast<V2*>(p + k) = a;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NS; k++) p[k] = v[k];
+  }
+}
+
+template <typename T, int NS, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(32)
+    k_sweep_lflow(SNOp<T> A, FlowGeom K, const SweepPtrs* __restrict__ P, int iso) {
+  using Shape = TileShape<TX, TY, TZ>;
+  constexpr int kCells = TX * TY * TZ, kDiags = TX + TY + TZ - 2;
+  constexpr int kFx = TY * TZ, kFy = TX * TZ, kFz = TX * TY, kFaces = kFx + kFy + kFz;
+  extern __shared__ __align__(16) unsigned char flow_smem[];
+  T* tpsi = reinterpret_cast<T*>(flow_smem);   // [kCells][NS]
+  T* tin = tpsi + kCells * NS;                  // [kFaces][NS]
+  T* tcoef = tin + kFaces * NS;                 // [kTileClasses][NS][4]
+  T* tsrc = tcoef + kTileClasses * NS * 4;      // [kCells]
+  int* tcls = reinterpret_cast<int*>(tsrc + kCells);  // [kCells]
+  __shared__ unsigned char s_cell[kCells];
+  __shared__ int s_dptr[kDiags + 1];
+  const int lane = threadIdx.x;
+  for (int k = lane; k < kCells; k += 32) s_cell[k] = (unsigned char)Shape::cell(k);
+  for (int k = lane; k <= kDiags; k += 32) s_dptr[k] = Shape::dptr(k);
+  const T* __restrict__ src = static_cast<const T*>(P->src);
+  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
+  T* psi = static_cast<T*>(P->psi);
+  T* mom = static_cast<T*>(P->mom);
+  const T* __restrict__ coef = static_cast<const T*>(K.coef);
+  const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
+  const int G = A.G, M = A.M, n = A.n;
+  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
+  // rows of NS contiguous directions start pair-aligned when M and the octant's first
+  // direction are even
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = (int)atomicAdd(&K.sync->next, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= K.ntasks) return;
+    const bool tr = K.trace && lane == 0 && *(volatile unsigned int*)&K.sync->trace_on;
+    if (tr) K.trace[(size_t)t * 5] = flow_clock();
+    const int tc = K.order ? K.order[t] : t;
+    const int jp = tc / K.nchunk, g = tc - jp * K.nchunk;  // one group per task
+    const int j = jp / K.npat, p = jp - j * K.npat;
+    const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
+    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
+    const int atx = sx > 0 ? tx : K.ntx - 1 - tx, aty = sy > 0 ? ty : K.nty - 1 - ty, atz = sz > 0 ? tz : K.ntz - 1 - tz;
+    const FlowTile<TX, TY, TZ> tile{atx * TX, aty * TY, atz * TZ, sx, sy, sz};
+    auto cell_index = [&](int c) {
+      return tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY));
+    };
+    const int m0 = K.pat_dirs[K.pat_dirs_ptr[p]];
+    const bool pairs = ((M | m0) & 1) == 0;
+    unsigned int* pflags = K.flags + ((size_t)p * K.nchunk + g) * ntiles;
+    const int tb = (atz * K.nty + aty) * K.ntx + atx;
+    const int nk = K.tile_ncls[tb];
+    const bool staged = nk <= kTileClasses;
+    T w[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) w[k] = A.w[m0 + k];
+    // 1. data that does not depend on the upwind tiles: source, cell classes, the
+    //    coefficient rows of the tile's classes, inflow on faces on the box boundary
+    for (int c = lane; c < kCells; c += 32) {
+      const int i = cell_index(c);
+      if (iso) tsrc[c] = src[(size_t)i * G + g];
+      tcls[c] = staged ? (int)K.cell_lcls[i] : (int)K.ccls[i];
+    }
+    if (staged)
+      for (int r = lane; r < nk * NS; r += 32) {
+        const int k = r / NS, d = r - k * NS;
+        flow_load4(coef + (((size_t)K.tile_cls[(size_t)tb * kTileClasses + k] * G + g) * M + m0 + d) * 4,
+                   *reinterpret_cast<T(*)[4]>(tcoef + (k * NS + d) * 4));
+      }
+    auto face_cell = [&](int fs, int& a, int& lx, int& ly, int& lz) {
+      if (fs < kFx) {
+        a = 0, lx = 0, ly = fs % TY, lz = fs / TY;
+      } else if (fs < kFx + kFy) {
+        a = 1, lx = (fs - kFx) % TX, ly = 0, lz = (fs - kFx) / TX;
+      } else {
+        a = 2, lx = (fs - kFx - kFy) % TX, ly = (fs - kFx - kFy) / TX, lz = 0;
+      }
+    };
+    const int inner = (tx > 0) | (ty > 0) << 1 | (tz > 0) << 2;  // upwind faces inside the box
+    if (inner != 7)
+      for (int fs = lane; fs < kFaces; fs += 32) {
+        int a, lx, ly, lz;
+        face_cell(fs, a, lx, ly, lz);
+        if ((inner >> a) & 1) continue;
+        T v[NS];
+#pragma unroll
+        for (int k = 0; k < NS; k++) v[k] = T(0);
+        if (bnd) {
+          const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
+          const size_t o = (size_t)f * n + (tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz));
+          if (A.kind[o] == PGPU_FACE_REFLECTIVE) {
+            const int rs = A.rslot[o];
+#pragma unroll
+            for (int k = 0; k < NS; k++) v[k] = bnd_val(A, bnd, rs, g, m0 + k);
+          }
+        }
+        row_store<T, NS>(tin + fs * NS, v, true);
+      }
+    // 2. wait for the upwind tiles of this pattern and group
+    if (lane < 3) {
+      const int a = lane;
+      const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
+      if (ux >= 0 && uy >= 0 && uz >= 0)
+        flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error, kFlowSpinLimit, K.sleep_ns);
+      if (a == 0 && *(volatile unsigned int*)&K.sync->stall == (unsigned int)t + 1u)
+        flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure: runs out
+    }
+    __syncwarp();
+    if (tr) K.trace[(size_t)t * 5 + 1] = flow_clock();
+    // 3. inflow from the upwind tiles (through L2)
+    if (inner)
+      for (int fs = lane; fs < kFaces; fs += 32) {
+        int a, lx, ly, lz;
+        face_cell(fs, a, lx, ly, lz);
+        if (!((inner >> a) & 1)) continue;
+        const int sg = a == 0 ? sx : (a == 1 ? sy : sz);
+        const int nb = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz) - sg * (a == 0 ? 1 : (a == 1 ? nx : nxy));
+        T v[NS];
+        row_load<T, NS>(psi + ((size_t)nb * G + g) * M + m0, v, pairs, true);
+        row_store<T, NS>(tin + fs * NS, v, true);
+      }
+    __syncwarp();
+    // 4. the tile's cell diagonals: a lane takes one cell and all NS directions
+    for (int dd = 0; dd < kDiags; dd++) {
+      const int cb = s_dptr[dd], cn = s_dptr[dd + 1] - cb;
+      if (lane < cn) {
+        const int c = s_cell[cb + lane];
+        const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
+        const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
+        const size_t l0 = ((size_t)i * G + g) * M + m0;
+        const T* px = lx > 0 ? tpsi + (c - 1) * NS : tin + (ly + TY * lz) * NS;
+        const T* py = ly > 0 ? tpsi + (c - TX) * NS : tin + (kFx + lx + TX * lz) * NS;
+        const T* pz = lz > 0 ? tpsi + (c - TX * TY) * NS : tin + (kFx + kFy + lx + TX * ly) * NS;
+        T ux[NS], uy[NS], uz[NS], q[NS];
+        row_load<T, NS>(px, ux, true, false);
+        row_load<T, NS>(py, uy, true, false);
+        row_load<T, NS>(pz, uz, true, false);
+        if (iso) {
+          const T qc = tsrc[c];
+#pragma unroll
+          for (int k = 0; k < NS; k++) q[k] = qc;
+        } else {
+          row_load<T, NS>(src + l0, q, pairs, false);
+        }
+        const int cls = tcls[c];
+        T v[NS];
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+          T cf[4];
+          if (staged) {
+            const T* sc = tcoef + (cls * NS + k) * 4;
+            cf[0] = sc[0], cf[1] = sc[1], cf[2] = sc[2], cf[3] = sc[3];
+          } else {
+            flow_load4(coef + (((size_t)cls * G + g) * M + m0 + k) * 4, cf);
+          }
+          T x = cf[0] * q[k];
+          x += cf[3] * uz[k];
+          x += cf[2] * uy[k];
+          x += cf[1] * ux[k];
+          v[k] = x;
+          acc += w[k] * x;
+        }
+        row_store<T, NS>(tpsi + c * NS, v, true);
+        row_store<T, NS>(psi + l0, v, pairs);
+        if (mom) mom[(size_t)p * n * G + (size_t)i * G + g] = acc;
+      }
+      __syncwarp();
+    }
+    if (tr) K.trace[(size_t)t * 5 + 2] = flow_clock();
+    // 5. publish: the warp barrier that ended the last diagonal orders every lane's stores
+    //    before lane 0's release (cumulative), which the consumer pairs with an acquire
+    if (lane == 0) st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
+    if (tr) {
+      K.trace[(size_t)t * 5 + 3] = flow_clock();
+      K.trace[(size_t)t * 5 + 4] = flow_smid();
+    }
+    __syncwarp();
   }
 }
 
@@ -1619,8 +1890,34 @@ int ensure_level_coef(pgpu_problem* p, const SNOp<T>& A) {
 // the same work: k_sweep_wflow (a warp per (group, direction) slot, warp-level steps
 // between cell diagonals) and k_sweep_flow (the slots' cells spread over the block, block
 // barriers between diagonals); flow_warp picks one per precision.
+// The lane-per-cell kernel applies to one group per task, contiguous octant directions
+// and a class table, with 6 or 10 directions per octant (S6, S8).
+inline int flow_lane_ns(const SNData& d, bool cls, int prec) {
+  if (!d.flow_lane[prec] || !cls || d.kba_gchunk != 1 || !d.kba_contig) return 0;
+  return (d.kba_nd == 10 || d.kba_nd == 6) ? d.kba_nd : 0;
+}
+
+template <typename T, int NS, int TX, int TY, int TZ>
+int flow_prepare_lane(SNData& d) {
+  constexpr size_t smem = flow_lsmem_bytes<T, NS, TX, TY, TZ>();
+  const void* fn = (const void*)k_sweep_lflow<T, NS, TX, TY, TZ>;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (smem > 48u * 1024u) PGPU_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PGPU_CUDA(cudaGetDevice(&dev));
+  PGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32, smem));
+  if (per_sm < 1) return fail(PGPU_ERR_CUDA, "the dataflow sweep does not fit on an SM");
+  const char* ce = std::getenv(sizeof(T) == 8 ? "PGPU_FLOW_CTAS64" : "PGPU_FLOW_CTAS32");
+  if (ce && std::atoi(ce) > 0) per_sm = std::min(per_sm, std::atoi(ce));
+  d.flow_grid[sizeof(T) == 8 ? 0 : 1] = std::min(d.kba_ntasks, sms * per_sm);
+  return PGPU_OK;
+}
+
 template <typename T, bool kClass, int TX, int TY, int TZ>
 int flow_prepare(SNData& d) {
+  const int prec = sizeof(T) == 8 ? 0 : 1;
+  if (const int ns = flow_lane_ns(d, kClass, prec))
+    return ns == 10 ? flow_prepare_lane<T, 10, TX, TY, TZ>(d) : flow_prepare_lane<T, 6, TX, TY, TZ>(d);
   const bool warp = d.flow_warp[sizeof(T) == 8 ? 0 : 1];
   const int S = d.kba_nd * d.kba_gchunk;
   const int nt = warp ? S * 32 : TileShape<TX, TY, TZ>::kThreads;
@@ -1644,6 +1941,13 @@ template <typename T, bool kClass, int TX, int TY, int TZ>
 void flow_launch(SNData& d, cudaStream_t s, const SNOp<T>& A, const SweepFaces<T>& W, const FlowGeom& K,
                  const SweepPtrs* P, int iso) {
   const int S = d.kba_nd * d.kba_gchunk, grid = d.flow_grid[sizeof(T) == 8 ? 0 : 1];
+  if (const int ns = flow_lane_ns(d, kClass, sizeof(T) == 8 ? 0 : 1)) {
+    if (ns == 10)
+      k_sweep_lflow<T, 10, TX, TY, TZ><<<grid, 32, flow_lsmem_bytes<T, 10, TX, TY, TZ>(), s>>>(A, K, P, iso);
+    else
+      k_sweep_lflow<T, 6, TX, TY, TZ><<<grid, 32, flow_lsmem_bytes<T, 6, TX, TY, TZ>(), s>>>(A, K, P, iso);
+    return;
+  }
   if (d.flow_warp[sizeof(T) == 8 ? 0 : 1]) {
     const size_t smem = flow_wsmem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
     k_sweep_wflow<T, kClass, TX, TY, TZ><<<grid, S * 32, smem, s>>>(A, W, K, P, iso);
@@ -1697,7 +2001,8 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
                        cls ? d.d_ccls.as<unsigned short>() : nullptr,
                        cls ? (sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr) : nullptr, d.d_tile_cls.as<int>(),
                        d.d_tile_ncls.as<int>(), d.d_cell_lcls.as<unsigned char>(), d.flow_sync.as<FlowSync>(),
-                       d.flow_flags.as<unsigned int>(), d.d_task_order.as<int>(), d.flow_sleep};
+                       d.flow_flags.as<unsigned int>(), d.d_task_order.as<int>(), d.flow_sleep,
+                       d.trace_buf.as<unsigned long long>()};
       k_flow_begin<<<1, 1, 0, p->stream>>>(K.sync);
       if (cls)
         flow_launch<T, true>(d, p->stream, A, W, K, P, iso);
@@ -1727,7 +2032,20 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   }
   cudaEvent_t e0;
   prof_begin(p, &e0);
+  const bool traced = d.kba && d.trace_sweep == d.sweeps && d.trace_buf.ptr;
+  if (traced) launch(p, k_put<unsigned int>, 1, 1, p->stream, &d.flow_sync.as<FlowSync>()->trace_on, 1u);
   PGPU_CUDA(cudaGraphLaunch(gx, p->stream));
+  if (traced) {
+    // measurement only: the timeline of this sweep to a file of [ntasks][5] unsigned 64-bit
+    launch(p, k_put<unsigned int>, 1, 1, p->stream, &d.flow_sync.as<FlowSync>()->trace_on, 0u);
+    std::vector<unsigned long long> tl((size_t)d.kba_ntasks * 5);
+    PGPU_CUDA(cudaMemcpyAsync(tl.data(), d.trace_buf.ptr, tl.size() * 8, cudaMemcpyDeviceToHost, p->stream));
+    PGPU_CUDA(cudaStreamSynchronize(p->stream));
+    if (FILE* fh = std::fopen(d.trace_file.c_str(), "wb")) {
+      std::fwrite(tl.data(), 8, tl.size(), fh);
+      std::fclose(fh);
+    }
+  }
   p->launches += nlaunch;
   p->prof_name = d.kba ? "k_sweep_flow" : "k_sweep_level";
   // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
@@ -2258,13 +2576,13 @@ static void flow_stagger(int& waves, int& offset) {
   }
 }
 
-// Which dataflow-sweep kernel each precision uses (SNData::flow_warp), overridable with
-// PGPU_FLOW_WARP64 / PGPU_FLOW_WARP32 = 0 or 1 (measurement).
-static void flow_kernels(bool* warp) {
-  const char* e64 = std::getenv("PGPU_FLOW_WARP64");
-  const char* e32 = std::getenv("PGPU_FLOW_WARP32");
-  if (e64) warp[0] = std::atoi(e64) != 0;
-  if (e32) warp[1] = std::atoi(e32) != 0;
+// Which dataflow-sweep kernel each precision uses (SNData::flow_lane, flow_warp),
+// overridable with PGPU_FLOW_LANE64 / LANE32 / WARP64 / WARP32 = 0 or 1 (measurement).
+static void flow_kernels(bool* warp, bool* lane) {
+  const char* names[4] = {"PGPU_FLOW_WARP64", "PGPU_FLOW_WARP32", "PGPU_FLOW_LANE64", "PGPU_FLOW_LANE32"};
+  bool* dst[4] = {&warp[0], &warp[1], &lane[0], &lane[1]};
+  for (int k = 0; k < 4; k++)
+    if (const char* e = std::getenv(names[k])) *dst[k] = std::atoi(e) != 0;
 }
 
 // Back-off between polls of an upwind tile's flag, in ns (PGPU_FLOW_SLEEP, default 32).
@@ -2615,7 +2933,21 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
       if (!kp.order.empty()) up(d.d_task_order, kp.order.data(), kp.order.size() * 4);
       d.flow_sleep = flow_sleep_ns();
-      flow_kernels(d.flow_warp);
+      flow_kernels(d.flow_warp, d.flow_lane);
+      d.kba_contig = true;
+      for (int q = 0; q < kp.npat; q++)
+        for (int k = kp.pat_dirs_ptr[q] + 1; k < kp.pat_dirs_ptr[q + 1]; k++)
+          if (kp.pat_dirs[k] != kp.pat_dirs[k - 1] + 1) d.kba_contig = false;
+      // PGPU_FLOW_TRACE = "<sweep index>:<file>": record the timeline of that sweep of every
+      // solve (measurement only)
+      if (const char* te = std::getenv("PGPU_FLOW_TRACE")) {
+        const char* colon = std::strchr(te, ':');
+        if (colon && colon[1]) {
+          d.trace_sweep = std::atoi(te);
+          d.trace_file = colon + 1;
+          al(d.trace_buf, (size_t)kp.ntasks * 5 * 8);
+        }
+      }
       up(d.d_pat_sign, kp.pat_sign.data(), kp.pat_sign.size() * 4);
       up(d.d_fpat_dirs_ptr, kp.pat_dirs_ptr.data(), kp.pat_dirs_ptr.size() * 4);
       up(d.d_fpat_dirs, kp.pat_dirs.data(), kp.pat_dirs.size() * 4);

@@ -79,6 +79,14 @@ struct Material {
       chi_delayed, chi, velocity;
   std::vector<double> sigma_s;  // [from][to]
 
+  // feedback nuclear data (FeedbackNuclearData.hxx): one constant set per reference
+  // temperature, interpolated linearly at a cell's temperature; empty for constant data
+  std::vector<double> tref;
+  std::vector<Material> feedback_sets;
+  bool feedback() const { return !feedback_sets.empty(); }
+  // the constant data of this material at temperature T (itself for constant data)
+  void at(double T, Material& out) const;
+
   int read(Tokens& tok);
   int read_file(const std::string& path);
   int check_for_solver(int G, bool diffusion, bool transient = false) const;
@@ -284,6 +292,8 @@ class NeutronicSolver : public Solver {
   // writeVTK / writePETSc of the solver (DiffusionSolver.cxx:410-432, SNSolver.cxx:753-780)
   virtual int writeFields(int n) const;
   void powerAndProduction();        // q, P, S and the total power from phi_ (host)
+  void buildCellMaterials();        // cell_mats_ / cell_mat_ at the current temperatures
+  bool temperatureChanged() const;  // feedback data and a temperature field changed since
   const std::map<int, BoundaryCondition>& boundaryConditions() const;
 
   const Mesh* mesh_ = nullptr;
@@ -300,6 +310,11 @@ class NeutronicSolver : public Solver {
   pgpu_stats stats_{};
   bool transient_ = false;
   std::vector<double> phi_prev_;     // scalar flux of the previous time step (phi0)
+  // the data each cell sees (FeedbackNuclearData at the cell's temperature)
+  bool feedback_ = false;
+  std::vector<Material> cell_mats_;
+  std::vector<int> cell_mat_;
+  std::vector<double> T_built_;
 };
 
 class DiffusionSolver : public NeutronicSolver {
@@ -343,6 +358,6 @@ int build_quadrature(int order, std::vector<double>& dirs, std::vector<double>& 
 int assemble_diffusion(const Mesh& mesh, const std::vector<Material>& mats, int G,
                        const std::map<int, BoundaryCondition>& bcs,
                        std::vector<int>& neighbors, std::vector<double>& offdiag,
-                       std::vector<double>& diag);
+                       std::vector<double>& diag, const std::vector<double>* T = nullptr);
 
 }  // namespace pg

@@ -13,6 +13,8 @@
 #include <sstream>
 #include <sys/stat.h>
 
+#include <algorithm>
+
 #include "pg_host.hpp"
 
 namespace pg {
@@ -187,7 +189,34 @@ int Material::read(Tokens& tok) {
       PG_TRY(read_nuclear_data(tok), "unable to read the constant nuclear data");
       has_nd = true;
     } else if (k == "nuclear-data-set") {
-      PG_CHECK(true, "feedback nuclear data (nuclear-data-set) is not supported by this build");
+      // FeedbackNuclearData::read (FeedbackNuclearData.cxx): reference temperatures and one
+      // constant data set per temperature
+      PG_CHECK(line.size() != 2 || line[1] != "{", "missing opening '{' for feedback nuclear data");
+      feedback_sets.clear();
+      tref.clear();
+      while (true) {
+        std::vector<std::string> l2 = tok.next();
+        if (l2.empty() || l2[0] == "}") break;
+        if (l2[0] == "temperature") {
+          PG_CHECK(l2.size() != 2, "wrong number of arguments for keyword 'temperature'");
+          int nt = 0;
+          PG_TRY(to_int(l2[1], 0, INT_MAX, nt), "wrong number of temperatures");
+          PG_TRY(tok.read_doubles(tref, nt, 0.0, DBL_MAX), "wrong temperature data");
+        } else if (l2[0] == "nuclear-data") {
+          PG_CHECK(l2.size() != 2 || l2[1] != "{", "missing opening '{' for nuclear data");
+          Material set;
+          PG_TRY(set.read_nuclear_data(tok), "unable to read the nuclear data");
+          set.has_nd = true;
+          feedback_sets.push_back(set);
+        } else {
+          PG_CHECK(true, "unrecognized keyword '" + l2[0] + "'");
+        }
+      }
+      PG_CHECK(feedback_sets.empty() || feedback_sets.size() != tref.size(),
+               "one nuclear-data set is needed per reference temperature");
+      for (size_t k2 = 1; k2 < tref.size(); k2++)
+        PG_CHECK(!(tref[k2] > tref[k2 - 1]), "reference temperatures must increase");
+      has_nd = true;
     } else if (k == "precursor-data") {
       PG_CHECK(line.size() != 2 || line[1] != "{", "missing opening '{' for precursor data");
       int npg = 0;
@@ -222,8 +251,69 @@ int Material::read(Tokens& tok) {
       PG_CHECK(true, "unrecognized keyword '" + k + "'");
     }
   }
-  if (has_nd) PG_TRY(finish_nuclear_data(), "wrong nuclear data");
+  if (!feedback_sets.empty()) {
+    // FeedbackNuclearData::check(beta_total): every set is completed as constant data is;
+    // the material's own arrays hold the first set (the data at the lowest temperature)
+    for (auto& set : feedback_sets) {
+      set.beta_total = beta_total;
+      PG_TRY(set.finish_nuclear_data(), "wrong nuclear data");
+      PG_CHECK(set.num_groups != feedback_sets[0].num_groups, "wrong number of energy groups");
+    }
+    const Material& s0 = feedback_sets[0];
+    num_groups = s0.num_groups;
+    sigma_t = s0.sigma_t, nu_sigma_f = s0.nu_sigma_f, kappa_sigma_f = s0.kappa_sigma_f, sigma_tr = s0.sigma_tr;
+    diffusion = s0.diffusion, chi_prompt = s0.chi_prompt, chi_delayed = s0.chi_delayed, chi = s0.chi;
+    velocity = s0.velocity, sigma_s = s0.sigma_s;
+  } else if (has_nd) {
+    PG_TRY(finish_nuclear_data(), "wrong nuclear data");
+  }
   return 0;
+}
+
+// FeedbackNuclearData::interpolate and its getters (FeedbackNuclearData.hxx:60-140): below
+// the first reference temperature the first set, above the last the last set, otherwise
+// the linear interpolation between the two sets around T (lower_bound of T).  A
+// temperature equal to the first reference value makes the reference read the set before
+// the first one; the first set is used here.
+void Material::at(double T, Material& out) const {
+  if (feedback_sets.empty()) {
+    out = *this;
+    return;
+  }
+  int i1, i2;
+  double f;
+  if (T < tref.front()) {
+    i1 = i2 = 0, f = 0.0;
+  } else if (T > tref.back()) {
+    i1 = i2 = (int)tref.size() - 1, f = 0.0;
+  } else {
+    i2 = (int)(std::lower_bound(tref.begin(), tref.end(), T) - tref.begin());
+    if (i2 == 0) {
+      i1 = 0, f = 0.0;
+    } else {
+      i1 = i2 - 1;
+      f = (T - tref[i1]) / (tref[i2] - tref[i1]);
+    }
+  }
+  const Material& a = feedback_sets[i1];
+  const Material& b = feedback_sets[i2];
+  auto mix = [&](const std::vector<double>& x, const std::vector<double>& y, std::vector<double>& o) {
+    o.resize(x.size());
+    for (size_t k = 0; k < x.size() && k < y.size(); k++) o[k] = (1.0 - f) * x[k] + f * y[k];
+  };
+  out = *this;
+  out.feedback_sets.clear();
+  out.tref.clear();
+  mix(a.sigma_t, b.sigma_t, out.sigma_t);
+  mix(a.nu_sigma_f, b.nu_sigma_f, out.nu_sigma_f);
+  mix(a.kappa_sigma_f, b.kappa_sigma_f, out.kappa_sigma_f);
+  mix(a.sigma_tr, b.sigma_tr, out.sigma_tr);
+  mix(a.diffusion, b.diffusion, out.diffusion);
+  mix(a.chi_prompt, b.chi_prompt, out.chi_prompt);
+  mix(a.chi_delayed, b.chi_delayed, out.chi_delayed);
+  mix(a.chi, b.chi, out.chi);
+  mix(a.velocity, b.velocity, out.velocity);
+  mix(a.sigma_s, b.sigma_s, out.sigma_s);
 }
 
 int Material::read_nuclear_data(Tokens& tok) {
@@ -300,6 +390,8 @@ int Material::finish_nuclear_data() {
 // ConstantNuclearData::check(G, diffusion, transient) (ConstantNuclearData.cxx:180-200).
 int Material::check_for_solver(int G, bool diffusion_solver, bool transient) const {
   PG_CHECK(!has_nd, "missing nuclear data");
+  for (const auto& set : feedback_sets)  // FeedbackNuclearData::check(G, diffusion, transient)
+    PG_TRY(set.check_for_solver(G, diffusion_solver, transient), "wrong nuclear data");
   PG_CHECK(num_groups != G, "wrong number of energy groups");
   PG_CHECK(sigma_t.empty(), "missing total cross sections");
   PG_CHECK(sigma_s.empty(), "missing scattering cross sections");

@@ -124,7 +124,14 @@ int NeutronicSolver::initialize(const Mesh& mesh, const std::vector<Material>& m
 // n > 0 a transient step.
 int NeutronicSolver::solve(int n, double dt, double t) {
   if (n > 0) return solveTransient(n, dt, t);
-  if (!problem_) PG_TRY(buildProblem(), "unable to build the coefficient matrices");
+  if (problem_ && temperatureChanged()) {  // feedback data: the operator follows the temperatures
+    pgpu_problem_destroy(problem_);
+    problem_ = nullptr;
+  }
+  if (!problem_) {
+    buildCellMaterials();
+    PG_TRY(buildProblem(), "unable to build the coefficient matrices");
+  }
   int st = pgpu_problem_solve(problem_, &opt_.gpu, &stats_);
   PG_CHECK(st != PGPU_OK, std::string("GPU k-eigenvalue solve failed: ") + pgpu_last_error());
   PG_TRY(pgpu_problem_get_keff(problem_, &keff_), "unable to get keff");
@@ -136,6 +143,41 @@ int NeutronicSolver::solve(int n, double dt, double t) {
   for (int i = 0; i < mesh_->num_cells; i++) S_[i] = (*mats_)[mesh_->materials[i]].beta_total * P_[i];
   PG_TRY(fetchSolution(), "unable to get the solution");
   return 0;
+}
+
+// The constant data every cell sees: its material at the cell's temperature (the
+// `temperature` field) when the material has feedback data, else the material itself;
+// cell_mats_ holds each distinct (material, temperature) once and cell_mat_ indexes it.
+void NeutronicSolver::buildCellMaterials() {
+  const Mesh& mesh = *mesh_;
+  cell_mats_.clear();
+  cell_mat_.assign(mesh.num_cells, 0);
+  feedback_ = false;
+  for (const auto& m : *mats_) feedback_ |= m.feedback();
+  if (!feedback_) {
+    cell_mats_ = *mats_;
+    cell_mat_ = mesh.materials;
+    return;
+  }
+  std::map<std::pair<int, double>, int> index;
+  for (int i = 0; i < mesh.num_cells; i++) {
+    const int m = mesh.materials[i];
+    const double t = (*mats_)[m].feedback() ? T_[i] : 0.0;
+    auto it = index.find({m, t});
+    if (it == index.end()) {
+      Material md;
+      (*mats_)[m].at(t, md);
+      cell_mats_.push_back(md);
+      it = index.emplace(std::make_pair(m, t), (int)cell_mats_.size() - 1).first;
+    }
+    cell_mat_[i] = it->second;
+  }
+  T_built_ = T_;
+}
+
+bool NeutronicSolver::temperatureChanged() const {
+  if (!feedback_) return false;
+  return T_ != T_built_;
 }
 
 int NeutronicSolver::solveTransient(int n, double dt, double t) {
@@ -152,7 +194,7 @@ void NeutronicSolver::powerAndProduction() {
   const int n = mesh_->num_cells;
   total_power_ = 0.0;
   for (int i = 0; i < n; i++) {
-    const Material& mat = (*mats_)[mesh_->materials[i]];
+    const Material& mat = cell_mats_[cell_mat_[i]];
     const double V = mesh_->volumes[i];
     q_[i] = 0.0;
     P_[i] = 0.0;
@@ -190,7 +232,10 @@ int NeutronicSolver::writeFields(int n) const {
 }
 
 int NeutronicSolver::problem(pgpu_problem** out) {
-  if (!problem_) PG_TRY(buildProblem(), "unable to build the coefficient matrices");
+  if (!problem_) {
+    buildCellMaterials();
+    PG_TRY(buildProblem(), "unable to build the coefficient matrices");
+  }
   *out = problem_;
   return 0;
 }
@@ -254,15 +299,31 @@ void material_tables(const std::vector<Material>& mats, int G, std::vector<doubl
 // R of DiffusionSolver::buildMatrices (DiffusionSolver.cxx:88-320, n = 0), cell-stencil
 // layout.  The diagonal accumulates in the reference's order: total, self-scatter, then
 // each face in turn.
+// With feedback nuclear data (T given) every cross section of row i is the material's at
+// the temperature of cell i, the neighbour's diffusion coefficient included (the reference
+// evaluates both with T_data[i], DiffusionSolver.cxx:250-279); "same material" still
+// compares the materials themselves.
 int assemble_diffusion(const Mesh& mesh, const std::vector<Material>& mats, int G,
                        const std::map<int, BoundaryCondition>& bcs, std::vector<int>& neighbors,
-                       std::vector<double>& offdiag, std::vector<double>& diag) {
+                       std::vector<double>& offdiag, std::vector<double>& diag, const std::vector<double>* T) {
   const int n = mesh.num_cells, F = mesh.fmax;
   neighbors.assign((size_t)F * n, -1);
   offdiag.assign((size_t)F * n * G, 0.0);
   diag.assign((size_t)n * G, 0.0);
+  std::map<std::pair<int, double>, Material> at_T;
+  auto data = [&](int m, int cell) -> const Material& {
+    if (!T || !mats[m].feedback()) return mats[m];
+    const double t = (*T)[cell];
+    auto it = at_T.find({m, t});
+    if (it == at_T.end()) {
+      Material md;
+      mats[m].at(t, md);
+      it = at_T.emplace(std::make_pair(m, t), md).first;
+    }
+    return it->second;
+  };
   for (int i = 0; i < n; i++) {
-    const Material& mat = mats[mesh.materials[i]];
+    const Material& mat = data(mesh.materials[i], i);
     const double V = mesh.volumes[i];
     for (int f = 0; f < mesh.num_faces[i]; f++) {
       int i2 = mesh.nbr(i, f);
@@ -288,7 +349,7 @@ int assemble_diffusion(const Mesh& mesh, const std::vector<Material>& mats, int 
           }
           continue;
         }
-        const Material& mat2 = mats[mesh.materials[i2]];
+        const Material& mat2 = data(mesh.materials[i2], i);
         double r;
         if (mesh.materials[i2] == mesh.materials[i]) {
           double w = slf(mesh.cc(i), mesh.cc(i2), mesh.nrm(i, f));
@@ -313,18 +374,18 @@ int DiffusionSolver::buildProblem() {
   const Mesh& mesh = *mesh_;
   std::vector<int> nbr;
   std::vector<double> off, diag, st, ss, chi, nsf, ksf;
-  PG_TRY(assemble_diffusion(mesh, *mats_, G_, boundaryConditions(), nbr, off, diag),
+  PG_TRY(assemble_diffusion(mesh, *mats_, G_, boundaryConditions(), nbr, off, diag, feedback_ ? &T_ : nullptr),
          "unable to assemble the diffusion operator");
-  material_tables(*mats_, G_, st, ss, chi, nsf, ksf);
+  material_tables(cell_mats_, G_, st, ss, chi, nsf, ksf);
   pgpu_diffusion_operator op;
   op.num_cells = mesh.num_cells;
   op.num_groups = G_;
   op.num_faces = mesh.fmax;
-  op.num_materials = (int)mats_->size();
+  op.num_materials = (int)cell_mats_.size();
   op.neighbors = nbr.data();
   op.offdiag = off.data();
   op.diag = diag.data();
-  op.materials = mesh.materials.data();
+  op.materials = cell_mat_.data();
   op.volumes = mesh.volumes.data();
   op.sigma_s = ss.data();
   op.chi = chi.data();
@@ -363,20 +424,21 @@ int DiffusionSolver::solveTransient(int n, double dt, double t) {
     phi_prev_ = phi_;
     n0_++;
   }
-  if (!transient_problem_ || dt != transient_dt_) {
+  if (!transient_problem_ || dt != transient_dt_ || temperatureChanged()) {
     if (transient_problem_) pgpu_problem_destroy(transient_problem_);
     transient_problem_ = nullptr;
+    buildCellMaterials();
     std::vector<int> nbr;
     std::vector<double> off, diag, st, ss, chi, nsf, ksf;
-    PG_TRY(assemble_diffusion(mesh, *mats_, G_, boundaryConditions(), nbr, off, diag),
+    PG_TRY(assemble_diffusion(mesh, *mats_, G_, boundaryConditions(), nbr, off, diag, feedback_ ? &T_ : nullptr),
            "unable to assemble the diffusion operator");
-    material_tables(*mats_, G_, st, ss, chi, nsf, ksf);
+    material_tables(cell_mats_, G_, st, ss, chi, nsf, ksf);
     for (int i = 0; i < nc; i++) {
-      const Material& mat = (*mats_)[mesh.materials[i]];
+      const Material& mat = cell_mats_[cell_mat_[i]];
       for (int g = 0; g < G_; g++) diag[(size_t)i * G_ + g] += mesh.volumes[i] / (mat.velocity[g] * dt);
     }
-    for (size_t m = 0; m < mats_->size(); m++) {
-      const Material& mat = (*mats_)[m];
+    for (size_t m = 0; m < cell_mats_.size(); m++) {
+      const Material& mat = cell_mats_[m];
       if (!mat.has_nd) continue;
       for (int g = 0; g < G_; g++) chi[m * G_ + g] = (1.0 - mat.beta_total) * mat.chi_prompt[g];
     }
@@ -384,11 +446,11 @@ int DiffusionSolver::solveTransient(int n, double dt, double t) {
     op.num_cells = nc;
     op.num_groups = G_;
     op.num_faces = mesh.fmax;
-    op.num_materials = (int)mats_->size();
+    op.num_materials = (int)cell_mats_.size();
     op.neighbors = nbr.data();
     op.offdiag = off.data();
     op.diag = diag.data();
-    op.materials = mesh.materials.data();
+    op.materials = cell_mat_.data();
     op.volumes = mesh.volumes.data();
     op.sigma_s = ss.data();
     op.chi = chi.data();
@@ -400,7 +462,7 @@ int DiffusionSolver::solveTransient(int n, double dt, double t) {
   }
   std::vector<double> b((size_t)nc * G_);
   for (int i = 0; i < nc; i++) {
-    const Material& mat = (*mats_)[mesh.materials[i]];
+    const Material& mat = cell_mats_[cell_mat_[i]];
     for (int g = 0; g < G_; g++) {
       const size_t l = (size_t)i * G_ + g;
       b[l] = mat.chi_delayed[g] * S_[i] + mesh.volumes[i] / (mat.velocity[g] * dt) * phi_prev_[l];
@@ -639,14 +701,14 @@ int SNSolver::buildProblem() {
     }
   }
   std::vector<double> st, ss, chi, nsf, ksf;
-  material_tables(*mats_, G, st, ss, chi, nsf, ksf);
+  material_tables(cell_mats_, G, st, ss, chi, nsf, ksf);
   pgpu_sn_operator op;
   std::memset(&op, 0, sizeof(op));
   op.num_cells = n;
   op.num_groups = G;
   op.num_dirs = M_;
   op.num_faces = F;
-  op.num_materials = (int)mats_->size();
+  op.num_materials = (int)cell_mats_.size();
   op.use_ls = ls_ ? 1 : 0;
   op.num_cell_faces = mesh.num_faces.data();
   op.face_kind = kind.data();
@@ -656,7 +718,7 @@ int SNSolver::buildProblem() {
   op.gauss = gauss.data();
   op.reflect_axis = raxis.data();
   op.ls_weight = ls_ ? lsw.data() : nullptr;
-  op.materials = mesh.materials.data();
+  op.materials = cell_mat_.data();
   op.volumes = mesh.volumes.data();
   op.directions = dirs.data();
   op.weights = w.data();

@@ -68,3 +68,58 @@ def bc_split_input(d: str, solver: str = "diffusion", right: str = "reflective")
     with open(os.path.join(d, "input.pmp"), "w") as fh:
         fh.write("\n".join(lines) + "\n")
     return os.path.join(d, "input.pmp")
+
+
+def feedback_input(d: str, solver: str = "diffusion") -> str:
+    """A 2D 10x10 input whose two fuel materials carry feedback nuclear data
+    (`nuclear-data-set`: 2 and 3 reference temperatures, cross sections changing with
+    temperature) beside a constant reflector."""
+    import os
+
+    from pampa_gb300 import workloads as wl
+
+    rng = np.random.default_rng(11)
+    self_scatter = (0.2, 0.5) if solver == "sn" else None
+    base = wl.materials_2g(rng, 3, self_scatter=self_scatter)
+    diffusion = solver == "diffusion"
+    temps = {0: [300.0, 900.0], 1: [300.0, 600.0, 1200.0]}
+    for k in (0, 1):
+        blocks = []
+        for j, t in enumerate(temps[k]):
+            m = dict(base[k])
+            f = 1.0 + 0.15 * j                                   # hotter: less fission, more absorption
+            m = dict(m, nsf=[x / f for x in m["nsf"]], sa=[x * f for x in m["sa"]],
+                     D=[x * (1.0 + 0.05 * j) for x in m["D"]])
+            path = os.path.join(d, f"tmp{k}{j}.pmp")
+            wl.write_material(path, m, diffusion)
+            blocks.append(open(path).read())
+            os.remove(path)
+        with open(os.path.join(d, f"mat{k + 1}.pmp"), "w") as fh:
+            fh.write("nuclear-data-set {\n")
+            fh.write(f"   temperature {len(temps[k])}\n   " + " ".join(str(t) for t in temps[k]) + "\n")
+            for b in blocks:
+                fh.write(b)
+            fh.write("}\n")
+    wl.write_material(os.path.join(d, "mat3.pmp"), base[2], diffusion)
+    nx = ny = 10
+    lay = np.full((1, ny, nx), 3)
+    lay[0, 2:8, 2:5] = 1
+    lay[0, 2:8, 5:8] = 2
+    wl.write_cartesian_mesh(os.path.join(d, "mesh.pmp"), 5.0, nx, ny, 0, lay,
+                            {"-x": "reflective", "+x": "vacuum", "-y": "reflective", "+y": "vacuum"})
+    lines = ["mesh cartesian mesh.pmp", "", "material fuel1 mat1.pmp", "material fuel2 mat2.pmp",
+             "material refl mat3.pmp", "", f"solver {solver} {{", "   energy-groups 2"]
+    if solver == "sn":
+        lines += ["   order 2", "   mixed-face-interpolation 1.0"]
+    lines += ["}"]
+    with open(os.path.join(d, "input.pmp"), "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return os.path.join(d, "input.pmp")
+
+
+def feedback_temperatures(n: int) -> np.ndarray:
+    """A temperature field crossing every interpolation case: below the first reference
+    temperature, between reference temperatures, on an inner one, above the last."""
+    rng = np.random.default_rng(3)
+    T = rng.choice([250.0, 450.0, 600.0, 750.0, 1000.0, 1500.0], size=n)
+    return T

@@ -49,3 +49,19 @@ def test_injected_stall_of_a_late_task_is_also_reported(tmp_path, monkeypatch):
         monkeypatch.delenv("PGPU_DEBUG_SWEEP_STALL")
         p.solve()
         assert p.keff > 0.0
+
+
+def test_injected_stall_in_the_lane_per_cell_sweep(tmp_path, monkeypatch):
+    """S8 with one group per task runs the lane-per-cell form of the sweep: the same
+    bounded wait and the same recovery."""
+    from pampa_gb300 import workloads as wl
+    path = wl.sn_3d(str(tmp_path), nx=16, ny=16, nz=8, order=8, block=2)
+    with pg.Pampa(path, "-silent") as p:
+        monkeypatch.setenv("PGPU_DEBUG_SWEEP_STALL", "30")
+        with pytest.raises(pg.PampaError, match="ran out"):
+            p.solve()
+        monkeypatch.delenv("PGPU_DEBUG_SWEEP_STALL")
+        p.solve()
+        k1 = p.keff
+        p.solve()
+        assert p.keff == k1 and k1 > 0.0
