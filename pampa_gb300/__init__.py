@@ -422,6 +422,28 @@ def diffusion_operator_struct(*, neighbors, offdiag, diag, materials, volumes, s
     return op, list(arrs.values())
 
 
+def sn_operator_struct(*, num_cell_faces, face_kind, neighbors, areas, normals, gauss, reflect_axis, materials,
+                       volumes, directions, weights, reflected, sigma_t, sigma_s, chi, nu_sigma_f, kappa_sigma_f,
+                       ls_weight=None, cart=(0, 0, 0)):
+    """(pgpu_sn_operator, arrays to keep alive) from numpy arrays (layouts of the header)."""
+    kind = _i32(face_kind)
+    F, n = kind.shape
+    w = _f64(weights)
+    nm, G = np.asarray(sigma_s).shape[:2]
+    arrs = dict(num_cell_faces=_i32(num_cell_faces), face_kind=kind, neighbors=_i32(neighbors),
+                areas=_f64(areas), normals=_f64(normals), gauss=_f64(gauss), reflect_axis=_i32(reflect_axis),
+                materials=_i32(materials), volumes=_f64(volumes), directions=_f64(directions), weights=w,
+                reflected=_i32(reflected), sigma_t=_f64(sigma_t), sigma_s=_f64(sigma_s), chi=_f64(chi),
+                nu_sigma_f=_f64(nu_sigma_f), kappa_sigma_f=_f64(kappa_sigma_f))
+    if ls_weight is not None:
+        arrs["ls_weight"] = _f64(ls_weight)
+    op = pgpu_sn_operator(n, G, w.size, F, nm, int(ls_weight is not None))
+    for k, a in arrs.items():
+        setattr(op, k, _ip(a) if a.dtype == np.int32 else _dp(a))
+    op.cart_nx, op.cart_ny, op.cart_nz = cart
+    return op, list(arrs.values())
+
+
 class Server:
     """Continuous-batching solve server (pgpu_serve_*): submit operators, wait for results."""
 
@@ -445,6 +467,16 @@ class Server:
                                                int(want_flux), C.byref(rid))
         if st != PGPU_OK:
             raise PampaError(f"pgpu_serve_submit_diffusion failed ({st})")
+        self._sizes[rid.value] = o.num_cells * o.num_groups if want_flux else 0
+        return rid.value
+
+    def submit_sn(self, op: dict, options: pgpu_options | None = None, want_flux: bool = False) -> int:
+        o, _keep = sn_operator_struct(**op)
+        rid = C.c_longlong(0)
+        st = lib().pgpu_serve_submit_sn(self._h, C.byref(o), C.byref(options) if options else None,
+                                        int(want_flux), C.byref(rid))
+        if st != PGPU_OK:
+            raise PampaError(f"pgpu_serve_submit_sn failed ({st})")
         self._sizes[rid.value] = o.num_cells * o.num_groups if want_flux else 0
         return rid.value
 

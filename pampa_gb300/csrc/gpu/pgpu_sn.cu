@@ -119,9 +119,6 @@ struct SNData {
   int kba_t[3] = {4, 4, 4};                // tile shape (4x4x4 or 8x8x4)
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
-  bool flow_warp[2] = {false, false};      // warp-per-slot sweep kernel per precision [fp32]
-  bool flow_lane[2] = {true, true};        // lane-per-cell sweep kernel where it applies [fp32]
-  bool kba_contig = false;                 // every pattern's directions are contiguous
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
   DevBuf d_task_order;  // hand-out order of the dataflow sweep's tasks (null: canonical)
   DevBuf trace_buf;     // timeline of one traced sweep (PGPU_FLOW_TRACE), [ntasks][5]
@@ -348,6 +345,7 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 // reciprocal diagonal instead (psi = (src - sum mu_f w_in,f psi_upwind) * rden).
 // ---------------------------------------------------------------------------------
 constexpr int kFlowSlots = 10;  // (group, direction) slots of one task at most
+constexpr int kFlowMaxDirs = 16;  // directions of one task at most (an S8 octant holds 10)
 constexpr int kTileClasses = 16;  // cell classes of a tile whose coefficients are staged
 constexpr unsigned int kFlowSpinLimit = 1u << 23;  // ~0.3-0.5 s of polling
 constexpr unsigned int kFlowStallLimit = 1u << 12;  // polls of the failure-injection wait (~1 ms)
@@ -488,14 +486,25 @@ struct FlowTile {
   __device__ __forceinline__ int z(int lz) const { return bz + (sz > 0 ? lz : TZ - 1 - lz); }
 };
 
-// Shared memory of one task with S slots and Gc groups: the tile's angular flux, the
-// inflow on its three upwind faces, the isotropic source and the cells' classes.
+// Shared memory of one task with S slots and Gc groups: the coefficients of the tile's
+// classes, the tile's angular flux with a one-cell halo on its three upwind sides (the
+// halo holds the inflow, so every update reads its upwind values at fixed offsets), the
+// isotropic source, and per cell its class and global index.
 template <typename T>
 __host__ __device__ constexpr size_t flow_smem_bytes(int TX, int TY, int TZ, int S, int Gc) {
-  return ((size_t)TX * TY * TZ * S + (size_t)(TY * TZ + TX * TZ + TX * TY) * S + (size_t)TX * TY * TZ * Gc +
-          (size_t)kTileClasses * S * 4) *
+  return ((size_t)kTileClasses * S * 4 + (size_t)(TX + 1) * (TY + 1) * (TZ + 1) * S + (size_t)TX * TY * TZ * Gc) *
              sizeof(T) +
-         (size_t)TX * TY * TZ * sizeof(int);
+         (size_t)TX * TY * TZ * 2 * sizeof(int);
+}
+
+__device__ __forceinline__ void smem_load4(const float* p, float (&o)[4]) {
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  o[0] = a.x, o[1] = a.y, o[2] = a.z, o[3] = a.w;
+}
+
+__device__ __forceinline__ void smem_load4(const double* p, double (&o)[4]) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+  o[0] = a.x, o[1] = a.y, o[2] = b.x, o[3] = b.y;
 }
 
 template <typename T, bool kClass, int TX, int TY, int TZ>
@@ -503,19 +512,40 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     k_sweep_flow(SNOp<T> A, SweepFaces<T> W, FlowGeom K, const SweepPtrs* __restrict__ P, int iso) {
   using Shape = TileShape<TX, TY, TZ>;
   constexpr int kCells = TX * TY * TZ, kDiags = TX + TY + TZ - 2;
-  constexpr int kFx = TY * TZ, kFy = TX * TZ, kFz = TX * TY;  // upwind face cells per axis
+  constexpr int kFx = TY * TZ, kFy = TX * TZ, kFz = TX * TY, kFaces = kFx + kFy + kFz;  // upwind face cells
+  constexpr int PX = TX + 1, PXY = (TX + 1) * (TY + 1), kPad = PXY * (TZ + 1);
   extern __shared__ __align__(16) unsigned char flow_smem[];
   const int G = A.G, M = A.M, n = A.n, Gc = K.gchunk, nd = K.nd, S = nd * Gc;
-  T* tcoef = reinterpret_cast<T*>(flow_smem);                 // [kTileClasses][S][4]
-  T* tpsi = tcoef + kTileClasses * S * 4;                     // [kCells][S]
-  T* tin = tpsi + kCells * S;                                 // [kFx + kFy + kFz][S]
-  T* tsrc = tin + (kFx + kFy + kFz) * S;                      // [kCells][Gc]
-  int* tcls = reinterpret_cast<int*>(tsrc + kCells * Gc);     // [kCells] class (local or global)
+  T* tcoef = reinterpret_cast<T*>(flow_smem);              // [kTileClasses][S][4]
+  T* tp = tcoef + kTileClasses * S * 4;                    // [kPad][S] padded tile
+  T* tsrc = tp + kPad * S;                                 // [kCells][Gc]
+  int* tcls = reinterpret_cast<int*>(tsrc + kCells * Gc);  // [kCells] class (local or global)
+  int* tgi = tcls + kCells;                                // [kCells] global cell index
   __shared__ int s_task;
-  // the tile's cell order, diagonal by diagonal (threads of a warp read different entries)
-  __shared__ unsigned char s_cell[kCells];
+  // Tables of the tile shape.  Local cell c = lx + TX (ly + TY lz) sits at padded index
+  // (lx+1) + PX (ly+1) + PXY (lz+1); its upwind neighbours are 1, PX and PXY below.
+  __shared__ int s_plan[kCells];  // cells diagonal by diagonal: c | padded index << 8
+  __shared__ int s_face[kFaces];  // upwind face slots: adjacent cell | halo index << 8 | axis << 24
   __shared__ int s_dptr[kDiags + 1];
-  for (int k = threadIdx.x; k < kCells; k += blockDim.x) s_cell[k] = (unsigned char)Shape::cell(k);
+  __shared__ T s_w[kFlowMaxDirs];  // quadrature weights of the task's directions
+  for (int k = threadIdx.x; k < kCells; k += blockDim.x) {
+    const int c = Shape::cell(k);
+    s_plan[k] = c | ((c % TX + 1) + PX * ((c / TX) % TY + 1) + PXY * (c / (TX * TY) + 1)) << 8;
+  }
+  for (int fs = threadIdx.x; fs < kFaces; fs += blockDim.x) {
+    int a, c, h;
+    if (fs < kFx) {  // x face (ly, lz)
+      const int ly = fs % TY, lz = fs / TY;
+      a = 0, c = TX * (ly + TY * lz), h = PX * (ly + 1) + PXY * (lz + 1);
+    } else if (fs < kFx + kFy) {  // y face (lx, lz)
+      const int lx = (fs - kFx) % TX, lz = (fs - kFx) / TX;
+      a = 1, c = lx + TX * TY * lz, h = (lx + 1) + PXY * (lz + 1);
+    } else {  // z face (lx, ly)
+      const int lx = (fs - kFx - kFy) % TX, ly = (fs - kFx - kFy) / TX;
+      a = 2, c = lx + TX * ly, h = (lx + 1) + PX * (ly + 1);
+    }
+    s_face[fs] = c | h << 8 | a << 24;
+  }
   for (int k = threadIdx.x; k <= kDiags; k += blockDim.x) s_dptr[k] = Shape::dptr(k);
   const T* __restrict__ src = static_cast<const T*>(P->src);
   const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
@@ -523,7 +553,11 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
   T* mom = static_cast<T*>(P->mom);
   const T* __restrict__ coef = static_cast<const T*>(K.coef);
   const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
-  const int nx = K.nx, ny = K.ny, nxy = K.nx * K.ny, nz = n / nxy, ntiles = K.ntx * K.nty * K.ntz;
+  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
+  // a sweep that forms moments (scalar-flux space) keeps psi only where it is read again:
+  // the tile's downwind faces, which hold the inflow of the downwind tiles and, on the box
+  // boundary, the outgoing flux of reflective faces
+  const bool all_psi = mom == nullptr;
   // fixed thread -> (slot, cell lane) map; slot = local group * nd + direction index
   const int slot = threadIdx.x % S, cl = threadIdx.x / S, ncl = blockDim.x / S;
   const int gl = slot / nd, di = slot - gl * nd;
@@ -542,9 +576,6 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
     const int atx = sx > 0 ? tx : K.ntx - 1 - tx, aty = sy > 0 ? ty : K.nty - 1 - ty, atz = sz > 0 ? tz : K.ntz - 1 - tz;
     const FlowTile<TX, TY, TZ> tile{atx * TX, aty * TY, atz * TZ, sx, sy, sz};
-    auto cell_index = [&](int c) {
-      return tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY));
-    };
     const int d0 = K.pat_dirs_ptr[p], ndp = K.pat_dirs_ptr[p + 1] - d0;
     const bool active = cl < ncl && gl < gn && di < ndp;
     const int g = g0 + gl;
@@ -554,56 +585,33 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     const int nk = kClass ? K.tile_ncls[tb] : 0;
     const bool staged = kClass && nk <= kTileClasses;
     // 1. data that does not depend on the upwind tiles, loaded while they finish: the
-    //    source, the cells' classes and the coefficients of the tile's classes, and the
-    //    inflow on upwind faces that lie on the box boundary
-    if (iso)
-      for (int r = threadIdx.x; r < kCells * Gc; r += blockDim.x) {
-        const int c = r / Gc, gg = r - c * Gc;
-        if (gg < gn) tsrc[r] = src[(size_t)cell_index(c) * G + g0 + gg];
-      }
-    if (kClass) {
-      for (int c = threadIdx.x; c < kCells; c += blockDim.x) {
-        const int i = cell_index(c);
-        tcls[c] = staged ? (int)K.cell_lcls[i] : (int)K.ccls[i];
-      }
-      if (staged && active)
-        for (int k = cl; k < nk; k += ncl)
-          flow_load4(coef + (((size_t)K.tile_cls[(size_t)tb * kTileClasses + k] * G + g) * M + m) * 4,
-                     *reinterpret_cast<T(*)[4]>(tcoef + (k * S + slot) * 4));
+    //    weights, the cells' global indices, source and classes, the coefficients of the
+    //    tile's classes, and the inflow on upwind faces that lie on the box boundary
+    if (mom && threadIdx.x < ndp) s_w[threadIdx.x] = A.w[K.pat_dirs[d0 + threadIdx.x]];
+    for (int c = threadIdx.x; c < kCells; c += blockDim.x) {
+      const int i = tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY));
+      tgi[c] = i;
+      if (iso)
+        for (int gg = 0; gg < gn; gg++) tsrc[c * Gc + gg] = src[(size_t)i * G + g0 + gg];
+      if (kClass) tcls[c] = staged ? (int)K.cell_lcls[i] : (int)K.ccls[i];
     }
-    // face a, position (u, v): x face (ly, lz) -> ly + TY lz; y face (lx, lz) -> kFx + lx +
-    // TX lz; z face (lx, ly) -> kFx + kFy + lx + TX ly
-    auto face_cell = [&](int fs, int& a, int& lx, int& ly, int& lz) {
-      if (fs < kFx) {
-        a = 0, lx = 0, ly = fs % TY, lz = fs / TY;
-      } else if (fs < kFx + kFy) {
-        a = 1, lx = (fs - kFx) % TX, ly = 0, lz = (fs - kFx) / TX;
-      } else {
-        a = 2, lx = (fs - kFx - kFy) % TX, ly = (fs - kFx - kFy) / TX, lz = 0;
-      }
-    };
+    if (staged && active)
+      for (int k = cl; k < nk; k += ncl)
+        flow_load4(coef + (((size_t)K.tile_cls[(size_t)tb * kTileClasses + k] * G + g) * M + m) * 4,
+                   *reinterpret_cast<T(*)[4]>(tcoef + (k * S + slot) * 4));
     const int inner = (tx > 0) | (ty > 0) << 1 | (tz > 0) << 2;  // upwind faces inside the box
-    if (active)
-      for (int fs = cl; fs < kFx + kFy + kFz; fs += ncl) {
-        int a, lx, ly, lz;
-        face_cell(fs, a, lx, ly, lz);
+    if (active && inner != 7)
+      for (int fs = cl; fs < kFaces; fs += ncl) {
+        const int e = s_face[fs], a = e >> 24, c = e & 255;
         if ((inner >> a) & 1) continue;
         T val = T(0);
         if (bnd) {
           const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
-          const size_t o = (size_t)f * n + (tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz));
+          const size_t o = (size_t)f * n + (tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY)));
           if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd_val(A, bnd, A.rslot[o], g, m);
         }
-        tin[fs * S + slot] = val;
+        tp[((e >> 8) & 0xffff) * S + slot] = val;
       }
-    // the source term of every update, rd * src, into the tile buffer (overwritten by psi
-    // in the passes); needs the staged coefficients and source
-    const bool fold = kClass && staged && iso;
-    if (fold) {
-      __syncthreads();
-      if (active)
-        for (int c = cl; c < kCells; c += ncl) tpsi[c * S + slot] = tcoef[(tcls[c] * S + slot) * 4] * tsrc[c * Gc + gl];
-    }
     // 2. wait for the upwind tiles of this pattern and chunk
     if (threadIdx.x < 3) {
       const int a = threadIdx.x;
@@ -615,16 +623,30 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     }
     __syncthreads();
     if (tr) K.trace[(size_t)t * 5 + 1] = flow_clock();
-    // 3. inflow from the upwind tiles (through L2)
-    if (active)
-      for (int fs = cl; fs < kFx + kFy + kFz; fs += ncl) {
-        int a, lx, ly, lz;
-        face_cell(fs, a, lx, ly, lz);
-        if (!((inner >> a) & 1)) continue;
-        const int s = a == 0 ? sx : (a == 1 ? sy : sz);
-        const int nb = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz) - s * (a == 0 ? 1 : (a == 1 ? nx : nxy));
-        tin[fs * S + slot] = __ldcg(psi + ((size_t)nb * G + g) * M + m);
+    // 3. inflow from the upwind tiles (through L2), four loads in flight per thread
+    if (active && inner) {
+      for (int f0 = cl; f0 < kFaces; f0 += 4 * ncl) {
+        T v[4];
+        int h[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int fs = f0 + u * ncl;
+          v[u] = T(0);
+          h[u] = -1;
+          if (fs < kFaces) {
+            const int e = s_face[fs], a = e >> 24;
+            if ((inner >> a) & 1) {
+              const int nb = tgi[e & 255] - (a == 0 ? sx : (a == 1 ? sy * nx : sz * nxy));
+              v[u] = __ldcg(psi + ((size_t)nb * G + g) * M + m);
+              h[u] = (e >> 8) & 0xffff;
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (h[u] >= 0) tp[h[u] * S + slot] = v[u];
       }
+    }
     __syncthreads();
     // 4. the tile's cell diagonals
     const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
@@ -638,36 +660,32 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
       const int cb = s_dptr[dd], cn = s_dptr[dd + 1] - cb;
       if (active)
         for (int q = cl; q < cn; q += ncl) {
-          const int c = s_cell[cb + q];
-          const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
-          const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
-          const size_t l = ((size_t)i * G + g) * M + m;
-          const int tl = c * S + slot;
-          const T ux = lx > 0 ? tpsi[tl - S] : tin[(ly + TY * lz) * S + slot];
-          const T uy = ly > 0 ? tpsi[tl - TX * S] : tin[(kFx + lx + TX * lz) * S + slot];
-          const T uz = lz > 0 ? tpsi[tl - TX * TY * S] : tin[(kFx + kFy + lx + TX * ly) * S + slot];
+          const int e = s_plan[cb + q], c = e & 255;
+          const int b = (e >> 8) * S + slot;
+          const T ux = tp[b - S], uy = tp[b - PX * S], uz = tp[b - PXY * S];
           T v;
           if (kClass) {
             T cf[4];
-            if (staged) {
-              const T* sc = tcoef + (tcls[c] * S + slot) * 4;
-              cf[0] = sc[0], cf[1] = sc[1], cf[2] = sc[2], cf[3] = sc[3];
-            } else {
+            if (staged)
+              smem_load4(tcoef + (tcls[c] * S + slot) * 4, cf);
+            else
               flow_load4(coef + (((size_t)tcls[c] * G + g) * M + m) * 4, cf);
-            }
-            v = fold ? tpsi[tl] : cf[0] * (iso ? tsrc[c * Gc + gl] : src[l]);
+            v = cf[0] * (iso ? tsrc[c * Gc + gl] : src[((size_t)tgi[c] * G + g) * M + m]);
             v += cf[3] * uz;
             v += cf[2] * uy;
             v += cf[1] * ux;
           } else {
+            const int i = tgi[c];
+            const size_t l = ((size_t)i * G + g) * M + m;
             T num = iso ? tsrc[c * Gc + gl] : src[l];
             num += (muz * W.win[(size_t)fz * n + i]) * uz;
             num += (muy * W.win[(size_t)fy * n + i]) * uy;
             num += (mux * W.win[(size_t)fx * n + i]) * ux;
             v = num * W.rden[l];
           }
-          psi[l] = v;
-          tpsi[tl] = v;
+          tp[b] = v;
+          if (all_psi || c % TX == TX - 1 || (c / TX) % TY == TY - 1 || c / (TX * TY) == TZ - 1)
+            psi[((size_t)tgi[c] * G + g) * M + m] = v;
         }
       __syncthreads();
     }
@@ -679,451 +697,16 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     if (mom) {
       for (int r = threadIdx.x; r < kCells * gn; r += blockDim.x) {
         const int c = r / gn, gg = r - c * gn;
+        const T* row = tp + ((c % TX + 1) + PX * ((c / TX) % TY + 1) + PXY * (c / (TX * TY) + 1)) * S + gg * nd;
         T acc = T(0);
-        for (int dj = 0; dj < ndp; dj++) acc += A.w[K.pat_dirs[d0 + dj]] * tpsi[c * S + gg * nd + dj];
-        mom[(size_t)p * n * G + (size_t)cell_index(c) * G + g0 + gg] = acc;
+        for (int dj = 0; dj < ndp; dj++) acc += s_w[dj] * row[dj];
+        mom[(size_t)p * n * G + (size_t)tgi[c] * G + g0 + gg] = acc;
       }
     }
     if (tr) {
       K.trace[(size_t)t * 5 + 3] = flow_clock();
       K.trace[(size_t)t * 5 + 4] = flow_smid();
     }
-  }
-}
-
-// ---------------------------------------------------------------------------------
-// Warp-per-slot form of the dataflow sweep.  Same tasks, flags, hand-out order and
-// arithmetic as k_sweep_flow, but each (group, direction) slot of a task is one warp that
-// walks the tile's cell diagonals on its own: a cell diagonal of an 8x8x4 tile holds at
-// most 28 cells (4x4x4: 12), so a lane takes one cell per diagonal, and the dependencies
-// of a slot (its upwind cells, same group and direction) stay inside the warp.  A diagonal
-// step ends with __syncwarp instead of a block barrier; block barriers remain only where
-// slots meet (task hand-out, the shared source and cell classes, the upwind wait, and the
-// end of the tile before the flag and the scalar-flux moment).  Shared memory per task:
-// the source and cell classes (shared), and per slot the staged coefficient rows, the
-// tile's angular flux and its inflow faces.
-// ---------------------------------------------------------------------------------
-template <typename T>
-__host__ __device__ constexpr size_t flow_wsmem_bytes(int TX, int TY, int TZ, int S, int Gc) {
-  return ((size_t)TX * TY * TZ * Gc +
-          (size_t)S * ((size_t)kTileClasses * 4 + (size_t)TX * TY * TZ + (size_t)(TY * TZ + TX * TZ + TX * TY))) *
-             sizeof(T) +
-         (size_t)TX * TY * TZ * sizeof(int);
-}
-
-template <typename T, bool kClass, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(kFlowSlots * 32)
-    k_sweep_wflow(SNOp<T> A, SweepFaces<T> W, FlowGeom K, const SweepPtrs* __restrict__ P, int iso) {
-  using Shape = TileShape<TX, TY, TZ>;
-  constexpr int kCells = TX * TY * TZ, kDiags = TX + TY + TZ - 2;
-  constexpr int kFx = TY * TZ, kFy = TX * TZ, kFz = TX * TY, kFaces = kFx + kFy + kFz;
-  constexpr int kPerSlot = kTileClasses * 4 + kCells + kFaces;
-  extern __shared__ __align__(16) unsigned char flow_smem[];
-  const int G = A.G, M = A.M, n = A.n, Gc = K.gchunk, nd = K.nd, S = nd * Gc;
-  T* tsrc = reinterpret_cast<T*>(flow_smem);                  // [kCells][Gc]
-  T* slotmem = tsrc + kCells * Gc;                            // [S][kPerSlot]
-  int* tcls = reinterpret_cast<int*>(slotmem + S * kPerSlot);  // [kCells]
-  __shared__ int s_task;
-  __shared__ unsigned char s_cell[kCells];
-  __shared__ int s_dptr[kDiags + 1];
-  for (int k = threadIdx.x; k < kCells; k += blockDim.x) s_cell[k] = (unsigned char)Shape::cell(k);
-  for (int k = threadIdx.x; k <= kDiags; k += blockDim.x) s_dptr[k] = Shape::dptr(k);
-  const T* __restrict__ src = static_cast<const T*>(P->src);
-  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
-  T* psi = static_cast<T*>(P->psi);
-  T* mom = static_cast<T*>(P->mom);
-  const T* __restrict__ coef = static_cast<const T*>(K.coef);
-  const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
-  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
-  const int lane = threadIdx.x & 31, slot = threadIdx.x >> 5;  // one warp per slot
-  const int gl = slot / nd, di = slot - gl * nd;
-  T* tcoef = slotmem + slot * kPerSlot;  // [kTileClasses][4]
-  T* tpsi = tcoef + kTileClasses * 4;    // [kCells]
-  T* tin = tpsi + kCells;                // [kFaces]
-  for (;;) {
-    if (threadIdx.x == 0) s_task = (int)atomicAdd(&K.sync->next, 1u);
-    __syncthreads();
-    const int t = s_task;
-    if (t >= K.ntasks) return;  // uniform over the CTA
-    const bool tr = K.trace && threadIdx.x == 0 && *(volatile unsigned int*)&K.sync->trace_on;
-    if (tr) K.trace[(size_t)t * 5] = flow_clock();
-    const int tc = K.order ? K.order[t] : t;
-    const int jp = tc / K.nchunk, ch = tc - jp * K.nchunk;
-    const int j = jp / K.npat, p = jp - j * K.npat;
-    const int g0 = ch * Gc, gn = min(Gc, G - g0);
-    const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
-    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
-    const int atx = sx > 0 ? tx : K.ntx - 1 - tx, aty = sy > 0 ? ty : K.nty - 1 - ty, atz = sz > 0 ? tz : K.ntz - 1 - tz;
-    const FlowTile<TX, TY, TZ> tile{atx * TX, aty * TY, atz * TZ, sx, sy, sz};
-    auto cell_index = [&](int c) {
-      return tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY));
-    };
-    const int d0 = K.pat_dirs_ptr[p], ndp = K.pat_dirs_ptr[p + 1] - d0;
-    const bool active = slot < S && gl < gn && di < ndp;  // uniform over the warp
-    const int g = g0 + gl;
-    const int m = active ? K.pat_dirs[d0 + di] : 0;
-    unsigned int* pflags = K.flags + ((size_t)p * K.nchunk + ch) * ntiles;
-    const int tb = (atz * K.nty + aty) * K.ntx + atx;
-    const int nk = kClass ? K.tile_ncls[tb] : 0;
-    const bool staged = kClass && nk <= kTileClasses;
-    // 1. shared data that does not depend on the upwind tiles: source and cell classes
-    if (iso)
-      for (int r = threadIdx.x; r < kCells * Gc; r += blockDim.x) {
-        const int c = r / Gc, gg = r - c * Gc;
-        if (gg < gn) tsrc[r] = src[(size_t)cell_index(c) * G + g0 + gg];
-      }
-    if (kClass)
-      for (int c = threadIdx.x; c < kCells; c += blockDim.x) {
-        const int i = cell_index(c);
-        tcls[c] = staged ? (int)K.cell_lcls[i] : (int)K.ccls[i];
-      }
-    // 2. per slot: coefficient rows of the tile's classes and the inflow on upwind faces
-    //    that lie on the box boundary
-    auto face_cell = [&](int fs, int& a, int& lx, int& ly, int& lz) {
-      if (fs < kFx) {
-        a = 0, lx = 0, ly = fs % TY, lz = fs / TY;
-      } else if (fs < kFx + kFy) {
-        a = 1, lx = (fs - kFx) % TX, ly = 0, lz = (fs - kFx) / TX;
-      } else {
-        a = 2, lx = (fs - kFx - kFy) % TX, ly = (fs - kFx - kFy) / TX, lz = 0;
-      }
-    };
-    const int inner = (tx > 0) | (ty > 0) << 1 | (tz > 0) << 2;  // upwind faces inside the box
-    if (active) {
-      if (staged)
-        for (int k = lane; k < nk; k += 32)
-          flow_load4(coef + (((size_t)K.tile_cls[(size_t)tb * kTileClasses + k] * G + g) * M + m) * 4,
-                     *reinterpret_cast<T(*)[4]>(tcoef + k * 4));
-      for (int fs = lane; fs < kFaces; fs += 32) {
-        int a, lx, ly, lz;
-        face_cell(fs, a, lx, ly, lz);
-        if ((inner >> a) & 1) continue;
-        T val = T(0);
-        if (bnd) {
-          const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
-          const size_t o = (size_t)f * n + (tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz));
-          if (A.kind[o] == PGPU_FACE_REFLECTIVE) val = bnd_val(A, bnd, A.rslot[o], g, m);
-        }
-        tin[fs] = val;
-      }
-    }
-    // 3. wait for the upwind tiles of this pattern and chunk
-    if (threadIdx.x < 3) {
-      const int a = threadIdx.x;
-      const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
-      if (ux >= 0 && uy >= 0 && uz >= 0)
-        flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error, kFlowSpinLimit, K.sleep_ns);
-      if (a == 0 && *(volatile unsigned int*)&K.sync->stall == (unsigned int)t + 1u)
-        flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure: runs out
-    }
-    __syncthreads();
-    if (tr) K.trace[(size_t)t * 5 + 1] = flow_clock();
-    if (active) {
-      // 4. inflow from the upwind tiles (through L2)
-      for (int fs = lane; fs < kFaces; fs += 32) {
-        int a, lx, ly, lz;
-        face_cell(fs, a, lx, ly, lz);
-        if (!((inner >> a) & 1)) continue;
-        const int sg = a == 0 ? sx : (a == 1 ? sy : sz);
-        const int nb = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz) - sg * (a == 0 ? 1 : (a == 1 ? nx : nxy));
-        tin[fs] = __ldcg(psi + ((size_t)nb * G + g) * M + m);
-      }
-      __syncwarp();
-      // 5. the tile's cell diagonals, one cell per lane, within the warp
-      const int fx = sx > 0 ? 3 : 1, fy = sy > 0 ? 0 : 2, fz = sz > 0 ? 4 : 5;
-      T mux = T(0), muy = T(0), muz = T(0);
-      if (!kClass) {
-        mux = fabs(A.dirs[(size_t)m * 3]);
-        muy = fabs(A.dirs[(size_t)m * 3 + 1]);
-        muz = fabs(A.dirs[(size_t)m * 3 + 2]);
-      }
-      for (int dd = 0; dd < kDiags; dd++) {
-        const int cb = s_dptr[dd], cn = s_dptr[dd + 1] - cb;
-        if (lane < cn) {
-          const int c = s_cell[cb + lane];
-          const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
-          const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
-          const size_t l = ((size_t)i * G + g) * M + m;
-          const T ux = lx > 0 ? tpsi[c - 1] : tin[ly + TY * lz];
-          const T uy = ly > 0 ? tpsi[c - TX] : tin[kFx + lx + TX * lz];
-          const T uz = lz > 0 ? tpsi[c - TX * TY] : tin[kFx + kFy + lx + TX * ly];
-          const T q = iso ? tsrc[c * Gc + gl] : src[l];
-          T v;
-          if (kClass) {
-            T cf[4];
-            if (staged) {
-              const T* sc = tcoef + tcls[c] * 4;
-              cf[0] = sc[0], cf[1] = sc[1], cf[2] = sc[2], cf[3] = sc[3];
-            } else {
-              flow_load4(coef + (((size_t)tcls[c] * G + g) * M + m) * 4, cf);
-            }
-            v = cf[0] * q;
-            v += cf[3] * uz;
-            v += cf[2] * uy;
-            v += cf[1] * ux;
-          } else {
-            T num = q;
-            num += (muz * W.win[(size_t)fz * n + i]) * uz;
-            num += (muy * W.win[(size_t)fy * n + i]) * uy;
-            num += (mux * W.win[(size_t)fx * n + i]) * ux;
-            v = num * W.rden[l];
-          }
-          psi[l] = v;
-          tpsi[c] = v;
-        }
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-    // 6. publish the tile (the barrier orders every warp's psi stores before the release),
-    //    then its scalar-flux moment over this pattern's directions
-    if (tr) K.trace[(size_t)t * 5 + 2] = flow_clock();
-    if (threadIdx.x == 0) st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
-    if (mom) {
-      for (int r = threadIdx.x; r < kCells * gn; r += blockDim.x) {
-        const int c = r / gn, gg = r - c * gn;
-        T acc = T(0);
-        for (int dj = 0; dj < ndp; dj++)
-          acc += A.w[K.pat_dirs[d0 + dj]] * slotmem[(gg * nd + dj) * kPerSlot + kTileClasses * 4 + c];
-        mom[(size_t)p * n * G + (size_t)cell_index(c) * G + g0 + gg] = acc;
-      }
-    }
-    if (tr) {
-      K.trace[(size_t)t * 5 + 3] = flow_clock();
-      K.trace[(size_t)t * 5 + 4] = flow_smid();
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------------
-// Lane-per-cell form of the dataflow sweep (one warp per task).  A task's critical path is
-// its 18 (8x8x4) or 10 (4x4x4) cell diagonals; in the forms above every diagonal step
-// costs a chain of dependent shared-memory loads, index arithmetic and a barrier per
-// update.  Here a lane owns one cell of the diagonal (at most 28 cells) and computes all
-// NS directions of the task's octant for it: the NS updates are independent chains that
-// share the cell's index arithmetic, class lookup and upwind addresses, the angular flux
-// of a cell is NS contiguous values (vector loads and stores), and the lane forms the
-// cell's scalar-flux moment directly.  Used when a task is one group and the octant's
-// directions are contiguous, NS of them (the level-symmetric sets order directions
-// octant by octant).
-// ---------------------------------------------------------------------------------
-template <typename T, int NS, int TX, int TY, int TZ>
-__host__ __device__ constexpr size_t flow_lsmem_bytes() {
-  return ((size_t)TX * TY * TZ * NS + (size_t)(TY * TZ + TX * TZ + TX * TY) * NS + (size_t)kTileClasses * NS * 4 +
-          (size_t)TX * TY * TZ) *
-             sizeof(T) +
-         (size_t)TX * TY * TZ * sizeof(int);
-}
-
-// NS values from / to p (T, 2-element vectors when pair-aligned).
-template <typename T, int NS>
-__device__ __forceinline__ void row_load(const T* p, T (&v)[NS], bool pairs, bool cg) {
-  using V2 = typename std::conditional<sizeof(T) == 8, double2, float2>::type;
-  if (pairs && NS % 2 == 0) {
-#pragma unroll
-    for (int k = 0; k < NS; k += 2) {
-      const V2 a = cg ? __ldcg(reinterpret_cast<const V2*>(p + k)) : *reinterpret_cast<const V2*>(p + k);
-      v[k] = a.x;
-      v[k + 1] = a.y;
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < NS; k++) v[k] = cg ? __ldcg(p + k) : p[k];
-  }
-}
-
-template <typename T, int NS>
-__device__ __forceinline__ void row_store(T* p, const T (&v)[NS], bool pairs) {
-  using V2 = typename std::conditional<sizeof(T) == 8, double2, float2>::type;
-  if (pairs && NS % 2 == 0) {
-#pragma unroll
-    for (int k = 0; k < NS; k += 2) {
-      V2 a;
-      a.x = v[k];
-      a.y = v[k + 1];
-      *reinterpret_cast<V2*>(p + k) = a;
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < NS; k++) p[k] = v[k];
-  }
-}
-
-template <typename T, int NS, int TX, int TY, int TZ>
-__global__ void __launch_bounds__(32)
-    k_sweep_lflow(SNOp<T> A, FlowGeom K, const SweepPtrs* __restrict__ P, int iso) {
-  using Shape = TileShape<TX, TY, TZ>;
-  constexpr int kCells = TX * TY * TZ, kDiags = TX + TY + TZ - 2;
-  constexpr int kFx = TY * TZ, kFy = TX * TZ, kFz = TX * TY, kFaces = kFx + kFy + kFz;
-  extern __shared__ __align__(16) unsigned char flow_smem[];
-  T* tpsi = reinterpret_cast<T*>(flow_smem);   // [kCells][NS]
-  T* tin = tpsi + kCells * NS;                  // [kFaces][NS]
-  T* tcoef = tin + kFaces * NS;                 // [kTileClasses][NS][4]
-  T* tsrc = tcoef + kTileClasses * NS * 4;      // [kCells]
-  int* tcls = reinterpret_cast<int*>(tsrc + kCells);  // [kCells]
-  __shared__ unsigned char s_cell[kCells];
-  __shared__ int s_dptr[kDiags + 1];
-  const int lane = threadIdx.x;
-  for (int k = lane; k < kCells; k += 32) s_cell[k] = (unsigned char)Shape::cell(k);
-  for (int k = lane; k <= kDiags; k += 32) s_dptr[k] = Shape::dptr(k);
-  const T* __restrict__ src = static_cast<const T*>(P->src);
-  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
-  T* psi = static_cast<T*>(P->psi);
-  T* mom = static_cast<T*>(P->mom);
-  const T* __restrict__ coef = static_cast<const T*>(K.coef);
-  const unsigned int epoch = *(volatile unsigned int*)&K.sync->epoch;
-  const int G = A.G, M = A.M, n = A.n;
-  const int nx = K.nx, nxy = K.nx * K.ny, ntiles = K.ntx * K.nty * K.ntz;
-  // rows of NS contiguous directions start pair-aligned when M and the octant's first
-  // direction are even
-  for (;;) {
-    int t = 0;
-    if (lane == 0) t = (int)atomicAdd(&K.sync->next, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= K.ntasks) return;
-    const bool tr = K.trace && lane == 0 && *(volatile unsigned int*)&K.sync->trace_on;
-    if (tr) K.trace[(size_t)t * 5] = flow_clock();
-    const int tc = K.order ? K.order[t] : t;
-    const int jp = tc / K.nchunk, g = tc - jp * K.nchunk;  // one group per task
-    const int j = jp / K.npat, p = jp - j * K.npat;
-    const int tx = K.tiles[3 * j], ty = K.tiles[3 * j + 1], tz = K.tiles[3 * j + 2];
-    const int sx = K.pat_sign[3 * p], sy = K.pat_sign[3 * p + 1], sz = K.pat_sign[3 * p + 2];
-    const int atx = sx > 0 ? tx : K.ntx - 1 - tx, aty = sy > 0 ? ty : K.nty - 1 - ty, atz = sz > 0 ? tz : K.ntz - 1 - tz;
-    const FlowTile<TX, TY, TZ> tile{atx * TX, aty * TY, atz * TZ, sx, sy, sz};
-    auto cell_index = [&](int c) {
-      return tile.x(c % TX) + nx * tile.y((c / TX) % TY) + nxy * tile.z(c / (TX * TY));
-    };
-    const int m0 = K.pat_dirs[K.pat_dirs_ptr[p]];
-    const bool pairs = ((M | m0) & 1) == 0;
-    unsigned int* pflags = K.flags + ((size_t)p * K.nchunk + g) * ntiles;
-    const int tb = (atz * K.nty + aty) * K.ntx + atx;
-    const int nk = K.tile_ncls[tb];
-    const bool staged = nk <= kTileClasses;
-    T w[NS];
-#pragma unroll
-    for (int k = 0; k < NS; k++) w[k] = A.w[m0 + k];
-    // 1. data that does not depend on the upwind tiles: source, cell classes, the
-    //    coefficient rows of the tile's classes, inflow on faces on the box boundary
-    for (int c = lane; c < kCells; c += 32) {
-      const int i = cell_index(c);
-      if (iso) tsrc[c] = src[(size_t)i * G + g];
-      tcls[c] = staged ? (int)K.cell_lcls[i] : (int)K.ccls[i];
-    }
-    if (staged)
-      for (int r = lane; r < nk * NS; r += 32) {
-        const int k = r / NS, d = r - k * NS;
-        flow_load4(coef + (((size_t)K.tile_cls[(size_t)tb * kTileClasses + k] * G + g) * M + m0 + d) * 4,
-                   *reinterpret_cast<T(*)[4]>(tcoef + (k * NS + d) * 4));
-      }
-    auto face_cell = [&](int fs, int& a, int& lx, int& ly, int& lz) {
-      if (fs < kFx) {
-        a = 0, lx = 0, ly = fs % TY, lz = fs / TY;
-      } else if (fs < kFx + kFy) {
-        a = 1, lx = (fs - kFx) % TX, ly = 0, lz = (fs - kFx) / TX;
-      } else {
-        a = 2, lx = (fs - kFx - kFy) % TX, ly = (fs - kFx - kFy) / TX, lz = 0;
-      }
-    };
-    const int inner = (tx > 0) | (ty > 0) << 1 | (tz > 0) << 2;  // upwind faces inside the box
-    if (inner != 7)
-      for (int fs = lane; fs < kFaces; fs += 32) {
-        int a, lx, ly, lz;
-        face_cell(fs, a, lx, ly, lz);
-        if ((inner >> a) & 1) continue;
-        T v[NS];
-#pragma unroll
-        for (int k = 0; k < NS; k++) v[k] = T(0);
-        if (bnd) {
-          const int f = a == 0 ? (sx > 0 ? 3 : 1) : (a == 1 ? (sy > 0 ? 0 : 2) : (sz > 0 ? 4 : 5));
-          const size_t o = (size_t)f * n + (tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz));
-          if (A.kind[o] == PGPU_FACE_REFLECTIVE) {
-            const int rs = A.rslot[o];
-#pragma unroll
-            for (int k = 0; k < NS; k++) v[k] = bnd_val(A, bnd, rs, g, m0 + k);
-          }
-        }
-        row_store<T, NS>(tin + fs * NS, v, true);
-      }
-    // 2. wait for the upwind tiles of this pattern and group
-    if (lane < 3) {
-      const int a = lane;
-      const int ux = tx - (a == 0), uy = ty - (a == 1), uz = tz - (a == 2);
-      if (ux >= 0 && uy >= 0 && uz >= 0)
-        flow_wait(pflags + (uz * K.nty + uy) * K.ntx + ux, epoch, &K.sync->error, kFlowSpinLimit, K.sleep_ns);
-      if (a == 0 && *(volatile unsigned int*)&K.sync->stall == (unsigned int)t + 1u)
-        flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure: runs out
-    }
-    __syncwarp();
-    if (tr) K.trace[(size_t)t * 5 + 1] = flow_clock();
-    // 3. inflow from the upwind tiles (through L2)
-    if (inner)
-      for (int fs = lane; fs < kFaces; fs += 32) {
-        int a, lx, ly, lz;
-        face_cell(fs, a, lx, ly, lz);
-        if (!((inner >> a) & 1)) continue;
-        const int sg = a == 0 ? sx : (a == 1 ? sy : sz);
-        const int nb = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz) - sg * (a == 0 ? 1 : (a == 1 ? nx : nxy));
-        T v[NS];
-        row_load<T, NS>(psi + ((size_t)nb * G + g) * M + m0, v, pairs, true);
-        row_store<T, NS>(tin + fs * NS, v, true);
-      }
-    __syncwarp();
-    // 4. the tile's cell diagonals: a lane takes one cell and all NS directions
-    for (int dd = 0; dd < kDiags; dd++) {
-      const int cb = s_dptr[dd], cn = s_dptr[dd + 1] - cb;
-      if (lane < cn) {
-        const int c = s_cell[cb + lane];
-        const int lx = c % TX, ly = (c / TX) % TY, lz = c / (TX * TY);
-        const int i = tile.x(lx) + nx * tile.y(ly) + nxy * tile.z(lz);
-        const size_t l0 = ((size_t)i * G + g) * M + m0;
-        const T* px = lx > 0 ? tpsi + (c - 1) * NS : tin + (ly + TY * lz) * NS;
-        const T* py = ly > 0 ? tpsi + (c - TX) * NS : tin + (kFx + lx + TX * lz) * NS;
-        const T* pz = lz > 0 ? tpsi + (c - TX * TY) * NS : tin + (kFx + kFy + lx + TX * ly) * NS;
-        T ux[NS], uy[NS], uz[NS], q[NS];
-        row_load<T, NS>(px, ux, true, false);
-        row_load<T, NS>(py, uy, true, false);
-        row_load<T, NS>(pz, uz, true, false);
-        if (iso) {
-          const T qc = tsrc[c];
-#pragma unroll
-          for (int k = 0; k < NS; k++) q[k] = qc;
-        } else {
-          row_load<T, NS>(src + l0, q, pairs, false);
-        }
-        const int cls = tcls[c];
-        T v[NS];
-        T acc = T(0);
-#pragma unroll
-        for (int k = 0; k < NS; k++) {
-          T cf[4];
-          if (staged) {
-            const T* sc = tcoef + (cls * NS + k) * 4;
-            cf[0] = sc[0], cf[1] = sc[1], cf[2] = sc[2], cf[3] = sc[3];
-          } else {
-            flow_load4(coef + (((size_t)cls * G + g) * M + m0 + k) * 4, cf);
-          }
-          T x = cf[0] * q[k];
-          x += cf[3] * uz[k];
-          x += cf[2] * uy[k];
-          x += cf[1] * ux[k];
-          v[k] = x;
-          acc += w[k] * x;
-        }
-        row_store<T, NS>(tpsi + c * NS, v, true);
-        row_store<T, NS>(psi + l0, v, pairs);
-        if (mom) mom[(size_t)p * n * G + (size_t)i * G + g] = acc;
-      }
-      __syncwarp();
-    }
-    if (tr) K.trace[(size_t)t * 5 + 2] = flow_clock();
-    // 5. publish: the warp barrier that ended the last diagonal orders every lane's stores
-    //    before lane 0's release (cumulative), which the consumer pairs with an acquire
-    if (lane == 0) st_release_gpu(pflags + (tz * K.nty + ty) * K.ntx + tx, epoch);
-    if (tr) {
-      K.trace[(size_t)t * 5 + 3] = flow_clock();
-      K.trace[(size_t)t * 5 + 4] = flow_smid();
-    }
-    __syncwarp();
   }
 }
 
@@ -1886,44 +1469,13 @@ int ensure_level_coef(pgpu_problem* p, const SNOp<T>& A) {
 
 // The dataflow sweep for the problem's tile shape runs on a persistent grid: every CTA
 // that fits on the device at once, at most one per task.  flow_prepare sizes it (before
-// the launch is captured in the sweep graph), flow_launch enqueues it.  Two kernels do
-// the same work: k_sweep_wflow (a warp per (group, direction) slot, warp-level steps
-// between cell diagonals) and k_sweep_flow (the slots' cells spread over the block, block
-// barriers between diagonals); flow_warp picks one per precision.
-// The lane-per-cell kernel applies to one group per task, contiguous octant directions
-// and a class table, with 6 or 10 directions per octant (S6, S8).
-inline int flow_lane_ns(const SNData& d, bool cls, int prec) {
-  if (!d.flow_lane[prec] || !cls || d.kba_gchunk != 1 || !d.kba_contig) return 0;
-  return (d.kba_nd == 10 || d.kba_nd == 6) ? d.kba_nd : 0;
-}
-
-template <typename T, int NS, int TX, int TY, int TZ>
-int flow_prepare_lane(SNData& d) {
-  constexpr size_t smem = flow_lsmem_bytes<T, NS, TX, TY, TZ>();
-  const void* fn = (const void*)k_sweep_lflow<T, NS, TX, TY, TZ>;
-  int dev = 0, sms = 0, per_sm = 0;
-  if (smem > 48u * 1024u) PGPU_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  PGPU_CUDA(cudaGetDevice(&dev));
-  PGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  PGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32, smem));
-  if (per_sm < 1) return fail(PGPU_ERR_CUDA, "the dataflow sweep does not fit on an SM");
-  const char* ce = std::getenv(sizeof(T) == 8 ? "PGPU_FLOW_CTAS64" : "PGPU_FLOW_CTAS32");
-  if (ce && std::atoi(ce) > 0) per_sm = std::min(per_sm, std::atoi(ce));
-  d.flow_grid[sizeof(T) == 8 ? 0 : 1] = std::min(d.kba_ntasks, sms * per_sm);
-  return PGPU_OK;
-}
-
+// the launch is captured in the sweep graph), flow_launch enqueues it.
 template <typename T, bool kClass, int TX, int TY, int TZ>
 int flow_prepare(SNData& d) {
-  const int prec = sizeof(T) == 8 ? 0 : 1;
-  if (const int ns = flow_lane_ns(d, kClass, prec))
-    return ns == 10 ? flow_prepare_lane<T, 10, TX, TY, TZ>(d) : flow_prepare_lane<T, 6, TX, TY, TZ>(d);
-  const bool warp = d.flow_warp[sizeof(T) == 8 ? 0 : 1];
   const int S = d.kba_nd * d.kba_gchunk;
-  const int nt = warp ? S * 32 : TileShape<TX, TY, TZ>::kThreads;
-  const size_t smem = warp ? flow_wsmem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk)
-                           : flow_smem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
-  const void* fn = warp ? (const void*)k_sweep_wflow<T, kClass, TX, TY, TZ> : (const void*)k_sweep_flow<T, kClass, TX, TY, TZ>;
+  constexpr int nt = TileShape<TX, TY, TZ>::kThreads;
+  const size_t smem = flow_smem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
+  const void* fn = (const void*)k_sweep_flow<T, kClass, TX, TY, TZ>;
   int dev = 0, sms = 0, per_sm = 0;
   if (smem > 48u * 1024u) PGPU_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   PGPU_CUDA(cudaGetDevice(&dev));
@@ -1941,21 +1493,9 @@ template <typename T, bool kClass, int TX, int TY, int TZ>
 void flow_launch(SNData& d, cudaStream_t s, const SNOp<T>& A, const SweepFaces<T>& W, const FlowGeom& K,
                  const SweepPtrs* P, int iso) {
   const int S = d.kba_nd * d.kba_gchunk, grid = d.flow_grid[sizeof(T) == 8 ? 0 : 1];
-  if (const int ns = flow_lane_ns(d, kClass, sizeof(T) == 8 ? 0 : 1)) {
-    if (ns == 10)
-      k_sweep_lflow<T, 10, TX, TY, TZ><<<grid, 32, flow_lsmem_bytes<T, 10, TX, TY, TZ>(), s>>>(A, K, P, iso);
-    else
-      k_sweep_lflow<T, 6, TX, TY, TZ><<<grid, 32, flow_lsmem_bytes<T, 6, TX, TY, TZ>(), s>>>(A, K, P, iso);
-    return;
-  }
-  if (d.flow_warp[sizeof(T) == 8 ? 0 : 1]) {
-    const size_t smem = flow_wsmem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
-    k_sweep_wflow<T, kClass, TX, TY, TZ><<<grid, S * 32, smem, s>>>(A, W, K, P, iso);
-  } else {
-    constexpr int nt = TileShape<TX, TY, TZ>::kThreads;
-    const size_t smem = flow_smem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
-    k_sweep_flow<T, kClass, TX, TY, TZ><<<grid, nt, smem, s>>>(A, W, K, P, iso);
-  }
+  constexpr int nt = TileShape<TX, TY, TZ>::kThreads;
+  const size_t smem = flow_smem_bytes<T>(TX, TY, TZ, S, d.kba_gchunk);
+  k_sweep_flow<T, kClass, TX, TY, TZ><<<grid, nt, smem, s>>>(A, W, K, P, iso);
 }
 
 template <typename T, bool kClass>
@@ -2576,15 +2116,6 @@ static void flow_stagger(int& waves, int& offset) {
   }
 }
 
-// Which dataflow-sweep kernel each precision uses (SNData::flow_lane, flow_warp),
-// overridable with PGPU_FLOW_LANE64 / LANE32 / WARP64 / WARP32 = 0 or 1 (measurement).
-static void flow_kernels(bool* warp, bool* lane) {
-  const char* names[4] = {"PGPU_FLOW_WARP64", "PGPU_FLOW_WARP32", "PGPU_FLOW_LANE64", "PGPU_FLOW_LANE32"};
-  bool* dst[4] = {&warp[0], &warp[1], &lane[0], &lane[1]};
-  for (int k = 0; k < 4; k++)
-    if (const char* e = std::getenv(names[k])) *dst[k] = std::atoi(e) != 0;
-}
-
 // Back-off between polls of an upwind tile's flag, in ns (PGPU_FLOW_SLEEP, default 32).
 static int flow_sleep_ns() {
   const char* e = std::getenv("PGPU_FLOW_SLEEP");
@@ -2653,7 +2184,7 @@ static bool kba_plan(const pgpu_sn_operator* op, const Schedule& S, KbaPlan& K) 
   K.t[0] = big ? 8 : 4;
   K.t[1] = big ? 8 : 4;
   K.t[2] = 4;
-  if (K.nd * K.gchunk > (big ? 256 : 128)) return false;
+  if (K.nd * K.gchunk > (big ? 256 : 128) || K.nd > kFlowMaxDirs) return false;
   K.ntx = nx / K.t[0];
   K.nty = ny / K.t[1];
   K.ntz = nz / K.t[2];
@@ -2933,11 +2464,6 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       up(d.d_tiles, kp.tiles.data(), kp.tiles.size() * 4);
       if (!kp.order.empty()) up(d.d_task_order, kp.order.data(), kp.order.size() * 4);
       d.flow_sleep = flow_sleep_ns();
-      flow_kernels(d.flow_warp, d.flow_lane);
-      d.kba_contig = true;
-      for (int q = 0; q < kp.npat; q++)
-        for (int k = kp.pat_dirs_ptr[q] + 1; k < kp.pat_dirs_ptr[q + 1]; k++)
-          if (kp.pat_dirs[k] != kp.pat_dirs[k - 1] + 1) d.kba_contig = false;
       // PGPU_FLOW_TRACE = "<sweep index>:<file>": record the timeline of that sweep of every
       // solve (measurement only)
       if (const char* te = std::getenv("PGPU_FLOW_TRACE")) {

@@ -123,3 +123,39 @@ def feedback_temperatures(n: int) -> np.ndarray:
     rng = np.random.default_rng(3)
     T = rng.choice([250.0, 450.0, 600.0, 750.0, 1000.0, 1500.0], size=n)
     return T
+
+
+def sn_operator_from_oracle(prob, cart=(0, 0, 0)):
+    """pgpu_sn_operator arrays of an SN problem read by the oracle (the layouts of
+    include/pampa_gb300.h), for calls below the drop-in driver (serving)."""
+    mesh = prob.mesh
+    n, F, G = mesh.n, mesh.F, prob.G
+    dirs, w, refl = po.quadrature(prob.order)
+    gc = po.gauss_coefs(mesh, prob.delta)
+    bcs = prob.boundary_conditions()
+    kind = np.full((F, n), 3, dtype=np.int32)
+    nbr = np.full((F, n), -1, dtype=np.int32)
+    raxis = np.zeros((F, n), dtype=np.int32)
+    for f in range(F):
+        has = f < mesh.num_faces
+        nb = mesh.neighbors[:, f]
+        inter = has & (nb >= 0) & (nb < po.PAD)
+        kind[f, inter] = 0
+        nbr[f, inter] = nb[inter]
+        # the reflection axis of face slot f: the axis of the normal of face f of cells 0, 1, 2
+        # (SNSolver.cxx:539-543)
+        ax = 0
+        for a in range(3):
+            if a < n and abs(float(mesh.normals[a, f, a])) > 1.0 - 1e-6:
+                ax = a
+        for c in np.nonzero(has & (nb < 0))[0]:
+            t = bcs.get(int(-nb[c]), po.BoundaryCondition()).type
+            kind[f, c] = 1 if t == po.BC_VACUUM else 2
+            if t == po.BC_REFLECTIVE:
+                raxis[f, c] = ax
+    eff, mat_c = po._cell_materials(prob)
+    st, nsf, ksf, chi, ss, _ = po._tables_of(eff, G)
+    return dict(num_cell_faces=mesh.num_faces, face_kind=kind, neighbors=nbr, areas=mesh.areas.T,
+                normals=np.transpose(mesh.normals, (1, 0, 2)), gauss=np.transpose(gc, (1, 0, 2)),
+                reflect_axis=raxis, materials=mat_c, volumes=mesh.volumes, directions=dirs, weights=w,
+                reflected=refl, sigma_t=st, sigma_s=ss, chi=chi, nu_sigma_f=nsf, kappa_sigma_f=ksf, cart=cart)

@@ -51,9 +51,9 @@ def test_injected_stall_of_a_late_task_is_also_reported(tmp_path, monkeypatch):
         assert p.keff > 0.0
 
 
-def test_injected_stall_in_the_lane_per_cell_sweep(tmp_path, monkeypatch):
-    """S8 with one group per task runs the lane-per-cell form of the sweep: the same
-    bounded wait and the same recovery."""
+def test_injected_stall_in_an_s8_sweep_with_one_group_per_task(tmp_path, monkeypatch):
+    """S8 (ten directions per octant, so one group per task): the same bounded wait and
+    the same recovery, and repeated solves give the same k."""
     from pampa_gb300 import workloads as wl
     path = wl.sn_3d(str(tmp_path), nx=16, ny=16, nz=8, order=8, block=2)
     with pg.Pampa(path, "-silent") as p:
