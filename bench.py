@@ -432,7 +432,9 @@ def run_ours(args, rank, world, local):
                 data="synthetic (seeded generator, reference .pmp format)",
                 config=dict(workload=args.workload, description=w["desc"], keff=keff,
                             sweeps_per_solve=sweeps, outer_iterations=results[-1]["outer_iterations"],
-                            gmres_iterations=results[-1]["inner_iterations"], l2="flushed (256 MB write) between steps",
+                            inner_iterations=results[-1]["inner_iterations"],
+                            inner_solver="GMRES over sweeps" if w["kind"].startswith("sn") else "BiCGStab",
+                            l2="flushed (256 MB write) between steps",
                             parallelism=f"replicas x{world}" if world > 1 else "1 GPU",
                             wall_ms_per_step=1e3 * wall / args.steps,
                             wielandt_shift=w.get("shift") or "solver default",

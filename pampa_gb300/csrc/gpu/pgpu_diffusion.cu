@@ -17,11 +17,14 @@
 // FP32 with FP32 accumulation, and y += d refines in FP64 (iterative refinement).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <array>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 #include "pgpu_internal.cuh"
 
@@ -58,20 +61,40 @@ struct OuterScal {
   int negatives, nonfinite;
 };
 
+// One coarse level of the aggregation multigrid (level l >= 1; the finer level is l - 1).
+struct MgLevel {
+  int n = 0, F = 0;    // cells, neighbour slots per cell
+  int nf = 0, Ff = 0;  // the finer level's cells and neighbour slots
+  DevBuf agg, mptr, mem;  // aggregates (MgMap)
+  DevBuf fslot;           // [Ff][nf] int8: slot of a finer face's neighbour aggregate, -1 inside, -2 none
+  DevBuf nbr;             // [F][n]
+  DevBuf bs, bf, off64, blk64, off32, blk32;  // Galerkin operator (bs + lam bf = in-cell blocks)
+  DevBuf v64[3], v32[3];  // restricted residual, pre-smoothed z, cycle output
+};
+constexpr int kMgMaxLevels = 12;
+
 struct DiffusionData {
   int n = 0, G = 0, F = 0, nm = 0;
   DevBuf nbr, mat, off64, diag64, vol64, ss64, chi, nsf, ksf;
   DevBuf off32, diag32, vol32, ss32, chi32, nsf32;
   DevBuf fold64, fold32;  // DiffOp::fold in each precision
   DevBuf x, y, b, r64, r32, fs, fs_old, phi, q, P;
-  DevBuf w64[9];  // BiCGStab vectors for FP64
-  DevBuf w32[9];  // BiCGStab vectors for FP32
+  DevBuf w64[11];  // BiCGStab vectors for FP64 (9, 10: V-cycle outputs)
+  DevBuf w32[11];  // BiCGStab vectors for FP32
   DevBuf partials, ticket, bscal, oscal;
   DevBuf lam;  // [2]: the Wielandt shift of the running solve, and a constant 0
   DevBuf bscal_tune;  // BiCGStab scalars of the launch-shape tuner's timing runs
   int shape[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};  // [fp32]: SpMV threads, blocks, cell-kernel threads,
                                                           // blocks, SpMV form (0 row, 1 cell, 2 folded row)
   bool have32 = false;
+  // aggregation multigrid (0 levels: the cell preconditioner alone)
+  MgLevel mg[kMgMaxLevels];
+  int mg_levels = 0;
+  double mg_lam = -1.0;  // shift the coarse operators were combined for (< 0: not yet)
+  bool mg_have32 = false;
+  DevBuf mg_inv64, mg_inv32;  // dense inverse of the coarsest operator
+  std::vector<double> mg_hbs, mg_hbf, mg_hoff;  // the coarsest operator on the host
+  std::vector<int> mg_hnbr;
   // BiCGStab iterations captured in CUDA graphs, [fp32][chunk 4, 8, 16]
   cudaGraphExec_t bicg_graph[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   ~DiffusionData() {
@@ -519,6 +542,299 @@ __global__ void k_bicg_t_cell(DiffOp<T> A, const T* __restrict__ shat, T* t, con
 }
 
 // ---------------------------------------------------------------------------------
+// Aggregation multigrid: a V(1,1)-cycle as the preconditioner of the BiCGStab corrections
+// on large operators.  Level 0 is the operator itself.  The cells of level l+1 are
+// aggregates of level-l cells (three passes of pairwise matching on the face graph, so
+// about 2x2x2 cells on a Cartesian box); the level-(l+1) operator is the Galerkin
+// product P^T A P with the piecewise-constant P of the aggregates, formed on the device:
+// per coarse cell a dense G x G in-cell block (the finer in-cell blocks plus the face
+// couplings between cells of the same aggregate) and per neighbour slot the summed face
+// couplings to that neighbour aggregate.  Smoothing: one damped cell-block forward
+// substitution before and after the coarse correction (the level-0 block is the
+// BiCGStab cell preconditioner); the coarsest level is solved with its dense inverse.
+// ---------------------------------------------------------------------------------
+constexpr double kMgOmega = 0.85;  // smoothing damping (CPU study on the 7-group family: 0.8-0.9 best)
+
+template <typename T>
+struct MgOp {
+  int n, F;
+  const int* __restrict__ nbr;  // [F][n], -1 past the cell's neighbour count
+  const T* __restrict__ off;    // [F][n*G]
+  const T* __restrict__ blk;    // [n][G][G]: row (i, g), column (i, g2)
+};
+
+// Aggregates of a level: the finer level's cells -> this level's cells, and the members
+// of each cell of this level (in increasing finer index).
+struct MgMap {
+  const int* __restrict__ agg;   // [n_fine]
+  const int* __restrict__ mptr;  // [n + 1]
+  const int* __restrict__ mem;   // [n_fine]
+};
+
+// y = (A u)_i at level 0 with u = w z (kSum false) or w z + P zc (kSum true), where z is
+// the undamped cell-preconditioned vector of the BiCGStab step and w the damping; the
+// operator arithmetic is that of apply_cell.
+template <typename T, int G, bool kSum>
+__device__ __forceinline__ void mg_apply0(const DiffOp<T>& A, const T* __restrict__ z, const T* __restrict__ zc,
+                                          const int* __restrict__ agg, int i, T (&y)[G]) {
+  const size_t base = (size_t)i * G;
+  const T w = (T)kMgOmega;
+  T xc[G];
+  const T* zi = kSum ? zc + (size_t)agg[i] * G : nullptr;
+#pragma unroll
+  for (int g = 0; g < G; g++) xc[g] = kSum ? w * z[base + g] + zi[g] : w * z[base + g];
+  const T* fm = A.fold + (size_t)A.mat[i] * G * G;
+  const T vol = A.vol[i];
+#pragma unroll
+  for (int g = 0; g < G; g++) {
+    T sc = T(0);
+#pragma unroll
+    for (int g2 = 0; g2 < G; g2++) sc += fm[g2 * G + g] * xc[g2];
+    y[g] = A.diag[base + g] * xc[g] - vol * sc;
+  }
+  const size_t nG = (size_t)A.n * G;
+  for (int fa = 0; fa < A.F; fa++) {
+    const int j = A.nbr[(size_t)fa * A.n + i];
+    if (j >= 0) {
+      const T* o = A.off + fa * nG + base;
+      const T* xj = z + (size_t)j * G;
+      const T* cj = kSum ? zc + (size_t)agg[j] * G : nullptr;
+#pragma unroll
+      for (int g = 0; g < G; g++) y[g] += o[g] * (kSum ? w * xj[g] + cj[g] : w * xj[g]);
+    }
+  }
+}
+
+// y = (A u)_i at a coarse level, u = z or z + P zc.
+template <typename T, int G, bool kSum>
+__device__ __forceinline__ void mg_apply(const MgOp<T>& C, const T* __restrict__ z, const T* __restrict__ zc,
+                                         const int* __restrict__ agg, int i, T (&y)[G]) {
+  const size_t base = (size_t)i * G;
+  T xc[G];
+  const T* zi = kSum ? zc + (size_t)agg[i] * G : nullptr;
+#pragma unroll
+  for (int g = 0; g < G; g++) xc[g] = kSum ? z[base + g] + zi[g] : z[base + g];
+  const T* b = C.blk + base * G;
+#pragma unroll
+  for (int g = 0; g < G; g++) {
+    T a = T(0);
+#pragma unroll
+    for (int g2 = 0; g2 < G; g2++) a += b[g * G + g2] * xc[g2];
+    y[g] = a;
+  }
+  const size_t nG = (size_t)C.n * G;
+  for (int s = 0; s < C.F; s++) {
+    const int j = C.nbr[(size_t)s * C.n + i];
+    if (j < 0) continue;
+    const T* o = C.off + s * nG + base;
+    const T* xj = z + (size_t)j * G;
+    const T* cj = kSum ? zc + (size_t)agg[j] * G : nullptr;
+#pragma unroll
+    for (int g = 0; g < G; g++) y[g] += o[g] * (kSum ? xj[g] + cj[g] : xj[g]);
+  }
+}
+
+// z = omega L^-1 r with L the lower triangle (diagonal included) of a coarse cell block.
+template <typename T, int G>
+__device__ __forceinline__ void mg_lower(const T* __restrict__ b, const T (&r)[G], T (&z)[G]) {
+#pragma unroll
+  for (int g = 0; g < G; g++) {
+    T s = r[g];
+#pragma unroll
+    for (int g2 = 0; g2 < g; g2++) s -= b[g * G + g2] * z[g2];
+    z[g] = s / b[g * G + g];
+  }
+#pragma unroll
+  for (int g = 0; g < G; g++) z[g] *= (T)kMgOmega;
+}
+
+// rc_I = sum over the members i of I of (r - A w z)_i, level 0 -> 1 (z = M^-1 r from the
+// BiCGStab step, w the damping).
+template <typename T, int G>
+__global__ void k_mg_restrict0(DiffOp<T> A, const T* __restrict__ r, const T* __restrict__ z, MgMap M, int nc,
+                               T* rc, const BiScal* sc) {
+  if (sc->converged) return;
+  for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nc; I += gridDim.x * blockDim.x) {
+    T acc[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) acc[g] = T(0);
+    for (int k = M.mptr[I]; k < M.mptr[I + 1]; k++) {
+      const int i = M.mem[k];
+      T y[G];
+      mg_apply0<T, G, false>(A, z, nullptr, nullptr, i, y);
+#pragma unroll
+      for (int g = 0; g < G; g++) acc[g] += r[(size_t)i * G + g] - y[g];
+    }
+#pragma unroll
+    for (int g = 0; g < G; g++) rc[(size_t)I * G + g] = acc[g];
+  }
+}
+
+// out_i = u_i + w M^-1 (r - A u)_i with u = w z + P zc, M the BiCGStab cell
+// preconditioner and z = M^-1 r from the BiCGStab step (level 0).
+template <typename T, int G>
+__global__ void k_mg_post0(DiffOp<T> A, const T* __restrict__ r, const T* __restrict__ z,
+                           const int* __restrict__ agg, const T* __restrict__ zc, T* out, const BiScal* sc) {
+  if (sc->converged) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    T y[G], res[G], dz[G];
+    mg_apply0<T, G, true>(A, z, zc, agg, i, y);
+    const size_t base = (size_t)i * G;
+    const T* zi = zc + (size_t)agg[i] * G;
+#pragma unroll
+    for (int g = 0; g < G; g++) res[g] = r[base + g] - y[g];
+    precond_cell_g<T, G>(A, i, res, dz);
+#pragma unroll
+    for (int g = 0; g < G; g++) out[base + g] = (T)kMgOmega * (z[base + g] + dz[g]) + zi[g];
+  }
+}
+
+// z = omega L^-1 r per cell (coarse pre-smoothing from a zero guess).
+template <typename T, int G>
+__global__ void k_mg_pre(MgOp<T> C, const T* __restrict__ r, T* z, const BiScal* sc) {
+  if (sc->converged) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C.n; i += gridDim.x * blockDim.x) {
+    const size_t base = (size_t)i * G;
+    T rv[G], zv[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) rv[g] = r[base + g];
+    mg_lower<T, G>(C.blk + base * G, rv, zv);
+#pragma unroll
+    for (int g = 0; g < G; g++) z[base + g] = zv[g];
+  }
+}
+
+// rc_I = sum over the members i of I of (r - A z)_i, coarse level l -> l+1.
+template <typename T, int G>
+__global__ void k_mg_restrict(MgOp<T> C, const T* __restrict__ r, const T* __restrict__ z, MgMap M, int nc, T* rc,
+                              const BiScal* sc) {
+  if (sc->converged) return;
+  for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nc; I += gridDim.x * blockDim.x) {
+    T acc[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) acc[g] = T(0);
+    for (int k = M.mptr[I]; k < M.mptr[I + 1]; k++) {
+      const int i = M.mem[k];
+      T y[G];
+      mg_apply<T, G, false>(C, z, nullptr, nullptr, i, y);
+#pragma unroll
+      for (int g = 0; g < G; g++) acc[g] += r[(size_t)i * G + g] - y[g];
+    }
+#pragma unroll
+    for (int g = 0; g < G; g++) rc[(size_t)I * G + g] = acc[g];
+  }
+}
+
+// out_i = u_i + omega L^-1 (r - A u)_i with u = z + P zc (coarse level).
+template <typename T, int G>
+__global__ void k_mg_post(MgOp<T> C, const T* __restrict__ r, const T* __restrict__ z, const int* __restrict__ agg,
+                          const T* __restrict__ zc, T* out, const BiScal* sc) {
+  if (sc->converged) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C.n; i += gridDim.x * blockDim.x) {
+    T y[G], res[G], dz[G];
+    mg_apply<T, G, true>(C, z, zc, agg, i, y);
+    const size_t base = (size_t)i * G;
+    const T* zi = zc + (size_t)agg[i] * G;
+#pragma unroll
+    for (int g = 0; g < G; g++) res[g] = r[base + g] - y[g];
+    mg_lower<T, G>(C.blk + base * G, res, dz);
+#pragma unroll
+    for (int g = 0; g < G; g++) out[base + g] = z[base + g] + zi[g] + dz[g];
+  }
+}
+
+// z = Ainv r on the coarsest level (one warp per row).
+template <typename T>
+__global__ void k_mg_dense(int N, const T* __restrict__ inv, const T* __restrict__ r, T* z, const BiScal* sc) {
+  if (sc->converged) return;
+  const int lane = threadIdx.x & 31;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < N; row += (gridDim.x * blockDim.x) >> 5) {
+    T acc = T(0);
+    for (int c = lane; c < N; c += 32) acc += inv[(size_t)row * N + c] * r[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) z[row] = acc;
+  }
+}
+
+// Level 1 from the operator (FP64): per coarse row (I, g), the lam-independent part of
+// the in-cell block (diagonal, scattering, couplings inside the aggregate), the fission
+// part (times lam when combined) and the face couplings per neighbour slot.
+__global__ void k_mg_build0(DiffOp<double> A, const signed char* __restrict__ fslot, MgMap M, int nc, int Fc,
+                            double* bs, double* bf, double* offc) {
+  const int G = A.G, n0 = A.n;
+  const size_t nG = (size_t)nc * G, nG0 = (size_t)n0 * G;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nc * G; t += gridDim.x * blockDim.x) {
+    const int I = t / G, g = t - I * G;
+    double rs[kMaxGroups], rf[kMaxGroups];
+    for (int g2 = 0; g2 < G; g2++) rs[g2] = rf[g2] = 0.0;
+    for (int s = 0; s < Fc; s++) offc[s * nG + t] = 0.0;
+    for (int k = M.mptr[I]; k < M.mptr[I + 1]; k++) {
+      const int i = M.mem[k], m = A.mat[i];
+      const double V = A.vol[i];
+      rs[g] += A.diag[(size_t)i * G + g];
+      for (int g2 = 0; g2 < G; g2++) {
+        if (g2 != g) rs[g2] -= V * A.ss[((size_t)m * G + g2) * G + g];
+        rf[g2] -= V * A.chi[(size_t)m * G + g] * A.nsf[(size_t)m * G + g2];
+      }
+      for (int f = 0; f < A.F; f++) {
+        const int sl = fslot[(size_t)f * n0 + i];
+        if (sl == -2) continue;
+        const double o = A.off[f * nG0 + (size_t)i * G + g];
+        if (sl == -1) rs[g] += o;
+        else offc[sl * nG + t] += o;
+      }
+    }
+    for (int g2 = 0; g2 < G; g2++) {
+      bs[(size_t)t * G + g2] = rs[g2];
+      bf[(size_t)t * G + g2] = rf[g2];
+    }
+  }
+}
+
+// Level l+1 from level l (FP64): the same sums over the members' blocks and faces.
+__global__ void k_mg_build(int G, int nf, int Ff, const double* __restrict__ bsf, const double* __restrict__ bff,
+                           const double* __restrict__ offf, const signed char* __restrict__ fslot, MgMap M, int nc,
+                           int Fc, double* bs, double* bf, double* offc) {
+  const size_t nG = (size_t)nc * G, nGf = (size_t)nf * G;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nc * G; t += gridDim.x * blockDim.x) {
+    const int I = t / G, g = t - I * G;
+    double rs[kMaxGroups], rf[kMaxGroups];
+    for (int g2 = 0; g2 < G; g2++) rs[g2] = rf[g2] = 0.0;
+    for (int s = 0; s < Fc; s++) offc[s * nG + t] = 0.0;
+    for (int k = M.mptr[I]; k < M.mptr[I + 1]; k++) {
+      const int i = M.mem[k];
+      const size_t row = (size_t)i * G + g;
+      for (int g2 = 0; g2 < G; g2++) {
+        rs[g2] += bsf[row * G + g2];
+        rf[g2] += bff[row * G + g2];
+      }
+      for (int f = 0; f < Ff; f++) {
+        const int sl = fslot[(size_t)f * nf + i];
+        if (sl == -2) continue;
+        const double o = offf[f * nGf + row];
+        if (sl == -1) rs[g] += o;
+        else offc[sl * nG + t] += o;
+      }
+    }
+    for (int g2 = 0; g2 < G; g2++) {
+      bs[(size_t)t * G + g2] = rs[g2];
+      bf[(size_t)t * G + g2] = rf[g2];
+    }
+  }
+}
+
+// blk = bs + lam bf (FP64, and an FP32 copy when asked).
+__global__ void k_mg_combine(long long N, const double* __restrict__ bs, const double* __restrict__ bf, double lam,
+                             double* blk, float* blk32) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < N; k += (long long)gridDim.x * blockDim.x) {
+    const double v = bs[k] + lam * bf[k];
+    blk[k] = v;
+    if (blk32) blk32[k] = (float)v;
+  }
+}
+
+// ---------------------------------------------------------------------------------
 // Outer-iteration kernels (always FP64)
 // ---------------------------------------------------------------------------------
 
@@ -758,6 +1074,364 @@ int make_fp32(pgpu_problem* p) {
 // SpMV kernels of BiCGStab: the cell form for G = 2, 4, 7, the row form otherwise.
 inline bool cell_form(int G) { return G == 2 || G == 4 || G == 7; }
 
+// ---------------------------------------------------------------------------------
+// Aggregation multigrid, host side: the hierarchy (integer work on the face graph, once
+// per problem), the Galerkin operators (device kernels), their update when the shift
+// changes, and the V-cycle's launches.
+// ---------------------------------------------------------------------------------
+constexpr long long kMgMinRows = 1LL << 17;  // smaller operators keep the cell preconditioner alone
+constexpr int kMgCoarseRows = 160;          // coarsen until a level has at most this many rows
+constexpr int kMgMaxDense = 512;            // largest coarsest level inverted densely
+constexpr double kMgRelam = 1e-3;            // relative shift change that recombines the coarse operators
+
+// Face graph of one level: nbr[f][i] (< 0: none), strength wt[f][i] (null: 1 per face).
+struct HostGraph {
+  int n = 0, F = 0;
+  const int* nbr = nullptr;
+  const int* wt = nullptr;
+  std::vector<int> own_nbr, own_wt;
+};
+
+// One pass of pairwise matching: cells in index order each take their unmatched
+// neighbour of largest strength (the first in slot order on ties), or stay alone.
+int mg_match(const HostGraph& g, std::vector<int>& m) {
+  const int n = g.n;
+  m.assign(n, -1);
+  int nc = 0;
+  for (int i = 0; i < n; i++) {
+    if (m[i] >= 0) continue;
+    int best = -1, bw = 0;
+    for (int f = 0; f < g.F; f++) {
+      const size_t o = (size_t)f * n + i;
+      const int j = g.nbr[o];
+      if (j < 0 || j == i || m[j] >= 0) continue;
+      const int w = g.wt ? g.wt[o] : 1;
+      if (w > bw) {
+        bw = w;
+        best = j;
+      }
+    }
+    m[i] = nc;
+    if (best >= 0) m[best] = nc;
+    nc++;
+  }
+  return nc;
+}
+
+// Members of each aggregate of m (CSR, increasing cell index).
+void mg_members(const std::vector<int>& m, int nc, std::vector<int>& ptr, std::vector<int>& mem) {
+  ptr.assign(nc + 1, 0);
+  for (int a : m) ptr[a + 1]++;
+  for (int c = 0; c < nc; c++) ptr[c + 1] += ptr[c];
+  mem.resize(m.size());
+  std::vector<int> pos(ptr.begin(), ptr.end() - 1);
+  for (size_t i = 0; i < m.size(); i++) mem[pos[m[i]]++] = (int)i;
+}
+
+// Face graph of the aggregates of m: an aggregate's neighbour aggregates in order of first
+// appearance over its members' faces; strength = the summed strengths of those faces.
+void mg_coarsen(const HostGraph& g, const std::vector<int>& m, int nc, HostGraph& cg) {
+  std::vector<int> ptr, mem;
+  mg_members(m, nc, ptr, mem);
+  std::vector<int> aptr(nc + 1, 0), adj, aw, ids, ws;
+  adj.reserve((size_t)nc * 8);
+  aw.reserve((size_t)nc * 8);
+  int Fc = 0;
+  for (int c = 0; c < nc; c++) {
+    ids.clear();
+    ws.clear();
+    for (int k = ptr[c]; k < ptr[c + 1]; k++) {
+      const int i = mem[k];
+      for (int f = 0; f < g.F; f++) {
+        const size_t o = (size_t)f * g.n + i;
+        const int j = g.nbr[o];
+        if (j < 0 || m[j] == c) continue;
+        const int J = m[j], w = g.wt ? g.wt[o] : 1;
+        size_t q = 0;
+        while (q < ids.size() && ids[q] != J) q++;
+        if (q == ids.size()) {
+          ids.push_back(J);
+          ws.push_back(w);
+        } else {
+          ws[q] += w;
+        }
+      }
+    }
+    adj.insert(adj.end(), ids.begin(), ids.end());
+    aw.insert(aw.end(), ws.begin(), ws.end());
+    aptr[c + 1] = (int)adj.size();
+    Fc = std::max(Fc, (int)ids.size());
+  }
+  cg.n = nc;
+  cg.F = Fc;
+  cg.own_nbr.assign((size_t)Fc * nc, -1);
+  cg.own_wt.assign((size_t)Fc * nc, 0);
+  for (int c = 0; c < nc; c++)
+    for (int k = aptr[c]; k < aptr[c + 1]; k++) {
+      cg.own_nbr[(size_t)(k - aptr[c]) * nc + c] = adj[k];
+      cg.own_wt[(size_t)(k - aptr[c]) * nc + c] = aw[k];
+    }
+  cg.nbr = cg.own_nbr.data();
+  cg.wt = cg.own_wt.data();
+}
+
+// Builds the hierarchy of a new problem (operators with at least kMgMinRows rows and
+// G = 2, 4 or 7; PGPU_DIFF_MG = 0 turns it off, 1 on at any size) and its Galerkin
+// operators.  Leaves mg_levels = 0 when it does not apply.
+int mg_setup(pgpu_problem* p, const pgpu_diffusion_operator* op) {
+  DiffusionData& d = *p->diff;
+  const int G = d.G;
+  const char* e = std::getenv("PGPU_DIFF_MG");
+  const int force = e ? std::atoi(e) : -1;
+  if (force == 0 || !cell_form(G) || d.F == 0) return PGPU_OK;
+  if (force != 1 && (long long)d.n * G < kMgMinRows) return PGPU_OK;
+  int st = PGPU_OK;
+  auto up = [&](DevBuf& b, const void* h, size_t bytes) {
+    if (st == PGPU_OK) st = dev_upload(b, h, bytes, &p->bytes, p->stream);
+  };
+  auto al = [&](DevBuf& b, size_t bytes) {
+    if (st == PGPU_OK) st = dev_alloc(b, bytes, &p->bytes, p->stream);
+  };
+  std::vector<std::unique_ptr<HostGraph>> keep;
+  HostGraph fine;
+  fine.n = d.n;
+  fine.F = d.F;
+  fine.nbr = op->neighbors;
+  const HostGraph* cur = &fine;
+  int L = 0;
+  while (st == PGPU_OK && L < kMgMaxLevels && (long long)cur->n * G > kMgCoarseRows) {
+    // three matching passes: pairs, pairs of pairs, and pairs of those
+    std::vector<int> m[3];
+    HostGraph g1, g2;
+    auto g3 = std::make_unique<HostGraph>();
+    const int n1 = mg_match(*cur, m[0]);
+    mg_coarsen(*cur, m[0], n1, g1);
+    const int n2 = mg_match(g1, m[1]);
+    mg_coarsen(g1, m[1], n2, g2);
+    const int n3 = mg_match(g2, m[2]);
+    mg_coarsen(g2, m[2], n3, *g3);
+    if (n3 > 0.6 * cur->n || g3->F > 127) break;  // coarsening stalled
+    std::vector<int> agg(cur->n), mptr, mem;
+    for (int i = 0; i < cur->n; i++) agg[i] = m[2][m[1][m[0][i]]];
+    mg_members(agg, n3, mptr, mem);
+    std::vector<signed char> fs((size_t)cur->F * cur->n);
+    for (int f = 0; f < cur->F; f++)
+      for (int i = 0; i < cur->n; i++) {
+        const size_t o = (size_t)f * cur->n + i;
+        const int j = cur->nbr[o];
+        signed char v = -2;
+        if (j >= 0) {
+          const int I = agg[i], J = agg[j];
+          if (I == J) {
+            v = -1;
+          } else {
+            int sl = 0;  // J is one of I's neighbour aggregates
+            while (sl < g3->F && g3->nbr[(size_t)sl * n3 + I] != J) sl++;
+            if (sl == g3->F) return fail(PGPU_ERR_INVALID, "multigrid: neighbour aggregate missing");
+            v = (signed char)sl;
+          }
+        }
+        fs[o] = v;
+      }
+    MgLevel& lv = d.mg[L];
+    lv.n = n3;
+    lv.F = g3->F;
+    lv.nf = cur->n;
+    lv.Ff = cur->F;
+    up(lv.agg, agg.data(), agg.size() * 4);
+    up(lv.mptr, mptr.data(), mptr.size() * 4);
+    up(lv.mem, mem.data(), mem.size() * 4);
+    up(lv.fslot, fs.data(), fs.size());
+    up(lv.nbr, g3->nbr, (size_t)lv.F * n3 * 4);
+    al(lv.bs, (size_t)n3 * G * G * 8);
+    al(lv.bf, (size_t)n3 * G * G * 8);
+    al(lv.blk64, (size_t)n3 * G * G * 8);
+    al(lv.off64, (size_t)lv.F * n3 * G * 8);
+    keep.push_back(std::move(g3));
+    cur = keep.back().get();
+    L++;
+  }
+  if (st != PGPU_OK) return st;
+  if (L == 0 || (long long)cur->n * G > kMgMaxDense) {
+    for (int l = 0; l < kMgMaxLevels; l++) {
+      MgLevel& lv = d.mg[l];
+      for (DevBuf* b : {&lv.agg, &lv.mptr, &lv.mem, &lv.fslot, &lv.nbr, &lv.bs, &lv.bf, &lv.blk64, &lv.off64})
+        b->release();
+    }
+    return PGPU_OK;
+  }
+  // Galerkin operators, finest first (FP64)
+  cudaStream_t s = p->stream;
+  const DiffOp<double> A = op64(d, false);
+  for (int l = 0; l < L; l++) {
+    MgLevel& lv = d.mg[l];
+    const MgMap M{lv.agg.as<int>(), lv.mptr.as<int>(), lv.mem.as<int>()};
+    const int gb = grid_for((long long)lv.n * G);
+    if (l == 0) {
+      launch(p, k_mg_build0, gb, kThreads, s, A, (const signed char*)lv.fslot.as<signed char>(), M, lv.n, lv.F,
+             lv.bs.as<double>(), lv.bf.as<double>(), lv.off64.as<double>());
+    } else {
+      const MgLevel& pf = d.mg[l - 1];
+      launch(p, k_mg_build, gb, kThreads, s, G, pf.n, pf.F, (const double*)pf.bs.as<double>(),
+             (const double*)pf.bf.as<double>(), (const double*)pf.off64.as<double>(),
+             (const signed char*)lv.fslot.as<signed char>(), M, lv.n, lv.F, lv.bs.as<double>(), lv.bf.as<double>(),
+             lv.off64.as<double>());
+    }
+  }
+  PGPU_CUDA(cudaGetLastError());
+  // the coarsest operator on the host, for its dense inverse at each shift
+  const MgLevel& lc = d.mg[L - 1];
+  d.mg_hbs.resize((size_t)lc.n * G * G);
+  d.mg_hbf.resize((size_t)lc.n * G * G);
+  d.mg_hoff.resize((size_t)lc.F * lc.n * G);
+  d.mg_hnbr.assign(cur->nbr, cur->nbr + (size_t)lc.F * lc.n);
+  PGPU_CUDA(cudaMemcpyAsync(d.mg_hbs.data(), lc.bs.ptr, d.mg_hbs.size() * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(cudaMemcpyAsync(d.mg_hbf.data(), lc.bf.ptr, d.mg_hbf.size() * 8, cudaMemcpyDeviceToHost, s));
+  if (!d.mg_hoff.empty())
+    PGPU_CUDA(cudaMemcpyAsync(d.mg_hoff.data(), lc.off64.ptr, d.mg_hoff.size() * 8, cudaMemcpyDeviceToHost, s));
+  PGPU_CUDA(cudaStreamSynchronize(s));
+  if ((st = dev_alloc(d.mg_inv64, (size_t)lc.n * G * lc.n * G * 8, &p->bytes, s))) return st;
+  d.mg_levels = L;
+  d.mg_lam = -1.0;
+  return PGPU_OK;
+}
+
+// Coarse operators for shift lam: blk = bs + lam bf on every level (FP32 copies when the
+// FP32 path is in use), and the dense inverse of the coarsest (Gauss-Jordan with partial
+// pivoting, FP64, on the host).  Skipped while the shift moved by less than kMgRelam.
+int mg_update(pgpu_problem* p, double lam) {
+  DiffusionData& d = *p->diff;
+  if (!d.mg_levels) return PGPU_OK;
+  const bool same = d.mg_lam >= 0.0 && std::fabs(lam - d.mg_lam) <= kMgRelam * std::fabs(lam);
+  if (same && (d.mg_have32 || !d.have32)) return PGPU_OK;
+  const int G = d.G;
+  cudaStream_t s = p->stream;
+  int st;
+  for (int l = 0; l < d.mg_levels; l++) {
+    MgLevel& lv = d.mg[l];
+    const long long nb = (long long)lv.n * G * G, no = (long long)lv.F * lv.n * G;
+    if (d.have32 && !lv.blk32.ptr) {
+      if ((st = dev_alloc(lv.blk32, (size_t)nb * 4, &p->bytes, s))) return st;
+      if ((st = dev_alloc(lv.off32, (size_t)no * 4, &p->bytes, s))) return st;
+      if (no > 0)
+        launch(p, k_convert<double, float>, grid_for(no), kThreads, s, no, (const double*)lv.off64.as<double>(),
+               lv.off32.as<float>());
+    }
+    launch(p, k_mg_combine, grid_for(nb), kThreads, s, nb, (const double*)lv.bs.as<double>(),
+           (const double*)lv.bf.as<double>(), lam, lv.blk64.as<double>(), d.have32 ? lv.blk32.as<float>() : nullptr);
+  }
+  PGPU_CUDA(cudaGetLastError());
+  const MgLevel& lc = d.mg[d.mg_levels - 1];
+  const int nc = lc.n, N = nc * G;
+  const size_t nG = (size_t)nc * G;
+  std::vector<double> a((size_t)N * N, 0.0), inv((size_t)N * N, 0.0);
+  for (int r = 0; r < N; r++) {
+    const int I = r / G;
+    for (int g2 = 0; g2 < G; g2++) a[(size_t)r * N + I * G + g2] = d.mg_hbs[(size_t)r * G + g2] + lam * d.mg_hbf[(size_t)r * G + g2];
+  }
+  for (int sl = 0; sl < lc.F; sl++)
+    for (int I = 0; I < nc; I++) {
+      const int J = d.mg_hnbr[(size_t)sl * nc + I];
+      if (J < 0) continue;
+      for (int g = 0; g < G; g++) a[(size_t)(I * G + g) * N + J * G + g] += d.mg_hoff[sl * nG + (size_t)I * G + g];
+    }
+  for (int r = 0; r < N; r++) inv[(size_t)r * N + r] = 1.0;
+  for (int c = 0; c < N; c++) {
+    int piv = c;
+    for (int r = c + 1; r < N; r++)
+      if (std::fabs(a[(size_t)r * N + c]) > std::fabs(a[(size_t)piv * N + c])) piv = r;
+    if (!(std::fabs(a[(size_t)piv * N + c]) > 0.0)) return fail(PGPU_ERR_NAN, "singular coarsest multigrid operator");
+    if (piv != c)
+      for (int k = 0; k < N; k++) {
+        std::swap(a[(size_t)piv * N + k], a[(size_t)c * N + k]);
+        std::swap(inv[(size_t)piv * N + k], inv[(size_t)c * N + k]);
+      }
+    const double dinv = 1.0 / a[(size_t)c * N + c];
+    for (int k = 0; k < N; k++) {
+      a[(size_t)c * N + k] *= dinv;
+      inv[(size_t)c * N + k] *= dinv;
+    }
+    for (int r = 0; r < N; r++) {
+      if (r == c) continue;
+      const double f = a[(size_t)r * N + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < N; k++) {
+        a[(size_t)r * N + k] -= f * a[(size_t)c * N + k];
+        inv[(size_t)r * N + k] -= f * inv[(size_t)c * N + k];
+      }
+    }
+  }
+  // pageable source: the copy is staged before cudaMemcpyAsync returns
+  PGPU_CUDA(cudaMemcpyAsync(d.mg_inv64.ptr, inv.data(), inv.size() * 8, cudaMemcpyHostToDevice, s));
+  if (d.have32) {
+    if (!d.mg_inv32.ptr && (st = dev_alloc(d.mg_inv32, inv.size() * 4, &p->bytes, s))) return st;
+    std::vector<float> inv32(inv.begin(), inv.end());
+    PGPU_CUDA(cudaMemcpyAsync(d.mg_inv32.ptr, inv32.data(), inv32.size() * 4, cudaMemcpyHostToDevice, s));
+  }
+  d.mg_lam = lam;
+  d.mg_have32 = d.have32;
+  return PGPU_OK;
+}
+
+// Level vectors and the two V-cycle outputs of BiCGStab (w[9], w[10]) in precision T.
+template <typename T>
+int mg_vectors(pgpu_problem* p, DevBuf* w) {
+  DiffusionData& d = *p->diff;
+  int st;
+  for (int l = 0; l < d.mg_levels; l++)
+    for (int k = 0; k < 3; k++) {
+      DevBuf& b = sizeof(T) == 8 ? d.mg[l].v64[k] : d.mg[l].v32[k];
+      if (!b.ptr && (st = dev_alloc(b, (size_t)d.mg[l].n * d.G * sizeof(T), &p->bytes, p->stream))) return st;
+    }
+  for (int k = 9; k < 11; k++)
+    if (!w[k].ptr && (st = dev_alloc(w[k], (size_t)d.n * d.G * sizeof(T), &p->bytes, p->stream))) return st;
+  return PGPU_OK;
+}
+
+// out = V-cycle applied to r, given z0 = M^-1 r from the BiCGStab step (3 launches per
+// level).
+template <typename T, int G>
+void mg_cycle_g(pgpu_problem* p, const DiffOp<T>& A, const T* r, const T* z0, T* out, const BiScal* sc) {
+  DiffusionData& d = *p->diff;
+  cudaStream_t s = p->stream;
+  const int L = d.mg_levels;
+  auto op = [&](int l) {
+    const MgLevel& lv = d.mg[l];
+    return MgOp<T>{lv.n, lv.F, lv.nbr.as<int>(), (const T*)(sizeof(T) == 8 ? lv.off64.ptr : lv.off32.ptr),
+                   (const T*)(sizeof(T) == 8 ? lv.blk64.ptr : lv.blk32.ptr)};
+  };
+  auto map = [&](int l) {
+    const MgLevel& lv = d.mg[l];
+    return MgMap{lv.agg.as<int>(), lv.mptr.as<int>(), lv.mem.as<int>()};
+  };
+  auto vec = [&](int l, int k) -> T* { return (T*)(sizeof(T) == 8 ? d.mg[l].v64[k].ptr : d.mg[l].v32[k].ptr); };
+  auto gr = [&](long long n) { return grid_for(n, p->sm_share, kThreads); };
+  launch(p, k_mg_restrict0<T, G>, gr(d.mg[0].n), kThreads, s, A, r, z0, map(0), d.mg[0].n, vec(0, 0), sc);
+  for (int l = 0; l + 1 < L; l++) {
+    launch(p, k_mg_pre<T, G>, gr(d.mg[l].n), kThreads, s, op(l), (const T*)vec(l, 0), vec(l, 1), sc);
+    launch(p, k_mg_restrict<T, G>, gr(d.mg[l + 1].n), kThreads, s, op(l), (const T*)vec(l, 0), (const T*)vec(l, 1),
+           map(l + 1), d.mg[l + 1].n, vec(l + 1, 0), sc);
+  }
+  const int Nc = d.mg[L - 1].n * G;
+  const T* inv = (const T*)(sizeof(T) == 8 ? d.mg_inv64.ptr : d.mg_inv32.ptr);
+  launch(p, k_mg_dense<T>, (Nc * 32 + kThreads - 1) / kThreads, kThreads, s, Nc, inv, (const T*)vec(L - 1, 0),
+         vec(L - 1, 2), sc);
+  for (int l = L - 2; l >= 0; l--)
+    launch(p, k_mg_post<T, G>, gr(d.mg[l].n), kThreads, s, op(l), (const T*)vec(l, 0), (const T*)vec(l, 1),
+           (const int*)d.mg[l + 1].agg.as<int>(), (const T*)vec(l + 1, 2), vec(l, 2), sc);
+  launch(p, k_mg_post0<T, G>, gr(d.n), kThreads, s, A, r, z0, (const int*)d.mg[0].agg.as<int>(), (const T*)vec(0, 2),
+         out, sc);
+}
+
+template <typename T>
+void mg_cycle(pgpu_problem* p, const DiffOp<T>& A, const T* r, const T* z0, T* out, const BiScal* sc) {
+  switch (A.G) {
+    case 2: return mg_cycle_g<T, 2>(p, A, r, z0, out, sc);
+    case 4: return mg_cycle_g<T, 4>(p, A, r, z0, out, sc);
+    case 7: return mg_cycle_g<T, 7>(p, A, r, z0, out, sc);
+  }
+}
+
 // form: 0 row (any G), 1 cell, 2 folded row (G = 2, 4, 7 with the fold table)
 template <typename T, int G>
 void launch_v_g(int form, int blocks, int threads, cudaStream_t st, const DiffOp<T>& A, const T* phat, T* v,
@@ -905,6 +1579,11 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
     *s = w[5].as<T>(), *t = w[6].as<T>(), *phat = w[7].as<T>(), *shat = w[8].as<T>();
   int tst = tune_bicg<T>(p, A, w);
   if (tst) return tst;
+  // the V-cycle preconditioner when the problem has a hierarchy (shifted operators only)
+  const bool mg = d.mg_levels > 0 && A.fold != nullptr;
+  if (mg && (tst = mg_vectors<T>(p, w))) return tst;
+  T* phf = mg ? w[9].as<T>() : phat;  // preconditioned directions fed to the SpMVs
+  T* shf = mg ? w[10].as<T>() : shat;
   const int* shp = d.shape[sizeof(T) == 8 ? 0 : 1];
   const int rT = shp[0], gS = shp[1], cT = shp[2], gC = shp[3], form = shp[4];  // SpMV and cell shapes
   const int gN = grid_for(N, p->sm_share, kThreads);              // element-wise kernels
@@ -923,14 +1602,16 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   auto iteration = [&](bool timed) {
     cudaEvent_t e0;
     launch_bicg_p<T>(gC, cT, st, A, r, pp, v, phat, sc);
+    if (mg) mg_cycle<T>(p, A, pp, phat, phf, sc);
     if (timed) prof_begin(p, &e0);
-    launch_bicg_v<T>(form, gS, rT, st, A, phat, v, rhat, sc, slots_of<1>(d));
+    launch_bicg_v<T>(form, gS, rT, st, A, phf, v, rhat, sc, slots_of<1>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
     launch_bicg_s<T>(gC, cT, st, A, r, v, s, shat, sc);
+    if (mg) mg_cycle<T>(p, A, s, shat, shf, sc);
     if (timed) prof_begin(p, &e0);
-    launch_bicg_t<T>(form, gS, rT, st, A, shat, t, s, sc, slots_of<2>(d));
+    launch_bicg_t<T>(form, gS, rT, st, A, shf, t, s, sc, slots_of<2>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
-    k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phat, shat, s, t, rhat, sc, slots_of<2>(d));
+    k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phf, shf, s, t, rhat, sc, slots_of<2>(d));
   };
   for (int launched = 0; launched < max_iters; launched += chunk) {
     if (p->profile) {
@@ -941,9 +1622,11 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
       cudaGraphExec_t& gx = d.bicg_graph[sizeof(T) == 8 ? 0 : 1][gi];
       if (!gx) {
         cudaGraph_t graph;
+        const long long counted = p->launches;  // captured launches run only when replayed
         PGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         for (int c = 0; c < chunk; c++) iteration(false);
         PGPU_CUDA(cudaStreamEndCapture(st, &graph));
+        p->launches = counted;
         cudaError_t e = cudaGraphInstantiate(&gx, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
@@ -952,6 +1635,7 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
         }
       }
       PGPU_CUDA(cudaGraphLaunch(gx, st));
+      if (mg) p->launches += 6LL * d.mg_levels * chunk;  // two V-cycles of 3 launches per level
     }
     p->launches += 5LL * chunk;
     PGPU_CUDA(cudaGetLastError());
@@ -980,6 +1664,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   const int gN = grid_for(N, p->sm_share, kThreads), gC = grid_for(n, p->sm_share, kThreads);
   PGPU_CUDA(cudaMemsetAsync(d.lam.ptr, 0, 2 * sizeof(double), s));
   refold(p);
+  if ((st = mg_update(p, 0.0))) return st;
   DiffOp<double> A = op64(d, true);
   OuterScal* dos = d.oscal.as<OuterScal>();
   cudaEvent_t e0, e1;
@@ -1079,6 +1764,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       lam_s = sh > 0.0 ? 1.0 / std::fmax(os.k * (1.0 + sh), os.k + kShiftMargin * dk) : 0.0;
       launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), lam_s);
       refold(p);
+      if ((st = mg_update(p, lam_s))) return st;
     }
   }
   if (!converged) status = PGPU_ERR_NOT_CONVERGED;
@@ -1129,6 +1815,7 @@ int diffusion_solve_linear(pgpu_problem* p, double lam, const double* b, double*
   PGPU_CUDA(cudaMemcpyAsync(d.y.ptr, x, (size_t)N * 8, cudaMemcpyHostToDevice, s));
   launch(p, k_set_scalar, 1, 1, s, d.lam.as<double>(), lam);
   refold(p);
+  if ((st = mg_update(p, lam))) return st;
   DiffOp<double> A = op64(d, true);
   const double tol = std::fmax(opt->tol_flux, 1e-14);
   OuterScal os;
@@ -1273,6 +1960,7 @@ int pgpu_diffusion_create(int device, const pgpu_diffusion_operator* op, pgpu_pr
   if (st == PGPU_OK && cudaMemsetAsync(d.lam.ptr, 0, 2 * sizeof(double), p->stream) != cudaSuccess)
     st = fail(PGPU_ERR_CUDA, "clearing the shift");
   if (st == PGPU_OK && cudaMemsetAsync(d.ticket.ptr, 0, 64, p->stream) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "memset");
+  if (st == PGPU_OK) st = mg_setup(p, op);
   if (st == PGPU_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(PGPU_ERR_CUDA, "upload");
   if (st != PGPU_OK) {
     std::string msg = pgpu_last_error();
