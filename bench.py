@@ -308,12 +308,10 @@ def run_ours(args, rank, world, local):
             raise RuntimeError(f"solve failed: {pg.last_error()}")
         return {k: getattr(stats, k) for k, _ in pg.pgpu_stats._fields_}
 
-    # Diffusion: with per-launch events an inner solve runs one BiCGStab iteration per host
-    # round trip (no graph chunks), which would slow the timed solves of small problems, so
-    # the timed region runs the normal path and the SpMV timing comes from one more solve
-    # with events right after it.  SN: the events bracket the sweep graph launches and
-    # change nothing, so they run inside the timed region.
-    timed_profile = 0 if w["kind"] in ("diffusion2d", "diffusion7g") else 1
+    # With per-launch events a solve drives its inner iterations from the host one at a time
+    # (no CUDA graph chunks for BiCGStab, no graph of conditional Arnoldi steps for GMRES),
+    # so the timed region runs the normal path and the dominant kernel's timing comes from
+    # one more solve with events right after it (same kernels, same launch shapes).
     for _ in range(args.warmup):
         solve(0)
     results = []
@@ -325,14 +323,14 @@ def run_ours(args, rank, world, local):
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
-            results.append(solve(timed_profile))
+            results.append(solve(0))
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     barrier()
     dev_time = reduce_over_ranks(sum(r["seconds"] for r in results), dist, f"cuda:{dev}", "max")
     keff = results[-1]["keff"]
-    kres = results if timed_profile else [solve(1)]
-    kres_time = dev_time if timed_profile else sum(r["seconds"] for r in kres)
+    kres = [solve(1)]
+    kres_time = sum(r["seconds"] for r in kres)
     kern_s = sum(r["kernel_seconds"] for r in kres)
     kern_b = sum(r["kernel_bytes"] for r in kres)
     kern_n = sum(r["kernel_launches"] for r in kres)
@@ -412,14 +410,15 @@ def run_ours(args, rank, world, local):
                 frac=(achieved / peaks["hbm_gbs"]) if achieved else None, peak_source=peaks["source"],
                 traffic=None, launches=kern_n,
                 kernel_share_of_solve=kern_s / kres_time if kres_time > 0 else None,
-                timing="CUDA events around every launch of the kernel in the timed solves" if timed_profile
-                else "CUDA events around every launch of the kernel in one solve right after the timed ones")
+                timing="CUDA events around every launch of the kernel in one solve right after the timed ones")
     if w["kind"] == "sn" and kern_s > 0:
         # the transport sweep is bound by FP64 issue on GB300 (FP64 = 1/64 of FP32): per
         # (cell, group, direction) update one multiply and three FMAs (7 flops); the
         # mixed-precision workload's correction sweeps are FP32 and only its residual
         # sweeps count here.  Peak: nominal GB300 FP64, 1.25 TFLOP/s (no measured figure).
-        sw = kern_n / 2.0 if kname == "k_sweep_flow" else float(sweeps * args.steps)
+        sw = kern_n / 2.0 if kname == "k_sweep_flow" else float(sum(r["sweeps"] for r in kres))
+        # the sweep's own rate: (cell, group, direction) updates per second of sweep time
+        roof["updates_per_s"] = n_psi * sw / kern_s
         if w["precision"] == "fp64":
             ach = 7.0 * n_psi * sw / kern_s / 1e12
             roof["fp64"] = dict(flops_per_update=7, achieved_tflops=ach, nominal_peak_tflops=1.25,

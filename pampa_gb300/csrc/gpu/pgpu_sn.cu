@@ -130,10 +130,22 @@ struct SNData {
   DevBuf d_tile_cls, d_tile_ncls, d_cell_lcls;  // per-tile class lists (FlowGeom)
   cudaGraphExec_t sweep_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][iso]
   double* hpin = nullptr;  // pinned host mirror of hbuf (GMRES scalars)
+  // GMRES cycles as graphs of conditional Arnoldi steps (see gmres), per precision [fp32]
+  cudaGraphExec_t arn_graph[2] = {nullptr, nullptr};
+  int arn_step_launches[2] = {0, 0};  // kernels of one captured step
+  bool capturing = false;             // sweeps enqueue their kernels into the graph being captured
+  DevBuf arn;                         // ArnoldiState
+  DevBuf lam_dev;                     // the running solve's Wielandt shift (device scalar)
+  void drop_arnoldi_graphs() {
+    for (auto& g : arn_graph)
+      if (g) cudaGraphExecDestroy(g);
+    arn_graph[0] = arn_graph[1] = nullptr;
+  }
   ~SNData() {
     for (auto& row : sweep_graph)
       for (auto& g : row)
         if (g) cudaGraphExecDestroy(g);
+    drop_arnoldi_graphs();
     if (hpin) cudaFreeHost(hpin);
   }
   bool use_tab = false;
@@ -834,8 +846,9 @@ __global__ void k_moment(int rows, int M, const T* __restrict__ w, const T* __re
 // (+ b[i,g] when given).  lam_s is the Wielandt shift (0 for plain power iteration).
 template <typename T>
 __global__ void k_scatter_source(SNOp<T> A, const T* __restrict__ phi0, const T* __restrict__ b, T* q,
-                                 double lam_s) {
+                                 double lam_val, const double* __restrict__ lam_dev) {
   const int G = A.G;
+  const double lam_s = lam_dev ? *lam_dev : lam_val;  // the solve's current shift, or a given factor
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n * G; r += gridDim.x * blockDim.x) {
     const int i = r / G, g = r - i * G;
     const int mt = A.mat[i];
@@ -965,6 +978,78 @@ __global__ void k_gs_gate(const double* ww, const double* hn, double* gate, doub
   *gate = need ? 1.0 : 0.0;
   if (!need)
     for (int k = 0; k < nh; k++) h2[k] = 0.0;
+}
+
+// Device-side state of one GMRES cycle run as a graph of conditional Arnoldi steps: the
+// Hessenberg columns (rotated), the Givens rotations, the rotated right-hand side g and
+// the cycle's progress.
+struct ArnoldiState {
+  double H[(kGsMax + 1) * kGsMax];  // column j at H + j (m + 1)
+  double cs[kGsMax], sn[kGsMax], g[kGsMax + 1];
+  double tol, res;
+  int j;          // columns kept in this cycle
+  int total;      // Arnoldi steps of the GMRES call so far
+  int max_it;
+  int stop;       // the cycle ended (converged, breakdown, the step cap or a non-finite value)
+  int nonfinite;
+  int reorth;     // steps of this cycle that ran the second Gram-Schmidt pass
+};
+
+__global__ void k_arnoldi_init(ArnoldiState* S, double beta, double tol, int total, int max_it) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int k = 0; k <= kGsMax; k++) S->g[k] = 0.0;
+  S->g[0] = beta;
+  S->tol = tol;
+  S->res = beta;
+  S->j = 0;
+  S->total = total;
+  S->max_it = max_it;
+  S->stop = 0;
+  S->nonfinite = 0;
+  S->reorth = 0;
+}
+
+// Arnoldi step j of an m-step cycle, after its Gram-Schmidt products: the new Hessenberg
+// column (first pass h1, plus the second pass h2 when the gate ran it), the rotations of
+// the earlier columns, a new rotation and the residual |g[j+1]|; then the condition of
+// step j+1's graph node (when there is one): 1 while the cycle goes on, 0 once it stops.
+// The later steps' conditions start each launch at 0, so they are all skipped.
+__global__ void k_arnoldi_step(ArnoldiState* S, int j, int m, const double* __restrict__ h1,
+                               const double* __restrict__ h2, const double* __restrict__ hn,
+                               const double* __restrict__ gate, cudaGraphConditionalHandle next, int has_next) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double* col = S->H + (size_t)j * (m + 1);
+  const bool second = *gate != 0.0;
+  for (int k = 0; k <= j; k++) col[k] = h1[k] + (second ? h2[k] : 0.0);
+  if (second) S->reorth++;
+  const double hnext = *hn;
+  S->total++;
+  col[j + 1] = hnext;
+  for (int k = 0; k < j; k++) {
+    const double a = S->cs[k] * col[k] + S->sn[k] * col[k + 1];
+    const double b = -S->sn[k] * col[k] + S->cs[k] * col[k + 1];
+    col[k] = a;
+    col[k + 1] = b;
+  }
+  const double rr = hypot(col[j], col[j + 1]);
+  bool stop = false;
+  if (rr == 0.0 || !(rr == rr)) {
+    stop = true;  // column j is not kept
+    S->nonfinite = !(rr == rr);
+  } else {
+    S->cs[j] = col[j] / rr;
+    S->sn[j] = col[j + 1] / rr;
+    col[j] = rr;
+    col[j + 1] = 0.0;
+    S->g[j + 1] = -S->sn[j] * S->g[j];
+    S->g[j] = S->cs[j] * S->g[j];
+    S->res = fabs(S->g[j + 1]);
+    S->j = j + 1;
+    if (S->res <= S->tol || hnext == 0.0) stop = true;
+  }
+  if (S->total >= S->max_it || j + 1 >= m) stop = true;
+  S->stop = stop ? 1 : 0;
+  if (has_next) cudaGraphSetConditional(next, stop ? 0u : 1u);
 }
 
 // out[k] = <V_k, w> for k < nv; reduction slots of chunk y at partials + y*kGsChunk*kMaxBlocks.
@@ -1512,29 +1597,37 @@ void flow_launch(SNData& d, cudaStream_t s, const SNOp<T>& A, const SweepFaces<T
     flow_launch<T, kClass, 4, 4, 4>(d, s, A, W, K, P, iso);
 }
 
+// Coefficient tables, the pointer block and the persistent grid of precision T's sweeps
+// (allocated on first use, so before any capture of a sweep into a graph).
+template <typename T>
+int sweep_prepare(pgpu_problem* p, const SNOp<T>& A) {
+  SNData& d = *p->sn;
+  const bool cls = d.kba && d.ncls > 0;
+  const bool level_cls = !d.kba && d.ncls > 0;  // level sets with per-class coefficients
+  int rst = cls ? ensure_coef<T>(p, A) : (level_cls ? ensure_level_coef<T>(p, A) : ensure_rden<T>(p, A));
+  if (rst) return rst;
+  if (!d.sweep_ptrs.ptr && (rst = dev_alloc(d.sweep_ptrs, sizeof(SweepPtrs), &p->bytes, p->stream))) return rst;
+  if (d.kba && !d.flow_grid[sizeof(T) == 8 ? 0 : 1] && (rst = cls ? flow_prepare<T, true>(d) : flow_prepare<T, false>(d)))
+    return rst;
+  return PGPU_OK;
+}
+
 template <typename T>
 int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd, T* psi, T* mom = nullptr) {
   SNData& d = *p->sn;
   const Schedule& S = d.sched;
   const bool cls = d.kba && d.ncls > 0;
   const bool level_cls = !d.kba && d.ncls > 0;  // level sets with per-class coefficients
-  int rst = cls ? ensure_coef<T>(p, A) : (level_cls ? ensure_level_coef<T>(p, A) : ensure_rden<T>(p, A));
+  int rst = sweep_prepare<T>(p, A);
   if (rst) return rst;
   const SweepFaces<T> W = make_faces<T>(d);
-  if (!d.sweep_ptrs.ptr && (rst = dev_alloc(d.sweep_ptrs, sizeof(SweepPtrs), &p->bytes, p->stream))) return rst;
   SweepPtrs* P = d.sweep_ptrs.as<SweepPtrs>();
   // the sweep's launches are captured once per (precision, source kind) and replayed; the
   // buffers of this sweep go through the device-side pointer block
   launch(p, k_set_sweep_ptrs, 1, 1, p->stream, P, (const void*)src, (const void*)bnd, (void*)psi,
          (void*)(d.kba ? mom : nullptr));
-  cudaGraphExec_t& gx = d.sweep_graph[sizeof(T) == 8 ? 0 : 1][iso ? 1 : 0];
   const int nlaunch = d.kba ? 2 : S.nlev;
-  if (!gx) {
-    if (d.kba && !d.flow_grid[sizeof(T) == 8 ? 0 : 1] &&
-        (rst = cls ? flow_prepare<T, true>(d) : flow_prepare<T, false>(d)))
-      return rst;
-    cudaGraph_t graph;
-    PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+  auto enqueue = [&](cudaStream_t st) {
     if (d.kba) {
       const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, d.kba_npat, d.kba_nd, d.kba_ntasks, d.kba_gchunk, d.kba_nchunk,
                        d.d_tiles.as<int>(), d.d_pat_sign.as<int>(), d.d_fpat_dirs_ptr.as<int>(), d.d_fpat_dirs.as<int>(),
@@ -1543,25 +1636,39 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
                        d.d_tile_ncls.as<int>(), d.d_cell_lcls.as<unsigned char>(), d.flow_sync.as<FlowSync>(),
                        d.flow_flags.as<unsigned int>(), d.d_task_order.as<int>(), d.flow_sleep,
                        d.trace_buf.as<unsigned long long>()};
-      k_flow_begin<<<1, 1, 0, p->stream>>>(K.sync);
+      k_flow_begin<<<1, 1, 0, st>>>(K.sync);
       if (cls)
-        flow_launch<T, true>(d, p->stream, A, W, K, P, iso);
+        flow_launch<T, true>(d, st, A, W, K, P, iso);
       else
-        flow_launch<T, false>(d, p->stream, A, W, K, P, iso);
+        flow_launch<T, false>(d, st, A, W, K, P, iso);
     } else {
       for (int L = 0; L < S.nlev; L++) {
         dim3 g(S.grid_x[L], S.npat);
         if (level_cls)
-          k_sweep_level_cls<T><<<g, kThreads, 0, p->stream>>>(
+          k_sweep_level_cls<T><<<g, kThreads, 0, st>>>(
               A, d.d_ccls.as<unsigned short>(), (const T*)(sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr), L,
               d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(), d.d_pat_nlev.as<int>(),
               d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
         else
-          k_sweep_level<T><<<g, kThreads, 0, p->stream>>>(
+          k_sweep_level<T><<<g, kThreads, 0, st>>>(
               A, W, L, d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_pat_lev_ptr.as<int>(),
               d.d_pat_nlev.as<int>(), d.d_lev_ptr.as<int>(), d.d_order.as<int>(), P, iso);
       }
     }
+  };
+  if (d.capturing) {
+    // inside a graph being captured (the GMRES cycle): the kernels themselves, no nested
+    // graph launch and no timing; the caller counts the sweeps that run
+    enqueue(p->stream);
+    p->launches += nlaunch;
+    PGPU_CUDA(cudaGetLastError());
+    return PGPU_OK;
+  }
+  cudaGraphExec_t& gx = d.sweep_graph[sizeof(T) == 8 ? 0 : 1][iso ? 1 : 0];
+  if (!gx) {
+    cudaGraph_t graph;
+    PGPU_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue(p->stream);
     PGPU_CUDA(cudaStreamEndCapture(p->stream, &graph));
     cudaError_t e = cudaGraphInstantiate(&gx, graph, 0);
     cudaGraphDestroy(graph);
@@ -1606,15 +1713,16 @@ T* psi_work(SNData& d) {
 }
 
 
-// y = T(x; b): sweep driven by the scattering (+ lam_s-shifted fission) source of x's phi0
-// part plus b, and the reflective inflow held in x's boundary part; returns [phi0' | inflow'].
+// y = T(x; b): sweep driven by the scattering (+ lam_s-shifted fission, lam_s the solve's
+// shift held on the device) source of x's phi0 part plus b, and the reflective inflow held
+// in x's boundary part; returns [phi0' | inflow'].
 template <typename T>
-int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y, double lam_s) {
+int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y) {
   SNData& d = *p->sn;
   const int nG = d.n * d.G;
   T* q = d.scat.as<T>();
   T* psi = psi_work<T>(d);
-  launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q, lam_s);
+  launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q, 0.0, (const double*)d.lam_dev.as<double>());
   int st;
   if (d.kba) {
     // the dataflow sweep writes per-pattern moments; they are summed in pattern order
@@ -1650,7 +1758,12 @@ int apply_R(pgpu_problem* p, const SNOp<T>& A, const T* x, T* y, T* tmp_phi0) {
 int ensure_krylov(pgpu_problem* p, size_t len, int restart, int es) {
   SNData& d = *p->sn;
   if (d.basis_len == len && d.restart == restart && d.krylov_prec == es) return PGPU_OK;
+  d.drop_arnoldi_graphs();  // they hold the buffers replaced here
   int st;
+  if (!d.lam_dev.ptr) {
+    if ((st = dev_alloc(d.lam_dev, sizeof(double), &p->bytes, p->stream))) return st;
+    PGPU_CUDA(cudaMemsetAsync(d.lam_dev.ptr, 0, sizeof(double), p->stream));
+  }
   if ((st = dev_alloc(d.basis, (size_t)(restart + 1) * len * es, &p->bytes, p->stream))) return st;
   if ((st = dev_alloc(d.wvec, len * es, &p->bytes, p->stream))) return st;
   if ((st = dev_alloc(d.xvec, len * es, &p->bytes, p->stream))) return st;
@@ -1675,8 +1788,15 @@ int ensure_krylov(pgpu_problem* p, size_t len, int restart, int es) {
 
 // GMRES(m) with classical Gram-Schmidt and one re-orthogonalisation (CGS2) for the
 // correction equation A d = r, d starting at zero.  applyA(v, w) computes w = A v.
-// Stops when ||r - A d|| <= max(rtol ||r||, atol) or after max_it Arnoldi steps.  The
-// small Hessenberg least-squares problem is solved on the host with Givens rotations.
+// Stops when ||r - A d|| <= max(rtol ||r||, atol) or after max_it Arnoldi steps.
+//
+// A cycle's Arnoldi steps run from a CUDA graph of m conditional nodes, one per step,
+// captured once per precision: each body holds the step's sweep, its Gram-Schmidt
+// products and k_arnoldi_step, which applies the Givens rotations on the device and
+// sets the graph's condition to 0 once the cycle stops, so the remaining steps are
+// skipped.  The host reads the cycle's state once per cycle (instead of once per step)
+// and solves the small triangular system.  With profiling or a traced sweep the steps are
+// driven from the host one at a time instead (same arithmetic).
 template <typename T, typename App>
 int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, double rtol, double atol,
           int max_it, int* iters, double* res_out) {
@@ -1689,6 +1809,7 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
   double* h2 = h1 + (m + 4);
   double* hn = h2 + (m + 4);
   double* yv = hn + (m + 4);
+  double* gate = hn + 1;
   const int gx = grid_for(len);
   std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
   double* hp = d.hpin;  // pinned mirror of hbuf
@@ -1697,6 +1818,95 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
   bool first = true;
   ReduceSlots<1> nslot{d.partials.as<double>() + (size_t)(m + 2) * kMaxBlocks, d.ticket.as<unsigned int>() + (m + 2)};
   if (m + 2 > kGsMax) return fail(PGPU_ERR_INVALID, "GMRES restart length above the Gram-Schmidt kernels' limit");
+  const int prec = sizeof(T) == 8 ? 0 : 1;
+  const bool graphs = !p->profile && d.trace_sweep < 0;
+  // Gram-Schmidt of step j: w_{j+1} (in V) against V_0..V_j, then normalised
+  auto gs_step = [&](int j) {
+    T* wj = V + (size_t)(j + 1) * len;
+    // classical Gram-Schmidt with re-orthogonalisation when needed ("twice is enough"):
+    // h1 = V^T w (and <w, w>), w -= V h1 with its norm; a second pass only when the
+    // norm fell below kReorth of the original (cancellation)
+    const dim3 gd1(std::min(gx, kMaxGrid / 2), (j + 2 + kGsChunk - 1) / kGsChunk);
+    const dim3 gd(std::min(gx, kMaxGrid / 2), (j + 1 + kGsChunk - 1) / kGsChunk);
+    double* part = d.partials.as<double>();
+    unsigned int* tick = d.ticket.as<unsigned int>();
+    launch(p, k_gs_dot<T>, gd1, kThreads, s, len, (const T*)V, len, j + 2, (const T*)wj, h1, part, tick,
+           (const double*)nullptr);
+    launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, wj, hn, nslot,
+           (const double*)nullptr);
+    // the second pass, decided and (if needed) run on the device
+    launch(p, k_gs_gate, 1, 1, s, (const double*)(h1 + j + 1), (const double*)hn, gate, h2, j + 1);
+    launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)wj, h2, part, tick,
+           (const double*)gate);
+    launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, wj, hn, nslot,
+           (const double*)gate);
+    launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)wj, (const double*)hn, 1, wj);
+  };
+  // the cycle graph, captured on first use
+  if (graphs && !d.arn_graph[prec]) {
+    if (!d.arn.ptr && (st = dev_alloc(d.arn, sizeof(ArnoldiState), &p->bytes, s))) return st;
+    ArnoldiState* AS = d.arn.as<ArnoldiState>();
+    cudaGraph_t graph = nullptr;
+    // one condition per step node (a condition belongs to one node): step 0's starts each
+    // launch at 1, the others at 0 until the step before sets them
+    std::vector<cudaGraphConditionalHandle> cond(m, 0);
+    const long long counted = p->launches;
+    int cst = PGPU_OK;
+    auto ck = [&](cudaError_t e, const char* what) {
+      if (cst == PGPU_OK && e != cudaSuccess)
+        cst = fail(PGPU_ERR_CUDA, std::string("GMRES cycle graph, ") + what + ": " + cudaGetErrorString(e));
+      return cst == PGPU_OK;
+    };
+    if (ck(cudaGraphCreate(&graph, 0), "create"))
+      for (int j = 0; j < m; j++)
+        if (!ck(cudaGraphConditionalHandleCreate(&cond[j], graph, j == 0 ? 1u : 0u, cudaGraphCondAssignDefault),
+                "condition"))
+          break;
+    cudaGraphNode_t prev = nullptr;
+    for (int j = 0; j < m && cst == PGPU_OK; j++) {
+      cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+      cp.conditional.handle = cond[j];
+      cp.conditional.type = cudaGraphCondTypeIf;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node = nullptr;
+      if (!ck(cudaGraphAddNode(&node, graph, prev ? &prev : nullptr, nullptr, prev ? 1 : 0, &cp), "step node")) break;
+      if (!ck(cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal),
+              "capture"))
+        break;
+      d.capturing = true;
+      const int ae = applyA(V + (size_t)j * len, V + (size_t)(j + 1) * len);
+      gs_step(j);
+      k_arnoldi_step<<<1, 1, 0, s>>>(AS, j, m, h1, h2, hn, gate, j + 1 < m ? cond[j + 1] : 0ull, j + 1 < m ? 1 : 0);
+      d.capturing = false;
+      cudaGraph_t body = nullptr;
+      const cudaError_t ee = cudaStreamEndCapture(s, &body);
+      if (ae != PGPU_OK && cst == PGPU_OK) cst = ae;
+      ck(ee, "end capture");
+      ck(cudaGetLastError(), "step launches");
+      prev = node;
+    }
+    if (cst == PGPU_OK) {
+      d.arn_step_launches[prec] = (int)((p->launches - counted) / m) + 1;  // + k_arnoldi_step
+      ck(cudaGraphInstantiate(&d.arn_graph[prec], graph, 0), "instantiate");
+    }
+    p->launches = counted;
+    if (graph) cudaGraphDestroy(graph);
+    if (cst != PGPU_OK) {
+      d.arn_graph[prec] = nullptr;
+      return cst;
+    }
+  }
+  // a sweep that returned early after a bounded wait ran out leaves unfinished tiles;
+  // report that cause rather than the NaN it may lead to
+  auto nan_cause = [&]() -> int {
+    if (d.kba) {
+      unsigned int err = 0;
+      if (int e = read_small(&err, &d.flow_sync.as<FlowSync>()->error, sizeof(err), s)) return e;
+      if (err) return fail(PGPU_ERR_TIMEOUT, "sweep: a wait for an upwind tile ran out (kernel returned early)");
+    }
+    return fail(PGPU_ERR_NAN, "NaN in the transport correction solve");
+  };
   PGPU_CUDA(cudaMemsetAsync(dvec, 0, len * sizeof(T), s));
   while (true) {
     if (first) {
@@ -1708,16 +1918,7 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
     launch(p, k_norm2<T>, gx, kThreads, s, len, (const T*)V, hn, nslot);
     double beta;
     if ((st = read_small(&beta, hn, 8, s))) return st;
-    if (!(beta == beta)) {
-      // a sweep that returned early after a bounded wait ran out leaves unfinished tiles;
-      // report that cause rather than the NaN it may lead to
-      if (d.kba) {
-        unsigned int err = 0;
-        if ((st = read_small(&err, &d.flow_sync.as<FlowSync>()->error, sizeof(err), s))) return st;
-        if (err) return fail(PGPU_ERR_TIMEOUT, "sweep: a wait for an upwind tile ran out (kernel returned early)");
-      }
-      return fail(PGPU_ERR_NAN, "NaN in the transport correction solve");
-    }
+    if (!(beta == beta)) return nan_cause();
     if (first) {
       tol = std::fmax(rtol * beta, atol);
       first = false;
@@ -1725,63 +1926,64 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
     res = beta;
     if (beta <= tol || total >= max_it) break;
     launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)V, (const double*)hn, 1, V);
-    std::fill(g.begin(), g.end(), 0.0);
-    g[0] = beta;
     int j = 0;
-    for (; j < m && total < max_it; j++) {
-      T* vj = V + (size_t)j * len;
-      T* wj = V + (size_t)(j + 1) * len;  // the new vector is built in place
-      if ((st = applyA(vj, wj))) return st;
-      // classical Gram-Schmidt with re-orthogonalisation when needed ("twice is enough"):
-      // h1 = V^T w (and <w, w>), w -= V h1 with its norm; a second pass only when the
-      // norm fell below kReorth of the original (cancellation).
-      const dim3 gd1(std::min(gx, kMaxGrid / 2), (j + 2 + kGsChunk - 1) / kGsChunk);
-      const dim3 gd(std::min(gx, kMaxGrid / 2), (j + 1 + kGsChunk - 1) / kGsChunk);
-      double* part = d.partials.as<double>();
-      unsigned int* tick = d.ticket.as<unsigned int>();
-      double* gate = hn + 1;
-      launch(p, k_gs_dot<T>, gd1, kThreads, s, len, (const T*)V, len, j + 2, (const T*)wj, h1, part, tick,
-             (const double*)nullptr);
-      launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, wj, hn, nslot,
-             (const double*)nullptr);
-      // the second pass, decided and (if needed) run on the device
-      launch(p, k_gs_gate, 1, 1, s, (const double*)(h1 + j + 1), (const double*)hn, gate, h2, j + 1);
-      launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)wj, h2, part, tick,
-             (const double*)gate);
-      launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, wj, hn, nslot,
-             (const double*)gate);
-      launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)wj, (const double*)hn, 1, wj);
-      PGPU_CUDA(cudaGetLastError());
-      // h1, h2, ||w|| and the gate (adjacent in hbuf): one copy into pinned host memory
-      PGPU_CUDA(cudaMemcpyAsync(hp, h1, (size_t)(2 * (m + 4) + 2) * 8, cudaMemcpyDeviceToHost, s));
-      PGPU_CUDA(cudaStreamSynchronize(s));
-      double hnext = hp[2 * (m + 4)];
-      double* col = &H[(size_t)j * (m + 1)];
-      for (int k = 0; k <= j; k++) col[k] = hp[k];
-      if (hp[2 * (m + 4) + 1] != 0.0) {
-        for (int k = 0; k <= j; k++) col[k] += hp[(m + 4) + k];
-        d.reorth++;
-      }
-      total++;
-      col[j + 1] = hnext;
-      for (int k = 0; k < j; k++) {
-        double a = cs[k] * col[k] + sn[k] * col[k + 1];
-        double b = -sn[k] * col[k] + cs[k] * col[k + 1];
-        col[k] = a;
-        col[k + 1] = b;
-      }
-      double rr = std::hypot(col[j], col[j + 1]);
-      if (rr == 0.0 || !(rr == rr)) break;
-      cs[j] = col[j] / rr;
-      sn[j] = col[j + 1] / rr;
-      col[j] = rr;
-      col[j + 1] = 0.0;
-      g[j + 1] = -sn[j] * g[j];
-      g[j] = cs[j] * g[j];
-      res = std::fabs(g[j + 1]);
-      if (res <= tol || hnext == 0.0) {
-        j++;
-        break;
+    if (graphs) {
+      ArnoldiState* AS = d.arn.as<ArnoldiState>();
+      launch(p, k_arnoldi_init, 1, 1, s, AS, beta, tol, total, max_it);
+      PGPU_CUDA(cudaGraphLaunch(d.arn_graph[prec], s));
+      ArnoldiState hs;
+      if ((st = read_small(&hs, AS, sizeof(hs), s))) return st;
+      const int steps = hs.total - total;
+      d.sweeps += steps;  // one sweep per step
+      p->launches += (long long)steps * d.arn_step_launches[prec];
+      d.reorth += hs.reorth;
+      total = hs.total;
+      if (hs.nonfinite) return nan_cause();
+      j = hs.j;
+      res = hs.res;
+      for (int c = 0; c < j; c++)
+        for (int k = 0; k <= c; k++) H[(size_t)c * (m + 1) + k] = hs.H[(size_t)c * (m + 1) + k];
+      for (int k = 0; k <= j; k++) g[k] = hs.g[k];
+    } else {
+      std::fill(g.begin(), g.end(), 0.0);
+      g[0] = beta;
+      for (; j < m && total < max_it; j++) {
+        T* vj = V + (size_t)j * len;
+        T* wj = V + (size_t)(j + 1) * len;  // the new vector is built in place
+        if ((st = applyA(vj, wj))) return st;
+        gs_step(j);
+        PGPU_CUDA(cudaGetLastError());
+        // h1, h2, ||w|| and the gate (adjacent in hbuf): one copy into pinned host memory
+        PGPU_CUDA(cudaMemcpyAsync(hp, h1, (size_t)(2 * (m + 4) + 2) * 8, cudaMemcpyDeviceToHost, s));
+        PGPU_CUDA(cudaStreamSynchronize(s));
+        double hnext = hp[2 * (m + 4)];
+        double* col = &H[(size_t)j * (m + 1)];
+        for (int k = 0; k <= j; k++) col[k] = hp[k];
+        if (hp[2 * (m + 4) + 1] != 0.0) {
+          for (int k = 0; k <= j; k++) col[k] += hp[(m + 4) + k];
+          d.reorth++;
+        }
+        total++;
+        col[j + 1] = hnext;
+        for (int k = 0; k < j; k++) {
+          double a = cs[k] * col[k] + sn[k] * col[k + 1];
+          double b = -sn[k] * col[k] + cs[k] * col[k + 1];
+          col[k] = a;
+          col[k + 1] = b;
+        }
+        double rr = std::hypot(col[j], col[j + 1]);
+        if (rr == 0.0 || !(rr == rr)) break;
+        cs[j] = col[j] / rr;
+        sn[j] = col[j + 1] / rr;
+        col[j] = rr;
+        col[j + 1] = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        res = std::fabs(g[j + 1]);
+        if (res <= tol || hnext == 0.0) {
+          j++;
+          break;
+        }
       }
     }
     if (j == 0) break;
@@ -1867,6 +2069,11 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   }
   SNOp<T> A = make_op<T>(d);
   SNOp<double> A64 = make_op<double>(d);
+  // everything the sweeps allocate on first use, before a GMRES cycle is captured
+  if ((st = sweep_prepare<double>(p, A64)) || (st = sweep_prepare<T>(p, A))) return st;
+  if (phi_space && d.kba && !d.mom.ptr &&
+      (st = dev_alloc(d.mom, (size_t)d.kba_npat * nG * sizeof(double), &p->bytes, p->stream)))
+    return st;
   SNOuter* dos = d.oscal.as<SNOuter>();
   double* x64 = d.x64.as<double>();
   double* r64 = d.r64.as<double>();
@@ -1913,15 +2120,16 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   PGPU_CUDA(cudaGetLastError());
 
   // Wielandt shift lam_s = 1/(k (1 + shift)), switched on once k has settled (scalar-flux
-  // space only); 0 means plain power iteration.
+  // space only); 0 means plain power iteration.  The sweeps' sources read it on the device.
   double lam_s = 0.0;
+  launch(p, k_put<double>, 1, 1, s, d.lam_dev.as<double>(), 0.0);
 
   // correction operators in precision T
   T* zT = psi_work<T>(d);
   auto applyA = [&](const T* v, T* w) -> int {
     int e;
     if (phi_space) {
-      if ((e = phi_space_T<T>(p, A, v, nullptr, w, lam_s))) return e;  // w = T (S + lam_s F) v
+      if ((e = phi_space_T<T>(p, A, v, nullptr, w))) return e;  // w = T (S + lam_s F) v
       launch(p, k_sub<T>, gl, kThreads, s, len, v, (const T*)w, w);  // w = v - T_s v
       return PGPU_OK;
     }
@@ -1939,7 +2147,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
     // FP64 residual of the inner system for the current fission source
     double scale = 0.0;
     if (phi_space) {
-      if ((st = phi_space_T<double>(p, A64, x64, bsrc, r64, lam_s))) return st;  // T((S + lam_s F) x + b)
+      if ((st = phi_space_T<double>(p, A64, x64, bsrc, r64))) return st;  // T((S + lam_s F) x + b)
       launch(p, k_sub<double>, gl, kThreads, s, len, (const double*)r64, (const double*)x64, r64);
       if ((st = norm_of<double>(p, len, x64, &scale))) return st;
     } else {
@@ -1995,8 +2203,10 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
       break;
     }
     const double sh = opt->shift < 0.0 ? kShiftDefault : opt->shift;
-    if (phi_space && outer >= kShiftAfter && dk < kShiftWhenDk && sh > 0.0)
+    if (phi_space && outer >= kShiftAfter && dk < kShiftWhenDk && sh > 0.0) {
       lam_s = 1.0 / std::fmax(os.k * (1.0 + sh), os.k + kShiftMargin * dk);  // above the fundamental k
+      launch(p, k_put<double>, 1, 1, s, d.lam_dev.as<double>(), lam_s);
+    }
   }
 
   // psi in FP64 from the converged state (one more sweep in scalar-flux space)
@@ -2004,7 +2214,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   if (phi_space) {
     // source of the eigen-equation: (S + F / k) phi0
     launch(p, k_scatter_source<double>, gG, kThreads, s, A64, (const double*)x64, (const double*)nullptr, ph64,
-           1.0 / k_prev);
+           1.0 / k_prev, (const double*)nullptr);
     if ((st = sweep<double>(p, A64, ph64, 1, d.nrefl ? x64 + nG : nullptr, psi))) return st;
   } else {
     PGPU_CUDA(cudaMemcpyAsync(psi, x64, (size_t)N * 8, cudaMemcpyDeviceToDevice, s));
