@@ -72,6 +72,7 @@ struct MgLevel {
   DevBuf v64[3], v32[3];  // restricted residual, pre-smoothed z, cycle output
 };
 constexpr int kMgMaxLevels = 12;
+constexpr int kBicgChain = 32;  // BiCGStab iterations per graph launch (conditional nodes)
 
 struct DiffusionData {
   int n = 0, G = 0, F = 0, nm = 0;
@@ -95,12 +96,11 @@ struct DiffusionData {
   DevBuf mg_inv64, mg_inv32;  // dense inverse of the coarsest operator
   std::vector<double> mg_hbs, mg_hbf, mg_hoff;  // the coarsest operator on the host
   std::vector<int> mg_hnbr;
-  // BiCGStab iterations captured in CUDA graphs, [fp32][chunk 4, 8, 16]
-  cudaGraphExec_t bicg_graph[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  // chains of conditional BiCGStab iterations captured in CUDA graphs, [fp32]
+  cudaGraphExec_t bicg_graph[2] = {nullptr, nullptr};
   ~DiffusionData() {
-    for (auto& row : bicg_graph)
-      for (auto& g : row)
-        if (g) cudaGraphExecDestroy(g);
+    for (auto& g : bicg_graph)
+      if (g) cudaGraphExecDestroy(g);
   }
 };
 
@@ -280,11 +280,13 @@ __global__ void k_bicg_t(DiffOp<T> A, const T* __restrict__ shat, T* t, const T*
   }
 }
 
-// x += alpha phat + omega shat; r = s - omega t; rho = (rhat, r); rr = (r, r).
+// x += alpha phat + omega shat; r = s - omega t; rho = (rhat, r); rr = (r, r).  Inside a
+// graph of conditional iterations (has_next), the last block also sets the condition of
+// the next iteration's node: 1 while the solve goes on.
 template <typename T>
 __global__ void k_bicg_x(int N, T* x, T* r, const T* __restrict__ phat, const T* __restrict__ shat,
                          const T* __restrict__ s, const T* __restrict__ t, const T* __restrict__ rhat,
-                         BiScal* sc, ReduceSlots<2> slots) {
+                         BiScal* sc, ReduceSlots<2> slots, cudaGraphConditionalHandle next, int has_next) {
   if (sc->converged) return;
   const T ta = (T)sc->alpha, tw = (T)sc->omega;
   T p0 = T(0), p1 = T(0);
@@ -305,6 +307,7 @@ __global__ void k_bicg_x(int N, T* x, T* r, const T* __restrict__ phat, const T*
     bool bad = !(tot[1] == tot[1]);
     if (tot[1] <= sc->tol2 || sc->iters >= sc->max_iters || sc->breakdown || bad) sc->converged = 1;
     if (tot[0] == 0.0) sc->converged = 1;
+    if (has_next) cudaGraphSetConditional(next, sc->converged ? 0u : 1u);
   }
 }
 
@@ -1603,17 +1606,16 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   const int gN = grid_for(N, p->sm_share, kThreads);              // element-wise kernels
   launch(p, k_bicg_init<T>, gN, kThreads, st, N, rin, r, rhat, x, pp, v, sc, slots_of<1>(d), rtol, max_iters);
   PGPU_CUDA(cudaGetLastError());
-  // When profiling, iterations go one per chunk so no timed SpMV launch is a no-op.
-  int chunk = p->profile ? 1 : 4;
   p->prof_name = "k_bicg_v+k_bicg_t";
   // Algorithmic bytes of one SpMV fused with its dot product: per row the diagonal, the
   // F face coefficients, x, y and the dot partner (F + 4 values), plus per cell the F
   // neighbour indices, the material id and the volume.
   const double sv = (double)sizeof(T);
   const double spmv_bytes = (double)N * (d.F + 4) * sv + (double)d.n * (4.0 * d.F + 4.0 + sv);
-  // one BiCGStab iteration: five kernels (every scalar stays on the device; after
-  // convergence the kernels return at once)
-  auto iteration = [&](bool timed) {
+  // one BiCGStab iteration: five kernels, plus two V-cycles of three per level (every
+  // scalar stays on the device; after convergence the kernels return at once)
+  const long long per_iter = 5LL + (mg ? 6LL * d.mg_levels : 0LL);
+  auto iteration = [&](bool timed, cudaGraphConditionalHandle next, int has_next) {
     cudaEvent_t e0;
     launch_bicg_p<T>(gC, cT, st, A, r, pp, v, phat, sc);
     if (mg) mg_cycle<T>(p, A, pp, phat, phf, sc);
@@ -1625,37 +1627,74 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
     if (timed) prof_begin(p, &e0);
     launch_bicg_t<T>(form, gS, rT, st, A, shf, t, s, sc, slots_of<2>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
-    k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phf, shf, s, t, rhat, sc, slots_of<2>(d));
+    k_bicg_x<T><<<gN, kThreads, 0, st>>>(N, x, r, phf, shf, s, t, rhat, sc, slots_of<2>(d), next, has_next);
   };
-  for (int launched = 0; launched < max_iters; launched += chunk) {
-    if (p->profile) {
-      for (int c = 0; c < chunk; c++) iteration(true);
-    } else {
-      // chunks of 4, 8 and 16 iterations are captured once per precision and replayed
-      const int gi = chunk == 4 ? 0 : (chunk == 8 ? 1 : 2);
-      cudaGraphExec_t& gx = d.bicg_graph[sizeof(T) == 8 ? 0 : 1][gi];
-      if (!gx) {
-        cudaGraph_t graph;
-        const long long counted = p->launches;  // captured launches run only when replayed
-        PGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        for (int c = 0; c < chunk; c++) iteration(false);
-        PGPU_CUDA(cudaStreamEndCapture(st, &graph));
-        p->launches = counted;
-        cudaError_t e = cudaGraphInstantiate(&gx, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) {
-          gx = nullptr;
-          return fail(PGPU_ERR_CUDA, std::string("BiCGStab graph instantiation: ") + cudaGetErrorString(e));
-        }
-      }
-      PGPU_CUDA(cudaGraphLaunch(gx, st));
-      if (mg) p->launches += 6LL * d.mg_levels * chunk;  // two V-cycles of 3 launches per level
+  if (p->profile) {
+    // one iteration per host round trip, so no timed SpMV launch is a no-op
+    for (int it = 0; it < max_iters; it++) {
+      iteration(true, 0, 0);
+      p->launches += 5;
+      PGPU_CUDA(cudaGetLastError());
+      if (int rst = read_small(&hs, sc, sizeof(hs), st)) return rst;
+      if (hs.converged) break;
     }
-    p->launches += 5LL * chunk;
-    PGPU_CUDA(cudaGetLastError());
-    if (int rst = read_small(&hs, sc, sizeof(hs), st)) return rst;
-    if (hs.converged) break;
-    if (chunk < 16 && !p->profile) chunk *= 2;
+  } else {
+    // kBicgChain iterations per graph launch, each a conditional node whose condition the
+    // previous iteration sets (the first starts at 1 each launch, the others at 0), so a
+    // converged solve skips the rest; captured once per precision and relaunched until
+    // the solve has converged or reached max_iters.
+    cudaGraphExec_t& gx = d.bicg_graph[sizeof(T) == 8 ? 0 : 1];
+    if (!gx) {
+      cudaGraph_t graph = nullptr;
+      std::vector<cudaGraphConditionalHandle> cond(kBicgChain, 0);
+      const long long counted = p->launches;  // captured launches run only when replayed
+      int cst = PGPU_OK;
+      auto ck = [&](cudaError_t e, const char* what) {
+        if (cst == PGPU_OK && e != cudaSuccess)
+          cst = fail(PGPU_ERR_CUDA, std::string("BiCGStab graph, ") + what + ": " + cudaGetErrorString(e));
+        return cst == PGPU_OK;
+      };
+      if (ck(cudaGraphCreate(&graph, 0), "create"))
+        for (int c = 0; c < kBicgChain; c++)
+          if (!ck(cudaGraphConditionalHandleCreate(&cond[c], graph, c == 0 ? 1u : 0u, cudaGraphCondAssignDefault),
+                  "condition"))
+            break;
+      cudaGraphNode_t prev = nullptr;
+      for (int c = 0; c < kBicgChain && cst == PGPU_OK; c++) {
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = cond[c];
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        if (!ck(cudaGraphAddNode(&node, graph, prev ? &prev : nullptr, nullptr, prev ? 1 : 0, &cp), "iteration node"))
+          break;
+        if (!ck(cudaStreamBeginCaptureToGraph(st, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal),
+                "capture"))
+          break;
+        const bool more = c + 1 < kBicgChain;
+        iteration(false, more ? cond[c + 1] : 0, more ? 1 : 0);
+        cudaGraph_t body = nullptr;
+        ck(cudaStreamEndCapture(st, &body), "end capture");
+        ck(cudaGetLastError(), "iteration launches");
+        prev = node;
+      }
+      if (cst == PGPU_OK) ck(cudaGraphInstantiate(&gx, graph, 0), "instantiate");
+      p->launches = counted;
+      if (graph) cudaGraphDestroy(graph);
+      if (cst != PGPU_OK) {
+        gx = nullptr;
+        return cst;
+      }
+    }
+    int done = 0;
+    for (;;) {
+      PGPU_CUDA(cudaGraphLaunch(gx, st));
+      if (int rst = read_small(&hs, sc, sizeof(hs), st)) return rst;
+      p->launches += per_iter * (hs.iters - done);
+      done = hs.iters;
+      if (hs.converged) break;
+    }
   }
   if (int rst = read_small(&hs, sc, sizeof(hs), st)) return rst;
   p->prof_bytes += p->profile ? 2.0 * hs.iters * spmv_bytes : 0.0;

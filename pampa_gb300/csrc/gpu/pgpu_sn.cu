@@ -119,6 +119,11 @@ struct SNData {
   int kba_t[3] = {4, 4, 4};                // tile shape (4x4x4 or 8x8x4)
   int ncls = 0;                            // cell classes of the coefficient table (0: per-row rden)
   int flow_grid[2] = {0, 0};               // persistent grid per precision [fp32]
+  // column sweep of an extruded mesh (k_sweep_col), when the operator qualifies
+  bool col = false;
+  int col_nxy = 0, col_nz = 0, col_nd = 0, col_ntasks = 0, col_gchunk = 1, col_nchunk = 1;
+  int col_grid[2] = {0, 0};
+  DevBuf d_col_up, d_col_zm, d_col_zp, d_col_sz, d_col_order;
   DevBuf d_tiles, d_pat_sign, d_ccls, d_crep, coef, coef32, flow_sync, flow_flags;
   DevBuf d_task_order;  // hand-out order of the dataflow sweep's tasks (null: canonical)
   DevBuf trace_buf;     // timeline of one traced sweep (PGPU_FLOW_TRACE), [ntasks][5]
@@ -358,6 +363,12 @@ __global__ void k_sweep_level(SNOp<T> A, SweepFaces<T> W, int level, const int* 
 // ---------------------------------------------------------------------------------
 constexpr int kFlowSlots = 10;  // (group, direction) slots of one task at most
 constexpr int kFlowMaxDirs = 16;  // directions of one task at most (an S8 octant holds 10)
+constexpr int kColUp = 4;         // column sweep: lateral inflow faces of a column per pattern, at most
+// column sweep: layers per batch (loads, then updates, then the progress flag)
+template <typename T>
+constexpr int kColBatch() {
+  return sizeof(T) == 8 ? 2 : 4;  // measured: 4 / 2 (FP32 / FP64) at 80 registers beat 8 / 4 at 128 and 2 / 2 at 64
+}
 constexpr int kTileClasses = 16;  // cell classes of a tile whose coefficients are staged
 constexpr unsigned int kFlowSpinLimit = 1u << 23;  // ~0.3-0.5 s of polling
 constexpr unsigned int kFlowStallLimit = 1u << 12;  // polls of the failure-injection wait (~1 ms)
@@ -718,6 +729,192 @@ __global__ void __launch_bounds__(TileShape<TX, TY, TZ>::kThreads, 1024 / TileSh
     if (tr) {
       K.trace[(size_t)t * 5 + 3] = flow_clock();
       K.trace[(size_t)t * 5 + 4] = flow_smid();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Column sweep of an extruded mesh (see col_plan): one warp per task = (column, sweep
+// pattern, chunk of groups); lane = (group of the chunk, direction of the pattern).  The
+// task takes the next index from the sweep's atomic counter and walks its layers in the
+// pattern's z order, B at a time.  Tasks are pipelined layer batch by layer batch: a
+// column publishes how many of its layers are done (with the sweep's epoch in the high
+// word), and a column waits (bounded, as the dataflow sweep of Cartesian boxes) only until
+// its lateral upwind columns have done the layers of its next batch.  Per batch: the
+// loads (cell classes, source, lateral inflow from the upwind columns or the reflective
+// inflow, then the coefficient rows), then per layer the update psi = rd q + sum of a_f
+// psi_in over the lateral inflow faces in face order, then the z inflow (the layer before
+// in sweep order, or the boundary) -- the terms and the order of k_sweep_level_cls.  The
+// pattern's share of the scalar-flux moment is summed per (cell, group) in direction
+// order.
+// ---------------------------------------------------------------------------------
+struct ColGeom {
+  int nxy, nz, npat, nd, ntasks, gchunk, nchunk;
+  const int* __restrict__ up;      // [npat][nxy][kColUp]
+  const int* __restrict__ zm;      // [nxy]
+  const int* __restrict__ zp;      // [nxy]
+  const int* __restrict__ pat_sz;  // [npat]
+  const int* __restrict__ pat_dirs_ptr;
+  const int* __restrict__ pat_dirs;
+  const int* __restrict__ order;   // [ntasks]
+  const unsigned short* __restrict__ ccls;
+  FlowSync* sync;
+  unsigned long long* prog;        // [npat][nchunk][nxy]: epoch << 32 | layers done
+  int sleep_ns;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_gpu64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_gpu64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Waits until *p >= target (relaxed polling, then one acquire load), as flow_wait.
+__device__ __forceinline__ void flow_wait_ge(const unsigned long long* p, unsigned long long target,
+                                             unsigned int* error, unsigned int limit, int sleep_ns) {
+  for (unsigned int it = 0;; it++) {
+    if (ld_relaxed_gpu64(p) >= target) break;
+    if (*(volatile unsigned int*)error) return;
+    if (it >= limit) {
+      atomicExch(error, 1u);
+      return;
+    }
+    if (sleep_ns > 0) __nanosleep(sleep_ns);
+  }
+  (void)ld_acquire_gpu64(p);
+}
+
+template <typename T, int B>
+__global__ void __launch_bounds__(128, 6) k_sweep_col(SNOp<T> A, ColGeom K, const T* __restrict__ coef,
+                                                   const SweepPtrs* __restrict__ P, int iso) {
+  __shared__ T s_mom[4][B][32];  // per warp: w_m psi of the batch's layers, by lane
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const T* __restrict__ src = static_cast<const T*>(P->src);
+  const T* __restrict__ bnd = static_cast<const T*>(P->bnd);
+  T* psi = static_cast<T*>(P->psi);
+  T* mom = static_cast<T*>(P->mom);
+  const unsigned long long ep = (unsigned long long)*(volatile unsigned int*)&K.sync->epoch << 32;
+  const int G = A.G, M = A.M, n = A.n, F = A.F, nxy = K.nxy, nz = K.nz;
+  const int gl = lane / K.nd, di = lane - gl * K.nd;
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = (int)atomicAdd(&K.sync->next, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= K.ntasks) return;
+    const int tc = K.order[t];
+    const int cp = tc / K.nchunk, ch = tc - cp * K.nchunk;
+    const int c = cp / K.npat, p = cp - c * K.npat;
+    const int d0 = K.pat_dirs_ptr[p], ndp = K.pat_dirs_ptr[p + 1] - d0;
+    const int g0 = ch * K.gchunk, gn = min(K.gchunk, G - g0);
+    const bool active = gl < gn && di < ndp;
+    const int g = g0 + gl;
+    const int m = active ? K.pat_dirs[d0 + di] : 0;
+    const T wm = active ? A.w[m] : T(0);
+    int fu[kColUp], cu[kColUp];  // lateral inflow faces and their layer-0 neighbour (-1: boundary)
+#pragma unroll
+    for (int u = 0; u < kColUp; u++) {
+      fu[u] = K.up[((size_t)p * nxy + c) * kColUp + u];
+      cu[u] = fu[u] >= 0 ? A.nbr[(size_t)fu[u] * n + c] : -1;
+    }
+    const int sz = K.pat_sz[p];
+    const int fz = sz > 0 ? K.zm[c] : (sz < 0 ? K.zp[c] : -1);  // the z inflow face
+    unsigned long long* prog = K.prog + ((size_t)p * K.nchunk + ch) * nxy;
+    const bool stall = lane == 0 && *(volatile unsigned int*)&K.sync->stall == (unsigned int)t + 1u;
+    T prev = T(0);
+    for (int kb = 0; kb < nz; kb += B) {
+      const int kn = min(B, nz - kb);
+      // wait until the lateral upwind columns have done this batch's layers
+      if (lane < kColUp) {
+        int c2 = -1;
+#pragma unroll
+        for (int u = 0; u < kColUp; u++)
+          if (u == lane) c2 = cu[u];
+        if (c2 >= 0) flow_wait_ge(prog + c2, ep | (unsigned long long)(kb + kn), &K.sync->error, kFlowSpinLimit, K.sleep_ns);
+        if (stall && kb == 0) flow_wait(&K.sync->stall, 0u, &K.sync->error, kFlowStallLimit);  // injected failure
+      }
+      __syncwarp();
+      T in[B][kColUp], sv[B], c0[B], az[B], af[B][kColUp];
+      int cl[B];
+#pragma unroll
+      for (int b = 0; b < B; b++) {
+        cl[b] = 0;
+        sv[b] = T(0);
+#pragma unroll
+        for (int u = 0; u < kColUp; u++) in[b][u] = T(0);
+        if (b < kn && active) {
+          const int kk = kb + b;
+          const int k = sz >= 0 ? kk : nz - 1 - kk;
+          const int i = k * nxy + c;
+          cl[b] = K.ccls[i];
+          sv[b] = iso ? src[(size_t)i * G + g] : src[((size_t)i * G + g) * M + m];
+#pragma unroll
+          for (int u = 0; u < kColUp; u++)
+            if (fu[u] >= 0) {
+              if (cu[u] >= 0) in[b][u] = __ldcg(psi + ((size_t)(cu[u] + k * nxy) * G + g) * M + m);
+              else if (bnd) in[b][u] = bnd_val(A, bnd, A.rslot[(size_t)fu[u] * n + i], g, m);
+            }
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < B; b++) {
+        c0[b] = az[b] = T(0);
+#pragma unroll
+        for (int u = 0; u < kColUp; u++) af[b][u] = T(0);
+        if (b < kn && active) {
+          const T* cf = coef + (((size_t)cl[b] * G + g) * M + m) * (1 + F);
+          c0[b] = cf[0];
+#pragma unroll
+          for (int u = 0; u < kColUp; u++)
+            if (fu[u] >= 0) af[b][u] = cf[1 + fu[u]];
+          if (fz >= 0) az[b] = cf[1 + fz];
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < B; b++) {
+        if (b >= kn) break;
+        const int kk = kb + b;
+        const int k = sz >= 0 ? kk : nz - 1 - kk;
+        const int i = k * nxy + c;
+        T v = T(0);
+        if (active) {
+          v = c0[b] * sv[b];
+#pragma unroll
+          for (int u = 0; u < kColUp; u++)
+            if (af[b][u] != T(0)) v += af[b][u] * in[b][u];
+          if (az[b] != T(0)) {
+            if (kk > 0) v += az[b] * prev;
+            else if (bnd) v += az[b] * bnd_val(A, bnd, A.rslot[(size_t)fz * n + i], g, m);
+          }
+          psi[((size_t)i * G + g) * M + m] = v;
+        }
+        prev = v;
+        s_mom[wid][b][lane] = wm * v;
+      }
+      // publish the batch: the warp barrier orders every lane's psi stores before lane
+      // 0's release
+      __syncwarp();
+      if (lane == 0) st_release_gpu64(prog + c, ep | (unsigned long long)(kb + kn));
+      // the batch's moments: lane (layer b, group gl) sums its segment in direction order
+      if (mom)
+        for (int r = lane; r < kn * gn; r += 32) {
+          const int b = r / gn, gg = r - b * gn;
+          const int kk = kb + b;
+          const int i = (sz >= 0 ? kk : nz - 1 - kk) * nxy + c;
+          T acc = T(0);
+          for (int dj = 0; dj < ndp; dj++) acc += s_mom[wid][b][gg * K.nd + dj];
+          mom[((size_t)p * n + i) * G + g0 + gg] = acc;
+        }
+      __syncwarp();
     }
   }
 }
@@ -1609,6 +1806,15 @@ int sweep_prepare(pgpu_problem* p, const SNOp<T>& A) {
   if (!d.sweep_ptrs.ptr && (rst = dev_alloc(d.sweep_ptrs, sizeof(SweepPtrs), &p->bytes, p->stream))) return rst;
   if (d.kba && !d.flow_grid[sizeof(T) == 8 ? 0 : 1] && (rst = cls ? flow_prepare<T, true>(d) : flow_prepare<T, false>(d)))
     return rst;
+  if (d.col && !d.col_grid[sizeof(T) == 8 ? 0 : 1]) {
+    // persistent grid of the column sweep: every CTA (four task warps) that fits at once
+    int dev = 0, sms = 0, per_sm = 0;
+    PGPU_CUDA(cudaGetDevice(&dev));
+    PGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_col<T, kColBatch<T>()>, 128, 0));
+    if (per_sm < 1) return fail(PGPU_ERR_CUDA, "the column sweep does not fit on an SM");
+    d.col_grid[sizeof(T) == 8 ? 0 : 1] = std::max(1, std::min((d.col_ntasks + 3) / 4, sms * per_sm));
+  }
   return PGPU_OK;
 }
 
@@ -1625,8 +1831,8 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
   // the sweep's launches are captured once per (precision, source kind) and replayed; the
   // buffers of this sweep go through the device-side pointer block
   launch(p, k_set_sweep_ptrs, 1, 1, p->stream, P, (const void*)src, (const void*)bnd, (void*)psi,
-         (void*)(d.kba ? mom : nullptr));
-  const int nlaunch = d.kba ? 2 : S.nlev;
+         (void*)(d.kba || d.col ? mom : nullptr));
+  const int nlaunch = d.kba || d.col ? 2 : S.nlev;
   auto enqueue = [&](cudaStream_t st) {
     if (d.kba) {
       const FlowGeom K{d.kba_nx, d.kba_ny, d.kba_ntx, d.kba_nty, d.kba_ntz, d.kba_npat, d.kba_nd, d.kba_ntasks, d.kba_gchunk, d.kba_nchunk,
@@ -1641,6 +1847,15 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
         flow_launch<T, true>(d, st, A, W, K, P, iso);
       else
         flow_launch<T, false>(d, st, A, W, K, P, iso);
+    } else if (d.col) {
+      const ColGeom K{d.col_nxy, d.col_nz, S.npat, d.col_nd, d.col_ntasks, d.col_gchunk, d.col_nchunk,
+                      d.d_col_up.as<int>(), d.d_col_zm.as<int>(), d.d_col_zp.as<int>(), d.d_col_sz.as<int>(),
+                      d.d_pat_dirs_ptr.as<int>(), d.d_pat_dirs.as<int>(), d.d_col_order.as<int>(),
+                      d.d_ccls.as<unsigned short>(), d.flow_sync.as<FlowSync>(),
+                      d.flow_flags.as<unsigned long long>(), d.flow_sleep};
+      k_flow_begin<<<1, 1, 0, st>>>(K.sync);
+      k_sweep_col<T, kColBatch<T>()><<<d.col_grid[sizeof(T) == 8 ? 0 : 1], 128, 0, st>>>(
+          A, K, (const T*)(sizeof(T) == 8 ? d.coef.ptr : d.coef32.ptr), P, iso);
     } else {
       for (int L = 0; L < S.nlev; L++) {
         dim3 g(S.grid_x[L], S.npat);
@@ -1694,7 +1909,7 @@ int sweep(pgpu_problem* p, const SNOp<T>& A, const T* src, int iso, const T* bnd
     }
   }
   p->launches += nlaunch;
-  p->prof_name = d.kba ? "k_sweep_flow" : "k_sweep_level";
+  p->prof_name = d.kba ? "k_sweep_flow" : (d.col ? "k_sweep_col" : "k_sweep_level");
   // Algorithmic bytes of one sweep: psi written once and read once per cell-group-
   // direction update (2 s_v), the source read per cell-group (s_v, or s_v per update for
   // an angular source), the scalar-flux moment written per cell-group (s_v) and the
@@ -1724,12 +1939,13 @@ int phi_space_T(pgpu_problem* p, const SNOp<T>& A, const T* x, const T* b, T* y)
   T* psi = psi_work<T>(d);
   launch(p, k_scatter_source<T>, grid_for(nG), kThreads, p->stream, A, x, b, q, 0.0, (const double*)d.lam_dev.as<double>());
   int st;
-  if (d.kba) {
-    // the dataflow sweep writes per-pattern moments; they are summed in pattern order
-    if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)d.kba_npat * nG * sizeof(double), &p->bytes, p->stream))) return st;
+  if (d.kba || d.col) {
+    // the dataflow sweeps write per-pattern moments; they are summed in pattern order
+    const int npat = d.kba ? d.kba_npat : d.sched.npat;
+    if (!d.mom.ptr && (st = dev_alloc(d.mom, (size_t)npat * nG * sizeof(double), &p->bytes, p->stream))) return st;
     T* mom = d.mom.as<T>();
     if ((st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi, mom))) return st;
-    launch(p, k_mom_reduce<T>, grid_for(nG), kThreads, p->stream, (long long)nG, d.kba_npat, (const T*)mom, y);
+    launch(p, k_mom_reduce<T>, grid_for(nG), kThreads, p->stream, (long long)nG, npat, (const T*)mom, y);
   } else {
     if ((st = sweep<T>(p, A, q, 1, d.nrefl ? x + nG : nullptr, psi))) return st;
     launch(p, k_moment<T>, grid_for((long long)nG * 32), kThreads, p->stream, nG, d.M, A.w, psi, y);
@@ -1900,7 +2116,7 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
   // a sweep that returned early after a bounded wait ran out leaves unfinished tiles;
   // report that cause rather than the NaN it may lead to
   auto nan_cause = [&]() -> int {
-    if (d.kba) {
+    if (d.kba || d.col) {
       unsigned int err = 0;
       if (int e = read_small(&err, &d.flow_sync.as<FlowSync>()->error, sizeof(err), s)) return e;
       if (err) return fail(PGPU_ERR_TIMEOUT, "sweep: a wait for an upwind tile ran out (kernel returned early)");
@@ -2027,7 +2243,7 @@ int read_outer(pgpu_problem* p, SNOuter& os) {
   SNData& d = *p->sn;
   FlowSync fs{0u, 0u, 0u, 0u};
   int st = read_small(&os, d.oscal.ptr, sizeof(os), p->stream);
-  if (st == PGPU_OK && d.kba) st = read_small(&fs, d.flow_sync.ptr, sizeof(fs), p->stream);
+  if (st == PGPU_OK && (d.kba || d.col)) st = read_small(&fs, d.flow_sync.ptr, sizeof(fs), p->stream);
   if (st) return st;
   if (fs.error) return fail(PGPU_ERR_TIMEOUT, "sweep: a wait for an upwind tile ran out (kernel returned early)");
   return PGPU_OK;
@@ -2071,8 +2287,8 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   SNOp<double> A64 = make_op<double>(d);
   // everything the sweeps allocate on first use, before a GMRES cycle is captured
   if ((st = sweep_prepare<double>(p, A64)) || (st = sweep_prepare<T>(p, A))) return st;
-  if (phi_space && d.kba && !d.mom.ptr &&
-      (st = dev_alloc(d.mom, (size_t)d.kba_npat * nG * sizeof(double), &p->bytes, p->stream)))
+  if (phi_space && (d.kba || d.col) && !d.mom.ptr &&
+      (st = dev_alloc(d.mom, (size_t)(d.kba ? d.kba_npat : d.sched.npat) * nG * sizeof(double), &p->bytes, p->stream)))
     return st;
   SNOuter* dos = d.oscal.as<SNOuter>();
   double* x64 = d.x64.as<double>();
@@ -2099,7 +2315,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   std::memset(&init, 0, sizeof(init));
   init.k = 1.0;
   launch(p, k_put<SNOuter>, 1, 1, s, dos, init);
-  if (d.kba) {
+  if (d.kba || d.col) {
     PGPU_CUDA(cudaMemsetAsync(&d.flow_sync.as<FlowSync>()->error, 0, sizeof(unsigned int), s));
     launch(p, k_put<unsigned int>, 1, 1, s, &d.flow_sync.as<FlowSync>()->stall, debug_sweep_stall());
   }
@@ -2290,6 +2506,153 @@ int sn_get_power(pgpu_problem* p, double* q, double* P, double* total) {
 void sn_destroy(pgpu_problem* p) {
   delete p->sn;
   p->sn = nullptr;
+}
+
+// Plan of the column sweep of an extruded mesh (prisms stacked in layers, cells numbered
+// layer by layer as the extruded-mesh reader does): every cell's lateral faces repeat the
+// layer-0 cell's (same normals, neighbours in the same layer), z faces link consecutive
+// layers.  A task is one column (all layers of a layer-0 cell) for one sweep pattern and
+// one chunk of groups; it waits for the columns upwind of it across lateral faces (the
+// columns' graph per pattern must be acyclic) and walks its layers in the pattern's z
+// direction.  Returns false (level sweeps are used) when the mesh does not qualify.
+struct ColPlan {
+  int nxy = 0, nz = 0, nd = 0, gchunk = 1, nchunk = 1, ntasks = 0;
+  std::vector<int> up;      // [npat][nxy][kColUp] lateral inflow face indices (-1: none)
+  std::vector<int> zm, zp;  // [nxy] index of the -z / +z face (-1: none)
+  std::vector<int> pat_sz;  // [npat] +1 / -1: the pattern's layer order (0: single layer)
+  std::vector<int> order;   // [ntasks] (column * npat + pattern) * nchunk + chunk, by column level
+};
+
+static bool col_plan(const pgpu_sn_operator* op, const Schedule& S, ColPlan& C) {
+  const int n = op->num_cells, F = op->num_faces;
+  auto nrm = [&](int f, int i) { return op->normals + ((size_t)f * n + i) * 3; };
+  auto is_z = [&](const double* v, double s) { return v[0] == 0.0 && v[1] == 0.0 && v[2] == s; };
+  // layer size: the +z neighbour of cell 0 (a single layer when it has none)
+  int nxy = n;
+  for (int f = 0; f < op->num_cell_faces[0]; f++)
+    if (is_z(nrm(f, 0), 1.0) && op->face_kind[(size_t)f * n] == PGPU_FACE_INTERIOR) nxy = op->neighbors[(size_t)f * n];
+  if (nxy <= 0 || n % nxy) return false;
+  const int nz = n / nxy;
+  C.nxy = nxy;
+  C.nz = nz;
+  C.zm.assign(nxy, -1);
+  C.zp.assign(nxy, -1);
+  for (int c = 0; c < nxy; c++)
+    for (int f = 0; f < op->num_cell_faces[c]; f++) {
+      if (is_z(nrm(f, c), -1.0)) C.zm[c] = f;
+      else if (is_z(nrm(f, c), 1.0)) C.zp[c] = f;
+      else if (nrm(f, c)[2] != 0.0) return false;  // tilted face
+    }
+  // a single layer has no z order: its z faces must not carry reflective inflow
+  if (nz == 1)
+    for (int c = 0; c < nxy; c++)
+      for (int f : {C.zm[c], C.zp[c]})
+        if (f >= 0 && op->face_kind[(size_t)f * n + c] == PGPU_FACE_REFLECTIVE) return false;
+  for (int k = 0; k < nz; k++)
+    for (int c = 0; c < nxy; c++) {
+      const int i = k * nxy + c;
+      if (op->num_cell_faces[i] != op->num_cell_faces[c]) return false;
+      for (int f = 0; f < op->num_cell_faces[c]; f++) {
+        const size_t o = (size_t)f * n + i, o0 = (size_t)f * n + c;
+        const double *a = nrm(f, i), *b = nrm(f, c);
+        if (a[0] != b[0] || a[1] != b[1] || a[2] != b[2]) return false;
+        const int kd = op->face_kind[o], j = op->neighbors[o];
+        if (f == C.zm[c] || f == C.zp[c]) {
+          const int k2 = f == C.zm[c] ? k - 1 : k + 1;
+          const bool inside = k2 >= 0 && k2 < nz;
+          if (inside != (kd == PGPU_FACE_INTERIOR)) return false;
+          if (inside && j != i + (k2 - k) * nxy) return false;
+        } else {
+          if (kd != op->face_kind[o0]) return false;
+          if (kd == PGPU_FACE_INTERIOR && j != op->neighbors[o0] + k * nxy) return false;
+        }
+      }
+    }
+  // per pattern: layer order, lateral inflow faces of every column, column levels
+  const int npat = S.npat;
+  C.nd = 0;
+  for (int p = 0; p < npat; p++) C.nd = std::max(C.nd, S.pat_dirs_ptr[p + 1] - S.pat_dirs_ptr[p]);
+  if (C.nd > 32) return false;
+  C.gchunk = std::max(1, std::min(op->num_groups, 32 / C.nd));
+  C.nchunk = (op->num_groups + C.gchunk - 1) / C.gchunk;
+  C.pat_sz.assign(npat, 0);
+  C.up.assign((size_t)npat * nxy * kColUp, -1);
+  std::vector<int> level((size_t)npat * nxy, 0);
+  int maxlev = 0;
+  for (int p = 0; p < npat; p++) {
+    const int d0 = S.pat_dirs_ptr[p];
+    const double* dir = op->directions + (size_t)S.pat_dirs[d0] * 3;
+    if (nz > 1) {
+      int sz = 0;
+      for (int k = d0; k < S.pat_dirs_ptr[p + 1]; k++) {
+        const double dz = op->directions[(size_t)S.pat_dirs[k] * 3 + 2];
+        const int s = dz > 0.0 ? 1 : (dz < 0.0 ? -1 : 0);
+        if (s == 0 || (sz != 0 && s != sz)) return false;
+        sz = s;
+      }
+      C.pat_sz[p] = sz;
+    }
+    std::vector<int> indeg(nxy, 0), head(nxy + 1, 0), adj;
+    for (int c = 0; c < nxy; c++) {
+      int u = 0;
+      for (int f = 0; f < op->num_cell_faces[c]; f++) {
+        if (f == C.zm[c] || f == C.zp[c]) continue;
+        const double* v = nrm(f, c);
+        const int kd = op->face_kind[(size_t)f * n + c];
+        if (!(kd == PGPU_FACE_INTERIOR || kd == PGPU_FACE_REFLECTIVE)) continue;
+        // an interior face's sign is the pattern's; a reflective face's normal need not be
+        // an interior normal, so it is an inflow face if any direction enters through it
+        // (the per-direction coefficient is zero for the others)
+        bool inflow = false;
+        for (int k = d0; k < S.pat_dirs_ptr[p + 1] && !inflow; k++) {
+          const double* dk = kd == PGPU_FACE_INTERIOR ? dir : op->directions + (size_t)S.pat_dirs[k] * 3;
+          inflow = dk[0] * v[0] + dk[1] * v[1] + dk[2] * v[2] < 0.0;
+        }
+        if (!inflow) continue;
+        if (u == kColUp) return false;
+        C.up[((size_t)p * nxy + c) * kColUp + u++] = f;
+        if (kd == PGPU_FACE_INTERIOR) {
+          head[op->neighbors[(size_t)f * n + c] + 1]++;
+          indeg[c]++;
+        }
+      }
+    }
+    for (int c = 0; c < nxy; c++) head[c + 1] += head[c];
+    adj.assign(head[nxy], 0);
+    std::vector<int> fill(head.begin(), head.end() - 1);
+    for (int c = 0; c < nxy; c++)
+      for (int u = 0; u < kColUp; u++) {
+        const int f = C.up[((size_t)p * nxy + c) * kColUp + u];
+        if (f >= 0 && op->face_kind[(size_t)f * n + c] == PGPU_FACE_INTERIOR) adj[fill[op->neighbors[(size_t)f * n + c]]++] = c;
+      }
+    std::vector<int> queue;
+    queue.reserve(nxy);
+    for (int c = 0; c < nxy; c++)
+      if (indeg[c] == 0) queue.push_back(c);
+    for (size_t q = 0; q < queue.size(); q++) {
+      const int c = queue[q];
+      for (int e = head[c]; e < head[c + 1]; e++) {
+        const int c2 = adj[e];
+        level[(size_t)p * nxy + c2] = std::max(level[(size_t)p * nxy + c2], level[(size_t)p * nxy + c] + 1);
+        if (--indeg[c2] == 0) queue.push_back(c2);
+      }
+    }
+    if ((int)queue.size() != nxy) return false;  // the columns' upwind graph has a cycle
+    for (int c = 0; c < nxy; c++) maxlev = std::max(maxlev, level[(size_t)p * nxy + c]);
+  }
+  // tasks level by level (every pattern's columns of level L, all chunks): a task's
+  // upwind tasks always come earlier
+  std::vector<int> cnt(maxlev + 2, 0);
+  for (int p = 0; p < npat; p++)
+    for (int c = 0; c < nxy; c++) cnt[level[(size_t)p * nxy + c] + 1] += C.nchunk;
+  for (int L = 0; L <= maxlev; L++) cnt[L + 1] += cnt[L];
+  C.ntasks = cnt[maxlev + 1];
+  C.order.assign(C.ntasks, 0);
+  for (int p = 0; p < npat; p++)
+    for (int c = 0; c < nxy; c++)
+      for (int ch = 0; ch < C.nchunk; ch++) C.order[cnt[level[(size_t)p * nxy + c]]++] = (c * npat + p) * C.nchunk + ch;
+  (void)F;
+  return true;
 }
 
 // Plan of the tiled sweep: verifies that the operator is a full Cartesian box in the
@@ -2729,6 +3092,31 @@ int pgpu_sn_create(int device, const pgpu_sn_operator* op, pgpu_problem** out) {
       d.ncls = (int)crep.size();
       up(d.d_ccls, ccls.data(), ccls.size() * 2);
       up(d.d_crep, crep.data(), crep.size() * 4);
+      // extruded meshes (and boxes the tiles do not fit): the column sweep instead of one
+      // launch per level (PGPU_SWEEP_COLUMNS=0 keeps the level sets, for measurement)
+      ColPlan cp;
+      const char* ce = std::getenv("PGPU_SWEEP_COLUMNS");
+      if (!(ce && std::atoi(ce) == 0) && col_plan(op, sched, cp)) {
+        d.col = true;
+        d.col_nxy = cp.nxy;
+        d.col_nz = cp.nz;
+        d.col_nd = cp.nd;
+        d.col_ntasks = cp.ntasks;
+        d.col_gchunk = cp.gchunk;
+        d.col_nchunk = cp.nchunk;
+        d.flow_sleep = flow_sleep_ns();
+        up(d.d_col_up, cp.up.data(), cp.up.size() * 4);
+        up(d.d_col_zm, cp.zm.data(), cp.zm.size() * 4);
+        up(d.d_col_zp, cp.zp.data(), cp.zp.size() * 4);
+        up(d.d_col_sz, cp.pat_sz.data(), cp.pat_sz.size() * 4);
+        up(d.d_col_order, cp.order.data(), cp.order.size() * 4);
+        const size_t nflags = (size_t)sched.npat * cp.nchunk * cp.nxy;  // 64-bit progress words
+        al(d.flow_sync, sizeof(FlowSync));
+        al(d.flow_flags, nflags * 8);
+        if (st == PGPU_OK && (cudaMemsetAsync(d.flow_sync.ptr, 0, sizeof(FlowSync), p->stream) != cudaSuccess ||
+                              cudaMemsetAsync(d.flow_flags.ptr, 0, nflags * 8, p->stream) != cudaSuccess))
+          st = fail(PGPU_ERR_CUDA, "clearing the sweep flags");
+      }
     }
   }
   if (d.nrefl) {

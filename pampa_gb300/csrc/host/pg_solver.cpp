@@ -180,10 +180,17 @@ bool NeutronicSolver::temperatureChanged() const {
   return T_ != T_built_;
 }
 
+// Time steps of solvers without one here.  For SN the reference assembles the step's
+// angular-flux system (SNSolver.cxx:371-441) but solves it into the scalar-flux vector,
+// whose size does not match (SNSolver.cxx:658-666), so its own step always stops with an
+// error; this build reports the same failure, with the reason.
 int NeutronicSolver::solveTransient(int n, double dt, double t) {
   (void)n;
   (void)dt;
   (void)t;
+  PG_CHECK(name_ == "sn",
+           "unable to solve the linear system (the SN time step solves an angular-flux system into the "
+           "scalar-flux vector in the reference, whose sizes do not match)");
   PG_CHECK(true, "transient steps (n > 0) are not available for the " + name_ + " solver in this build");
 }
 

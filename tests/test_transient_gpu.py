@@ -97,3 +97,15 @@ def test_transient_input_without_velocities_is_rejected(case_input):
     path = _with_steps(case_input("slabs/reflected-diffusion"), 1, 0.01)
     with pytest.raises(pg.PampaError, match="pampa_initialize"):
         pg.Pampa(path, "-silent")
+
+
+def test_sn_time_step_fails_as_in_the_reference(case_input):
+    """The reference's SN step solves its angular-flux system into the scalar-flux vector
+    (SNSolver.cxx:658-666), which PETSc rejects; the drop-in reports the same failure
+    after a normal steady state."""
+    path = _with_steps(case_input("pwr-iaea-benchmark/cartesian-sn"), 1, 0.01)
+    with pg.Pampa(path, "-silent") as p:
+        p.solve()
+        assert p.keff > 0.0
+        with pytest.raises(pg.PampaError, match="pampa_solve failed"):
+            p.solve(1, 0.01, 0.01)
