@@ -1707,7 +1707,11 @@ int read_outer(pgpu_problem* p, OuterScal& os) { return read_small(&os, p->diff-
 
 }  // namespace
 
-int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
+namespace {
+
+// The power iteration with the given default relative Wielandt shift (options.shift, when
+// set, takes precedence).
+int diffusion_solve_shift(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats, double sh_default) {
   DiffusionData& d = *p->diff;
   const int n = d.n, G = d.G, N = n * G;
   const bool mixed = opt->precision == PGPU_MIXED;
@@ -1811,7 +1815,7 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
       break;
     }
     if (outer >= kShiftAfter && dk < kShiftWhenDk) {
-      const double sh = opt->shift < 0.0 ? (d.mg_levels ? kShiftDefaultMg : kShiftDefault) : opt->shift;
+      const double sh = opt->shift < 0.0 ? sh_default : opt->shift;
       // the shifted k must stay above the fundamental one; with dominance ratio rho the
       // estimate is still about dk rho / (1 - rho) below it, so keep 50 |dk| of margin
       lam_s = sh > 0.0 ? 1.0 / std::fmax(os.k * (1.0 + sh), os.k + kShiftMargin * dk) : 0.0;
@@ -1844,6 +1848,26 @@ int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats)
   if (status != PGPU_OK) return fail(status, "power iteration reached max_outer without converging");
   if (os.negatives > 0) return fail(PGPU_ERR_NEGATIVE_FLUX, "negative values in the scalar-flux solution");
   return PGPU_OK;
+}
+
+}  // namespace
+
+// Problems with a multigrid hierarchy default to the closer shift kShiftDefaultMg.  The
+// fundamental mode is the only eigenvector without sign changes, so a solution with
+// negative flux means the closer shift led the iteration to a higher mode (one request of
+// a 4096-request serving stream did): the solve is then repeated from a flat flux with the
+// default shift, and the statistics cover both attempts.
+int diffusion_solve(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
+  const bool close = p->diff->mg_levels > 0 && opt->shift < 0.0;
+  int st = diffusion_solve_shift(p, opt, stats, close ? kShiftDefaultMg : kShiftDefault);
+  if (st == PGPU_ERR_NEGATIVE_FLUX && close) {
+    const pgpu_stats first = *stats;
+    st = diffusion_solve_shift(p, opt, stats, kShiftDefault);
+    stats->outer_iterations += first.outer_iterations;
+    stats->inner_iterations += first.inner_iterations;
+    stats->seconds += first.seconds;
+  }
+  return st;
 }
 
 // Linear solve (R - lam F) y = b with the problem's operator (the transient step of

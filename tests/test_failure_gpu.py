@@ -65,3 +65,19 @@ def test_injected_stall_in_an_s8_sweep_with_one_group_per_task(tmp_path, monkeyp
         k1 = p.keff
         p.solve()
         assert p.keff == k1 and k1 > 0.0
+
+
+def test_injected_stall_in_the_column_sweep(tmp_path, monkeypatch):
+    """A box whose sides are not multiples of 4 is swept by columns: the same bounded
+    wait, error word and recovery."""
+    from pampa_gb300 import workloads as wl
+    path = wl.sn_3d(str(tmp_path), nx=10, ny=6, nz=5, order=4, block=2)
+    ref = po.run_input(path)
+    with pg.Pampa(path, "-silent") as p:
+        monkeypatch.setenv("PGPU_DEBUG_SWEEP_STALL", "20")
+        with pytest.raises(pg.PampaError, match="ran out"):
+            p.solve()
+        monkeypatch.delenv("PGPU_DEBUG_SWEEP_STALL")
+        p.solve()
+        assert abs(p.keff - ref["keff"]) <= 1e-6, (p.keff, ref["keff"])
+        assert rel_l2(p.field("scalar-flux"), ref["phi"]) <= 1e-5
