@@ -379,6 +379,10 @@ def run_ours(args, rank, world, local):
                      flux_l2_vs_fp64=rel(phim, phi64), psi_l2_vs_fp64=rel(psim, psi64),
                      sweeps_per_solve=mres[-1]["sweeps"], outer_iterations=mres[-1]["outer_iterations"],
                      gmres_iterations=mres[-1]["inner_iterations"],
+                     # one FP64 residual sweep per outer iteration and the final FP64 sweep for
+                     # psi; the GMRES correction sweeps are FP32
+                     sweeps_fp64=mres[-1]["outer_iterations"] + 1,
+                     sweeps_fp32=mres[-1]["sweeps"] - mres[-1]["outer_iterations"] - 1,
                      gpu_launches=int(sum(r["launches"] for r in mres)),
                      timing="device time (CUDA events) of the same number of complete solves as the FP64 "
                             "line, same problem resident in HBM, L2 flushed between solves")

@@ -26,6 +26,8 @@
 #include <tuple>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "pgpu_internal.cuh"
 
 namespace pgpu {
@@ -45,6 +47,10 @@ struct DiffOp {
   // [nm][G][G] in-cell coupling g2 -> g of the shifted operator, sigma_s(g2->g) (g2 != g)
   // + lam_s chi_g nu_sigma_f(g2), rebuilt when lam_s changes; null for the plain operator
   const T* __restrict__ fold;
+  // BF16 copies of off and diag read by the multigrid cycle's level-0 kernels in mixed
+  // precision (null: they read off and diag)
+  const __nv_bfloat16* __restrict__ off_lo = nullptr;
+  const __nv_bfloat16* __restrict__ diag_lo = nullptr;
 };
 
 // Device-resident BiCGStab state; every scalar of the iteration stays on the GPU.
@@ -59,7 +65,24 @@ struct OuterScal {
   double k, k_old, S, change, p0, total_power;
   double rr, bb;
   int negatives, nonfinite;
+  unsigned long long amax;  // bit pattern of max |x| (>= 0) for the zero flush
 };
+
+// Entries of the converged flux whose exact value is tiny (fast flux deep in a reflector)
+// come out of an iterative solve as +-(solver tolerance), where the reference's exact
+// factorisation gives small non-negative values and it rejects any negative entry.
+// Entries within max(kZeroFlush, tol_flux) of the maximum are set to zero; anything more
+// negative is a genuine negative flux (a mode with sign changes) and is reported.
+constexpr double kZeroFlush = 1e-9;
+
+// *out = max(*out, max |x|) on the bit patterns of non-negative doubles.
+__global__ void k_absmax_d(long long N, const double* __restrict__ x, unsigned long long* out) {
+  double m = 0.0;
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    m = fmax(m, fabs(x[l]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
 
 // One coarse level of the aggregation multigrid (level l >= 1; the finer level is l - 1).
 struct MgLevel {
@@ -94,6 +117,7 @@ struct DiffusionData {
   double mg_lam = -1.0;  // shift the coarse operators were combined for (< 0: not yet)
   bool mg_have32 = false;
   DevBuf mg_inv64, mg_inv32;  // dense inverse of the coarsest operator
+  DevBuf off_lo, diag_lo;      // BF16 copies of the level-0 operator for the mixed-precision cycle
   std::vector<double> mg_hbs, mg_hbf, mg_hoff;  // the coarsest operator on the host
   std::vector<int> mg_hnbr;
   // chains of conditional BiCGStab iterations captured in CUDA graphs, [fp32]
@@ -574,6 +598,17 @@ struct MgMap {
   const int* __restrict__ mem;   // [n_fine]
 };
 
+// Level-0 operator entries for the cycle: the BF16 copies when present (mixed precision),
+// else the operator's own.
+template <typename T>
+__device__ __forceinline__ T mg_off0(const DiffOp<T>& A, size_t k) {
+  return A.off_lo ? (T)__bfloat162float(A.off_lo[k]) : A.off[k];
+}
+template <typename T>
+__device__ __forceinline__ T mg_diag0(const DiffOp<T>& A, size_t k) {
+  return A.diag_lo ? (T)__bfloat162float(A.diag_lo[k]) : A.diag[k];
+}
+
 // y = (A u)_i at level 0 with u = w z (kSum false) or w z + P zc (kSum true), where z is
 // the undamped cell-preconditioned vector of the BiCGStab step and w the damping; the
 // operator arithmetic is that of apply_cell.
@@ -593,18 +628,34 @@ __device__ __forceinline__ void mg_apply0(const DiffOp<T>& A, const T* __restric
     T sc = T(0);
 #pragma unroll
     for (int g2 = 0; g2 < G; g2++) sc += fm[g2 * G + g] * xc[g2];
-    y[g] = A.diag[base + g] * xc[g] - vol * sc;
+    y[g] = mg_diag0(A, base + g) * xc[g] - vol * sc;
   }
   const size_t nG = (size_t)A.n * G;
   for (int fa = 0; fa < A.F; fa++) {
     const int j = A.nbr[(size_t)fa * A.n + i];
     if (j >= 0) {
-      const T* o = A.off + fa * nG + base;
+      const size_t o = fa * nG + base;
       const T* xj = z + (size_t)j * G;
       const T* cj = kSum ? zc + (size_t)agg[j] * G : nullptr;
 #pragma unroll
-      for (int g = 0; g < G; g++) y[g] += o[g] * (kSum ? w * xj[g] + cj[g] : w * xj[g]);
+      for (int g = 0; g < G; g++) y[g] += mg_off0(A, o + g) * (kSum ? w * xj[g] + cj[g] : w * xj[g]);
     }
+  }
+}
+
+// The cell preconditioner of the cycle's level-0 smoothing (precond_cell_g with the
+// cycle's diagonal).
+template <typename T, int G>
+__device__ __forceinline__ void mg_precond0(const DiffOp<T>& A, int i, const T (&rin)[G], T (&z)[G]) {
+  const T* ssm = A.ss + (size_t)A.mat[i] * G * G;
+  const T V = A.vol[i];
+  const size_t base = (size_t)i * G;
+#pragma unroll
+  for (int g = 0; g < G; g++) {
+    T s = rin[g];
+#pragma unroll
+    for (int g2 = 0; g2 < g; g2++) s += V * ssm[g2 * G + g] * z[g2];
+    z[g] = s / mg_diag0(A, base + g);
   }
 }
 
@@ -686,7 +737,7 @@ __global__ void k_mg_post0(DiffOp<T> A, const T* __restrict__ r, const T* __rest
     const T* zi = zc + (size_t)agg[i] * G;
 #pragma unroll
     for (int g = 0; g < G; g++) res[g] = r[base + g] - y[g];
-    precond_cell_g<T, G>(A, i, res, dz);
+    mg_precond0<T, G>(A, i, res, dz);
 #pragma unroll
     for (int g = 0; g < G; g++) out[base + g] = (T)kMgOmega * (z[base + g] + dz[g]) + zi[g];
   }
@@ -963,10 +1014,11 @@ __global__ void k_power_norm(int n, int G, const int* __restrict__ mat, const do
 // counts negative entries.
 __global__ void k_power_fields(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
                                const double* __restrict__ ksf, const double* __restrict__ nsf,
-                               const double* __restrict__ x, double power, double* phi, double* q,
-                               double* P, OuterScal* os, ReduceSlots<2> slots) {
+                               const double* __restrict__ x, double power, double rel_flush, double* phi,
+                               double* q, double* P, OuterScal* os, ReduceSlots<2> slots) {
   const double f = power / os->p0;
   const double k = os->k;
+  const double flush = rel_flush * __longlong_as_double((long long)os->amax) * fabs(f);
   double acc[2] = {0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double* ks = ksf + (size_t)mat[i] * G;
@@ -975,6 +1027,7 @@ __global__ void k_power_fields(int n, int G, const int* __restrict__ mat, const 
     double qi = 0.0, Pi = 0.0;
     for (int g = 0; g < G; g++) {
       double v = x[(size_t)i * G + g] * f;
+      if (v < 0.0 && v >= -flush) v = 0.0;
       phi[(size_t)i * G + g] = v;
       if (v < 0.0) acc[1] += 1.0;
       qi += v * ks[g] * V;
@@ -998,6 +1051,11 @@ __global__ void k_apply(DiffOp<double> A, const double* __restrict__ x, double* 
     const int i = l / A.G, g = l - i * A.G;
     y[l] = apply_row(A, x, i, g);
   }
+}
+
+__global__ void k_to_bf16(long long N, const double* __restrict__ a, __nv_bfloat16* b) {
+  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
+    b[l] = __float2bfloat16((float)a[l]);
 }
 
 template <typename S, typename D>
@@ -1402,6 +1460,20 @@ int mg_vectors(pgpu_problem* p, DevBuf* w) {
     }
   for (int k = 9; k < 11; k++)
     if (!w[k].ptr && (st = dev_alloc(w[k], (size_t)d.n * d.G * sizeof(T), &p->bytes, p->stream))) return st;
+  // the FP32 cycle reads a BF16 copy of the level-0 operator (PGPU_DIFF_MG_BF16=0: FP32)
+  const char* e = std::getenv("PGPU_DIFF_MG_BF16");
+  if (sizeof(T) == 4 && !d.off_lo.ptr && !(e && std::atoi(e) == 0)) {
+    const long long nG = (long long)d.n * d.G, no = (long long)d.F * nG;
+    if ((st = dev_alloc(d.off_lo, (size_t)std::max(no, 1LL) * 2, &p->bytes, p->stream)) ||
+        (st = dev_alloc(d.diag_lo, (size_t)nG * 2, &p->bytes, p->stream)))
+      return st;
+    if (no > 0)
+      launch(p, k_to_bf16, grid_for(no), kThreads, p->stream, no, (const double*)d.off64.as<double>(),
+             d.off_lo.as<__nv_bfloat16>());
+    launch(p, k_to_bf16, grid_for(nG), kThreads, p->stream, nG, (const double*)d.diag64.as<double>(),
+           d.diag_lo.as<__nv_bfloat16>());
+    PGPU_CUDA(cudaGetLastError());
+  }
   return PGPU_OK;
 }
 
@@ -1599,6 +1671,11 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   // the V-cycle preconditioner when the problem has a hierarchy (shifted operators only)
   const bool mg = d.mg_levels > 0 && A.fold != nullptr;
   if (mg && (tst = mg_vectors<T>(p, w))) return tst;
+  DiffOp<T> Amg = A;  // the operator the cycle's level-0 kernels read
+  if (mg && sizeof(T) == 4 && d.off_lo.ptr) {
+    Amg.off_lo = d.off_lo.as<__nv_bfloat16>();
+    Amg.diag_lo = d.diag_lo.as<__nv_bfloat16>();
+  }
   T* phf = mg ? w[9].as<T>() : phat;  // preconditioned directions fed to the SpMVs
   T* shf = mg ? w[10].as<T>() : shat;
   const int* shp = d.shape[sizeof(T) == 8 ? 0 : 1];
@@ -1618,12 +1695,12 @@ int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, doubl
   auto iteration = [&](bool timed, cudaGraphConditionalHandle next, int has_next) {
     cudaEvent_t e0;
     launch_bicg_p<T>(gC, cT, st, A, r, pp, v, phat, sc);
-    if (mg) mg_cycle<T>(p, A, pp, phat, phf, sc);
+    if (mg) mg_cycle<T>(p, Amg, pp, phat, phf, sc);
     if (timed) prof_begin(p, &e0);
     launch_bicg_v<T>(form, gS, rT, st, A, phf, v, rhat, sc, slots_of<1>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
     launch_bicg_s<T>(gC, cT, st, A, r, v, s, shat, sc);
-    if (mg) mg_cycle<T>(p, A, s, shat, shf, sc);
+    if (mg) mg_cycle<T>(p, Amg, s, shat, shf, sc);
     if (timed) prof_begin(p, &e0);
     launch_bicg_t<T>(form, gS, rT, st, A, shf, t, s, sc, slots_of<2>(d));
     if (timed) prof_end(p, e0, 1, 0.0);
@@ -1827,10 +1904,13 @@ int diffusion_solve_shift(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* 
   if (!converged) status = PGPU_ERR_NOT_CONVERGED;
 
   // normalisation and power (NeutronicSolver.cxx:46-116)
+  PGPU_CUDA(cudaMemsetAsync(&dos->amax, 0, sizeof(unsigned long long), s));
+  launch(p, k_absmax_d, gN, kThreads, s, (long long)N, (const double*)d.x.as<double>(), &dos->amax);
   launch(p, k_power_norm, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.ksf.as<double>(),
                                        d.x.as<double>(), dos, slots_of<1>(d));
   launch(p, k_power_fields, gC, kThreads, s, n, G, d.mat.as<int>(), d.vol64.as<double>(), d.ksf.as<double>(),
-                                         d.nsf.as<double>(), d.x.as<double>(), opt->power, d.phi.as<double>(),
+                                         d.nsf.as<double>(), d.x.as<double>(), opt->power,
+                                         std::fmax(kZeroFlush, opt->tol_flux), d.phi.as<double>(),
                                          d.q.as<double>(), d.P.as<double>(), dos, slots_of<2>(d));
   PGPU_CUDA(cudaGetLastError());
   PGPU_CUDA(cudaEventRecord(e1, s));

@@ -178,11 +178,12 @@ struct SNOuter {
   unsigned long long amax_phi, amax_psi;  // bit patterns of max |phi0|, max |psi| (>= 0)
 };
 
-// Entries of the converged flux whose exact value is zero (e.g. fast flux in a source-free,
-// non-scattering region) come out of an iterative solve as +-(solver tolerance).  The
-// reference, which factors R exactly, gets exact zeros there and rejects any negative
-// entry.  Entries within kZeroFlush of the maximum are therefore set to zero; anything
-// more negative is a genuine negative flux and is reported.
+// Entries of the converged flux whose exact value is zero or tiny (e.g. fast flux in a
+// source-free, non-scattering region) come out of an iterative solve as +-(solver
+// tolerance).  The reference, which factors R exactly, gets exact (non-negative) values
+// there and rejects any negative entry.  Entries within max(kZeroFlush, tol_flux) of the
+// maximum are therefore set to zero; anything more negative is a genuine negative flux
+// (a mode with sign changes) and is reported.
 constexpr double kZeroFlush = 1e-9;
 
 template <typename T>
@@ -1417,11 +1418,11 @@ __global__ void k_sn_power_norm(int n, int G, const int* __restrict__ mat, const
 // phi = 4 pi phi0 * power / p0 (SNSolver::calculateScalarFlux + normalizeScalarFlux), q, P.
 __global__ void k_sn_power_fields(int n, int G, const int* __restrict__ mat, const double* __restrict__ vol,
                                   const double* __restrict__ ksf, const double* __restrict__ nsf,
-                                  const double* __restrict__ phi0, double power, double* phi, double* q,
-                                  double* P, SNOuter* os, ReduceSlots<2> slots) {
+                                  const double* __restrict__ phi0, double power, double rel_flush, double* phi,
+                                  double* q, double* P, SNOuter* os, ReduceSlots<2> slots) {
   const double f = 4.0 * M_PI * power / os->p0;
   const double k = os->k;
-  const double flush = kZeroFlush * __longlong_as_double((long long)os->amax_phi) * fabs(f);
+  const double flush = rel_flush * __longlong_as_double((long long)os->amax_phi) * fabs(f);
   double acc[2] = {0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double* ks = ksf + (size_t)mat[i] * G;
@@ -1448,9 +1449,10 @@ __global__ void k_sn_power_fields(int n, int G, const int* __restrict__ mat, con
 }
 
 // psi *= power / (p0 / 4 pi)  (SNSolver::normalizeAngularFlux); counts negatives.
-__global__ void k_sn_psi_norm(long long N, double* psi, double power, SNOuter* os, ReduceSlots<1> slots) {
+__global__ void k_sn_psi_norm(long long N, double* psi, double power, double rel_flush, SNOuter* os,
+                              ReduceSlots<1> slots) {
   const double f = 4.0 * M_PI * power / os->p0;
-  const double flush = kZeroFlush * __longlong_as_double((long long)os->amax_psi) * fabs(f);
+  const double flush = rel_flush * __longlong_as_double((long long)os->amax_psi) * fabs(f);
   double acc[1] = {0.0};
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
     double v = psi[l] * f;
@@ -2444,8 +2446,9 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
          (const double*)d.ksf.as<double>(), (const double*)phi0, dos, s1);
   launch(p, k_sn_power_fields, gn, kThreads, s, n, G, (const int*)d.mat.as<int>(), (const double*)d.vol.as<double>(),
          (const double*)d.ksf.as<double>(), (const double*)d.nsf.as<double>(), (const double*)phi0, opt->power,
-         d.phi.as<double>(), d.q.as<double>(), d.P.as<double>(), dos, s2);
-  launch(p, k_sn_psi_norm, grid_for(N), kThreads, s, N, psi, opt->power, dos, s1);
+         std::fmax(kZeroFlush, opt->tol_flux), d.phi.as<double>(), d.q.as<double>(), d.P.as<double>(), dos, s2);
+  launch(p, k_sn_psi_norm, grid_for(N), kThreads, s, N, psi, opt->power, std::fmax(kZeroFlush, opt->tol_flux), dos,
+         s1);
   PGPU_CUDA(cudaGetLastError());
   PGPU_CUDA(cudaEventRecord(e1, s));
   if ((st = read_outer(p, os))) return st;
