@@ -74,11 +74,12 @@ WORKLOADS["serve_diffusion"] = dict(
          "p50/p99 latency with Poisson arrivals at 80% of capacity")
 DEFAULT = "sn_s8_64x64x32_g2"
 # DRAM bytes (read + write) of one launch of each workload's dominant kernel, from ncu
-# captures summarised under profiles/: k_sweep_flow on the full S8 workload
+# captures summarised under profiles/: k_sweep_flow on the full S8 workload, FP64 and FP32
 # (k_sweep_flow_sn_s8_64x64x32.md); k_bicg_v_cell<float, 7> captured at 128x128x64
 # (7.34M rows, 320.7 MB) and scaled by the 8x rows of 256x256x128, its traffic being
 # proportional to the rows (k_bicg_v_cell_diffusion_7g_128x128x64.md).
-TRAFFIC = {"sn_s8_64x64x32_g2": 256460032, "diffusion_7g_256x256x128_mixed": 2565486592}
+TRAFFIC = {"sn_s8_64x64x32_g2": 108907520, "sn_s8_64x64x32_g2_mixed": 58752768,
+           "diffusion_7g_256x256x128_mixed": 2565486592}
 
 
 def reduce_over_ranks(value: float, dist, device: str, op: str = "max") -> float:

@@ -1833,6 +1833,8 @@ int diffusion_solve_shift(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* 
   // Wielandt shift lam_s = 1/(k (1 + shift)) once k has settled; the inner operator is
   // R - lam_s F, whose solve maps the normalised fission source to x / (1/k - lam_s).
   double lam_s = 0.0;
+  const char* swe = std::getenv("PGPU_DIFF_SHIFT_WHEN_DK");  // measurement override of kShiftWhenDk
+  const double shift_when_dk = swe ? std::atof(swe) : kShiftWhenDk;
   for (outer = 1; outer <= opt->max_outer; outer++) {
     launch(p, k_scale_copy, gN, kThreads, s, N, (const double*)d.x.as<double>(), 1.0 / (1.0 / k_prev - lam_s),
            d.y.as<double>());
@@ -1891,7 +1893,7 @@ int diffusion_solve_shift(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* 
       converged = true;
       break;
     }
-    if (outer >= kShiftAfter && dk < kShiftWhenDk) {
+    if (outer >= kShiftAfter && dk < shift_when_dk) {
       const double sh = opt->shift < 0.0 ? sh_default : opt->shift;
       // the shifted k must stay above the fundamental one; with dominance ratio rho the
       // estimate is still about dk rho / (1 - rho) below it, so keep 50 |dk| of margin

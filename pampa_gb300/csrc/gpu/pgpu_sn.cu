@@ -2267,7 +2267,11 @@ constexpr int kShiftAfter = 3;
 constexpr double kShiftDefault = 0.05;  // relative shift of k (measured best on the S8 workload)
 constexpr double kShiftMargin = 50.0;   // the shifted k is at least k + kShiftMargin |dk| (the estimate
                                         // lags the fundamental k by about dk rho / (1 - rho))
-constexpr double kShiftWhenDk = 1e-3;
+// |dk| below which the shift starts.  The margin already keeps an early shift weak, and
+// waiting for |dk| < 1e-3 spent 21 unshifted outer iterations of the S8 workload's 37 on
+// getting k to 1e-3: from 0.1, 28 outer iterations and 0.21 against 0.26 s per FP64 solve
+// (mixed 0.155 against 0.19 s; hexagonal workload 6.14 against 6.31 s), same k to 1e-11.
+constexpr double kShiftWhenDk = 0.1;
 
 template <typename T>
 int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
@@ -2340,6 +2344,12 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
   // Wielandt shift lam_s = 1/(k (1 + shift)), switched on once k has settled (scalar-flux
   // space only); 0 means plain power iteration.  The sweeps' sources read it on the device.
   double lam_s = 0.0;
+  const char* swe = std::getenv("PGPU_SN_SHIFT_WHEN_DK");  // measurement override of kShiftWhenDk
+  const double shift_when_dk = swe ? std::atof(swe) : kShiftWhenDk;
+  const char* sae = std::getenv("PGPU_SN_SHIFT_AFTER");  // measurement override of kShiftAfter
+  const int shift_after = sae ? std::atoi(sae) : kShiftAfter;
+  const char* ete = std::getenv("PGPU_SN_ETA");  // measurement override of kEta
+  const double eta = ete ? std::atof(ete) : kEta;
   launch(p, k_put<double>, 1, 1, s, d.lam_dev.as<double>(), 0.0);
 
   // correction operators in precision T
@@ -2386,7 +2396,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
         launch(p, k_cast<double, T>, gl, kThreads, s, len, (const double*)r64, rT);
         rin = rT;
       }
-      if ((st = gmres<T>(p, len, applyA, rin, dT, kEta, sizeof(T) == 8 ? atol : 0.0, opt->max_inner, &it, &res))) return st;
+      if ((st = gmres<T>(p, len, applyA, rin, dT, eta, sizeof(T) == 8 ? atol : 0.0, opt->max_inner, &it, &res))) return st;
       if (phi_space) {
         launch(p, k_add_cast<T>, gl, kThreads, s, len, (const T*)dT, x64);
       } else {
@@ -2421,7 +2431,7 @@ int solve_T(pgpu_problem* p, const pgpu_options* opt, pgpu_stats* stats) {
       break;
     }
     const double sh = opt->shift < 0.0 ? kShiftDefault : opt->shift;
-    if (phi_space && outer >= kShiftAfter && dk < kShiftWhenDk && sh > 0.0) {
+    if (phi_space && outer >= shift_after && dk < shift_when_dk && sh > 0.0) {
       lam_s = 1.0 / std::fmax(os.k * (1.0 + sh), os.k + kShiftMargin * dk);  // above the fundamental k
       launch(p, k_put<double>, 1, 1, s, d.lam_dev.as<double>(), lam_s);
     }
