@@ -286,8 +286,11 @@ class SNCpu:
 
     # ---- eigen-solve -----------------------------------------------------------------
     def solve(self, tol_k: float = 1e-10, tol_flux: float = 1e-9, shift: float = 0.05, eta: float = 0.2,
-              restart: int = 30, max_outer: int = 5000, power: float | None = None) -> dict:
-        """Power iteration with Wielandt shift and GMRES(restart) over sweeps, in FP64."""
+              restart: int = 30, max_outer: int = 5000, power: float | None = None,
+              shift_when_dk: float = 0.1) -> dict:
+        """Power iteration with Wielandt shift and GMRES(restart) over sweeps, in FP64 (the
+        GPU solver's algorithm: the shift starts after three outer iterations once
+        |dk| < shift_when_dk)."""
         t0 = time.perf_counter()
         self.sweeps = 0
         nG, n, G = self.nG, self.n, self.G
@@ -326,7 +329,7 @@ class SNCpu:
             if dk < tol_k and change < tol_flux:
                 converged = True
                 break
-            if outer >= 3 and dk < 1e-3 and shift > 0.0:
+            if outer >= 3 and dk < shift_when_dk and shift > 0.0:
                 lam = 1.0 / max(k * (1.0 + shift), k + 50.0 * dk)
         if not converged:
             raise RuntimeError("CPU SN power iteration did not converge")
