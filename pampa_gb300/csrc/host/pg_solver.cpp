@@ -5,6 +5,9 @@
 // iterates on the flux.
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -610,6 +613,7 @@ int small_inverse(int n, const double* A, double* Ainv) {
 }  // namespace
 
 int SNSolver::buildProblem() {
+  const auto t_start = std::chrono::steady_clock::now();
   const Mesh& mesh = *mesh_;
   const int n = mesh.num_cells, F = mesh.fmax, G = G_;
   std::vector<double> dirs, w;
@@ -738,8 +742,15 @@ int SNSolver::buildProblem() {
   op.cart_nx = mesh.cart_nx;
   op.cart_ny = mesh.cart_ny;
   op.cart_nz = mesh.cart_nz;
+  const auto t_assembled = std::chrono::steady_clock::now();
   int code = pgpu_sn_create(opt_.device, &op, &problem_);
   PG_CHECK(code != PGPU_OK, std::string("unable to upload the SN operator: ") + pgpu_last_error());
+  if (std::getenv("PGPU_HOST_TIMING")) {  // measurement: host assembly and device setup of the operator
+    const auto t_end = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "pgpu host: SN assembly %.3f s, pgpu_sn_create %.3f s\n",
+                 std::chrono::duration<double>(t_assembled - t_start).count(),
+                 std::chrono::duration<double>(t_end - t_assembled).count());
+  }
   return 0;
 }
 
