@@ -119,34 +119,39 @@ struct ReduceSlots {
   unsigned int* ticket;   // one counter
 };
 
+// Sums the first nv (<= NV, the same in every lane) of v over the warp, into lane 0.
 template <int NV>
-__device__ inline void warp_sum(double (&v)[NV]) {
+__device__ inline void warp_sum(double (&v)[NV], int nv = NV) {
 #pragma unroll
   for (int k = 0; k < NV; k++)
+    if (k < nv)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
 }
 
 // Returns true in every thread of the last block, with `tot` filled in thread 0..NV-1's
-// view (all threads see the same totals through shared memory).
+// view (all threads see the same totals through shared memory).  Only the first nv
+// values (the same in every thread) are reduced; the others come back as zero.
 template <int NV>
-__device__ inline bool block_reduce_last(double (&v)[NV], ReduceSlots<NV> slots, double (&tot)[NV]) {
+__device__ inline bool block_reduce_last(double (&v)[NV], ReduceSlots<NV> slots, double (&tot)[NV], int nv = NV) {
   __shared__ double sh[NV][32];
   __shared__ bool last;
-  warp_sum<NV>(v);
+  warp_sum<NV>(v, nv);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < NV; k++) sh[k][warp] = v[k];
+    for (int k = 0; k < NV; k++)
+      if (k < nv) sh[k][warp] = v[k];
   __syncthreads();
   if (warp == 0) {
     double w[NV];
 #pragma unroll
-    for (int k = 0; k < NV; k++) w[k] = lane < nw ? sh[k][lane] : 0.0;
-    warp_sum<NV>(w);
+    for (int k = 0; k < NV; k++) w[k] = lane < nw && k < nv ? sh[k][lane] : 0.0;
+    warp_sum<NV>(w, nv);
     if (lane == 0) {
 #pragma unroll
-      for (int k = 0; k < NV; k++) slots.partials[k * kMaxBlocks + blockIdx.x] = w[k];
+      for (int k = 0; k < NV; k++)
+        if (k < nv) slots.partials[k * kMaxBlocks + blockIdx.x] = w[k];
       __threadfence();
       unsigned int t = atomicAdd(slots.ticket, 1u);
       last = (t == gridDim.x - 1);
@@ -163,16 +168,19 @@ __device__ inline bool block_reduce_last(double (&v)[NV], ReduceSlots<NV> slots,
   // loads of one thread overlap
   for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
 #pragma unroll
-    for (int k = 0; k < NV; k++) acc[k] += __ldcg(slots.partials + k * kMaxBlocks + b);
-  warp_sum<NV>(acc);
+    for (int k = 0; k < NV; k++)
+      if (k < nv) acc[k] += __ldcg(slots.partials + k * kMaxBlocks + b);
+  warp_sum<NV>(acc, nv);
   __syncthreads();
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < NV; k++) sh[k][warp] = acc[k];
+    for (int k = 0; k < NV; k++)
+      if (k < nv) sh[k][warp] = acc[k];
   __syncthreads();
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; k++) {
+      if (k >= nv) continue;
       double s = 0.0;
       for (int w2 = 0; w2 < nw; w2++) s += sh[k][w2];
       sh[k][0] = s;
@@ -181,7 +189,7 @@ __device__ inline bool block_reduce_last(double (&v)[NV], ReduceSlots<NV> slots,
   }
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < NV; k++) tot[k] = sh[k][0];
+  for (int k = 0; k < NV; k++) tot[k] = k < nv ? sh[k][0] : 0.0;
   return true;
 }
 

@@ -1273,7 +1273,7 @@ __global__ void k_gs_dot(long long N, const T* __restrict__ V, long long ld, int
   for (int k = 0; k < kGsChunk; k++) acc[k] = (double)part[k];
   ReduceSlots<kGsChunk> slots{partials + (size_t)blockIdx.y * kGsChunk * kMaxBlocks, tickets + blockIdx.y};
   double tot[kGsChunk];
-  if (block_reduce_last<kGsChunk>(acc, slots, tot) && threadIdx.x == 0)
+  if (block_reduce_last<kGsChunk>(acc, slots, tot, nk) && threadIdx.x == 0)
     for (int k = 0; k < nk; k++) out[k0 + k] = tot[k];
 }
 

@@ -169,3 +169,18 @@ def test_column_sweep_equals_level_sweep(shape, tmp_path, monkeypatch):
     assert abs(out["1"][0] - out["0"][0]) <= 1e-10
     assert rel_l2(out["1"][1], out["0"][1]) <= 1e-9
     assert rel_l2(out["1"][2], out["0"][2]) <= 1e-9
+
+
+def test_hex_lattice_column_sweep_equals_level_sweep(tmp_path, monkeypatch):
+    """A hexagonal-prism lattice is swept by pipelined columns; the level-set sweep
+    (PGPU_SWEEP_COLUMNS=0) makes the same updates in the same order."""
+    from pampa_gb300 import workloads as wl
+    path = wl.sn_hex(str(tmp_path), nq=12, nr=10, nz=9, order=4, block=3)
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("PGPU_SWEEP_COLUMNS", mode)
+        with pg.Pampa(path, "-silent", "-pgpu_precision", "mixed") as p:
+            p.solve()
+            out[mode] = (p.keff, p.field("scalar-flux"))
+    assert abs(out["1"][0] - out["0"][0]) <= 1e-9
+    assert rel_l2(out["1"][1], out["0"][1]) <= 1e-8
