@@ -2044,19 +2044,22 @@ int gmres(pgpu_problem* p, long long len, App applyA, const T* r, T* dvec, doubl
     // classical Gram-Schmidt with re-orthogonalisation when needed ("twice is enough"):
     // h1 = V^T w (and <w, w>), w -= V h1 with its norm; a second pass only when the
     // norm fell below kReorth of the original (cancellation)
-    const dim3 gd1(std::min(gx, kMaxGrid / 2), (j + 2 + kGsChunk - 1) / kGsChunk);
-    const dim3 gd(std::min(gx, kMaxGrid / 2), (j + 1 + kGsChunk - 1) / kGsChunk);
+    // grids of 2 (products) and 4 (subtraction) CTAs per SM: FP64 issue bounds these kernels,
+    // and fewer threads mean fewer per-thread reductions for the same products
+    const dim3 gd1(std::min(gx, kMaxGrid / 4), (j + 2 + kGsChunk - 1) / kGsChunk);
+    const dim3 gd(std::min(gx, kMaxGrid / 4), (j + 1 + kGsChunk - 1) / kGsChunk);
+    const int gsub = std::min(gx, kMaxGrid / 2);
     double* part = d.partials.as<double>();
     unsigned int* tick = d.ticket.as<unsigned int>();
     launch(p, k_gs_dot<T>, gd1, kThreads, s, len, (const T*)V, len, j + 2, (const T*)wj, h1, part, tick,
            (const double*)nullptr);
-    launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, wj, hn, nslot,
+    launch(p, k_gs_sub_norm<T>, gsub, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h1, wj, hn, nslot,
            (const double*)nullptr);
     // the second pass, decided and (if needed) run on the device
     launch(p, k_gs_gate, 1, 1, s, (const double*)(h1 + j + 1), (const double*)hn, gate, h2, j + 1);
     launch(p, k_gs_dot<T>, gd, kThreads, s, len, (const T*)V, len, j + 1, (const T*)wj, h2, part, tick,
            (const double*)gate);
-    launch(p, k_gs_sub_norm<T>, gx, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, wj, hn, nslot,
+    launch(p, k_gs_sub_norm<T>, gsub, kThreads, s, len, (const T*)V, len, j + 1, (const double*)h2, wj, hn, nslot,
            (const double*)gate);
     launch(p, k_scale_to<T>, gx, kThreads, s, len, (const T*)wj, (const double*)hn, 1, wj);
   };
