@@ -6,6 +6,9 @@ PGPU_DIFF_MG=1 builds the hierarchy at any size (by default only operators of at
 created.  Bars as for the other diffusion tests: FP64 |dk| <= 1e-6 and flux relative L2
 <= 1e-5 against the oracle; mixed precision 1e-5 and 1e-4.
 """
+import os
+import sys
+
 import numpy as np
 import pytest
 
@@ -84,3 +87,31 @@ def test_vcycle_linear_solve(monkeypatch):
         with pg.DiffusionProblem(**op) as dp:
             xs[mg], _ = dp.solve_linear(0.3, b, tol_flux=1e-12)
     assert rel_l2(xs["1"], xs["0"]) <= 1e-10
+
+
+@pytest.mark.parametrize("precision", [pg.PGPU_FP64, pg.PGPU_MIXED])
+def test_default_size_threshold_box_against_oracle_fixture(precision, monkeypatch):
+    """A 7-group box of 40x40x12 cells (134,400 rows, above the 2^17 rows from which the
+    solver builds the V-cycle by itself) against the oracle's direct solve, kept as a
+    fixture (tests/golden/make_diffusion_7g_fixture.py: the direct solve takes minutes).
+    The default path (V-cycle) and the cell preconditioner alone both reach the oracle's
+    eigenpair, and the default path takes far fewer inner iterations."""
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_diffusion_7g_fixture as fx
+    fix = np.load(fx.FIXTURE)
+    op, _, _ = fx.problem()
+    assert np.allclose(fx.checksums(op), fix["checksums"], rtol=1e-12, atol=0), "generator changed"
+    k_tol, f_tol = _tols(precision)
+    out = {}
+    for mg in (None, "0"):
+        if mg is None:
+            monkeypatch.delenv("PGPU_DIFF_MG", raising=False)
+        else:
+            monkeypatch.setenv("PGPU_DIFF_MG", mg)
+        with pg.DiffusionProblem(**op) as dp:
+            res = dp.solve(precision=precision)
+            phi = dp.scalar_flux()
+        assert abs(res.keff - float(fix["keff"])) <= k_tol, (mg, res.keff, float(fix["keff"]))
+        assert rel_l2(phi, fix["phi"]) <= f_tol, mg
+        out[mg] = res.stats["inner_iterations"]
+    assert out[None] * 2 < out["0"], out

@@ -21,3 +21,19 @@ def test_generated_operator_equals_oracle_assembly(shape, G, tmp_path):
         assert np.array_equal(np.asarray(op[key]), np.asarray(ref[key])), key
     for key in ("diag", "offdiag", "volumes", "sigma_s", "chi", "nu_sigma_f", "kappa_sigma_f"):
         assert np.array_equal(np.asarray(op[key], float), np.asarray(ref[key], float)), key
+
+
+def test_diffusion_7g_fixture_matches_its_generator():
+    """The kept oracle answer of the 7-group 40x40x12 box (used by the GPU multigrid test)
+    belongs to the operator the seeded generator builds today, and its flux is normalised
+    as the oracle normalises (positive, finite)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_diffusion_7g_fixture as fx
+    fix = np.load(fx.FIXTURE)
+    op, _, _ = fx.problem()
+    assert np.allclose(fx.checksums(op), fix["checksums"], rtol=1e-12, atol=0)
+    phi = fix["phi"]
+    assert phi.size == 40 * 40 * 12 * 7 and np.all(np.isfinite(phi)) and phi.min() >= 0
+    assert 0.3 < float(fix["keff"]) < 1.5
