@@ -165,13 +165,20 @@ def sn_3d(out_dir: str, nx: int = 64, ny: int = 64, nz: int = 32, cell: float = 
     return path
 
 
+def diffusion_3d_7g_data(nx: int = 256, ny: int = 256, nz: int = 128, seed: int = 3, block: int = 8,
+                         G: int = 7) -> tuple[list[dict], np.ndarray]:
+    """Materials and (nz, ny, nx) layout of diffusion_3d_7g's problem."""
+    rng = np.random.default_rng(seed)
+    mats = materials_multigroup(rng, 6, G)
+    layout = _block_layout(rng, (nz, ny, nx), (block, block, block), 6)
+    return mats, layout
+
+
 def diffusion_3d_7g(out_dir: str, nx: int = 256, ny: int = 256, nz: int = 128, cell: float = 2.0,
                     seed: int = 3, block: int = 8, G: int = 7) -> str:
     """7-group 3D diffusion (256x256x128 of 2 cm cells by default)."""
     os.makedirs(out_dir, exist_ok=True)
-    rng = np.random.default_rng(seed)
-    mats = materials_multigroup(rng, 6, G)
-    layout = _block_layout(rng, (nz, ny, nx), (block, block, block), 6)
+    mats, layout = diffusion_3d_7g_data(nx, ny, nz, seed, block, G)
     write_cartesian_mesh(os.path.join(out_dir, "mesh.pmp"), cell, nx, ny, nz, layout,
                          {"-x": "reflective", "+x": "vacuum", "-y": "reflective", "+y": "vacuum",
                           "-z": "reflective", "+z": "vacuum"})
@@ -246,14 +253,21 @@ def write_hex_prism_mesh(path: str, nq: int, nr: int, pitch: float, nz: int, dz:
         fh.write("\n".join(lines) + "\n")
 
 
+def sn_hex_data(nq: int = 200, nr: int = 200, nz: int = 40, seed: int = 5,
+                block: int = 10) -> tuple[list[dict], np.ndarray]:
+    """Materials and (nz, nr, nq) layout of sn_hex's problem."""
+    rng = np.random.default_rng(seed)
+    mats = materials_4g(rng, 5)
+    layout = _block_layout(rng, (nz, nr, nq), (max(1, nz // 4), block, block), 5)
+    return mats, layout
+
+
 def sn_hex(out_dir: str, nq: int = 200, nr: int = 200, nz: int = 40, pitch: float = 2.0, dz: float = 2.0,
            order: int = 8, seed: int = 5, block: int = 10) -> str:
     """4-group S_N on a hexagonal-prism lattice (200 x 200 hexagons x 40 layers by default,
     1.6M cells), 5 materials in blocks of `block` hexagons, vacuum boundaries."""
     os.makedirs(out_dir, exist_ok=True)
-    rng = np.random.default_rng(seed)
-    mats = materials_4g(rng, 5)
-    layout = _block_layout(rng, (nz, nr, nq), (max(1, nz // 4), block, block), 5)
+    mats, layout = sn_hex_data(nq, nr, nz, seed, block)
     write_hex_prism_mesh(os.path.join(out_dir, "mesh.pmp"), nq, nr, pitch, nz, dz, layout)
     for k, m in enumerate(mats):
         write_material(os.path.join(out_dir, f"mat{k + 1}.pmp"), m, diffusion=False)

@@ -159,3 +159,50 @@ def sn_operator_from_oracle(prob, cart=(0, 0, 0)):
                 normals=np.transpose(mesh.normals, (1, 0, 2)), gauss=np.transpose(gc, (1, 0, 2)),
                 reflect_axis=raxis, materials=mat_c, volumes=mesh.volumes, directions=dirs, weights=w,
                 reflected=refl, sigma_t=st, sigma_s=ss, chi=chi, nu_sigma_f=nsf, kappa_sigma_f=ksf, cart=cart)
+
+
+# --------------------------------------------------------------------------------------
+# Fission operators applied on the host, for eigen-residual checks of solves too large for
+# the oracle: F of DiffusionSolver::buildMatrices (DiffusionSolver.cxx:88-320: chi_g
+# nu_sigma_f_g2 V in each cell's group block) and of SNSolver::buildMatrices
+# (SNSolver.cxx:344-631: chi_g nu_sigma_f_g2 w_m2 V), with the material values as the
+# solvers read them from the written files (workloads.material_arrays).
+# --------------------------------------------------------------------------------------
+
+
+def fission_source(mats, layout, phi) -> np.ndarray:
+    """f[i, g] = chi_g(m_i) sum_g2 nu_sigma_f_g2(m_i) phi[i, g2] (no volume), m_i the cell's
+    material from the 1-based `layout` in cell order."""
+    from pampa_gb300 import workloads as wl
+    t = wl.material_arrays(mats)
+    G = t["G"]
+    mat = np.asarray(layout).reshape(-1) - 1
+    phi = np.asarray(phi, dtype=np.float64).reshape(-1, G)
+    f = np.zeros_like(phi)
+    for m in range(len(mats)):
+        idx = np.nonzero(mat == m)[0]
+        if idx.size and np.any(t["nu_sigma_f"][m]):
+            f[idx] = np.outer(phi[idx] @ t["nu_sigma_f"][m], t["chi"][m])
+    return f
+
+
+def sn_scalar_flux(psi, weights, G: int) -> np.ndarray:
+    """phi[i, g] = sum_m w_m psi[(i G + g) M + m]."""
+    w = np.asarray(weights, dtype=np.float64)
+    return (np.asarray(psi, dtype=np.float64).reshape(-1, w.size) @ w).reshape(-1, G)
+
+
+def eigen_residual(Rx, f, M: int = 1, chunk: int = 1 << 22) -> tuple[float, float]:
+    """For R x = (V/k) F' x with F' x = f broadcast over M directions: the least-squares
+    scale c = <f, R x> / <f, f> (c = V/k for an eigenpair) and ||R x - c f|| / ||c f||,
+    summed chunk by chunk of rows (no cancellation between the two norms)."""
+    Rx = np.asarray(Rx, dtype=np.float64).reshape(-1, M)
+    fv = np.asarray(f, dtype=np.float64).reshape(-1)
+    num = float(fv @ Rx.sum(axis=1))
+    den = float(M * (fv @ fv))
+    c = num / den
+    ss = 0.0
+    for a in range(0, fv.size, chunk):
+        r = Rx[a:a + chunk] - c * fv[a:a + chunk, None]
+        ss += float(np.sum(r * r))
+    return c, float(np.sqrt(ss / (c * c * den)))
