@@ -295,7 +295,7 @@ typedef struct pgpu_server pgpu_server;
 int pgpu_serve_create(int device, int slots, double hbm_fraction, pgpu_server** out);
 long long pgpu_serve_budget_bytes(pgpu_server* s);
 /* SMs each solve started from now on sizes its grids for (pgpu_problem_set_sm_share);
- * the server's default is 2 / slots of the device (0, the whole device, for one slot). */
+ * the server's default is 3 / slots of the device (0, the whole device, for one slot). */
 int pgpu_serve_set_sm_share(pgpu_server* s, int sms);
 int pgpu_serve_submit_diffusion(pgpu_server* s, const pgpu_diffusion_operator* op, const pgpu_options* opt,
                                 int want_flux, long long* id);
