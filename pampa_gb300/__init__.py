@@ -234,7 +234,9 @@ class Pampa:
             raise PampaError(f"pampa_get_problem failed: {last_error()}")
         x = _f64(x)
         y = np.zeros_like(x)
-        fn = lib().pgpu_sn_apply if self.field_size("angular-flux") else lib().pgpu_diffusion_apply
+        # a vector of the scalar flux's length is a diffusion vector, anything else an SN
+        # angular flux (the library checks the problem's kind either way)
+        fn = lib().pgpu_diffusion_apply if x.size == self.field_size("scalar-flux") else lib().pgpu_sn_apply
         st = fn(h, _dp(x), _dp(y))
         if st != PGPU_OK:
             raise PampaError(f"operator apply failed: {last_error()}")
