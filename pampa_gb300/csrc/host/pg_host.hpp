@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdio>
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -165,6 +166,11 @@ struct Field {
   std::vector<double>* vec = nullptr;
   bool input = false, output = false;
   std::shared_ptr<ConvergenceError> delta;  // convergence of an output field (coupling)
+  // A field without a host vector (vec == nullptr) whose values stay where the solver
+  // keeps them until asked for: its size and the copies out of and into a caller's buffer.
+  size_t size = 0;
+  std::function<int(double*)> get;
+  std::function<int(const double*)> set;
 };
 
 struct RunOptions {
@@ -347,7 +353,11 @@ class SNSolver : public NeutronicSolver {
   double delta_ = 0.1;  // SNSolver.hxx:16
   bool ls_ = false;
   int M_ = 0;
+  // The angular flux stays on the device: pampa_get_field copies it from there into the
+  // caller's buffer.  psi_ holds a host copy only when the .vtk or PETSc outputs need it
+  // or a caller set the field (psi_host_); psi_solved_ once the problem holds a solution.
   std::vector<double> psi_;
+  bool psi_host_ = false, psi_solved_ = false;
 };
 
 // Quadrature of AngularQuadratureSet::build (AngularQuadratureSet.cxx:4-209).

@@ -25,6 +25,7 @@ namespace pg {
 int Solver::getField(double* v, const std::string& name) const {
   for (const auto& f : fields_)
     if (f.name == name) {
+      if (!f.vec) return f.get(v);
       std::memcpy(v, f.vec->data(), f.vec->size() * sizeof(double));
       return 0;
     }
@@ -34,6 +35,7 @@ int Solver::getField(double* v, const std::string& name) const {
 int Solver::setField(const double* v, const std::string& name) {
   for (auto& f : fields_)
     if (f.name == name) {
+      if (!f.vec) return f.set(v);
       std::memcpy(f.vec->data(), v, f.vec->size() * sizeof(double));
       return 0;
     }
@@ -43,7 +45,7 @@ int Solver::setField(const double* v, const std::string& name) {
 int Solver::fieldSize(const std::string& name, int& size) const {
   for (const auto& f : fields_)
     if (f.name == name) {
-      size = (int)f.vec->size();
+      size = (int)(f.vec ? f.vec->size() : f.size);
       return 0;
     }
   PG_CHECK(true, "unable to find field '" + name + "'");
@@ -614,6 +616,7 @@ int small_inverse(int n, const double* A, double* Ainv) {
 
 int SNSolver::buildProblem() {
   const auto t_start = std::chrono::steady_clock::now();
+  psi_solved_ = false;  // a new device problem holds no solution yet
   const Mesh& mesh = *mesh_;
   const int n = mesh.num_cells, F = mesh.fmax, G = G_;
   std::vector<double> dirs, w;
@@ -759,13 +762,39 @@ int SNSolver::initialize(const Mesh& mesh, const std::vector<Material>& mats,
   PG_TRY(NeutronicSolver::initialize(mesh, mats, opt, transient), "unable to initialize");
   PG_CHECK(order_ != 2 && order_ != 4 && order_ != 6 && order_ != 8, "SN order not implemented");
   M_ = order_ * (order_ + 2);
-  psi_.assign((size_t)mesh.num_cells * G_ * M_, 0.0);
-  fields_.push_back({"angular-flux", &psi_, false, false, nullptr});  // SNSolver.cxx:745-747
+  // SNSolver.cxx:745-747; zero until the first solve, as the reference's new vector
+  const size_t N = (size_t)mesh.num_cells * G_ * M_;
+  psi_.clear();
+  psi_host_ = psi_solved_ = false;
+  Field f{"angular-flux", nullptr, false, false, nullptr};
+  f.size = N;
+  f.get = [this, N](double* v) -> int {
+    if (psi_host_) {
+      std::memcpy(v, psi_.data(), N * sizeof(double));
+    } else if (psi_solved_ && problem_) {
+      PG_TRY(pgpu_problem_get_angular_flux(problem_, v), "unable to get the angular flux");
+    } else {
+      std::memset(v, 0, N * sizeof(double));
+    }
+    return 0;
+  };
+  f.set = [this, N](const double* v) -> int {
+    psi_.assign(v, v + N);
+    psi_host_ = true;
+    return 0;
+  };
+  fields_.push_back(f);
   return 0;
 }
 
 int SNSolver::fetchSolution() {
-  PG_TRY(pgpu_problem_get_angular_flux(problem_, psi_.data()), "unable to get the angular flux");
+  psi_solved_ = true;
+  psi_host_ = false;
+  if (opt_.vtk || opt_.dump) {  // the outputs write the angular flux from the host
+    psi_.resize((size_t)mesh_->num_cells * G_ * M_);
+    PG_TRY(pgpu_problem_get_angular_flux(problem_, psi_.data()), "unable to get the angular flux");
+    psi_host_ = true;
+  }
   return 0;
 }
 

@@ -67,6 +67,18 @@ def test_set_field_roundtrip(case_input):
             p.field("no-such-field")
 
 
+def test_angular_flux_field_before_a_solve_and_set(case_input):
+    """The SN angular flux (kept on the device after a solve) reads as zeros before any
+    solve, as the reference's new vector, and a value set by the caller reads back."""
+    import numpy as np
+    with pg.Pampa(case_input("slabs/reflected-s4"), "-silent") as p:
+        psi = p.field("angular-flux")
+        assert psi.size > 0 and not np.any(psi)
+        v = np.arange(psi.size, dtype=np.float64) * 0.5
+        p.set_field("angular-flux", v)
+        assert np.array_equal(p.field("angular-flux"), v)
+
+
 @pytest.mark.parametrize("opts,msg", [(["-pgpu_precision", "fp16"], "wrong -pgpu_precision"),
                                       (["-pgpu_shift", "-1"], "wrong -pgpu_shift"),
                                       (["-pgpu_max_outer", "0"], "wrong -pgpu_max_outer"),
