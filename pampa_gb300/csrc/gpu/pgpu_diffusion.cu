@@ -1145,7 +1145,6 @@ int make_fp32(pgpu_problem* p) {
   return PGPU_OK;
 }
 
-// BiCGStab on A d = rin in precision T.  Kernels are launched in chunks; each kernel
 // SpMV kernels of BiCGStab: the cell form for G = 2, 4, 7, the row form otherwise.
 inline bool cell_form(int G) { return G == 2 || G == 4 || G == 7; }
 
@@ -1654,8 +1653,11 @@ int tune_bicg(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w) {
   return PGPU_OK;
 }
 
-// returns at once when the device-side `converged` flag is set, so the host only reads
-// the state once per chunk.  The solution is left in w[0].
+// BiCGStab on A d = rin in precision T.  Every scalar stays on the device and each
+// kernel returns at once when the device-side `converged` flag is set; the iterations run
+// as replayed graphs of kBicgChain conditional iterations, so the host reads the state
+// once per chain (with per-launch profiling, once per iteration).  The solution is left
+// in w[0].
 template <typename T>
 int bicgstab(pgpu_problem* p, const DiffOp<T>& A, DevBuf* w, const T* rin, double rtol, int max_iters,
              int* iters_out) {
