@@ -2829,7 +2829,8 @@ static bool kba_classes(const pgpu_sn_operator* op, const std::vector<unsigned c
   const int n = op->num_cells, F = op->num_faces, G = op->num_groups, M = op->num_dirs;
   const size_t per_class = (size_t)G * M * values_per_row * sizeof(double);
   std::map<std::vector<unsigned long long>, int> ids;
-  std::vector<unsigned long long> key((size_t)2 + (size_t)F * 5);
+  std::vector<unsigned long long> key((size_t)2 + (size_t)F * 5), last;
+  int last_id = -1;  // the previous cell's class: neighbouring cells mostly share one
   // values that differ only in their last 16 mantissa bits (relative 2^-36, e.g. cell
   // volumes of a lattice computed from rounded coordinates) share a class; the class
   // uses its first cell's exact values
@@ -2852,15 +2853,21 @@ static bool kba_classes(const pgpu_sn_operator* op, const std::vector<unsigned c
       k[3] = bits(windiag[o]);
       k[4] = bits(win[o]);
     }
-    auto it = ids.find(key);
     int id;
-    if (it == ids.end()) {
-      id = (int)rep.size();
-      if (id > 65535 || (size_t)(id + 1) * per_class > max_bytes) return false;
-      ids.emplace(key, id);
-      rep.push_back(i);
+    if (last_id >= 0 && key == last) {
+      id = last_id;
     } else {
-      id = it->second;
+      auto it = ids.find(key);
+      if (it == ids.end()) {
+        id = (int)rep.size();
+        if (id > 65535 || (size_t)(id + 1) * per_class > max_bytes) return false;
+        ids.emplace(key, id);
+        rep.push_back(i);
+      } else {
+        id = it->second;
+      }
+      last = key;
+      last_id = id;
     }
     ccls[i] = (unsigned short)id;
   }
