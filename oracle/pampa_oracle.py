@@ -1062,15 +1062,31 @@ def gauss_coefs(mesh: Mesh, delta: float) -> np.ndarray:
     return c
 
 
+# Starting values of the LS Gram matrix G.  The reference declares `Eigen::MatrixXd
+# G(num_dims, num_dims)` per boundary cell and accumulates into it without initialising it
+# (SNSolver.cxx:247-252).  "zero" is its evident intent and what the product implements.
+# The "heap-*" models restate what glibc's allocator leaves there when G's chunk is freed
+# at the end of one boundary cell and handed back, last-in first-out, to the next: G(0,0)
+# holds the free-list pointer (a denormal, taken as 0) and G(0,1), G(1,1) the previous
+# cell's final values; "heap-key-kept" also carries G(1,0), which glibc before 2.29 (no
+# tcache key) leaves untouched (32-byte-aligned Eigen allocations carry G(0,0) as well,
+# which moves keff by 4e-8 more), "heap-key-cleared" sets it to 0 as glibc 2.29+ does
+# when it hands a chunk out.  The first boundary cell
+# starts from zero in both: what its chunk held before is not determined by the input.
+LS_GRAM_START = "zero"
+
+
 def ls_coefs(mesh: Mesh, ic_to_ibc: np.ndarray) -> np.ndarray:
     """SNSolver::buildLSGradientScheme for boundary cells (SNSolver.cxx:211-269).
 
     Reproduces the reference exactly: d is a (faces x dims) row-major array, and d(jg, f)
-    reads its flat element jg*dims + f; G starts from zero.
+    reads its flat element jg*dims + f; G starts from LS_GRAM_START (zero by default).
     """
     nd = mesh.num_dims
     nbc = int((ic_to_ibc >= 0).sum())
     coefs = np.zeros((nbc, mesh.F, 3))
+    carry = LS_GRAM_START != "zero" and nd == 2
+    prev = np.zeros((nd, nd))
     for i in np.nonzero(ic_to_ibc >= 0)[0]:
         ic = ic_to_ibc[i]
         nf = int(mesh.num_faces[i])
@@ -1083,10 +1099,15 @@ def ls_coefs(mesh: Mesh, ic_to_ibc: np.ndarray) -> np.ndarray:
                 d[f, a] = c2[a] - ci[a]
         flat = d.reshape(-1)
         Gm = np.zeros((nd, nd))
+        if carry:
+            Gm[0, 1], Gm[1, 1] = prev[0, 1], prev[1, 1]
+            if LS_GRAM_START == "heap-key-kept":
+                Gm[1, 0] = prev[1, 0]
         for jg in range(nd):
             for ig in range(nd):
                 for f in range(nf):
                     Gm[jg, ig] += flat[jg * nd + f] * d[f, ig]
+        prev = Gm.copy()
         Ginv = np.linalg.inv(Gm)
         for f in range(nf):
             for a in range(nd):
